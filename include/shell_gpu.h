@@ -1,0 +1,199 @@
+/*
+ * shell_gpu.h — C ABI of the GB300 RLWE polynomial hot path.
+ *
+ * A drop-in device backend for google/shell-encryption's RNS polynomial,
+ * ciphertext and key-switching calls.  Every entry point takes plain pointers
+ * and sizes; polynomial data are DEVICE pointers to uint64 residues in SHELL's
+ * MontgomeryInt<uint64> representation (x * 2^64 mod q), laid out as
+ *
+ *   poly        [num_limbs][n]                 limb l is modulo q_l
+ *   ciphertext  [num_components][num_limbs][n]
+ *   batches     [count][...]                   contiguous
+ *
+ * so results compare bit-for-bit (memcmp) with the reference's
+ * RnsPolynomial::Coeffs() / Polynomial::Coeffs().  Calls are asynchronous on
+ * the given stream (0 = legacy default stream); argument validation happens
+ * on the host before any launch and mirrors the reference's absl::Status
+ * checks.  Return values are absl::StatusCode numbers (0 = OK,
+ * 3 = INVALID_ARGUMENT, 9 = FAILED_PRECONDITION, 8 = RESOURCE_EXHAUSTED,
+ * 13 = INTERNAL); shg_last_error() returns the message of the calling
+ * thread's last failure.
+ *
+ * Reference interfaces cited below are paths inside google/shell-encryption.
+ */
+#ifndef SHELL_GPU_H_
+#define SHELL_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct shg_context shg_context;  /* RNS context resident on the GPU */
+typedef struct shg_key shg_key;          /* gadget key-switching key */
+typedef void* shg_stream;                /* a cudaStream_t */
+
+enum {
+  SHG_OK = 0,
+  SHG_INVALID_ARGUMENT = 3,
+  SHG_RESOURCE_EXHAUSTED = 8,
+  SHG_FAILED_PRECONDITION = 9,
+  SHG_INTERNAL = 13,
+};
+
+/* Message of this thread's most recent failed call ("" if none). */
+const char* shg_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Context
+ * ------------------------------------------------------------------------- */
+
+/* RnsContext<MontgomeryInt<uint64>>::Create(log_n, qs, {}, t)
+ * (shell_encryption/rns/rns_context.h:62-72, rns/rns_context.cc:22-76):
+ * validates every prime like MontgomeryIntParams::Create (montgomery.cc:44-59)
+ * and InitializeNttParameters (ntt_parameters.h:183-235), derives psi with the
+ * reference's smallest-t search and uploads twiddle and CRT tables. */
+int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
+                       uint64_t plaintext_modulus, shg_context** out);
+void shg_context_destroy(shg_context* ctx);
+int shg_context_log_n(const shg_context* ctx);
+int shg_context_num_moduli(const shg_context* ctx);
+
+/* Host copy of limb i's Montgomery parameters (montgomery.h:77-202):
+ * out[0..9] = q, log_q, inv_modulus, r_mod_q, r_mod_q_barrett, inv_r,
+ * inv_r_barrett, barrett_numerator, psi (plain), n_inv (Montgomery). */
+int shg_context_prime_info(const shg_context* ctx, int i, uint64_t out[10]);
+/* Host copies of NttParameters::psis_bitrev / psis_inv_bitrev for limb i
+ * (Montgomery reps, n each) (ntt_parameters.h:117-157). */
+int shg_context_ntt_tables(const shg_context* ctx, int i, uint64_t* psis_bitrev,
+                           uint64_t* psis_inv_bitrev);
+/* MainPrimeModulusInverseResidues()[level].Prefix(level): q_level^{-1} mod q_j
+ * for j < level, Montgomery reps (rns/rns_context.h:145-147). */
+int shg_context_ql_inv(const shg_context* ctx, int level, uint64_t* out);
+
+/* ---------------------------------------------------------------------------
+ * RnsPolynomial operations.  `polys` hold `count` polynomials of `num_limbs`
+ * limbs each (limb l modulo q_l, num_limbs <= num_moduli).
+ * ------------------------------------------------------------------------- */
+
+/* RnsPolynomial::ConvertToNttForm (rns/rns_polynomial.cc:171-188) /
+ * ForwardNumberTheoreticTransform (dft_transformations.h:158-176). In place. */
+int shg_ntt_forward(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                    shg_stream stream);
+/* RnsPolynomial::ConvertToCoeffForm (rns/rns_polynomial.cc:190-207) /
+ * InverseNumberTheoreticTransform (dft_transformations.h:181-201). In place. */
+int shg_ntt_inverse(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                    shg_stream stream);
+
+/* RnsPolynomial::Add / Sub / Negate / Mul(poly) / FusedMulAddInPlace
+ * (rns/rns_polynomial.h:150-365) -> MontgomeryInt Batch* ops
+ * (montgomery.cc:229-440).  out may alias an input.  fma: acc += a * b. */
+int shg_poly_add(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream stream);
+int shg_poly_sub(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream stream);
+int shg_poly_neg(shg_context* ctx, uint64_t* out, const uint64_t* a, int count,
+                 int num_limbs, shg_stream stream);
+int shg_poly_mul(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream stream);
+int shg_poly_fma(shg_context* ctx, uint64_t* acc, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream stream);
+/* RnsPolynomial::MulInPlace(RnsInt / Span<ModularInt>) with a per-limb
+ * Montgomery-form scalar (host array, num_limbs entries)
+ * (rns/rns_polynomial.h:236-262). */
+int shg_poly_mul_rns_scalar(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                            const uint64_t* scalar_mont, int count,
+                            int num_limbs, shg_stream stream);
+/* RnsPolynomial::MulInPlace(Integer scalar) (rns/rns_polynomial.h:214-227). */
+int shg_poly_mul_integer(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                         uint64_t scalar, int count, int num_limbs,
+                         shg_stream stream);
+/* RnsPolynomial::Substitute (rns/rns_polynomial.cc:209-260); NTT form; out
+ * must not alias in. */
+int shg_poly_substitute(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                        int power, int count, int num_limbs, shg_stream stream);
+/* RnsPolynomial::ModReduceLsb (rns/rns_polynomial.cc:262-344): in
+ * [count][num_limbs][n] -> out [count][num_limbs-1][n]; ql_inv holds the
+ * num_limbs-1 Montgomery residues of q_{num_limbs-1}^{-1} (host array);
+ * is_ntt selects the input form. */
+int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                           uint64_t t, const uint64_t* ql_inv, int is_ntt,
+                           int count, int num_limbs, shg_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Ciphertexts
+ * ------------------------------------------------------------------------- */
+
+/* RnsRlweCiphertext::Mul / RnsBgvCiphertext::operator* for degree-1 inputs
+ * (rns/rns_ciphertext.h:501-524, rns/rns_bgv_ciphertext.h:134-139):
+ * a, b [count][2][L][n] -> out [count][3][L][n]. */
+int shg_ct_tensor(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                  const uint64_t* b, int count, int num_limbs,
+                  shg_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Gadget key switching (relinearization and Galois keys)
+ * ------------------------------------------------------------------------- */
+
+/* Uploads a gadget key: key_b, key_a [k][num_limbs][n] host arrays in NTT
+ * form (Montgomery reps) with the RnsGadget of log_bs[num_limbs]
+ * (rns/rns_gadget.cc:42-102).  `power` is the key's substitution power: 1
+ * for an RnsRelinKey (GetKeyB/GetKeyA, rns/rns_relinearization_key.h:99-104),
+ * the Galois power for an RnsGaloisKey (CreateFromKeyComponents,
+ * rns/rns_galois_key.cc:183-202).  A single-modulus RelinearizationKey /
+ * GaloisKey part is the num_limbs == 1 case (relinearization_key.cc:99-141;
+ * galois_key.h:43-111). */
+int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
+                   int power, const uint64_t* key_b, const uint64_t* key_a,
+                   shg_key** out);
+void shg_key_destroy(shg_key* key);
+int shg_key_dimension(const shg_key* key);
+/* Device bytes held by the key. */
+size_t shg_key_device_bytes(const shg_key* key);
+
+/* RnsRelinKey::ApplyTo for degree-2 ciphertexts
+ * (rns/rns_relinearization_key.h:82-92, .cc:184-232):
+ * ct [count][3][L][n] (NTT) -> out [count][2][L][n].  out may not alias ct. */
+int shg_relin_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
+                    const uint64_t* ct, int count, shg_stream stream);
+/* RnsGaloisKey::ApplyTo (rns/rns_galois_key.h:146-156, .cc:238-287) on
+ * ciphertexts already substituted to the key's power: ct [count][2][L][n]
+ * -> out [count][2][L][n]. */
+int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
+                     const uint64_t* ct, int count, shg_stream stream);
+
+/* Batched fused form of RnsBgvCiphertext::operator* followed by
+ * RnsRelinKey::ApplyTo (rns/rns_bgv_ciphertext.h:134-139 +
+ * rns/rns_relinearization_key.cc:184-232): a, b [count][2][L][n] ->
+ * out [count][2][L][n], bit-identical to calling both per ciphertext. */
+int shg_bgv_mul_relin(shg_context* ctx, const shg_key* relin_key, uint64_t* out,
+                      const uint64_t* a, const uint64_t* b, int count,
+                      shg_stream stream);
+/* RnsBgvCiphertext::Substitute(power) then RnsGaloisKey::ApplyTo
+ * (rns/rns_bgv_ciphertext.h:161-174): ct [count][2][L][n] -> out. */
+int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,
+                   const uint64_t* ct, int count, shg_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * Single-modulus oblivious expansion (PIR), on a one-prime context
+ * ------------------------------------------------------------------------- */
+
+/* GaloisKeysObliviousExpander::ObliviousExpand for `count` query ciphertexts
+ * (oblivious_expand.h:95-138, 173-227, 273-282): keys[levels] with powers
+ * n/2^i + 1, ct [count][2][n] -> out [count][2^levels][2][n]. */
+int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
+                         int levels, uint64_t* out, const uint64_t* ct,
+                         int count, shg_stream stream);
+/* Sum_i cts[i] * db[i] via SymmetricRlweCiphertext::FusedAbsorbAddInPlace
+ * (symmetric_encryption.h:250-275): cts [count][num_items][2][n],
+ * db [num_items][n] -> out [count][2][n]. */
+int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,
+                   const uint64_t* db, int num_items, int count,
+                   shg_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHELL_GPU_H_ */

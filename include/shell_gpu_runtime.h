@@ -1,0 +1,55 @@
+/*
+ * shell_gpu_runtime.h — device-memory, stream, event and graph plumbing for
+ * callers of shell_gpu.h that do not link the CUDA runtime themselves (the
+ * Python tests and benchmark use these through ctypes).  These have no
+ * counterpart in google/shell-encryption, which is CPU-only.
+ */
+#ifndef SHELL_GPU_RUNTIME_H_
+#define SHELL_GPU_RUNTIME_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "shell_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int shg_device_count(int* count);
+int shg_set_device(int device);
+int shg_device_alloc(size_t bytes, void** out);
+int shg_device_free(void* ptr);
+int shg_host_alloc(size_t bytes, void** out); /* page-locked */
+int shg_host_free(void* ptr);
+int shg_memcpy_h2d(void* dst, const void* src, size_t bytes, shg_stream stream);
+int shg_memcpy_d2h(void* dst, const void* src, size_t bytes, shg_stream stream);
+int shg_memcpy_d2d(void* dst, const void* src, size_t bytes, shg_stream stream);
+int shg_memset_device(void* dst, int value, size_t bytes, shg_stream stream);
+int shg_stream_create(shg_stream* out);
+int shg_stream_destroy(shg_stream stream);
+int shg_stream_synchronize(shg_stream stream);
+int shg_device_synchronize(void);
+int shg_event_create(void** out);
+int shg_event_destroy(void* event);
+int shg_event_record(void* event, shg_stream stream);
+int shg_event_elapsed_ms(void* start, void* stop, float* ms);
+/* Stream capture into a CUDA graph and replay. */
+int shg_graph_capture_begin(shg_stream stream);
+int shg_graph_capture_end(shg_stream stream, void** graph_exec);
+int shg_graph_launch(void* graph_exec, shg_stream stream);
+int shg_graph_destroy(void* graph_exec);
+/* Number of kernels launched by this library so far (host-side count of
+ * launch calls; graph replays are not counted). */
+uint64_t shg_launch_count(void);
+/* Reserve scratch space for batched calls up front (so a later call can be
+ * captured into a graph without allocating). */
+int shg_context_reserve(shg_context* ctx, size_t bytes);
+/* Ciphertexts per internal chunk of the batched key-switch pipeline
+ * (0 = default). */
+int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHELL_GPU_RUNTIME_H_ */

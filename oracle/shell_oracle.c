@@ -1,0 +1,769 @@
+/*
+ * CPU oracle for the SHELL RLWE polynomial hot path — TEST INFRASTRUCTURE ONLY.
+ * Plain-C restatement of google/shell-encryption's CPU algorithms; each
+ * function names the reference file:line it follows.  Only tests, the smoke
+ * check and the benchmark's CPU-baseline leg use it.
+ */
+#include "shell_oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef unsigned __int128 u128;
+
+struct so_prime {
+  /* MontgomeryIntParams<uint64> (montgomery.h:77-202) */
+  uint64_t q;
+  int log_q;
+  uint64_t inv_modulus;      /* R*inv_r - q*inv_modulus = 1 */
+  uint64_t r_mod_q;          /* 2^64 mod q */
+  uint64_t r_mod_q_barrett;  /* floor(r_mod_q * 2^64 / q) */
+  uint64_t inv_r;            /* 2^-64 mod q */
+  uint64_t inv_r_barrett;    /* floor(inv_r * 2^64 / q) */
+  uint64_t barrett_num;      /* floor(2^64 / q) */
+  /* NttParameters (ntt_parameters.h:160-235) */
+  int log_n, n;
+  uint64_t psi;              /* plain value of the primitive 2n-th root */
+  uint64_t n_inv;            /* Montgomery rep of n^{-1} */
+  uint64_t* psis_bitrev;     /* Montgomery reps, n */
+  uint64_t* psis_bitrev_c;   /* GetConstant(): plain value */
+  uint64_t* psis_bitrev_cb;  /* GetConstant(): barrett */
+  uint64_t* psis_inv_bitrev;
+  uint64_t* psis_inv_bitrev_c;
+  uint64_t* psis_inv_bitrev_cb;
+  uint32_t* bitrevs;
+};
+
+struct so_rns {
+  int log_n, L;
+  so_prime** primes;
+  /* prime_q_invs_[i][j] = q_i^{-1} mod q_j, 1 when i == j
+   * (rns/rns_context.cc:169-200), Montgomery reps */
+  uint64_t* q_invs;
+  /* prime_qs_[i][j] = q_i mod q_j, 0 when i == j */
+  uint64_t* q_mods;
+};
+
+/* ---------------------------------------------------------------------------
+ * Montgomery arithmetic (montgomery.h / montgomery.cc)
+ * ------------------------------------------------------------------------- */
+
+static int bit_length(uint64_t x) {  /* bits_util.h BitLength */
+  int b = 0;
+  while (x) { b++; x >>= 1; }
+  return b;
+}
+
+/* ToMontgomeryInt: Shoup multiply by r_mod_q (montgomery.cc:27-40). */
+static inline uint64_t mont_import(const so_prime* p, uint64_t x) {
+  uint64_t hi = (uint64_t)(((u128)p->r_mod_q_barrett * x) >> 64);
+  uint64_t r = x * p->r_mod_q - hi * p->q;
+  return r >= p->q ? r - p->q : r;
+}
+
+/* ExportInt (montgomery.h:156-164). */
+static inline uint64_t mont_export(const so_prime* p, uint64_t x) {
+  uint64_t hi = (uint64_t)(((u128)p->inv_r_barrett * x) >> 64);
+  uint64_t r = x * p->inv_r - hi * p->q;
+  return r >= p->q ? r - p->q : r;
+}
+
+/* MulInPlace: REDC (montgomery.h:318-336). */
+static inline uint64_t mont_mul(const so_prime* p, uint64_t a, uint64_t b) {
+  u128 prod = (u128)a * b;
+  uint64_t u = (uint64_t)prod * p->inv_modulus;
+  u128 t = prod + (u128)p->q * u;
+  uint64_t r = (uint64_t)(t >> 64);
+  return r >= p->q ? r - p->q : r;
+}
+
+/* FusedMulAddInPlace (montgomery.h:446-465). */
+static inline uint64_t mont_fma(const so_prime* p, uint64_t acc, uint64_t a,
+                                uint64_t b) {
+  u128 t = (u128)p->r_mod_q * acc + (u128)a * b;
+  uint64_t u = (uint64_t)t * p->inv_modulus;
+  t += (u128)p->q * u;
+  uint64_t r = (uint64_t)(t >> 64);
+  return r >= p->q ? r - p->q : r;
+}
+
+/* MulConstantInPlace (montgomery.h:362-372); input may be in [0, 4q). */
+static inline uint64_t mul_const(const so_prime* p, uint64_t x, uint64_t c,
+                                 uint64_t cb) {
+  uint64_t hi = (uint64_t)(((u128)cb * x) >> 64);
+  uint64_t r = x * c - hi * p->q;
+  return r >= p->q ? r - p->q : r;
+}
+
+/* BarrettReduce (montgomery.h:126-133); input < 4q. */
+static inline uint64_t barrett(const so_prime* p, uint64_t x) {
+  uint64_t hi = (uint64_t)(((u128)p->barrett_num * x) >> 64);
+  uint64_t r = x - hi * p->q;
+  return r >= p->q ? r - p->q : r;
+}
+
+/* AddInPlace / SubInPlace / NegateInPlace (montgomery.h:383-415). */
+static inline uint64_t mont_add(const so_prime* p, uint64_t a, uint64_t b) {
+  return barrett(p, a + b);
+}
+static inline uint64_t mont_sub(const so_prime* p, uint64_t a, uint64_t b) {
+  return barrett(p, a + (p->q - b));
+}
+static inline uint64_t mont_neg(const so_prime* p, uint64_t a) {
+  return p->q - a;
+}
+
+/* ModExp on Montgomery reps (montgomery.cc:472-492). */
+static uint64_t mont_pow(const so_prime* p, uint64_t base, uint64_t e) {
+  uint64_t result = p->r_mod_q;  /* ImportOne */
+  while (e > 0) {
+    if (e & 1) result = mont_mul(p, result, base);
+    base = mont_mul(p, base, base);
+    e >>= 1;
+  }
+  return result;
+}
+
+/* GetConstant (montgomery.cc:221-227). */
+static void get_constant(const so_prime* p, uint64_t m, uint64_t* c,
+                         uint64_t* cb) {
+  *c = mont_export(p, m);
+  *cb = (uint64_t)(((u128)(*c) << 64) / p->q);
+}
+
+/* Bitrev (ntt_parameters.cc:21-31). */
+static uint32_t bitrev(uint32_t x, int log_n) {
+  uint32_t out = 0;
+  for (int i = 0; i < log_n; i++) {
+    out = (out << 1) | (x & 1);
+    x >>= 1;
+  }
+  return out;
+}
+
+/* MontgomeryIntParams::Create and constructor (montgomery.cc:44-92,
+ * montgomery.h:179-193), InitializeNttParameters (ntt_parameters.h:183-235). */
+so_prime* so_prime_create(uint64_t q, int log_n) {
+  if ((q >> 62) != 0 || (q & 1) == 0) return NULL;
+  if (log_n <= 0 || log_n > 15) return NULL;
+  uint64_t two_n = (uint64_t)1 << (log_n + 1);
+  if (q % two_n != 1) return NULL;
+  so_prime* p = (so_prime*)calloc(1, sizeof(so_prime));
+  p->q = q;
+  p->log_q = bit_length(q);
+  /* Inverses via the halving loop of montgomery.cc:61-92: x*2^64 - y*q = 1 */
+  u128 x = 1, y = 0;
+  const u128 R = (u128)1 << 64;
+  for (int i = 64; i > 0; i--) {
+    if (x & 1) { x += q; y += R; }
+    x >>= 1;
+    y >>= 1;
+  }
+  p->inv_r = (uint64_t)x;
+  p->inv_modulus = (uint64_t)y;
+  p->r_mod_q = (uint64_t)(R % q);
+  p->r_mod_q_barrett = (uint64_t)(((u128)p->r_mod_q << 64) / q);
+  p->inv_r_barrett = (uint64_t)(((u128)p->inv_r << 64) / q);
+  p->barrett_num = (uint64_t)(R / q);
+
+  int n = 1 << log_n;
+  p->log_n = log_n;
+  p->n = n;
+  /* n^{-1}: ImportInt(n).MultiplicativeInverse() (ntt_parameters.h:207-210,
+   * montgomery.cc:494-498) */
+  p->n_inv = mont_pow(p, mont_import(p, (uint64_t)n), q - 2);
+
+  /* PrimitiveNthRootOfUnity(log_n + 1) (ntt_parameters.h:41-71): first t >= 2
+   * with (t^k)^{n} != 1 where k = (q-1)/2n. */
+  uint64_t k = (q - 1) / two_n;
+  uint64_t one = p->r_mod_q;
+  uint64_t psi_m = 0;
+  for (uint64_t t = 2; t < q; t++) {
+    uint64_t cand = mont_pow(p, mont_import(p, t), k);
+    if (mont_pow(p, cand, (uint64_t)n) != one) { psi_m = cand; break; }
+  }
+  p->psi = mont_export(p, psi_m);
+
+  p->bitrevs = (uint32_t*)malloc(sizeof(uint32_t) * n);
+  for (int i = 0; i < n; i++) p->bitrevs[i] = bitrev((uint32_t)i, log_n);
+
+  /* NttPsis: row[i] = psi^i (ntt_parameters.h:79-92). */
+  uint64_t* row = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < n; i++) row[i] = mont_pow(p, psi_m, (uint64_t)i);
+  /* NttPsisBitrev (ntt_parameters.h:117-127). */
+  p->psis_bitrev = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < n; i++) p->psis_bitrev[i] = row[p->bitrevs[i]];
+  /* NttPsisInvBitrev (ntt_parameters.h:131-157): reverse row[1..n-1],
+   * bit-reverse, then multiply row[0] by psi^{-1} = -row[1] and the others by
+   * row[1] (= -psi^{-1}). */
+  uint64_t* rev = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  rev[0] = row[0];
+  for (int i = 1; i < n; i++) rev[i] = row[n - i];
+  uint64_t psi_inv = mont_neg(p, rev[1 % n]);
+  uint64_t neg_psi_inv = rev[1 % n];
+  if (n == 1) { psi_inv = 0; neg_psi_inv = 0; }
+  p->psis_inv_bitrev = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < n; i++) p->psis_inv_bitrev[i] = rev[p->bitrevs[i]];
+  p->psis_inv_bitrev[0] = mont_mul(p, p->psis_inv_bitrev[0], psi_inv);
+  for (int i = 1; i < n; i++)
+    p->psis_inv_bitrev[i] = mont_mul(p, p->psis_inv_bitrev[i], neg_psi_inv);
+  free(rev);
+  free(row);
+
+  p->psis_bitrev_c = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  p->psis_bitrev_cb = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  p->psis_inv_bitrev_c = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  p->psis_inv_bitrev_cb = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < n; i++) {
+    get_constant(p, p->psis_bitrev[i], &p->psis_bitrev_c[i],
+                 &p->psis_bitrev_cb[i]);
+    get_constant(p, p->psis_inv_bitrev[i], &p->psis_inv_bitrev_c[i],
+                 &p->psis_inv_bitrev_cb[i]);
+  }
+  return p;
+}
+
+void so_prime_destroy(so_prime* p) {
+  if (!p) return;
+  free(p->psis_bitrev); free(p->psis_bitrev_c); free(p->psis_bitrev_cb);
+  free(p->psis_inv_bitrev); free(p->psis_inv_bitrev_c);
+  free(p->psis_inv_bitrev_cb); free(p->bitrevs);
+  free(p);
+}
+
+void so_prime_info(const so_prime* p, uint64_t out[10]) {
+  out[0] = p->q; out[1] = (uint64_t)p->log_q; out[2] = p->inv_modulus;
+  out[3] = p->r_mod_q; out[4] = p->r_mod_q_barrett; out[5] = p->inv_r;
+  out[6] = p->inv_r_barrett; out[7] = p->barrett_num; out[8] = p->psi;
+  out[9] = p->n_inv;
+}
+
+void so_prime_tables(const so_prime* p, uint64_t* fwd, uint64_t* inv) {
+  memcpy(fwd, p->psis_bitrev, sizeof(uint64_t) * p->n);
+  memcpy(inv, p->psis_inv_bitrev, sizeof(uint64_t) * p->n);
+}
+
+void so_import(const so_prime* p, const uint64_t* in, uint64_t* out,
+               size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_import(p, in[i]);
+}
+void so_export(const so_prime* p, const uint64_t* in, uint64_t* out,
+               size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_export(p, in[i]);
+}
+void so_add(const so_prime* p, const uint64_t* a, const uint64_t* b,
+            uint64_t* out, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_add(p, a[i], b[i]);
+}
+void so_sub(const so_prime* p, const uint64_t* a, const uint64_t* b,
+            uint64_t* out, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_sub(p, a[i], b[i]);
+}
+void so_neg(const so_prime* p, const uint64_t* a, uint64_t* out, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_neg(p, a[i]);
+}
+void so_mul(const so_prime* p, const uint64_t* a, const uint64_t* b,
+            uint64_t* out, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_mul(p, a[i], b[i]);
+}
+void so_fma(const so_prime* p, uint64_t* acc, const uint64_t* a,
+            const uint64_t* b, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) acc[i] = mont_fma(p, acc[i], a[i], b[i]);
+}
+void so_mul_scalar(const so_prime* p, const uint64_t* a, uint64_t s,
+                   uint64_t* out, size_t cnt) {
+  for (size_t i = 0; i < cnt; i++) out[i] = mont_mul(p, a[i], s);
+}
+
+/* ---------------------------------------------------------------------------
+ * NTT (dft_transformations.h)
+ * ------------------------------------------------------------------------- */
+
+/* IterativeCooleyTukey (dft_transformations.h:59-100). */
+void so_ntt_fwd(const so_prime* p, uint64_t* a) {
+  int index_psi = 1;
+  const int n = p->n;
+  for (int i = p->log_n - 1; i >= 0; i--) {
+    const int half_m = 1 << i;
+    const int m = half_m << 1;
+    for (int k = 0; k < n; k += m) {
+      const uint64_t c = p->psis_bitrev_c[index_psi];
+      const uint64_t cb = p->psis_bitrev_cb[index_psi];
+      for (int j = 0; j < half_m; j++) {
+        uint64_t t = mul_const(p, a[k + j + half_m], c, cb);
+        uint64_t u = a[k + j];
+        if (i & 1) {  /* lazy layer: LazyAdd / LazySub */
+          a[k + j] = a[k + j] + t;
+          a[k + j + half_m] = u + (p->q - t);
+        } else {
+          a[k + j] = mont_add(p, a[k + j], t);
+          a[k + j + half_m] = mont_sub(p, u, t);
+        }
+      }
+      index_psi++;
+    }
+  }
+}
+
+/* IterativeGentlemanSande + normalisation (dft_transformations.h:118-153,
+ * 181-201). */
+void so_ntt_inv(const so_prime* p, uint64_t* a) {
+  int index_psi_inv = 0;
+  const int n = p->n;
+  for (int i = 0; i < p->log_n; i++) {
+    const int half_m = 1 << i;
+    const int m = half_m << 1;
+    for (int k = 0; k < n; k += m) {
+      const uint64_t c = p->psis_inv_bitrev_c[index_psi_inv];
+      const uint64_t cb = p->psis_inv_bitrev_cb[index_psi_inv];
+      for (int j = 0; j < half_m; j++) {
+        uint64_t t = a[k + j + half_m];
+        uint64_t u = a[k + j];
+        a[k + j] = mont_add(p, a[k + j], t);
+        a[k + j + half_m] = mul_const(p, u + (p->q - t), c, cb);
+      }
+      index_psi_inv++;
+    }
+  }
+  for (int i = 0; i < n; i++) a[i] = mont_mul(p, a[i], p->n_inv);
+}
+
+/* Polynomial::Substitute (polynomial.h:226-260) and
+ * RnsPolynomial::Substitute (rns/rns_polynomial.cc:209-260). */
+int so_substitute(const so_prime* p, int power, const uint64_t* in,
+                  uint64_t* out) {
+  const int n = p->n;
+  if (power < 0 || (power % 2) == 0 || power >= 2 * n) return 3;
+  int psi_power_index = (power - 1) / 2;
+  for (int j = 0; j < n; j++) {
+    out[p->bitrevs[j]] = in[p->bitrevs[psi_power_index]];
+    psi_power_index = (psi_power_index + power) % n;
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * RNS context (rns/rns_context.cc)
+ * ------------------------------------------------------------------------- */
+
+so_rns* so_rns_create(int log_n, const uint64_t* qs, int num_qs) {
+  so_rns* r = (so_rns*)calloc(1, sizeof(so_rns));
+  r->log_n = log_n;
+  r->L = num_qs;
+  r->primes = (so_prime**)calloc(num_qs, sizeof(so_prime*));
+  for (int i = 0; i < num_qs; i++) {
+    r->primes[i] = so_prime_create(qs[i], log_n);
+    if (!r->primes[i]) { so_rns_destroy(r); return NULL; }
+  }
+  /* GenerateCrtConstantsForMainModulus (rns/rns_context.cc:169-200). */
+  r->q_invs = (uint64_t*)calloc((size_t)num_qs * num_qs, sizeof(uint64_t));
+  r->q_mods = (uint64_t*)calloc((size_t)num_qs * num_qs, sizeof(uint64_t));
+  for (int i = 0; i < num_qs; i++) {
+    for (int j = 0; j < num_qs; j++) {
+      const so_prime* pj = r->primes[j];
+      if (i == j) {
+        r->q_mods[i * num_qs + j] = 0;
+        r->q_invs[i * num_qs + j] = pj->r_mod_q;
+      } else {
+        uint64_t qi_mod_qj = mont_import(pj, qs[i]);
+        r->q_mods[i * num_qs + j] = qi_mod_qj;
+        r->q_invs[i * num_qs + j] = mont_pow(pj, qi_mod_qj, pj->q - 2);
+      }
+    }
+  }
+  return r;
+}
+
+void so_rns_destroy(so_rns* r) {
+  if (!r) return;
+  for (int i = 0; i < r->L; i++) so_prime_destroy(r->primes[i]);
+  free(r->primes); free(r->q_invs); free(r->q_mods);
+  free(r);
+}
+
+const so_prime* so_rns_prime(const so_rns* r, int i) { return r->primes[i]; }
+
+/* MainPrimeModulusInverseResidues()[level].Prefix(level)
+ * (rns/rns_context.h:145-147, rns/rns_integer.h:37-40). */
+void so_rns_ql_inv(const so_rns* r, int level, uint64_t* out) {
+  for (int j = 0; j < level; j++) out[j] = r->q_invs[level * r->L + j];
+}
+
+/* MainPrimeModulusComplements / MainPrimeModulusCrtFactors
+ * (rns/rns_context.cc:234-282). */
+void so_rns_complements(const so_rns* r, int level, uint64_t* q_hats,
+                        uint64_t* q_hat_invs) {
+  for (int i = 0; i <= level; i++) {
+    const so_prime* pi = r->primes[i];
+    uint64_t h = pi->r_mod_q, hi = pi->r_mod_q;
+    for (int j = 0; j <= level; j++) {
+      if (j == i) continue;
+      h = mont_mul(pi, h, r->q_mods[j * r->L + i]);
+      hi = mont_mul(pi, hi, r->q_invs[j * r->L + i]);
+    }
+    q_hats[i] = h;
+    q_hat_invs[i] = hi;
+  }
+}
+
+/* GadgetSize (gadget.h:43-47). */
+static int gadget_size(const so_prime* p, int log_b) {
+  return (p->log_q + (log_b - 1)) / log_b;
+}
+
+int so_rns_gadget_dim(const so_rns* r, int L, const int* log_bs) {
+  int k = 0;
+  for (int i = 0; i < L; i++) k += gadget_size(r->primes[i], log_bs[i]);
+  return k;
+}
+
+/* RnsGadget::Create (rns/rns_gadget.cc:42-102), with q_hats / q_hat_invs at
+ * level L-1. */
+void so_rns_gadget_vector(const so_rns* r, int L, const int* log_bs,
+                          uint64_t* g) {
+  uint64_t* qh = (uint64_t*)malloc(sizeof(uint64_t) * L);
+  uint64_t* qhi = (uint64_t*)malloc(sizeof(uint64_t) * L);
+  so_rns_complements(r, L - 1, qh, qhi);
+  int row = 0;
+  for (int i = 0; i < L; i++) {
+    const so_prime* pi = r->primes[i];
+    uint64_t bi = mont_import(pi, (uint64_t)1 << log_bs[i]);
+    uint64_t cur = mont_mul(pi, qh[i], qhi[i]);
+    int ki = gadget_size(pi, log_bs[i]);
+    for (int j = 0; j < ki; j++) {
+      for (int l = 0; l < L; l++) g[(size_t)row * L + l] = (l == i) ? cur : 0;
+      row++;
+      cur = mont_mul(pi, cur, bi);
+    }
+  }
+  free(qh);
+  free(qhi);
+}
+
+void so_rns_ntt_fwd(const so_rns* r, uint64_t* poly, int L) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int i = 0; i < L; i++) so_ntt_fwd(r->primes[i], poly + i * n);
+}
+
+void so_rns_ntt_inv(const so_rns* r, uint64_t* poly, int L) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int i = 0; i < L; i++) so_ntt_inv(r->primes[i], poly + i * n);
+}
+
+int so_rns_substitute(const so_rns* r, int L, int power, const uint64_t* in,
+                      uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int i = 0; i < L; i++) {
+    int st = so_substitute(r->primes[i], power, in + i * n, out + i * n);
+    if (st) return st;
+  }
+  return 0;
+}
+
+/* ConvertModulusBalanced of one exported value x (modulus_conversion.h:30-83):
+ * x > floor(q/2) denotes x - q.  Returns the Montgomery rep mod p. */
+static inline uint64_t convert_balanced(const so_prime* from,
+                                        const so_prime* to, uint64_t x) {
+  if (from->q == to->q) return mont_import(to, x);
+  uint64_t xp = mont_import(to, x);
+  if (x > (from->q >> 1)) {
+    if (to->q > from->q) {
+      uint64_t diff = mont_import(to, to->q - from->q);
+      xp = mont_add(to, xp, diff);
+    } else {
+      uint64_t diff = mont_import(to, from->q - to->q);
+      xp = mont_sub(to, xp, diff);
+    }
+  }
+  return xp;
+}
+
+/* RnsGadget::Decompose (rns/rns_gadget.cc:108-153) with BaseDecompose
+ * (gadget.h:52-79): digits LSB first, each lifted (balanced) to every limb. */
+void so_rns_decompose(const so_rns* r, int L, const int* log_bs,
+                      const uint64_t* a, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  int row = 0;
+  uint64_t* x = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < L; i++) {
+    const so_prime* pi = r->primes[i];
+    int ki = gadget_size(pi, log_bs[i]);
+    uint64_t mask = ((uint64_t)1 << log_bs[i]) - 1;
+    for (size_t c = 0; c < n; c++) x[c] = mont_export(pi, a[i * n + c]);
+    for (int d = 0; d < ki; d++) {
+      uint64_t* dst = out + (size_t)row * L * n;
+      for (size_t c = 0; c < n; c++) {
+        uint64_t digit_m = mont_import(pi, x[c] & mask);
+        uint64_t digit = mont_export(pi, digit_m);
+        for (int l = 0; l < L; l++) {
+          dst[l * n + c] =
+              (l == i) ? digit_m : convert_balanced(pi, r->primes[l], digit);
+        }
+        x[c] >>= log_bs[i];
+      }
+      row++;
+    }
+  }
+  free(x);
+}
+
+/* RnsRlweCiphertext::Mul (rns/rns_ciphertext.h:501-524) for 2x2 components. */
+void so_rns_tensor(const so_rns* r, int L, const uint64_t* a, const uint64_t* b,
+                   uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  const size_t P = (size_t)L * n;
+  memset(out, 0, sizeof(uint64_t) * 3 * P);
+  for (int i = 0; i < 2; i++) {
+    for (int j = 0; j < 2; j++) {
+      for (int l = 0; l < L; l++) {
+        so_fma(r->primes[l], out + (i + j) * P + l * n, a + i * P + l * n,
+               b + j * P + l * n, n);
+      }
+    }
+  }
+}
+
+static void rns_fma_poly(const so_rns* r, int L, uint64_t* acc,
+                         const uint64_t* a, const uint64_t* b) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int l = 0; l < L; l++)
+    so_fma(r->primes[l], acc + l * n, a + l * n, b + l * n, n);
+}
+
+/* Key-switch core shared by relinearization and Galois keys:
+ * acc0 += sum_j NTT(g^{-1}(c))_j * key_b[j], acc1 += ... * key_a[j]. */
+static void rns_keyswitch_accumulate(const so_rns* r, int L, const int* log_bs,
+                                     const uint64_t* c_ntt,
+                                     const uint64_t* key_b,
+                                     const uint64_t* key_a, uint64_t* acc0,
+                                     uint64_t* acc1) {
+  const size_t n = (size_t)1 << r->log_n;
+  const size_t P = (size_t)L * n;
+  int k = so_rns_gadget_dim(r, L, log_bs);
+  uint64_t* coeff = (uint64_t*)malloc(sizeof(uint64_t) * P);
+  memcpy(coeff, c_ntt, sizeof(uint64_t) * P);
+  so_rns_ntt_inv(r, coeff, L);  /* ConvertToCoeffForm */
+  uint64_t* digits = (uint64_t*)malloc(sizeof(uint64_t) * P * k);
+  so_rns_decompose(r, L, log_bs, coeff, digits);
+  for (int j = 0; j < k; j++) {
+    uint64_t* dj = digits + (size_t)j * P;
+    so_rns_ntt_fwd(r, dj, L);
+    rns_fma_poly(r, L, acc0, dj, key_b + (size_t)j * P);
+    rns_fma_poly(r, L, acc1, dj, key_a + (size_t)j * P);
+  }
+  free(digits);
+  free(coeff);
+}
+
+/* RnsRelinKey::ApplyToRlweCiphertext for a degree-2 ciphertext
+ * (rns/rns_relinearization_key.cc:184-232); key index (i-2)*l + j = j. */
+void so_rns_relin(const so_rns* r, int L, const int* log_bs, const uint64_t* ct,
+                  const uint64_t* key_b, const uint64_t* key_a, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  const size_t P = (size_t)L * n;
+  memcpy(out, ct, sizeof(uint64_t) * 2 * P);
+  rns_keyswitch_accumulate(r, L, log_bs, ct + 2 * P, key_b, key_a, out,
+                           out + P);
+}
+
+/* RnsGaloisKey::ApplyToRlweCiphertext (rns/rns_galois_key.cc:238-287). */
+void so_rns_galois(const so_rns* r, int L, const int* log_bs,
+                   const uint64_t* ct, const uint64_t* key_b,
+                   const uint64_t* key_a, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  const size_t P = (size_t)L * n;
+  memset(out, 0, sizeof(uint64_t) * 2 * P);
+  rns_keyswitch_accumulate(r, L, log_bs, ct + P, key_b, key_a, out, out + P);
+  for (int l = 0; l < L; l++)
+    so_add(r->primes[l], out + l * n, ct + l * n, out + l * n, n);
+}
+
+/* RnsPolynomial::ModReduceLsb (rns/rns_polynomial.cc:262-344). */
+int so_rns_modreduce_lsb(const so_rns* r, int L, uint64_t t, int is_ntt,
+                         const uint64_t* in, uint64_t* out) {
+  if (L <= 1) return 3;
+  const size_t n = (size_t)1 << r->log_n;
+  const int Lr = L - 1;
+  const so_prime* pl = r->primes[L - 1];
+  uint64_t rr = pl->q % t;
+  uint64_t kk = (pl->q - rr) / t;
+  uint64_t k_mod_ql = mont_import(pl, kk);
+  uint64_t* delta = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (size_t c = 0; c < n; c++)
+    delta[c] = mont_mul(pl, in[(size_t)(L - 1) * n + c], k_mod_ql);
+  uint64_t* ql_inv = (uint64_t*)malloc(sizeof(uint64_t) * (Lr > 0 ? Lr : 1));
+  so_rns_ql_inv(r, L - 1, ql_inv);
+  /* r * a (mod Q/ql) */
+  for (int i = 0; i < Lr; i++) {
+    uint64_t r_m = mont_import(r->primes[i], rr);
+    so_mul_scalar(r->primes[i], in + i * n, r_m, out + i * n, n);
+  }
+  if (is_ntt) so_ntt_inv(pl, delta);
+  uint64_t* dq = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  for (int i = 0; i < Lr; i++) {
+    const so_prime* pi = r->primes[i];
+    for (size_t c = 0; c < n; c++)
+      dq[c] = convert_balanced(pl, pi, mont_export(pl, delta[c]));
+    if (is_ntt) so_ntt_fwd(pi, dq);
+    uint64_t t_m = mont_import(pi, t);
+    for (size_t c = 0; c < n; c++) {
+      uint64_t d = mont_mul(pi, dq[c], t_m);
+      uint64_t v = mont_add(pi, out[i * n + c], d);
+      out[i * n + c] = mont_mul(pi, v, ql_inv[i]);
+    }
+  }
+  free(dq);
+  free(ql_inv);
+  free(delta);
+  return 0;
+}
+
+typedef struct {
+  const so_rns* r;
+  int L;
+  const int* log_bs;
+  const uint64_t *a, *b, *key_b, *key_a;
+  uint64_t* out;
+  int begin, end;
+} mul_relin_job;
+
+static void* mul_relin_worker(void* arg) {
+  mul_relin_job* job = (mul_relin_job*)arg;
+  const size_t n = (size_t)1 << job->r->log_n;
+  const size_t P = (size_t)job->L * n;
+  uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * 3 * P);
+  for (int c = job->begin; c < job->end; c++) {
+    so_rns_tensor(job->r, job->L, job->a + (size_t)c * 2 * P,
+                  job->b + (size_t)c * 2 * P, tmp);
+    so_rns_relin(job->r, job->L, job->log_bs, tmp, job->key_b, job->key_a,
+                 job->out + (size_t)c * 2 * P);
+  }
+  free(tmp);
+  return NULL;
+}
+
+void so_rns_mul_relin_batch(const so_rns* r, int L, const int* log_bs,
+                            const uint64_t* a, const uint64_t* b,
+                            const uint64_t* key_b, const uint64_t* key_a,
+                            uint64_t* out, int count, int threads) {
+  if (threads < 1) threads = 1;
+  if (threads > count) threads = count > 0 ? count : 1;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * threads);
+  mul_relin_job* jobs = (mul_relin_job*)malloc(sizeof(mul_relin_job) * threads);
+  for (int t = 0; t < threads; t++) {
+    jobs[t] = (mul_relin_job){r, L, log_bs, a, b, key_b, key_a, out,
+                              (int)((long)count * t / threads),
+                              (int)((long)count * (t + 1) / threads)};
+    pthread_create(&th[t], NULL, mul_relin_worker, &jobs[t]);
+  }
+  for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+}
+
+/* ---------------------------------------------------------------------------
+ * Single-modulus key switching and oblivious expansion
+ * ------------------------------------------------------------------------- */
+
+int so_gadget_size(const so_prime* p, int log_b) { return gadget_size(p, log_b); }
+
+/* RelinearizationKeyPart::ApplyPartTo + MatrixMultiply
+ * (relinearization_key.cc:76-96, 143-162); BaseDecompose (gadget.h:52-79)
+ * imports the digits into the same modulus. */
+void so_keyswitch_part(const so_prime* p, int log_b, int dim, const uint64_t* c,
+                       const uint64_t* k0, const uint64_t* k1, uint64_t* out0,
+                       uint64_t* out1) {
+  const size_t n = (size_t)p->n;
+  uint64_t* x = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  uint64_t* d = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  memcpy(x, c, sizeof(uint64_t) * n);
+  so_ntt_inv(p, x);
+  for (size_t i = 0; i < n; i++) x[i] = mont_export(p, x[i]);
+  uint64_t mask = ((uint64_t)1 << log_b) - 1;
+  memset(out0, 0, sizeof(uint64_t) * n);
+  memset(out1, 0, sizeof(uint64_t) * n);
+  for (int j = 0; j < dim; j++) {
+    for (size_t i = 0; i < n; i++) {
+      d[i] = mont_import(p, x[i] & mask);
+      x[i] >>= log_b;
+    }
+    so_ntt_fwd(p, d);
+    so_fma(p, out0, d, k0 + (size_t)j * n, n);
+    so_fma(p, out1, d, k1 + (size_t)j * n, n);
+  }
+  free(d);
+  free(x);
+}
+
+/* RelinearizationKey::ApplyTo for a Galois key (num_parts 2, target s)
+ * (relinearization_key.cc:288-344): part(c1) + (c0, 0). */
+void so_galois_apply(const so_prime* p, int log_b, int dim, const uint64_t* ct,
+                     const uint64_t* k0, const uint64_t* k1, uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  so_keyswitch_part(p, log_b, dim, ct + n, k0, k1, out, out + n);
+  so_add(p, out, ct, out, n);
+}
+
+/* ObliviousExpander::ExpandCiphertext with GaloisKeysObliviousExpander's
+ * SubstitutionWithKeys (oblivious_expand.h:173-227, 273-282). */
+int so_oblivious_expand(const so_prime* p, int levels, int log_b,
+                        const uint64_t* keys, const uint64_t* ct,
+                        uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  const int dim = gadget_size(p, log_b);
+  const size_t key_sz = (size_t)2 * dim * n;
+  if (levels < 0 || levels >= 32) return 3;
+  if ((n >> levels) == 0) return 3;
+  memcpy(out, ct, sizeof(uint64_t) * 2 * n);
+  uint64_t* monomial = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  uint64_t* sub = (uint64_t*)malloc(sizeof(uint64_t) * 2 * n);
+  uint64_t* ks = (uint64_t*)malloc(sizeof(uint64_t) * 2 * n);
+  for (int j = 0; j < levels; j++) {
+    memset(monomial, 0, sizeof(uint64_t) * n);
+    monomial[n - ((size_t)1 << j)] = mont_neg(p, p->r_mod_q);  /* -x^{N-2^j} */
+    so_ntt_fwd(p, monomial);
+    int power = (int)(n >> j) + 1;
+    const uint64_t* key = keys + (size_t)j * key_sz;
+    for (int k = 0; k < (1 << j); k++) {
+      uint64_t* c = out + (size_t)k * 2 * n;
+      uint64_t* c_hi = out + ((size_t)k + ((size_t)1 << j)) * 2 * n;
+      so_substitute(p, power, c, sub);
+      so_substitute(p, power, c + n, sub + n);
+      so_galois_apply(p, log_b, dim, sub, key, key + (size_t)dim * n, ks);
+      /* result[k + 2^j] = (c - sub) * monomial */
+      for (int comp = 0; comp < 2; comp++) {
+        so_sub(p, c + comp * n, ks + comp * n, c_hi + comp * n, n);
+        so_mul(p, c_hi + comp * n, monomial, c_hi + comp * n, n);
+      }
+      /* result[k] += sub */
+      so_add(p, c, ks, c, 2 * n);
+    }
+  }
+  free(ks);
+  free(sub);
+  free(monomial);
+  return 0;
+}
+
+/* SymmetricRlweCiphertext::FusedAbsorbAddInPlace chain
+ * (symmetric_encryption.h:250-275). */
+void so_absorb_sum(const so_prime* p, int count, const uint64_t* cts,
+                   const uint64_t* db, uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  memset(out, 0, sizeof(uint64_t) * 2 * n);
+  for (int i = 0; i < count; i++) {
+    const uint64_t* c = cts + (size_t)i * 2 * n;
+    so_fma(p, out, c, db + (size_t)i * n, n);
+    so_fma(p, out + n, c + n, db + (size_t)i * n, n);
+  }
+}
+
+/* ObliviousExpander::ComputeNormalizer (oblivious_expand.h:143-157). */
+uint64_t so_compute_normalizer(int k, int log_t) {
+  int log_t_minus_r = log_t - (k % log_t);
+  int pp = k / log_t;
+  if (pp % 2 == 0)
+    return (((uint64_t)1 << log_t) + 1) - ((uint64_t)1 << log_t_minus_r);
+  return (uint64_t)1 << log_t_minus_r;
+}

@@ -1,0 +1,983 @@
+// C ABI of the GB300 RLWE hot path: host-side validation (mirroring the
+// reference's absl::Status checks), parameter derivation and kernel
+// orchestration.  No CPU fallback: every operation runs on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/shell_gpu.h"
+#include "../../include/shell_gpu_runtime.h"
+#include "kernels.cuh"
+
+using shg::CtMap;
+using shg::CtxDev;
+using shg::DigitDesc;
+using shg::PrimeDev;
+using shg::ScalarPack;
+using shg::Tw;
+typedef unsigned __int128 u128;
+
+namespace {
+
+thread_local std::string t_last_error;
+
+int fail(int code, const std::string& msg) {
+  t_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(SHG_INTERNAL, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SHG_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);  \
+  } while (0)
+
+// ---- host modular arithmetic (parameter setup only) -----------------------
+uint64_t mulmod(uint64_t a, uint64_t b, uint64_t q) {
+  return (uint64_t)(((u128)a * b) % q);
+}
+uint64_t powmod(uint64_t b, uint64_t e, uint64_t q) {
+  uint64_t r = 1 % q;
+  b %= q;
+  while (e) {
+    if (e & 1) r = mulmod(r, b, q);
+    b = mulmod(b, b, q);
+    e >>= 1;
+  }
+  return r;
+}
+uint64_t to_mont(uint64_t x, uint64_t q) {
+  return (uint64_t)(((u128)(x % q) << 64) % q);
+}
+uint64_t from_mont(uint64_t xm, uint64_t q, uint64_t inv_r) {
+  return mulmod(xm, inv_r, q);
+}
+uint64_t shoup_of(uint64_t w, uint64_t q) {
+  return (uint64_t)(((u128)w << 64) / q);
+}
+int bit_length(uint64_t x) {
+  int b = 0;
+  while (x) {
+    ++b;
+    x >>= 1;
+  }
+  return b;
+}
+uint32_t bitrev(uint32_t x, int bits) {
+  uint32_t r = 0;
+  for (int i = 0; i < bits; ++i) {
+    r = (r << 1) | (x & 1);
+    x >>= 1;
+  }
+  return r;
+}
+
+// Everything the host keeps about one prime at the context's ring degree.
+struct HostPrime {
+  uint64_t q = 0;
+  int log_q = 0;
+  uint64_t inv_modulus = 0, r_mod_q = 0, r_mod_q_barrett = 0, inv_r = 0,
+           inv_r_barrett = 0, barrett_num = 0;
+  uint64_t psi = 0;      // plain
+  uint64_t n_inv = 0;    // plain
+  std::vector<uint64_t> fwd, inv;  // plain twiddles (psi^{brv i}, psi^{-(brv i + 1)})
+};
+
+// Validations of MontgomeryIntParams::Create (montgomery.cc:44-59) and
+// InitializeNttParameters (ntt_parameters.h:183-203).
+int make_prime(uint64_t q, int log_n, HostPrime* hp) {
+  if ((q >> 62) != 0)
+    return fail(SHG_INVALID_ARGUMENT, "The modulus should be less than 2^62.");
+  if ((q & 1) == 0) return fail(SHG_INVALID_ARGUMENT, "The modulus should be odd.");
+  const uint64_t two_n = (uint64_t)1 << (log_n + 1);
+  if (q % two_n != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "modulus is not 1 mod 2n for logn, " + std::to_string(log_n));
+  const int n = 1 << log_n;
+  hp->q = q;
+  hp->log_q = bit_length(q);
+  const u128 R = (u128)1 << 64;
+  hp->r_mod_q = (uint64_t)(R % q);
+  hp->inv_r = powmod(hp->r_mod_q, q - 2, q);  // R^{-1} (q prime)
+  // inv_modulus = -q^{-1} mod 2^64 via Newton iteration.
+  uint64_t inv = q;
+  for (int i = 0; i < 6; ++i) inv *= 2 - q * inv;
+  hp->inv_modulus = (uint64_t)0 - inv;
+  hp->r_mod_q_barrett = shoup_of(hp->r_mod_q, q);
+  hp->inv_r_barrett = shoup_of(hp->inv_r, q);
+  hp->barrett_num = (uint64_t)(R / q);
+  // n^{-1} = n^{q-2} as MultiplicativeInverse does (montgomery.cc:494-498).
+  hp->n_inv = powmod((uint64_t)n, q - 2, q);
+  // psi: the first t >= 2 whose t^{(q-1)/2n} has order exactly 2n
+  // (PrimitiveNthRootOfUnity, ntt_parameters.h:41-71).
+  const uint64_t k = (q - 1) / two_n;
+  uint64_t psi = 0;
+  for (uint64_t t = 2; t < q; ++t) {
+    uint64_t cand = powmod(t, k, q);
+    if (powmod(cand, (uint64_t)n, q) != 1) {
+      psi = cand;
+      break;
+    }
+  }
+  if (psi == 0)
+    return fail(SHG_INTERNAL, "Loop in PrimitiveNthRootOfUnity terminated.");
+  hp->psi = psi;
+  const uint64_t psi_inv = powmod(psi, q - 2, q);
+  std::vector<uint64_t> pw(n + 1), pwi(n + 1);
+  pw[0] = 1;
+  pwi[0] = 1;
+  for (int e = 1; e <= n; ++e) {
+    pw[e] = mulmod(pw[e - 1], psi, q);
+    pwi[e] = mulmod(pwi[e - 1], psi_inv, q);
+  }
+  hp->fwd.resize(n);
+  hp->inv.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const uint32_t b = bitrev((uint32_t)i, log_n);
+    hp->fwd[i] = pw[b];        // psis_bitrev[i]
+    hp->inv[i] = pwi[b + 1];   // psis_inv_bitrev[i] (ntt_parameters.h:131-157)
+  }
+  return SHG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Context and key objects
+// ---------------------------------------------------------------------------
+
+struct shg_context {
+  int log_n = 0, n = 0, L = 0;
+  uint64_t t = 0;
+  int device = 0;
+  std::vector<HostPrime> hp;
+  PrimeDev* d_primes = nullptr;
+  Tw* d_tw_fwd = nullptr;
+  Tw* d_tw_inv = nullptr;
+  uint64_t* d_qmod = nullptr;
+  std::vector<uint64_t> qmod;  // [L][L] q_i mod q_j
+  uint64_t* ws = nullptr;      // scratch for batched pipelines
+  size_t ws_bytes = 0;
+  int chunk_cts = 0;
+  std::mutex mu;
+
+  CtxDev dev() const {
+    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod};
+  }
+  int ensure_ws(size_t bytes) {
+    if (bytes <= ws_bytes) return SHG_OK;
+    if (ws) {
+      SHG_CUDA(cudaDeviceSynchronize());
+      cudaFree(ws);
+      ws = nullptr;
+      ws_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ws, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(SHG_RESOURCE_EXHAUSTED,
+                  "cannot reserve " + std::to_string(bytes) +
+                      " bytes of device scratch: " + cudaGetErrorString(e));
+    }
+    ws_bytes = bytes;
+    return SHG_OK;
+  }
+};
+
+struct shg_key {
+  shg_context* ctx = nullptr;
+  int L = 0, k = 0, power = 1;
+  std::vector<int> log_bs;
+  DigitDesc* d_digits = nullptr;
+  uint64_t* kb = nullptr;  // [k][L][n], premultiplied by 2^64 mod q
+  uint64_t* ka = nullptr;
+  int need_lift = 0;
+  int chunk = 1;
+  size_t bytes = 0;
+};
+
+namespace {
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+int check_ptrs(std::initializer_list<const void*> ps) {
+  for (const void* p : ps) {
+    if (p == nullptr) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+    if (!aligned16(p))
+      return fail(SHG_INVALID_ARGUMENT, "buffers must be 16-byte aligned");
+  }
+  return SHG_OK;
+}
+
+int check_limbs(const shg_context* ctx, int count, int num_limbs) {
+  if (ctx == nullptr) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (num_limbs <= 0 || num_limbs > ctx->L)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`moduli` must contain " + std::to_string(num_limbs) +
+                    " RNS moduli.");
+  return SHG_OK;
+}
+
+int launch_status(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return SHG_OK;
+}
+
+// Cts per pipeline chunk, bounded by the scratch budget.
+int chunk_for(shg_context* ctx, size_t per_ct_bytes, int count) {
+  int c = ctx->chunk_cts > 0 ? ctx->chunk_cts : 16;
+  const size_t budget = (size_t)1 << 30;  // 1 GiB default scratch ceiling
+  const size_t cap = std::max<size_t>(1, budget / std::max<size_t>(per_ct_bytes, 1));
+  if ((size_t)c > cap) c = (int)cap;
+  if (c > count) c = count;
+  return std::max(c, 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* shg_last_error(void) { return t_last_error.c_str(); }
+
+int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
+                       uint64_t plaintext_modulus, shg_context** out) {
+  if (out == nullptr) return fail(SHG_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  if (plaintext_modulus == 0)
+    return fail(SHG_INVALID_ARGUMENT, "`plaintext_modulus` must be positive.");
+  if (log_n <= 0) return fail(SHG_INVALID_ARGUMENT, "`log_n` must be positive.");
+  if (log_n > 15)
+    return fail(SHG_INVALID_ARGUMENT,
+                "log_n, " + std::to_string(log_n) + ", must be less than 15.");
+  if (log_n > 14)
+    return fail(SHG_INVALID_ARGUMENT,
+                "log_n = 15 is not supported by this build of the GPU library");
+  if (qs == nullptr || num_qs <= 0 || num_qs > shg::kMaxLimbs)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`qs` must hold between 1 and " + std::to_string(shg::kMaxLimbs) +
+                    " prime moduli");
+  shg_context* ctx = new shg_context();
+  ctx->log_n = log_n;
+  ctx->n = 1 << log_n;
+  ctx->L = num_qs;
+  ctx->t = plaintext_modulus;
+  cudaGetDevice(&ctx->device);
+  ctx->hp.resize(num_qs);
+  for (int i = 0; i < num_qs; ++i) {
+    int st = make_prime(qs[i], log_n, &ctx->hp[i]);
+    if (st != SHG_OK) {
+      delete ctx;
+      return st;
+    }
+  }
+  const int n = ctx->n, L = num_qs;
+  std::vector<PrimeDev> pd(L);
+  std::vector<Tw> twf((size_t)L * n), twi((size_t)L * n);
+  for (int i = 0; i < L; ++i) {
+    const HostPrime& h = ctx->hp[i];
+    PrimeDev& d = pd[i];
+    memset(&d, 0, sizeof(d));
+    d.q = h.q;
+    d.two_q = 2 * h.q;
+    d.inv_modulus = h.inv_modulus;
+    d.r_mod_q = h.r_mod_q;
+    d.r_mod_q_shoup = shoup_of(h.r_mod_q, h.q);
+    d.inv_r = h.inv_r;
+    d.inv_r_shoup = shoup_of(h.inv_r, h.q);
+    d.n_inv = h.n_inv;
+    d.n_inv_shoup = shoup_of(h.n_inv, h.q);
+    d.n_inv_r = mulmod(h.n_inv, h.inv_r, h.q);
+    d.n_inv_r_shoup = shoup_of(d.n_inv_r, h.q);
+    d.half_q = h.q >> 1;
+    d.log_q = (uint64_t)h.log_q;
+    d.barrett = h.barrett_num;
+    for (int j = 0; j < n; ++j) {
+      twf[(size_t)i * n + j] = Tw{h.fwd[j], shoup_of(h.fwd[j], h.q)};
+      twi[(size_t)i * n + j] = Tw{h.inv[j], shoup_of(h.inv[j], h.q)};
+    }
+  }
+  ctx->qmod.resize((size_t)L * L);
+  for (int i = 0; i < L; ++i)
+    for (int j = 0; j < L; ++j) ctx->qmod[(size_t)i * L + j] = qs[i] % qs[j];
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_primes, sizeof(PrimeDev) * L);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_fwd, sizeof(Tw) * L * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_inv, sizeof(Tw) * L * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_qmod, sizeof(uint64_t) * L * L);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ctx->d_primes, pd.data(), sizeof(PrimeDev) * L,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ctx->d_tw_fwd, twf.data(), sizeof(Tw) * L * n,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ctx->d_tw_inv, twi.data(), sizeof(Tw) * L * n,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ctx->d_qmod, ctx->qmod.data(), sizeof(uint64_t) * L * L,
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    shg_context_destroy(ctx);
+    return cuda_fail(e, "context upload");
+  }
+  *out = ctx;
+  return SHG_OK;
+}
+
+void shg_context_destroy(shg_context* ctx) {
+  if (!ctx) return;
+  cudaFree(ctx->d_primes);
+  cudaFree(ctx->d_tw_fwd);
+  cudaFree(ctx->d_tw_inv);
+  cudaFree(ctx->d_qmod);
+  cudaFree(ctx->ws);
+  delete ctx;
+}
+
+int shg_context_log_n(const shg_context* ctx) { return ctx ? ctx->log_n : -1; }
+int shg_context_num_moduli(const shg_context* ctx) { return ctx ? ctx->L : -1; }
+
+int shg_context_prime_info(const shg_context* ctx, int i, uint64_t out[10]) {
+  if (!ctx || i < 0 || i >= ctx->L || !out)
+    return fail(SHG_INVALID_ARGUMENT, "bad prime index");
+  const HostPrime& h = ctx->hp[i];
+  out[0] = h.q;
+  out[1] = (uint64_t)h.log_q;
+  out[2] = h.inv_modulus;
+  out[3] = h.r_mod_q;
+  out[4] = h.r_mod_q_barrett;
+  out[5] = h.inv_r;
+  out[6] = h.inv_r_barrett;
+  out[7] = h.barrett_num;
+  out[8] = h.psi;
+  out[9] = to_mont(h.n_inv, h.q);
+  return SHG_OK;
+}
+
+int shg_context_ntt_tables(const shg_context* ctx, int i, uint64_t* fwd,
+                           uint64_t* inv) {
+  if (!ctx || i < 0 || i >= ctx->L || !fwd || !inv)
+    return fail(SHG_INVALID_ARGUMENT, "bad prime index");
+  const HostPrime& h = ctx->hp[i];
+  for (int j = 0; j < ctx->n; ++j) {
+    fwd[j] = to_mont(h.fwd[j], h.q);
+    inv[j] = to_mont(h.inv[j], h.q);
+  }
+  return SHG_OK;
+}
+
+int shg_context_ql_inv(const shg_context* ctx, int level, uint64_t* out) {
+  if (!ctx || level < 0 || level >= ctx->L || (!out && level > 0))
+    return fail(SHG_INVALID_ARGUMENT,
+                "`level` must be non-negative and at most " +
+                    std::to_string(ctx ? ctx->L - 1 : 0));
+  const uint64_t ql = ctx->hp[level].q;
+  for (int j = 0; j < level; ++j) {
+    const uint64_t qj = ctx->hp[j].q;
+    out[j] = to_mont(powmod(ql % qj, qj - 2, qj), qj);
+  }
+  return SHG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Polynomial operations
+// ---------------------------------------------------------------------------
+
+int shg_ntt_forward(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                    shg_stream stream) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({polys}))) return st;
+  shg::launch_ntt_fwd(ctx->dev(), polys, polys, count * num_limbs, num_limbs,
+                      (cudaStream_t)stream);
+  return launch_status("ntt_forward");
+}
+
+int shg_ntt_inverse(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                    shg_stream stream) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({polys}))) return st;
+  shg::launch_ntt_inv(ctx->dev(), polys, polys, count * num_limbs, num_limbs, 0,
+                      (cudaStream_t)stream);
+  return launch_status("ntt_inverse");
+}
+
+static int pointwise(shg_context* ctx, shg::PwOp op, uint64_t* out,
+                     const uint64_t* a, const uint64_t* b,
+                     const ScalarPack& sc, int count, int num_limbs,
+                     shg_stream stream) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, a}))) return st;
+  if (b && (st = check_ptrs({b}))) return st;
+  shg::launch_pointwise(ctx->dev(), op, out, a, b, sc, count, num_limbs,
+                        (cudaStream_t)stream);
+  return launch_status("pointwise");
+}
+
+int shg_poly_add(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream s) {
+  if (!b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  return pointwise(ctx, shg::PW_ADD, out, a, b, ScalarPack{}, count, num_limbs, s);
+}
+int shg_poly_sub(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream s) {
+  if (!b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  return pointwise(ctx, shg::PW_SUB, out, a, b, ScalarPack{}, count, num_limbs, s);
+}
+int shg_poly_neg(shg_context* ctx, uint64_t* out, const uint64_t* a, int count,
+                 int num_limbs, shg_stream s) {
+  return pointwise(ctx, shg::PW_NEG, out, a, nullptr, ScalarPack{}, count,
+                   num_limbs, s);
+}
+int shg_poly_mul(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream s) {
+  if (!b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  return pointwise(ctx, shg::PW_MUL, out, a, b, ScalarPack{}, count, num_limbs, s);
+}
+int shg_poly_fma(shg_context* ctx, uint64_t* acc, const uint64_t* a,
+                 const uint64_t* b, int count, int num_limbs, shg_stream s) {
+  if (!b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  return pointwise(ctx, shg::PW_FMA, acc, a, b, ScalarPack{}, count, num_limbs, s);
+}
+int shg_poly_mul_rns_scalar(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                            const uint64_t* scalar_mont, int count,
+                            int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (!scalar_mont) return fail(SHG_INVALID_ARGUMENT, "null scalar array");
+  ScalarPack sc{};
+  for (int l = 0; l < num_limbs; ++l) sc.v[l] = scalar_mont[l];
+  return pointwise(ctx, shg::PW_MUL_MONT, out, a, nullptr, sc, count, num_limbs, s);
+}
+int shg_poly_mul_integer(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                         uint64_t scalar, int count, int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  ScalarPack sc{};
+  for (int l = 0; l < num_limbs; ++l) {
+    const uint64_t q = ctx->hp[l].q;
+    const uint64_t w = scalar % q;
+    sc.v[2 * l] = w;
+    sc.v[2 * l + 1] = shoup_of(w, q);
+  }
+  return pointwise(ctx, shg::PW_MUL_SHOUP, out, a, nullptr, sc, count, num_limbs, s);
+}
+
+int shg_poly_substitute(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                        int power, int count, int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (power < 0 || (power % 2) == 0 || power >= 2 * ctx->n)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Substitution power must be a non-negative odd integer less "
+                "than 2*n.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  if (out == in) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `in`");
+  shg::launch_substitute(ctx->dev(), out, in, power, count, num_limbs,
+                         (cudaStream_t)s);
+  return launch_status("substitute");
+}
+
+int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                           uint64_t t, const uint64_t* ql_inv, int is_ntt,
+                           int count, int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (num_limbs <= 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "ModReduceLsb cannot apply with only one prime modulus.");
+  if (!ql_inv)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`ql_inv` must be defined with respect to " +
+                    std::to_string(num_limbs - 1) + " moduli.");
+  if (t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  const int Lr = num_limbs - 1;
+  const HostPrime& hl = ctx->hp[Lr];
+  const uint64_t r = hl.q % t;
+  const uint64_t k = (hl.q - r) / t;
+  ScalarPack sc{};
+  for (int i = 0; i < Lr; ++i) {
+    const HostPrime& h = ctx->hp[i];
+    const uint64_t qlinv_plain = from_mont(ql_inv[i], h.q, h.inv_r);
+    // out = (in * r + delta * t) * ql^{-1}; in and out are Montgomery, delta
+    // is produced in plain form, hence c2 carries an extra 2^64.
+    const uint64_t c1 = mulmod(r % h.q, qlinv_plain, h.q);
+    const uint64_t c2 = mulmod(mulmod(t % h.q, h.r_mod_q, h.q), qlinv_plain, h.q);
+    sc.v[4 * i] = c1;
+    sc.v[4 * i + 1] = shoup_of(c1, h.q);
+    sc.v[4 * i + 2] = c2;
+    sc.v[4 * i + 3] = shoup_of(c2, h.q);
+  }
+  if (is_ntt) {
+    // Scale of the top-limb inverse NTT: k * n^{-1} * 2^-64 mod q_l.
+    const uint64_t kp = mulmod(mulmod(k % hl.q, hl.n_inv, hl.q), hl.inv_r, hl.q);
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const size_t need = (size_t)count * ctx->n * sizeof(uint64_t);
+    if ((st = ctx->ensure_ws(need))) return st;
+    shg::launch_modreduce_ntt(ctx->dev(), out, ctx->ws, in, kp,
+                              shoup_of(kp, hl.q), sc, count, num_limbs,
+                              (cudaStream_t)s);
+  } else {
+    const uint64_t kp = mulmod(k % hl.q, hl.inv_r, hl.q);
+    shg::launch_modreduce_coeff(ctx->dev(), out, in, kp, shoup_of(kp, hl.q), sc,
+                                count, num_limbs, (cudaStream_t)s);
+  }
+  return launch_status("modreduce_lsb");
+}
+
+int shg_ct_tensor(shg_context* ctx, uint64_t* out, const uint64_t* a,
+                  const uint64_t* b, int count, int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, a, b}))) return st;
+  shg::launch_tensor(ctx->dev(), out, a, b, count, num_limbs, (cudaStream_t)s);
+  return launch_status("ct_tensor");
+}
+
+// ---------------------------------------------------------------------------
+// Keys and key switching
+// ---------------------------------------------------------------------------
+
+int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
+                   int power, const uint64_t* key_b, const uint64_t* key_a,
+                   shg_key** out) {
+  if (!out) return fail(SHG_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  int st = check_limbs(ctx, 1, num_limbs);
+  if (st) return st;
+  if (!log_bs)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`log_bs` must contain " + std::to_string(num_limbs) + " elements.");
+  if (!key_b || !key_a) return fail(SHG_INVALID_ARGUMENT, "null key component");
+  if (power <= 0 || (power % 2) == 0 || power >= 2 * ctx->n)
+    return fail(SHG_INVALID_ARGUMENT,
+                "key power must be a positive odd integer less than 2*n");
+  shg_key* key = new shg_key();
+  key->ctx = ctx;
+  key->L = num_limbs;
+  key->power = power;
+  std::vector<DigitDesc> dd;
+  uint64_t qmax = 0;
+  for (int i = 0; i < num_limbs; ++i) {
+    const int b = log_bs[i];
+    const HostPrime& h = ctx->hp[i];
+    if (b <= 0 || b >= 63) {
+      delete key;
+      return fail(SHG_INVALID_ARGUMENT, "log_b must lie in [1, 62]");
+    }
+    key->log_bs.push_back(b);
+    const int dims = (h.log_q + (b - 1)) / b;  // GadgetSize (gadget.h:43-47)
+    const uint64_t mask = ((uint64_t)1 << b) - 1;
+    for (int d = 0; d < dims; ++d) dd.push_back(DigitDesc{i, d * b, mask});
+    if (mask > (h.q >> 1)) key->need_lift = 1;
+    for (int j = 0; j < num_limbs; ++j)
+      if (mask >= ctx->hp[j].q) key->need_lift = 1;
+    qmax = std::max(qmax, h.q);
+  }
+  key->k = (int)dd.size();
+  key->chunk = (int)std::max<uint64_t>(
+      1, std::min<uint64_t>((uint64_t)key->k, (~(uint64_t)0) / qmax));
+  const size_t elems = (size_t)key->k * num_limbs * ctx->n;
+  key->bytes = 2 * elems * sizeof(uint64_t) + dd.size() * sizeof(DigitDesc);
+  cudaError_t e = cudaMalloc(&key->kb, elems * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&key->ka, elems * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&key->d_digits, dd.size() * sizeof(DigitDesc));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(key->kb, key_b, elems * sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(key->ka, key_a, elems * sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(key->d_digits, dd.data(), dd.size() * sizeof(DigitDesc),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    shg_key_destroy(key);
+    return fail(SHG_RESOURCE_EXHAUSTED,
+                std::string("key upload failed: ") + cudaGetErrorString(e));
+  }
+  // Key form: multiply by 2^64 mod q so that REDC of (plain digit NTT) x
+  // (key) yields the Montgomery representation of their product.
+  ScalarPack sc{};
+  for (int l = 0; l < num_limbs; ++l) {
+    sc.v[2 * l] = ctx->hp[l].r_mod_q;
+    sc.v[2 * l + 1] = shoup_of(ctx->hp[l].r_mod_q, ctx->hp[l].q);
+  }
+  shg::launch_pointwise(ctx->dev(), shg::PW_MUL_SHOUP, key->kb, key->kb, nullptr,
+                        sc, key->k, num_limbs, 0);
+  shg::launch_pointwise(ctx->dev(), shg::PW_MUL_SHOUP, key->ka, key->ka, nullptr,
+                        sc, key->k, num_limbs, 0);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    shg_key_destroy(key);
+    return cuda_fail(e, "key conversion");
+  }
+  *out = key;
+  return SHG_OK;
+}
+
+void shg_key_destroy(shg_key* key) {
+  if (!key) return;
+  cudaFree(key->kb);
+  cudaFree(key->ka);
+  cudaFree(key->d_digits);
+  delete key;
+}
+
+int shg_key_dimension(const shg_key* key) { return key ? key->k : -1; }
+size_t shg_key_device_bytes(const shg_key* key) { return key ? key->bytes : 0; }
+
+namespace {
+
+// Shared key-switch pipeline: X = export(iNTT(component)), D = NTT(digits),
+// out = base + <D, key>.
+struct KsArgs {
+  const uint64_t* ct;  // source ciphertexts
+  int ncomp;           // components per source ciphertext
+  int comp;            // component to decompose
+  int subst_power;     // > 0: substitute first (Galois rotation)
+  int base1_zero;      // Galois: c1' has no base term
+};
+
+int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
+              const KsArgs& a, int count, cudaStream_t s) {
+  const int L = key->L, n = ctx->n, k = key->k;
+  const size_t Ln = (size_t)L * n;
+  const size_t per_ct = (Ln + (size_t)k * Ln) * sizeof(uint64_t);
+  const int C = chunk_for(ctx, per_ct, count);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int st = ctx->ensure_ws(per_ct * C);
+  if (st) return st;
+  uint64_t* X = ctx->ws;
+  uint64_t* D = X + (size_t)C * Ln;
+  const CtxDev dv = ctx->dev();
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    const uint64_t* src = a.ct + (size_t)c0 * a.ncomp * Ln;
+    shg::launch_intt_export(dv, X, src, a.ncomp, a.comp, a.subst_power,
+                            CtMap::identity(), cc, L, s);
+    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
+    shg::launch_ks_inner(dv, out + (size_t)c0 * 2 * Ln, D, key->kb, key->ka, k,
+                         key->chunk, src, (size_t)a.ncomp * Ln, CtMap::identity(),
+                         a.base1_zero, a.subst_power, cc, L, s);
+  }
+  return launch_status("keyswitch");
+}
+
+int check_key(const shg_context* ctx, const shg_key* key) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (!key) return fail(SHG_INVALID_ARGUMENT, "null key");
+  if (key->ctx != ctx)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`ciphertext` does not have a matching RNS moduli set.");
+  return SHG_OK;
+}
+
+}  // namespace
+
+int shg_relin_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
+                    const uint64_t* ct, int count, shg_stream s) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (key->power != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Relinearization key can only apply to a ciphertext of power 1.");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  return keyswitch(ctx, key, out, KsArgs{ct, 3, 2, 0, 0}, count, (cudaStream_t)s);
+}
+
+int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
+                     const uint64_t* ct, int count, shg_stream s) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  return keyswitch(ctx, key, out, KsArgs{ct, 2, 1, 0, 1}, count, (cudaStream_t)s);
+}
+
+int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,
+                   const uint64_t* ct, int count, shg_stream s) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  return keyswitch(ctx, key, out, KsArgs{ct, 2, 1, key->power, 1}, count,
+                   (cudaStream_t)s);
+}
+
+int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
+                      const uint64_t* a, const uint64_t* b, int count,
+                      shg_stream stream) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (key->power != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Relinearization key can only apply to a ciphertext of power 1.");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, a, b}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = key->L, n = ctx->n, k = key->k;
+  const size_t Ln = (size_t)L * n;
+  const size_t per_ct = (Ln + (size_t)k * Ln) * sizeof(uint64_t);
+  const int C = chunk_for(ctx, per_ct, count);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(per_ct * C))) return st;
+  uint64_t* X = ctx->ws;
+  uint64_t* D = X + (size_t)C * Ln;
+  const CtxDev dv = ctx->dev();
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    uint64_t* o = out + (size_t)c0 * 2 * Ln;
+    shg::launch_tensor_intt(dv, o, X, a + (size_t)c0 * 2 * Ln,
+                            b + (size_t)c0 * 2 * Ln, cc, L, s);
+    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
+    shg::launch_ks_inner(dv, o, D, key->kb, key->ka, k, key->chunk, o, 2 * Ln,
+                         CtMap::identity(), 0, 0, cc, L, s);
+  }
+  return launch_status("bgv_mul_relin");
+}
+
+int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
+                         int levels, uint64_t* out, const uint64_t* ct,
+                         int count, shg_stream stream) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (levels < 0 || levels >= 32)
+    return fail(SHG_INVALID_ARGUMENT,
+                "The number of levels of expansion must fall within [0, 32)");
+  if ((1 << std::min(levels, 30)) > ctx->n)
+    return fail(SHG_INVALID_ARGUMENT, "levels of expansion exceed log n");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  int st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  for (int j = 0; j < levels; ++j) {
+    if (!keys || !keys[j]) return fail(SHG_INVALID_ARGUMENT, "null Galois key");
+    if (keys[j]->ctx != ctx || keys[j]->L != 1)
+      return fail(SHG_INVALID_ARGUMENT, "Galois key does not match the context");
+    if (keys[j]->power != (ctx->n >> j) + 1)
+      return fail(SHG_INVALID_ARGUMENT,
+                  "Substitution power of the i'th GaloisKey must be (N / (2 ^ "
+                  "i)) + 1");
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = ctx->n;
+  const size_t per_query = ((size_t)2 * n) << levels;
+  // Place each query at slot 0 of its output block.
+  for (int qi = 0; qi < count; ++qi) {
+    SHG_CUDA(cudaMemcpyAsync(out + (size_t)qi * per_query, ct + (size_t)qi * 2 * n,
+                             2 * n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  }
+  if (levels == 0) return SHG_OK;
+  const int kmax = keys[0]->k;
+  // Monomials -x^{n - 2^j} in NTT form (ExpandCiphertext, oblivious_expand.h:
+  // 197-200), built on the device from a coefficient vector.
+  const size_t per_member = ((size_t)n + (size_t)kmax * n + 2 * (size_t)n) *
+                            sizeof(uint64_t);
+  const int members_max = std::max(1, count << (levels - 1));
+  const int C = std::max(1, (int)std::min<size_t>((size_t)members_max,
+                                                  ((size_t)256 << 20) / per_member));
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  const size_t mono_bytes = (size_t)levels * n * sizeof(uint64_t);
+  if ((st = ctx->ensure_ws(mono_bytes + per_member * C))) return st;
+  uint64_t* mono = ctx->ws;
+  uint64_t* X = mono + (size_t)levels * n;
+  uint64_t* D = X + (size_t)C * n;
+  uint64_t* KS = D + (size_t)C * kmax * n;
+  {
+    std::vector<uint64_t> h((size_t)levels * n, 0);
+    const HostPrime& hp = ctx->hp[0];
+    for (int j = 0; j < levels; ++j)
+      h[(size_t)j * n + (n - (1 << j))] = hp.q - hp.r_mod_q;  // -1 (Montgomery)
+    SHG_CUDA(cudaMemcpyAsync(mono, h.data(), mono_bytes, cudaMemcpyHostToDevice, s));
+    SHG_CUDA(cudaStreamSynchronize(s));
+    shg::launch_ntt_fwd(ctx->dev(), mono, mono, levels, 1, s);
+  }
+  const CtxDev dv = ctx->dev();
+  for (int j = 0; j < levels; ++j) {
+    const shg_key* key = keys[j];
+    const int power = (n >> j) + 1;
+    const CtMap map{j, levels};
+    // Members of a level are processed in chunks of whole queries.
+    const int q_per_chunk = std::max(1, C >> j);
+    for (int q0 = 0; q0 < count; q0 += q_per_chunk) {
+      const int qc = std::min(q_per_chunk, count - q0);
+      const int mc = qc << j;
+      uint64_t* blk = out + (size_t)q0 * per_query;
+      shg::launch_intt_export(dv, X, blk, 2, 1, power, map, mc, 1, s);
+      shg::launch_digit_ntt(dv, D, X, key->d_digits, key->k, key->need_lift, mc,
+                            1, s);
+      shg::launch_ks_inner(dv, KS, D, key->kb, key->ka, key->k, key->chunk, blk,
+                           2 * (size_t)n, map, 1, power, mc, 1, s);
+      shg::launch_expand_combine(dv, blk, KS, mono + (size_t)j * n, map, 1 << j,
+                                 mc, s);
+    }
+  }
+  return launch_status("oblivious_expand");
+}
+
+int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,
+                   const uint64_t* db, int num_items, int count,
+                   shg_stream stream) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (count < 0 || num_items < 0)
+    return fail(SHG_INVALID_ARGUMENT, "sizes must be non-negative");
+  if (count == 0) return SHG_OK;
+  int st = check_ptrs({out, cts, db});
+  if (st) return st;
+  const uint64_t q = ctx->hp[0].q;
+  const int chunk = (int)std::max<uint64_t>(1, std::min<uint64_t>(1u << 20, (~(uint64_t)0) / q));
+  shg::launch_absorb_sum(ctx->dev(), out, cts, db, num_items, chunk, count,
+                         (cudaStream_t)stream);
+  return launch_status("absorb_sum");
+}
+
+// ---------------------------------------------------------------------------
+// Runtime plumbing
+// ---------------------------------------------------------------------------
+
+int shg_device_count(int* count) {
+  SHG_CUDA(cudaGetDeviceCount(count));
+  return SHG_OK;
+}
+int shg_set_device(int device) {
+  SHG_CUDA(cudaSetDevice(device));
+  return SHG_OK;
+}
+int shg_device_alloc(size_t bytes, void** out) {
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SHG_RESOURCE_EXHAUSTED, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return SHG_OK;
+}
+int shg_device_free(void* ptr) {
+  SHG_CUDA(cudaFree(ptr));
+  return SHG_OK;
+}
+int shg_host_alloc(size_t bytes, void** out) {
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SHG_RESOURCE_EXHAUSTED, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+  }
+  return SHG_OK;
+}
+int shg_host_free(void* ptr) {
+  SHG_CUDA(cudaFreeHost(ptr));
+  return SHG_OK;
+}
+int shg_memcpy_h2d(void* dst, const void* src, size_t bytes, shg_stream s) {
+  SHG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_memcpy_d2h(void* dst, const void* src, size_t bytes, shg_stream s) {
+  SHG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_memcpy_d2d(void* dst, const void* src, size_t bytes, shg_stream s) {
+  SHG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_memset_device(void* dst, int value, size_t bytes, shg_stream s) {
+  SHG_CUDA(cudaMemsetAsync(dst, value, bytes, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_stream_create(shg_stream* out) {
+  cudaStream_t s;
+  SHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *out = (shg_stream)s;
+  return SHG_OK;
+}
+int shg_stream_destroy(shg_stream s) {
+  SHG_CUDA(cudaStreamDestroy((cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_stream_synchronize(shg_stream s) {
+  SHG_CUDA(cudaStreamSynchronize((cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_device_synchronize(void) {
+  SHG_CUDA(cudaDeviceSynchronize());
+  return SHG_OK;
+}
+int shg_event_create(void** out) {
+  cudaEvent_t e;
+  SHG_CUDA(cudaEventCreate(&e));
+  *out = (void*)e;
+  return SHG_OK;
+}
+int shg_event_destroy(void* ev) {
+  SHG_CUDA(cudaEventDestroy((cudaEvent_t)ev));
+  return SHG_OK;
+}
+int shg_event_record(void* ev, shg_stream s) {
+  SHG_CUDA(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_event_elapsed_ms(void* a, void* b, float* ms) {
+  SHG_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));
+  return SHG_OK;
+}
+int shg_graph_capture_begin(shg_stream s) {
+  SHG_CUDA(cudaStreamBeginCapture((cudaStream_t)s, cudaStreamCaptureModeThreadLocal));
+  return SHG_OK;
+}
+int shg_graph_capture_end(shg_stream s, void** exec) {
+  cudaGraph_t g;
+  SHG_CUDA(cudaStreamEndCapture((cudaStream_t)s, &g));
+  cudaGraphExec_t ge;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  *exec = (void*)ge;
+  return SHG_OK;
+}
+int shg_graph_launch(void* exec, shg_stream s) {
+  SHG_CUDA(cudaGraphLaunch((cudaGraphExec_t)exec, (cudaStream_t)s));
+  return SHG_OK;
+}
+int shg_graph_destroy(void* exec) {
+  SHG_CUDA(cudaGraphExecDestroy((cudaGraphExec_t)exec));
+  return SHG_OK;
+}
+uint64_t shg_launch_count(void) { return shg::g_launch_count.load(); }
+int shg_context_reserve(shg_context* ctx, size_t bytes) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return ctx->ensure_ws(bytes);
+}
+int shg_context_set_chunk(shg_context* ctx, int cts) {
+  if (!ctx || cts < 0) return fail(SHG_INVALID_ARGUMENT, "bad chunk size");
+  ctx->chunk_cts = cts;
+  return SHG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,765 @@
+// CUDA kernels of the RLWE polynomial hot path (sm_103a).
+//
+// Every kernel reads and writes residues in SHELL's Montgomery representation
+// and returns canonical values, so results are bit-identical to the
+// reference CPU path; see the per-kernel comments for the reference
+// functions each one replaces.
+#include "kernels.cuh"
+
+namespace shg {
+
+std::atomic<uint64_t> g_launch_count{0};
+
+namespace {
+
+template <int LOG_N>
+struct Cfg {
+  using C = NttCore<LOG_N>;
+  static constexpr int N = C::N;
+  static constexpr int E = C::E;
+  static constexpr int T = C::T;
+  static constexpr int LPC = T >= 256 ? 1 : 256 / T;  // limbs per CTA
+  static constexpr int THREADS = T * LPC;
+  static constexpr int SMEM = LPC * N * 8;
+};
+
+template <class K>
+void set_smem(K kernel, int smem) {
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem);
+  }
+}
+
+template <int E>
+__device__ __forceinline__ void load_contig(uint64_t (&x)[E],
+                                            const uint64_t* p) {
+#pragma unroll
+  for (int k = 0; k < E; k += 2) {
+    ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p + k);
+    x[k] = v.x;
+    x[k + 1] = v.y;
+  }
+}
+
+template <int E>
+__device__ __forceinline__ void store_contig(uint64_t* p,
+                                             const uint64_t (&x)[E]) {
+#pragma unroll
+  for (int k = 0; k < E; k += 2) {
+    *reinterpret_cast<ulonglong2*>(p + k) = make_ulonglong2(x[k], x[k + 1]);
+  }
+}
+
+// Source position of NTT-domain slot `pos` under X -> X^power
+// (rns/rns_polynomial.cc:236-256): out[brv(j)] = in[brv((power-1)/2 +
+// j*power mod n)].
+template <int LOG_N>
+__device__ __forceinline__ int subst_src(int pos, int power) {
+  const unsigned j = __brev((unsigned)pos) >> (32 - LOG_N);
+  const unsigned t =
+      ((unsigned)((power - 1) >> 1) + j * (unsigned)power) & ((1u << LOG_N) - 1);
+  return (int)(__brev(t) >> (32 - LOG_N));
+}
+
+__device__ __forceinline__ int subst_src_rt(int pos, int power, int log_n) {
+  const unsigned j = __brev((unsigned)pos) >> (32 - log_n);
+  const unsigned t =
+      ((unsigned)((power - 1) >> 1) + j * (unsigned)power) & ((1u << log_n) - 1);
+  return (int)(__brev(t) >> (32 - log_n));
+}
+
+// --------------------------------------------------------------------------
+// Forward / inverse NTT (ForwardNumberTheoreticTransform /
+// InverseNumberTheoreticTransform, dft_transformations.h:158-201).
+// --------------------------------------------------------------------------
+
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_ntt_fwd(const uint64_t* in, uint64_t* out, int num, int L, CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const int l = g % L;
+  const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
+  const uint64_t* src = in + (size_t)g * C::N;
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) x[k] = src[C::fwd_in_idx(tid, k)];
+  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)l * C::N, 1, q,
+             two_q);
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) x[k] = reduce_4q(x[k], q, two_q);
+  if (active) store_contig(out + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
+}
+
+// scale_mode: 0 -> x n^{-1}; 1 -> x n^{-1} 2^-64 (iNTT fused with ExportInt);
+// 2 -> x (sw, swp) given by the caller.
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_ntt_inv(const uint64_t* in, uint64_t* out, int num, int L, int in_first,
+              int in_stride, int scale_mode, uint64_t sw, uint64_t swp,
+              CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const size_t src_limb = (size_t)in_first + (size_t)g * in_stride;
+  const int l = (int)(src_limb % (size_t)L);
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  uint64_t x[C::E];
+  load_contig(x, in + src_limb * C::N + C::inv_in_idx(tid, 0));
+  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
+             two_q);
+  if (scale_mode == 0) {
+    sw = P->n_inv;
+    swp = P->n_inv_shoup;
+  } else if (scale_mode == 1) {
+    sw = P->n_inv_r;
+    swp = P->n_inv_r_shoup;
+  }
+  if (active) {
+    uint64_t* dst = out + (size_t)g * C::N;
+#pragma unroll
+    for (int k = 0; k < C::E; ++k)
+      dst[C::inv_out_idx(tid, k)] = shoup(x[k], sw, swp, q);
+  }
+}
+
+// --------------------------------------------------------------------------
+// Fused kernels built on the NTT core.
+// --------------------------------------------------------------------------
+
+// RnsRlweCiphertext::Mul (rns/rns_ciphertext.h:501-524) for degree-1 inputs,
+// fused with ConvertToCoeffForm + ExportInt of the degree-2 component as
+// RnsRelinKey::ApplyToRlweCiphertext needs it (rns_relinearization_key.cc:
+// 215-218, rns_gadget.cc:130-134).  One CTA per (ciphertext, limb).
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_tensor_intt(uint64_t* out01, uint64_t* X, const uint64_t* a,
+                  const uint64_t* b, int num, int L, CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const int ct = g / L, l = g % L;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q, qinv = P->inv_modulus;
+  const size_t Ln = (size_t)L * C::N;
+  const size_t off = (size_t)ct * 2 * Ln + (size_t)l * C::N + C::inv_in_idx(tid, 0);
+  // Two coefficients at a time keeps the live register set at the 16
+  // degree-2 values plus one vector of each input.
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; k += 2) {
+    const ulonglong2 va0 = *reinterpret_cast<const ulonglong2*>(a + off + k);
+    const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a + off + Ln + k);
+    const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b + off + k);
+    const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b + off + Ln + k);
+    ulonglong2 r0, r1;
+    r0.x = mont_mul(va0.x, vb0.x, q, qinv);
+    r0.y = mont_mul(va0.y, vb0.y, q, qinv);
+    uint64_t lo = 0, hi = 0;
+    mac128(lo, hi, va0.x, vb1.x);
+    mac128(lo, hi, va1.x, vb0.x);
+    r1.x = redc128(lo, hi, q, qinv);
+    lo = 0;
+    hi = 0;
+    mac128(lo, hi, va0.y, vb1.y);
+    mac128(lo, hi, va1.y, vb0.y);
+    r1.y = redc128(lo, hi, q, qinv);
+    x[k] = mont_mul(va1.x, vb1.x, q, qinv);  // degree-2 component
+    x[k + 1] = mont_mul(va1.y, vb1.y, q, qinv);
+    if (active) {
+      *reinterpret_cast<ulonglong2*>(out01 + off + k) = r0;
+      *reinterpret_cast<ulonglong2*>(out01 + off + Ln + k) = r1;
+    }
+  }
+  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0,
+             q, two_q);
+  if (active) {
+    uint64_t* dst = X + (size_t)g * C::N;
+#pragma unroll
+    for (int k = 0; k < C::E; ++k)
+      dst[C::inv_out_idx(tid, k)] = shoup(x[k], P->n_inv_r, P->n_inv_r_shoup, q);
+  }
+}
+
+// ConvertToCoeffForm + ExportInt of one component (optionally substituted
+// first), as the key-switch input (rns_galois_key.cc:257-263,
+// relinearization_key.cc:148-150).
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_intt_export(uint64_t* X, const uint64_t* ct, int ncomp, int comp,
+                  int subst_power, CtMap map, int num, int L, CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const int p = g / L, l = g % L;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t* src =
+      ct + (map(p) * ncomp + comp) * (size_t)L * C::N + (size_t)l * C::N;
+  uint64_t x[C::E];
+  if (subst_power > 0) {
+#pragma unroll
+    for (int k = 0; k < C::E; ++k)
+      x[k] = src[subst_src<LOG_N>(C::inv_in_idx(tid, k), subst_power)];
+  } else {
+    load_contig(x, src + C::inv_in_idx(tid, 0));
+  }
+  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
+             two_q);
+  if (active) {
+    uint64_t* dst = X + (size_t)g * C::N;
+#pragma unroll
+    for (int k = 0; k < C::E; ++k)
+      dst[C::inv_out_idx(tid, k)] = shoup(x[k], P->n_inv_r, P->n_inv_r_shoup, q);
+  }
+}
+
+// RnsGadget::Decompose (rns/rns_gadget.cc:108-153, BaseDecompose gadget.h:
+// 52-79, ConvertModulusBalanced modulus_conversion.h:30-83) fused with the
+// per-digit ConvertToNttForm of the key-switch loop
+// (rns_relinearization_key.cc:219-226).  One CTA per (ct, digit, out limb).
+// The NTT runs on the plain digits; the key is premultiplied by 2^64 so the
+// inner product's REDC restores Montgomery form.
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_digit_ntt(uint64_t* D, const uint64_t* X, const DigitDesc* digits, int k,
+                int need_lift, int num, int L, CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const int j = g % L;
+  const int pd = g / L;
+  const int idx = pd % k, p = pd / k;
+  const DigitDesc dd = digits[idx];
+  const PrimeDev* P = c.primes + j;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t* src = X + ((size_t)p * L + dd.src_limb) * C::N;
+  uint64_t x[C::E];
+  if (!need_lift) {
+#pragma unroll
+    for (int kk = 0; kk < C::E; ++kk)
+      x[kk] = (src[C::fwd_in_idx(tid, kk)] >> dd.shift) & dd.mask;
+  } else {
+    const PrimeDev* Pi = c.primes + dd.src_limb;
+    const uint64_t half_qi = Pi->half_q;
+    const uint64_t qi_mod_qj = c.qmod[dd.src_limb * c.L + j];
+    const uint64_t bar = P->barrett;
+#pragma unroll
+    for (int kk = 0; kk < C::E; ++kk) {
+      uint64_t v = (src[C::fwd_in_idx(tid, kk)] >> dd.shift) & dd.mask;
+      const bool neg = v > half_qi;
+      v = reduce_2q(v - mulhi64(v, bar) * q, q);  // v mod q_j
+      if (neg && dd.src_limb != j) v += q - qi_mod_qj;
+      x[kk] = v;
+    }
+  }
+  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)j * C::N, 1, q,
+             two_q);
+#pragma unroll
+  for (int kk = 0; kk < C::E; ++kk) x[kk] = reduce_4q(x[kk], q, two_q);
+  if (active) store_contig(D + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
+}
+
+// RnsPolynomial::ModReduceLsb, NTT form, second half (rns/rns_polynomial.cc:
+// 302-323): balanced lift of the top limb's plain coefficients Y to q_i,
+// forward NTT, and out_i = in_i * c1_i + delta_i * c2_i.
+template <int LOG_N>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_modreduce_lift(uint64_t* out, const uint64_t* Y, const uint64_t* in,
+                     ScalarPack sc, int num, int L, CtxDev c) {
+  using C = NttCore<LOG_N>;
+  using G = Cfg<LOG_N>;
+  extern __shared__ uint64_t smem[];
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  int g = blockIdx.x * G::LPC + sub;
+  const bool active = g < num;
+  if (!active) g = num - 1;
+  const int Lr = L - 1;
+  const int i = g % Lr, p = g / Lr;
+  const PrimeDev* P = c.primes + i;
+  const PrimeDev* Pl = c.primes + Lr;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t half_ql = Pl->half_q;
+  const uint64_t ql_mod_qi = c.qmod[Lr * c.L + i];
+  const uint64_t bar = P->barrett;
+  const uint64_t* src = Y + (size_t)p * C::N;
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) {
+    uint64_t y = src[C::fwd_in_idx(tid, k)];
+    const bool neg = y > half_ql;
+    y = reduce_2q(y - mulhi64(y, bar) * q, q);
+    if (neg) y += q - ql_mod_qi;
+    x[k] = y;
+  }
+  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)i * C::N, 1, q,
+             two_q);
+  const uint64_t c1 = sc.v[4 * i], c1p = sc.v[4 * i + 1];
+  const uint64_t c2 = sc.v[4 * i + 2], c2p = sc.v[4 * i + 3];
+  const size_t off = ((size_t)p * L + i) * C::N + C::fwd_out_idx(tid, 0);
+  uint64_t a[C::E];
+  load_contig(a, in + off);
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) {
+    const uint64_t d = reduce_4q(x[k], q, two_q);
+    x[k] = reduce_2q_full(shoup(a[k], c1, c1p, q) + shoup(d, c2, c2p, q), q);
+  }
+  if (active)
+    store_contig(out + ((size_t)p * Lr + i) * C::N + C::fwd_out_idx(tid, 0), x);
+}
+
+// --------------------------------------------------------------------------
+// Element-wise kernels.
+// --------------------------------------------------------------------------
+
+__global__ void k_pointwise(PwOp op, uint64_t* out, const uint64_t* a,
+                            const uint64_t* b, ScalarPack sc, size_t total,
+                            int log_n, int L, CtxDev c) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x * 2;
+  for (size_t e = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+       e < total; e += stride) {
+    const int l = (int)((e >> log_n) % (size_t)L);
+    const PrimeDev* P = c.primes + l;
+    const uint64_t q = P->q;
+    const ulonglong2 va = *reinterpret_cast<const ulonglong2*>(a + e);
+    ulonglong2 r;
+    switch (op) {
+      case PW_ADD: {
+        const ulonglong2 vb = *reinterpret_cast<const ulonglong2*>(b + e);
+        r.x = add_mod(va.x, vb.x, q);
+        r.y = add_mod(va.y, vb.y, q);
+        break;
+      }
+      case PW_SUB: {
+        const ulonglong2 vb = *reinterpret_cast<const ulonglong2*>(b + e);
+        r.x = sub_mod(va.x, vb.x, q);
+        r.y = sub_mod(va.y, vb.y, q);
+        break;
+      }
+      case PW_NEG:
+        r.x = neg_mod(va.x, q);
+        r.y = neg_mod(va.y, q);
+        break;
+      case PW_MUL: {
+        const ulonglong2 vb = *reinterpret_cast<const ulonglong2*>(b + e);
+        r.x = mont_mul(va.x, vb.x, q, P->inv_modulus);
+        r.y = mont_mul(va.y, vb.y, q, P->inv_modulus);
+        break;
+      }
+      case PW_FMA: {
+        // acc (out) += a * b  (FusedMulAddInPlace, montgomery.h:446-465)
+        const ulonglong2 vb = *reinterpret_cast<const ulonglong2*>(b + e);
+        const ulonglong2 acc = *reinterpret_cast<const ulonglong2*>(out + e);
+        r.x = add_mod(acc.x, mont_mul(va.x, vb.x, q, P->inv_modulus), q);
+        r.y = add_mod(acc.y, mont_mul(va.y, vb.y, q, P->inv_modulus), q);
+        break;
+      }
+      case PW_MUL_MONT: {
+        const uint64_t s = sc.v[l];
+        r.x = mont_mul(va.x, s, q, P->inv_modulus);
+        r.y = mont_mul(va.y, s, q, P->inv_modulus);
+        break;
+      }
+      case PW_MUL_SHOUP:
+      default: {
+        const uint64_t w = sc.v[2 * l], wp = sc.v[2 * l + 1];
+        r.x = shoup(va.x, w, wp, q);
+        r.y = shoup(va.y, w, wp, q);
+        break;
+      }
+    }
+    *reinterpret_cast<ulonglong2*>(out + e) = r;
+  }
+}
+
+__global__ void k_substitute(uint64_t* out, const uint64_t* in, int power,
+                             size_t total, int log_n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t nmask = ((size_t)1 << log_n) - 1;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const int pos = (int)(e & nmask);
+    out[e] = in[(e & ~nmask) | (size_t)subst_src_rt(pos, power, log_n)];
+  }
+}
+
+__global__ void k_tensor(uint64_t* out, const uint64_t* a, const uint64_t* b,
+                         size_t total /* count*L*n */, int log_n, int L,
+                         CtxDev c) {
+  const size_t Ln = (size_t)L << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t ct = e / Ln, r = e % Ln;
+    const int l = (int)(r >> log_n);
+    const PrimeDev* P = c.primes + l;
+    const uint64_t q = P->q, qinv = P->inv_modulus;
+    const uint64_t a0 = a[ct * 2 * Ln + r], a1 = a[ct * 2 * Ln + Ln + r];
+    const uint64_t b0 = b[ct * 2 * Ln + r], b1 = b[ct * 2 * Ln + Ln + r];
+    uint64_t lo = 0, hi = 0;
+    mac128(lo, hi, a0, b1);
+    mac128(lo, hi, a1, b0);
+    out[ct * 3 * Ln + r] = mont_mul(a0, b0, q, qinv);
+    out[ct * 3 * Ln + Ln + r] = redc128(lo, hi, q, qinv);
+    out[ct * 3 * Ln + 2 * Ln + r] = mont_mul(a1, b1, q, qinv);
+  }
+}
+
+// Key inner product of the gadget key switch (rns_relinearization_key.cc:
+// 219-226, rns_galois_key.cc:265-283, relinearization_key.cc:76-96): 128-bit
+// lazy accumulation of raw products, one REDC per `chunk` terms.
+__global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
+                           const uint64_t* ka, int k, int chunk,
+                           const uint64_t* base, size_t base_ct_elems,
+                           CtMap map, int base1_zero, int subst_power,
+                           size_t total /* count*L*n */, int log_n, int L,
+                           CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t Ln = (size_t)L * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e / Ln, r = e % Ln;
+    const int l = (int)(r >> log_n);
+    const size_t pos = r & (n - 1);
+    const PrimeDev* P = c.primes + l;
+    const uint64_t q = P->q, qinv = P->inv_modulus;
+    const uint64_t* dp = D + p * (size_t)k * Ln + r;
+    uint64_t s0 = 0, s1 = 0;
+    for (int j0 = 0; j0 < k; j0 += chunk) {
+      const int j1 = min(k, j0 + chunk);
+      uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+      for (int j = j0; j < j1; ++j) {
+        const uint64_t d = dp[(size_t)j * Ln];
+        mac128(lo0, hi0, d, __ldg(kb + (size_t)j * Ln + r));
+        mac128(lo1, hi1, d, __ldg(ka + (size_t)j * Ln + r));
+      }
+      s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
+      s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
+    }
+    const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
+    const size_t pos0 =
+        subst_power > 0 ? (size_t)subst_src_rt((int)pos, subst_power, log_n)
+                        : pos;
+    const uint64_t b0 = bp[pos0];
+    const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
+    out[p * 2 * Ln + r] = add_mod(b0, s0, q);
+    out[p * 2 * Ln + Ln + r] = add_mod(b1, s1, q);
+  }
+}
+
+// ModReduceLsb, coefficient form (rns/rns_polynomial.cc:324-342).
+__global__ void k_modreduce_coeff(uint64_t* out, const uint64_t* in,
+                                  uint64_t k_plain, uint64_t k_shoup,
+                                  ScalarPack sc, size_t total /*count*(L-1)*n*/,
+                                  int log_n, int L, CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const int Lr = L - 1;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const PrimeDev* Pl = c.primes + Lr;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e / ((size_t)Lr * n), r = e % ((size_t)Lr * n);
+    const int i = (int)(r >> log_n);
+    const size_t pos = r & (n - 1);
+    const PrimeDev* P = c.primes + i;
+    const uint64_t q = P->q;
+    // plain value of (a_l * k) mod q_l
+    uint64_t y = shoup(in[(p * L + Lr) * n + pos], k_plain, k_shoup, Pl->q);
+    const bool neg = y > Pl->half_q;
+    y = reduce_2q(y - mulhi64(y, P->barrett) * q, q);
+    if (neg) y = reduce_2q(y + q - c.qmod[Lr * c.L + i], q);
+    const uint64_t a = in[(p * L + i) * n + pos];
+    out[e] = reduce_2q_full(shoup(a, sc.v[4 * i], sc.v[4 * i + 1], q) +
+                                shoup(y, sc.v[4 * i + 2], sc.v[4 * i + 3], q),
+                            q);
+  }
+}
+
+// ExpandCiphertext's per-level update (oblivious_expand.h:216-223).
+__global__ void k_expand_combine(uint64_t* base, const uint64_t* ks,
+                                 const uint64_t* mono, CtMap map, int half,
+                                 size_t total /* count*2*n */, int log_n,
+                                 CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const uint64_t q = c.primes[0].q, qinv = c.primes[0].inv_modulus;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e / (2 * n), r = e % (2 * n);
+    uint64_t* cp = base + map(p) * 2 * n + r;
+    uint64_t* hp = cp + (size_t)half * 2 * n;
+    const uint64_t cv = *cp, kv = ks[e];
+    *hp = mont_mul(sub_mod(cv, kv, q), mono[r & (n - 1)], q, qinv);
+    *cp = add_mod(cv, kv, q);
+  }
+}
+
+// FusedAbsorbAddInPlace chain (symmetric_encryption.h:250-275).
+__global__ void k_absorb_sum(uint64_t* out, const uint64_t* cts,
+                             const uint64_t* db, int num_items, int chunk,
+                             size_t total /* count*2*n */, int log_n,
+                             CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const uint64_t q = c.primes[0].q, qinv = c.primes[0].inv_modulus;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t qi = e / (2 * n), r = e % (2 * n);
+    const size_t pos = r & (n - 1);
+    const uint64_t* cp = cts + qi * (size_t)num_items * 2 * n + r;
+    uint64_t s = 0;
+    for (int i0 = 0; i0 < num_items; i0 += chunk) {
+      const int i1 = min(num_items, i0 + chunk);
+      uint64_t lo = 0, hi = 0;
+      for (int i = i0; i < i1; ++i)
+        mac128(lo, hi, cp[(size_t)i * 2 * n], __ldg(db + (size_t)i * n + pos));
+      s = add_mod(s, redc128(lo, hi, q, qinv), q);
+    }
+    out[e] = s;
+  }
+}
+
+int grid_for(size_t work, int threads) {
+  size_t blocks = (work + threads - 1) / threads;
+  const size_t cap = 152 * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+// Runtime log_n -> template dispatch for CTA-resident transforms.
+#define SHG_DISPATCH_LOGN(log_n, F)                                  \
+  switch (log_n) {                                                   \
+    case 1: F(1); break;                                             \
+    case 2: F(2); break;                                             \
+    case 3: F(3); break;                                             \
+    case 4: F(4); break;                                             \
+    case 5: F(5); break;                                             \
+    case 6: F(6); break;                                             \
+    case 7: F(7); break;                                             \
+    case 8: F(8); break;                                             \
+    case 9: F(9); break;                                             \
+    case 10: F(10); break;                                           \
+    case 11: F(11); break;                                           \
+    case 12: F(12); break;                                           \
+    case 13: F(13); break;                                           \
+    case 14: F(14); break;                                           \
+    default: break;                                                  \
+  }
+
+template <int LOG_N>
+int blocks_for(int num) {
+  return (num + Cfg<LOG_N>::LPC - 1) / Cfg<LOG_N>::LPC;
+}
+
+}  // namespace
+
+void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                    int L, cudaStream_t s) {
+  if (num <= 0) return;
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_ntt_fwd<LN>;                                                \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        in, out, num, L, c);                                                  \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
+                                  uint64_t* out, int num, int L, int in_first,
+                                  int in_stride, int mode, uint64_t sw,
+                                  uint64_t swp, cudaStream_t s) {
+  if (num <= 0) return;
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_ntt_inv<LN>;                                                \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        in, out, num, L, in_first, in_stride, mode, sw, swp, c);              \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+void launch_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                    int L, int scale_export, cudaStream_t s) {
+  launch_ntt_inv_scaled(c, in, out, num, L, 0, 1, scale_export ? 1 : 0, 0, 0,
+                        s);
+}
+
+void launch_pointwise(const CtxDev& c, PwOp op, uint64_t* out, const uint64_t* a,
+                      const uint64_t* b, const ScalarPack& sc, int count, int L,
+                      cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  k_pointwise<<<grid_for(total / 2, 256), 256, 0, s>>>(op, out, a, b, sc, total,
+                                                       c.log_n, L, c);
+  g_launch_count++;
+}
+
+void launch_substitute(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                       int power, int count, int L, cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  k_substitute<<<grid_for(total, 256), 256, 0, s>>>(out, in, power, total,
+                                                    c.log_n);
+  g_launch_count++;
+}
+
+void launch_tensor(const CtxDev& c, uint64_t* out, const uint64_t* a,
+                   const uint64_t* b, int count, int L, cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  k_tensor<<<grid_for(total, 256), 256, 0, s>>>(out, a, b, total, c.log_n, L,
+                                                c);
+  g_launch_count++;
+}
+
+void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
+                        const uint64_t* a, const uint64_t* b, int count, int L,
+                        cudaStream_t s) {
+  const int num = count * L;
+  if (num <= 0) return;
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_tensor_intt<LN>;                                            \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        out01, X, a, b, num, L, c);                                           \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
+                        int ncomp, int comp, int subst_power, CtMap map,
+                        int count, int L, cudaStream_t s) {
+  const int num = count * L;
+  if (num <= 0) return;
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_intt_export<LN>;                                            \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        X, ct, ncomp, comp, subst_power, map, num, L, c);                     \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                      const DigitDesc* digits, int k, int need_lift, int count,
+                      int L, cudaStream_t s) {
+  const int num = count * k * L;
+  if (num <= 0) return;
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_digit_ntt<LN>;                                              \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        D, X, digits, k, need_lift, num, L, c);                               \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
+                     const uint64_t* kb, const uint64_t* ka, int k, int chunk,
+                     const uint64_t* base, size_t base_ct_elems, CtMap map,
+                     int base1_zero, int subst_power, int count, int L,
+                     cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  k_ks_inner<<<grid_for(total, 256), 256, 0, s>>>(
+      out, D, kb, ka, k, chunk, base, base_ct_elems, map, base1_zero,
+      subst_power, total, c.log_n, L, c);
+  g_launch_count++;
+}
+
+void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
+                          const uint64_t* in, uint64_t k_plain,
+                          uint64_t k_shoup, const ScalarPack& sc, int count,
+                          int L, cudaStream_t s) {
+  if (count <= 0) return;
+  // Stage 1 (rns_polynomial.cc:286-306): the top limb of every poly (limb
+  // L-1, stride L limbs), multiplied by k, inverse NTT and ExportInt, all
+  // folded into one scale k * n^{-1} * 2^-64 -> Y [count][n] plain.
+  launch_ntt_inv_scaled(c, in, Y, count, L, L - 1, L, 2, k_plain, k_shoup, s);
+  // Stage 2: lift, forward NTT, combine.
+#define F(LN)                                                                 \
+  {                                                                           \
+    auto kern = k_modreduce_lift<LN>;                                         \
+    set_smem(kern, Cfg<LN>::SMEM);                                            \
+    const int num = count * (L - 1);                                          \
+    kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
+        out, Y, in, sc, num, L, c);                                           \
+  }
+  SHG_DISPATCH_LOGN(c.log_n, F)
+#undef F
+  g_launch_count++;
+}
+
+void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                            uint64_t k_plain, uint64_t k_shoup,
+                            const ScalarPack& sc, int count, int L,
+                            cudaStream_t s) {
+  const size_t total = (size_t)count * (L - 1) * c.n;
+  if (total == 0) return;
+  k_modreduce_coeff<<<grid_for(total, 256), 256, 0, s>>>(
+      out, in, k_plain, k_shoup, sc, total, c.log_n, L, c);
+  g_launch_count++;
+}
+
+void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
+                           const uint64_t* mono, CtMap map, int half,
+                           int count, cudaStream_t s) {
+  const size_t total = (size_t)count * 2 * c.n;
+  if (total == 0) return;
+  k_expand_combine<<<grid_for(total, 256), 256, 0, s>>>(base, ks, mono, map,
+                                                        half, total, c.log_n, c);
+  g_launch_count++;
+}
+
+void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
+                       const uint64_t* db, int num_items, int chunk, int count,
+                       cudaStream_t s) {
+  const size_t total = (size_t)count * 2 * c.n;
+  if (total == 0) return;
+  k_absorb_sum<<<grid_for(total, 256), 256, 0, s>>>(out, cts, db, num_items,
+                                                    chunk, total, c.log_n, c);
+  g_launch_count++;
+}
+
+}  // namespace shg

@@ -1,0 +1,136 @@
+// Internal interface between the C ABI (capi.cu) and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "modarith.cuh"
+#include "ntt.cuh"
+
+namespace shg {
+
+constexpr int kMaxLimbs = 32;
+
+// Device view of a context: per-limb constants and twiddle tables.
+struct CtxDev {
+  int log_n;
+  int n;
+  int L;                      // number of moduli in the context
+  const PrimeDev* primes;     // [L]
+  const Tw* tw_fwd;           // [L][n]  plain psi^{brv(i)} + Shoup constant
+  const Tw* tw_inv;           // [L][n]  plain psis_inv_bitrev + Shoup constant
+  const uint64_t* qmod;       // [L][L]  q_i mod q_j (plain), row i
+};
+
+// Per-digit description of a gadget key (RnsGadget::Decompose order,
+// rns/rns_gadget.cc:108-153: prime-major, least significant digit first).
+struct DigitDesc {
+  int src_limb;   // limb i whose residue is decomposed
+  int shift;      // d * log_b_i
+  uint64_t mask;  // 2^log_b_i - 1
+};
+
+// Small per-limb constant arrays passed by value.
+struct ScalarPack {
+  uint64_t v[4 * kMaxLimbs];
+};
+
+// Ciphertext addressing for batches whose members are not contiguous
+// (oblivious expansion): member p lives at index
+//   ((p >> grp_log) << stride_log) | (p & (2^grp_log - 1)).
+struct CtMap {
+  int grp_log;
+  int stride_log;
+  __host__ __device__ static CtMap identity() { return CtMap{30, 30}; }
+  __host__ __device__ __forceinline__ size_t operator()(size_t p) const {
+    return ((p >> grp_log) << stride_log) | (p & ((size_t(1) << grp_log) - 1));
+  }
+};
+
+// Number of kernels this library has launched (host-side counter).
+extern std::atomic<uint64_t> g_launch_count;
+
+// `num` limb transforms; limb index of transform g is g % L.
+void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                    int L, cudaStream_t s);
+// scale_export = 1 folds ExportInt into the n^{-1} scaling (plain output).
+void launch_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                    int L, int scale_export, cudaStream_t s);
+
+enum PwOp {
+  PW_ADD = 0,
+  PW_SUB,
+  PW_NEG,
+  PW_MUL,         // REDC(a, b)
+  PW_FMA,         // out += REDC(a, b)
+  PW_MUL_MONT,    // REDC(a, scalar_l)      v[l] = Montgomery scalar
+  PW_MUL_SHOUP,   // a * w_l mod q          v[2l], v[2l+1] = w, Shoup(w)
+};
+void launch_pointwise(const CtxDev& c, PwOp op, uint64_t* out, const uint64_t* a,
+                      const uint64_t* b, const ScalarPack& sc, int count, int L,
+                      cudaStream_t s);
+
+void launch_substitute(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                       int power, int count, int L, cudaStream_t s);
+
+// out [count][3][L][n] = a (x) b.
+void launch_tensor(const CtxDev& c, uint64_t* out, const uint64_t* a,
+                   const uint64_t* b, int count, int L, cudaStream_t s);
+
+// Fused tensor product + inverse NTT of the degree-2 part:
+// out01 [count][2][L][n] <- (a0*b0, a0*b1 + a1*b0); X [count][L][n] <- plain
+// coefficients of a1*b1.
+void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
+                        const uint64_t* a, const uint64_t* b, int count, int L,
+                        cudaStream_t s);
+
+// Inverse NTT + export of component `comp` of ciphertexts with `ncomp`
+// components (member p at map(p)); X [count][L][n] plain coefficients.  If
+// subst_power > 0 the component is substituted (NTT-domain gather) first.
+void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
+                        int ncomp, int comp, int subst_power, CtMap map,
+                        int count, int L, cudaStream_t s);
+
+// Digit decomposition + forward NTT: D [count][k][L][n] (canonical NTT values
+// of the plain digits) from X [count][L][n].
+void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                      const DigitDesc* digits, int k, int need_lift, int count,
+                      int L, cudaStream_t s);
+
+// Key inner product, per ciphertext p and limb:
+//   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
+// kb/ka hold the key premultiplied by 2^64 mod q (so REDC lands in Montgomery
+// form); `chunk` products are summed per REDC (chunk * q < 2^64).  out [count][2][L][n]; base component c of member p lives at
+// base + map(p) * base_ct_elems + c * L * n; base1_zero drops base1.  If
+// subst_power > 0, base0 is read through that substitution.
+void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
+                     const uint64_t* kb, const uint64_t* ka, int k, int chunk,
+                     const uint64_t* base, size_t base_ct_elems, CtMap map,
+                     int base1_zero, int subst_power, int count, int L,
+                     cudaStream_t s);
+
+// ModReduceLsb (NTT form): Y [count][n] scratch; out [count][L-1][n].
+// sc.v[4i..4i+3] = (c1, Shoup(c1), c2, Shoup(c2)) for output limb i with
+// out = in_i * c1 + delta_i * c2.  (k_plain, k_shoup) multiply the top limb.
+void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
+                          const uint64_t* in, uint64_t k_plain,
+                          uint64_t k_shoup, const ScalarPack& sc, int count,
+                          int L, cudaStream_t s);
+void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                            uint64_t k_plain, uint64_t k_shoup,
+                            const ScalarPack& sc, int count, int L,
+                            cudaStream_t s);
+
+// Oblivious-expand level combine for members p (ciphertext at map(p) of
+// `base`, partner at map(p) + half): hi = (c - ks[p]) * mono; c = c + ks[p].
+void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
+                           const uint64_t* mono, CtMap map, int half,
+                           int count, cudaStream_t s);
+
+// out [count][2][n] = sum_i cts[count][i][2][n] * db[i][n].
+void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
+                       const uint64_t* db, int num_items, int chunk, int count,
+                       cudaStream_t s);
+
+}  // namespace shg

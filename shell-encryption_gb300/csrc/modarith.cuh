@@ -1,0 +1,112 @@
+// Device-side 64-bit modular arithmetic for residues mod q < 2^62.
+//
+// Stored residues follow SHELL's MontgomeryInt<uint64> convention
+// (montgomery.h:226-300): a value x is held as x * 2^64 mod q, canonical in
+// [0, q).  Internally the kernels use Harvey-style lazy ranges ([0, 2q) or
+// [0, 4q)) and Shoup constant multiplication; every value that leaves a
+// kernel is canonical, so outputs are bit-identical to the reference.
+#pragma once
+#include <stdint.h>
+
+namespace shg {
+
+// Per-prime constants, resident in device memory (one entry per RNS limb).
+struct PrimeDev {
+  uint64_t q;
+  uint64_t two_q;
+  uint64_t inv_modulus;    // -q^{-1} mod 2^64 (montgomery.h inv_modulus)
+  uint64_t r_mod_q;        // 2^64 mod q  (Montgomery one)
+  uint64_t r_mod_q_shoup;  // floor(r_mod_q * 2^64 / q)
+  uint64_t inv_r;          // 2^-64 mod q
+  uint64_t inv_r_shoup;
+  uint64_t n_inv;          // n^{-1} mod q (plain)
+  uint64_t n_inv_shoup;
+  uint64_t n_inv_r;        // n^{-1} * 2^-64 mod q (iNTT fused with export)
+  uint64_t n_inv_r_shoup;
+  uint64_t half_q;         // floor(q / 2): balanced-lift threshold
+  uint64_t log_q;
+  uint64_t barrett;        // floor(2^64 / q): x mod q for any 64-bit x
+  uint64_t pad[2];
+};
+static_assert(sizeof(PrimeDev) == 128, "PrimeDev is one cache line");
+
+__device__ __forceinline__ uint64_t mulhi64(uint64_t a, uint64_t b) {
+  return __umul64hi(a, b);
+}
+
+// x * w mod q using the Shoup constant wp = floor(w * 2^64 / q).
+// Valid for any x < 2^64 and w < q; result in [0, 2q).
+__device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w,
+                                               uint64_t wp, uint64_t q) {
+  return x * w - mulhi64(x, wp) * q;
+}
+
+__device__ __forceinline__ uint64_t reduce_2q(uint64_t x, uint64_t q) {
+  return x >= q ? x - q : x;
+}
+
+__device__ __forceinline__ uint64_t reduce_4q(uint64_t x, uint64_t q,
+                                              uint64_t two_q) {
+  x = x >= two_q ? x - two_q : x;
+  return x >= q ? x - q : x;
+}
+
+__device__ __forceinline__ uint64_t shoup(uint64_t x, uint64_t w, uint64_t wp,
+                                          uint64_t q) {
+  return reduce_2q(shoup_lazy(x, w, wp, q), q);
+}
+
+// Montgomery product a*b*2^-64 mod q (REDC, montgomery.h:318-336); a*b < q*2^64.
+// The low halves of a*b and u*q sum to 0 mod 2^64, so the carry into the high
+// half is (lo != 0).
+__device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b,
+                                             uint64_t q, uint64_t qinv) {
+  uint64_t lo = a * b;
+  uint64_t hi = mulhi64(a, b);
+  uint64_t u = lo * qinv;
+  uint64_t r = hi + mulhi64(u, q) + (lo != 0);
+  return reduce_2q(r, q);
+}
+
+// REDC of a 128-bit accumulator (hi:lo) < q * 2^64.
+__device__ __forceinline__ uint64_t redc128(uint64_t lo, uint64_t hi,
+                                            uint64_t q, uint64_t qinv) {
+  uint64_t u = lo * qinv;
+  uint64_t r = hi + mulhi64(u, q) + (lo != 0);
+  return reduce_2q(r, q);
+}
+
+// 128-bit multiply-accumulate: (hi:lo) += a*b.
+__device__ __forceinline__ void mac128(uint64_t& lo, uint64_t& hi, uint64_t a,
+                                       uint64_t b) {
+  uint64_t plo = a * b;
+  uint64_t phi = mulhi64(a, b);
+  uint64_t nlo = lo + plo;
+  hi += phi + (nlo < lo);
+  lo = nlo;
+}
+
+// Inputs may be any value in [0, q] (SHELL's NegateInPlace maps 0 to q,
+// montgomery.h:405-408); results are canonical like the reference's Barrett
+// AddInPlace / SubInPlace (montgomery.h:383-415).
+__device__ __forceinline__ uint64_t reduce_2q_full(uint64_t x, uint64_t q) {
+  x = x >= q ? x - q : x;
+  return x >= q ? x - q : x;
+}
+
+__device__ __forceinline__ uint64_t add_mod(uint64_t a, uint64_t b,
+                                            uint64_t q) {
+  return reduce_2q_full(a + b, q);
+}
+
+__device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b,
+                                            uint64_t q) {
+  return reduce_2q_full(a + (q - b), q);
+}
+
+// NegateInPlace (montgomery.h:405-408): q - a, which is q (not 0) for a == 0.
+__device__ __forceinline__ uint64_t neg_mod(uint64_t a, uint64_t q) {
+  return q - a;
+}
+
+}  // namespace shg

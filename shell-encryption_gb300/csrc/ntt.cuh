@@ -1,0 +1,212 @@
+// Negacyclic NTT core for one CTA-resident limb (n = 2^LOG_N <= 2^14).
+//
+// The transform is the same linear map as SHELL's IterativeCooleyTukey
+// (dft_transformations.h:59-100): psi is the reference's primitive 2n-th root
+// (ntt_parameters.h:41-71), twiddles are psi^{brv(i)} (ntt_parameters.h:
+// 117-127) and the output is in bit-reversed evaluation order.  The inverse is
+// the exact inverse map, consuming the reference's psis_inv_bitrev table in
+// the order of IterativeGentlemanSande (dft_transformations.h:118-153).
+//
+// GPU organisation: each thread holds E = 16 coefficients in registers and
+// runs up to four butterfly levels on them per pass; passes exchange through
+// a swizzled shared-memory tile.  Butterflies are Harvey-style with Shoup
+// twiddles: forward values stay in [0, 4q), inverse values in [0, 2q), and the
+// final pass reduces to canonical residues.
+#pragma once
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "modarith.cuh"
+
+namespace shg {
+
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>{});
+    static_for<I + 1, N>(f);
+  }
+}
+
+struct Tw {
+  uint64_t w;   // plain twiddle value
+  uint64_t wp;  // floor(w * 2^64 / q)
+};
+
+__device__ __forceinline__ Tw load_tw(const Tw* p) {
+  ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p));
+  return Tw{v.x, v.y};
+}
+
+// Cooley-Tukey butterfly, inputs/outputs in [0, 4q).
+__device__ __forceinline__ void bf_ct(uint64_t& X, uint64_t& Y, Tw w,
+                                      uint64_t q, uint64_t two_q) {
+  uint64_t x = X >= two_q ? X - two_q : X;
+  uint64_t t = shoup_lazy(Y, w.w, w.wp, q);
+  X = x + t;
+  Y = x - t + two_q;
+}
+
+// Gentleman-Sande butterfly, inputs/outputs in [0, 2q).
+__device__ __forceinline__ void bf_gs(uint64_t& X, uint64_t& Y, Tw w,
+                                      uint64_t q, uint64_t two_q) {
+  uint64_t s = X + Y;
+  s = s >= two_q ? s - two_q : s;
+  uint64_t d = X - Y + two_q;
+  X = s;
+  Y = shoup_lazy(d, w.w, w.wp, q);
+}
+
+// Shared-memory swizzle: XOR the low 4 index bits with bits 4..7 so that every
+// pass's per-register access pattern is bank-conflict free.
+__device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
+
+template <int LOG_N>
+struct NttCore {
+  static_assert(LOG_N >= 1 && LOG_N <= 14, "CTA-resident NTT handles n <= 2^14");
+  static constexpr int N = 1 << LOG_N;
+  static constexpr int ELOG = LOG_N < 4 ? LOG_N : 4;
+  static constexpr int E = 1 << ELOG;
+  static constexpr int T = N / E;  // threads per limb
+  static constexpr int P = (LOG_N + ELOG - 1) / ELOG;  // passes
+
+  // Pass p covers R(p) butterfly levels.  Its registers span the contiguous
+  // index-bit range [clo, clo + ELOG); within that range the butterfly bits
+  // start at local bit plo.
+  __host__ __device__ static constexpr int R(int p) {
+    return (LOG_N - p * ELOG) < ELOG ? (LOG_N - p * ELOG) : ELOG;
+  }
+  // Forward: top bits first; the short last pass sits at bits [0, R) with the
+  // remaining register bits above it.
+  __host__ __device__ static constexpr int fwd_clo(int p) {
+    return p == P - 1 ? 0 : LOG_N - p * ELOG - ELOG;
+  }
+  __host__ __device__ static constexpr int fwd_plo(int) { return 0; }
+  // Inverse: bottom bits first; the short last pass sits at the top bits
+  // with the remaining register bits below it.
+  __host__ __device__ static constexpr int inv_clo(int p) {
+    return p == P - 1 ? LOG_N - ELOG : p * ELOG;
+  }
+  __host__ __device__ static constexpr int inv_plo(int p) {
+    return p == P - 1 ? ELOG - R(p) : 0;
+  }
+
+  __device__ __forceinline__ static int idx(int tid, int k, int clo) {
+    return (tid & ((1 << clo) - 1)) | (k << clo) | ((tid >> clo) << (clo + ELOG));
+  }
+  // Register layouts at the boundaries.
+  __device__ __forceinline__ static int fwd_in_idx(int tid, int k) {
+    return idx(tid, k, fwd_clo(0));
+  }
+  __device__ __forceinline__ static int fwd_out_idx(int tid, int k) {
+    return idx(tid, k, fwd_clo(P - 1));
+  }
+  __device__ __forceinline__ static int inv_in_idx(int tid, int k) {
+    return idx(tid, k, inv_clo(0));
+  }
+  __device__ __forceinline__ static int inv_out_idx(int tid, int k) {
+    return idx(tid, k, inv_clo(P - 1));
+  }
+
+  // One forward pass on registers.  tw is the limb's psi_bitrev table; stage s
+  // reads tw[tw_mult * 2^s + (i >> (b+1))] (tw_mult = 1 for a full transform;
+  // 2 + h for half h of a 2n transform whose first level ran elsewhere).
+  template <int p>
+  __device__ __forceinline__ static void fwd_pass(uint64_t (&x)[E], int tid,
+                                                  const Tw* __restrict__ tw,
+                                                  int tw_mult, uint64_t q,
+                                                  uint64_t two_q) {
+    constexpr int clo = fwd_clo(p);
+    constexpr int plo = fwd_plo(p);
+    constexpr int RR = R(p);
+    const int tid_high = tid >> clo;
+    static_for<0, RR>([&](auto ii) {
+      constexpr int lb = plo + RR - 1 - decltype(ii)::value;  // high to low
+      constexpr int b = clo + lb;
+      constexpr int s = LOG_N - 1 - b;
+      const int base = tw_mult * (1 << s) + (tid_high << (ELOG - lb - 1));
+      static_for<0, (E >> (lb + 1))>([&](auto uu) {
+        constexpr int u = decltype(uu)::value;
+        const Tw w = load_tw(tw + base + u);
+        static_for<0, (1 << lb)>([&](auto ll) {
+          constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
+          constexpr int k1 = k0 | (1 << lb);
+          bf_ct(x[k0], x[k1], w, q, two_q);
+        });
+      });
+    });
+  }
+
+  // One inverse pass.  Layer b reads tw[inv_base(b) + (i >> (b+1))] where
+  // inv_base(b) = Nfull - Nfull/2^b + h * Nfull/2^(b+2) (h = 0, Nfull = N for a
+  // full transform).
+  template <int p>
+  __device__ __forceinline__ static void inv_pass(uint64_t (&x)[E], int tid,
+                                                  const Tw* __restrict__ tw,
+                                                  int nfull, int h, uint64_t q,
+                                                  uint64_t two_q) {
+    constexpr int clo = inv_clo(p);
+    constexpr int plo = inv_plo(p);
+    constexpr int RR = R(p);
+    const int tid_high = tid >> clo;
+    static_for<0, RR>([&](auto ii) {
+      constexpr int lb = plo + decltype(ii)::value;  // low to high
+      constexpr int b = clo + lb;
+      const int base = nfull - (nfull >> b) + h * (nfull >> (b + 2)) +
+                       (tid_high << (ELOG - lb - 1));
+      static_for<0, (E >> (lb + 1))>([&](auto uu) {
+        constexpr int u = decltype(uu)::value;
+        const Tw w = load_tw(tw + base + u);
+        static_for<0, (1 << lb)>([&](auto ll) {
+          constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
+          constexpr int k1 = k0 | (1 << lb);
+          bf_gs(x[k0], x[k1], w, q, two_q);
+        });
+      });
+    });
+  }
+
+  // Register exchange through shared memory from layout clo_a to clo_b.
+  // Caller guarantees sm is not being read by a previous exchange.
+  __device__ __forceinline__ static void exchange(uint64_t (&x)[E], int tid,
+                                                  uint64_t* sm, int clo_a,
+                                                  int clo_b) {
+#pragma unroll
+    for (int k = 0; k < E; ++k) sm[swz(idx(tid, k, clo_a))] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < E; ++k) x[k] = sm[swz(idx(tid, k, clo_b))];
+    __syncthreads();
+  }
+
+  // Full forward transform on registers (input in fwd_in layout, values in
+  // [0, 4q); output in fwd_out layout, values in [0, 4q)).
+  __device__ __forceinline__ static void forward(uint64_t (&x)[E], int tid,
+                                                 uint64_t* sm,
+                                                 const Tw* __restrict__ tw,
+                                                 int tw_mult, uint64_t q,
+                                                 uint64_t two_q) {
+    static_for<0, P>([&](auto pp) {
+      constexpr int p = decltype(pp)::value;
+      fwd_pass<p>(x, tid, tw, tw_mult, q, two_q);
+      if constexpr (p + 1 < P) exchange(x, tid, sm, fwd_clo(p), fwd_clo(p + 1));
+    });
+  }
+
+  // Full inverse transform without the n^{-1} scaling (input in inv_in
+  // layout, values in [0, 2q); output in inv_out layout, values in [0, 2q)).
+  __device__ __forceinline__ static void inverse(uint64_t (&x)[E], int tid,
+                                                 uint64_t* sm,
+                                                 const Tw* __restrict__ tw,
+                                                 int nfull, int h, uint64_t q,
+                                                 uint64_t two_q) {
+    static_for<0, P>([&](auto pp) {
+      constexpr int p = decltype(pp)::value;
+      inv_pass<p>(x, tid, tw, nfull, h, q, two_q);
+      if constexpr (p + 1 < P) exchange(x, tid, sm, inv_clo(p), inv_clo(p + 1));
+    });
+  }
+};
+
+}  // namespace shg

@@ -1,0 +1,39 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "shell-encryption_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+# Primes used across the tests (the reference's configs; SURVEY appendix B
+# values re-derived in tests/test_oracle.py).
+Q45 = [35184371138561, 35184370941953, 35184370352129, 35184370155521,
+       35184369893377, 35184368877569]
+Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,
+       1125899902124033, 1125899901665281, 1125899899174913, 1125899896160257,
+       1125899887312897, 1125899886395393, 1125899885740033, 1125899885412353]
+Q59 = 576460752303415297
+Q60 = 1152921504606830593
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle import oracle as O
+    O.lib()
+    return O
+
+
+@pytest.fixture(scope="session")
+def sg():
+    import shell_gpu
+    shell_gpu.lib()
+    return shell_gpu

@@ -1,0 +1,391 @@
+"""GPU parity tests: every entry point of include/shell_gpu.h against the CPU
+oracle (a restatement of google/shell-encryption's algorithms, pinned to the
+reference by tests/golden), bit for bit, on seeded inputs.
+
+Mirrors the reference's own tests: NTT round trip and delta -> constant
+(dft_transformations_test.cc:84-140), NTT product == negacyclic schoolbook
+(polynomial_test.cc:310-337), Substitute (polynomial_test.cc:487-505), RNS
+pointwise ops (rns/rns_polynomial_test.cc:618-1110), ModReduceLsb
+(rns/rns_polynomial_test.cc:1150-1450), key switching
+(rns/rns_relinearization_key_test.cc, rns/rns_galois_key_test.cc) and
+oblivious expansion (oblivious_expand_test.cc:219-259).
+"""
+import numpy as np
+import pytest
+
+from conftest import Q45, Q50, Q59, Q60
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(sg, fn, *args):
+    sg.check(fn(*args))
+    sg.synchronize()
+
+
+def _dev(sg, arr):
+    return sg.DeviceBuffer.from_array(arr)
+
+
+# --------------------------------------------------------------------------
+# Context parameters
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("q,log_n", [(Q45[0], 14), (Q50[3], 11), (Q59, 12), (Q60, 12),
+                                     (Q45[5], 3), (Q50[0], 1)])
+def test_context_tables_match_reference(sg, oracle, q, log_n):
+    ctx = sg.Context(log_n, [q])
+    p = oracle.Prime(q, log_n)
+    info_gpu = ctx.prime_info(0)
+    info_ref = p.info()
+    assert [int(x) for x in info_gpu] == [info_ref[k] for k in
+                                          ["q", "log_q", "inv_modulus", "r_mod_q",
+                                           "r_mod_q_barrett", "inv_r", "inv_r_barrett",
+                                           "barrett_num", "psi", "n_inv"]]
+    f_gpu, i_gpu = ctx.ntt_tables(0)
+    f_ref, i_ref = p.tables()
+    assert np.array_equal(f_gpu, f_ref)
+    assert np.array_equal(i_gpu, i_ref)
+
+
+def test_context_validation(sg):
+    with pytest.raises(sg.ShgError, match="less than 2\\^62"):
+        sg.Context(4, [1 << 62 | 1])
+    with pytest.raises(sg.ShgError, match="should be odd"):
+        sg.Context(4, [1 << 40])
+    with pytest.raises(sg.ShgError, match="not 1 mod 2n"):
+        sg.Context(14, [Q59])  # 2^13 | q-1 only
+    with pytest.raises(sg.ShgError, match="plaintext_modulus"):
+        sg.Context(4, [Q45[0]], t=0)
+    with pytest.raises(sg.ShgError, match="must be positive"):
+        sg.Context(0, [Q45[0]])
+
+
+# --------------------------------------------------------------------------
+# NTT
+# --------------------------------------------------------------------------
+
+NTT_CASES = [(log_n, qs) for log_n in range(1, 15) for qs in ([Q45[0], Q45[1]],)] + [
+    (12, [Q59]), (12, [Q60]), (11, Q50[:4]), (13, Q50[:3]), (14, Q45)]
+
+
+@pytest.mark.parametrize("log_n,qs", NTT_CASES)
+def test_ntt_forward_inverse(sg, oracle, log_n, qs):
+    n = 1 << log_n
+    count = 3
+    x = oracle.uniform_limbs(100 + log_n, qs, n, count)
+    rns = oracle.Rns(log_n, qs)
+    want = np.stack([rns.ntt_fwd(x[i]) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    d = _dev(sg, x)
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, d.ptr, count, len(qs), None)
+    got = d.download(x.shape)
+    assert np.array_equal(got, want)
+    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, d.ptr, count, len(qs), None)
+    assert np.array_equal(d.download(x.shape), x)
+    # inverse alone vs oracle on fresh data
+    y = oracle.uniform_limbs(200 + log_n, qs, n, count)
+    want_inv = np.stack([rns.ntt_inv(y[i]) for i in range(count)])
+    d2 = _dev(sg, y)
+    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, d2.ptr, count, len(qs), None)
+    assert np.array_equal(d2.download(y.shape), want_inv)
+
+
+def test_ntt_delta_is_constant(sg, oracle):
+    """dft_transformations_test.cc:84-110: NTT(delta) is a constant vector."""
+    q, log_n = Q50[0], 13
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    one = p.import_(np.array([1], np.uint64))[0]
+    x = np.zeros((1, 1, n), np.uint64)
+    x[0, 0, 0] = one
+    ctx = sg.Context(log_n, [q])
+    d = _dev(sg, x)
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, d.ptr, 1, 1, None)
+    got = d.download(x.shape)
+    assert np.all(got == one)
+
+
+def test_ntt_product_is_negacyclic_schoolbook(sg, oracle):
+    """polynomial_test.cc:310-337."""
+    q, log_n = Q59, 6
+    n = 1 << log_n
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, q, n, dtype=np.uint64)
+    b = rng.integers(0, q, n, dtype=np.uint64)
+    p = oracle.Prime(q, log_n)
+    ctx = sg.Context(log_n, [q])
+    da = _dev(sg, p.import_(a).reshape(1, 1, n))
+    db = _dev(sg, p.import_(b).reshape(1, 1, n))
+    lib = sg.lib()
+    for d in (da, db):
+        _run(sg, lib.shg_ntt_forward, ctx.h, d.ptr, 1, 1, None)
+    _run(sg, lib.shg_poly_mul, ctx.h, da.ptr, da.ptr, db.ptr, 1, 1, None)
+    _run(sg, lib.shg_ntt_inverse, ctx.h, da.ptr, 1, 1, None)
+    got = [int(v) for v in p.export(da.download((n,)))]
+    ai, bi = [int(v) for v in a], [int(v) for v in b]
+    ref = [0] * n
+    for i in range(n):
+        for j in range(n):
+            k = i + j
+            if k >= n:
+                ref[k - n] -= ai[i] * bi[j]
+            else:
+                ref[k] += ai[i] * bi[j]
+    assert got == [r % q for r in ref]
+
+
+# --------------------------------------------------------------------------
+# Pointwise ops
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("log_n,qs", [(4, Q45[:2]), (12, Q50[:5]), (14, Q45)])
+def test_pointwise_ops(sg, oracle, log_n, qs):
+    n = 1 << log_n
+    count, L = 2, len(qs)
+    a = oracle.uniform_limbs(7, qs, n, count)
+    b = oracle.uniform_limbs(8, qs, n, count)
+    a[0, 0, :4] = 0  # negation of zero yields q in the reference
+    c = oracle.uniform_limbs(9, qs, n, count)
+    rns = oracle.Rns(log_n, qs)
+    P = rns.primes
+    ctx = sg.Context(log_n, qs)
+    lib = sg.lib()
+    da, db, dc = _dev(sg, a), _dev(sg, b), _dev(sg, c)
+    out = sg.DeviceBuffer(a.nbytes)
+
+    def per_limb(fn):
+        return np.stack([np.stack([fn(P[l], i, l) for l in range(L)]) for i in range(count)])
+
+    cases = {
+        "add": (lib.shg_poly_add, (out.ptr, da.ptr, db.ptr),
+                per_limb(lambda p, i, l: p.add(a[i, l], b[i, l]))),
+        "sub": (lib.shg_poly_sub, (out.ptr, da.ptr, db.ptr),
+                per_limb(lambda p, i, l: p.sub(a[i, l], b[i, l]))),
+        "mul": (lib.shg_poly_mul, (out.ptr, da.ptr, db.ptr),
+                per_limb(lambda p, i, l: p.mul(a[i, l], b[i, l]))),
+    }
+    for name, (fn, args, want) in cases.items():
+        _run(sg, fn, ctx.h, *args, count, L, None)
+        assert np.array_equal(out.download(a.shape), want), name
+    _run(sg, lib.shg_poly_neg, ctx.h, out.ptr, da.ptr, count, L, None)
+    want = per_limb(lambda p, i, l: p.neg(a[i, l]))
+    got = out.download(a.shape)
+    assert np.array_equal(got, want)
+    assert int(got[0, 0, 0]) == qs[0]
+    # neg output (holding q) fed back into add / mul stays exact
+    _run(sg, lib.shg_poly_add, ctx.h, out.ptr, out.ptr, out.ptr, count, L, None)
+    want2 = per_limb(lambda p, i, l: p.add(want[i, l], want[i, l]))
+    assert np.array_equal(out.download(a.shape), want2)
+    # fma: c += a*b
+    _run(sg, lib.shg_poly_fma, ctx.h, dc.ptr, da.ptr, db.ptr, count, L, None)
+    want = per_limb(lambda p, i, l: p.fma(c[i, l], a[i, l], b[i, l]))
+    assert np.array_equal(dc.download(a.shape), want)
+    # RNS scalar (Montgomery) and integer scalar
+    sc = np.array([P[l].import_(np.array([12345 + l], np.uint64))[0] for l in range(L)],
+                  np.uint64)
+    _run(sg, lib.shg_poly_mul_rns_scalar, ctx.h, out.ptr, da.ptr, sc.ctypes.data_as(
+        __import__("ctypes").POINTER(__import__("ctypes").c_uint64)), count, L, None)
+    want = per_limb(lambda p, i, l: p.mul_scalar(a[i, l], sc[l]))
+    assert np.array_equal(out.download(a.shape), want)
+    _run(sg, lib.shg_poly_mul_integer, ctx.h, out.ptr, da.ptr, 65537, count, L, None)
+    want = per_limb(lambda p, i, l: p.mul_scalar(a[i, l], p.import_(np.array([65537],
+                                                                              np.uint64))[0]))
+    assert np.array_equal(out.download(a.shape), want)
+
+
+# --------------------------------------------------------------------------
+# Substitute
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("log_n,power", [(3, 3), (6, 5), (10, 1023), (12, 4097), (14, 5),
+                                         (14, 2 * 16384 - 1), (13, 1)])
+def test_substitute(sg, oracle, log_n, power):
+    qs = Q45[:3]
+    n = 1 << log_n
+    x = oracle.uniform_limbs(31, qs, n, 2)
+    rns = oracle.Rns(log_n, qs)
+    want = np.stack([rns.substitute(x[i], power) for i in range(2)])
+    ctx = sg.Context(log_n, qs)
+    d, out = _dev(sg, x), sg.DeviceBuffer(x.nbytes)
+    _run(sg, sg.lib().shg_poly_substitute, ctx.h, out.ptr, d.ptr, power, 2, len(qs), None)
+    assert np.array_equal(out.download(x.shape), want)
+
+
+def test_substitute_validation(sg):
+    ctx = sg.Context(4, [Q45[0]])
+    d, out = sg.DeviceBuffer(16 * 8), sg.DeviceBuffer(16 * 8)
+    for bad in (2, -1, 32, 33):
+        with pytest.raises(sg.ShgError, match="Substitution power"):
+            sg.check(sg.lib().shg_poly_substitute(ctx.h, out.ptr, d.ptr, bad, 1, 1, None))
+
+
+# --------------------------------------------------------------------------
+# Ciphertext tensor, key switching
+# --------------------------------------------------------------------------
+
+def _ct_pair(oracle, qs, n, count, seed):
+    a = oracle.uniform_limbs(seed, qs, n, 2 * count).reshape(count, 2, len(qs), n)
+    b = oracle.uniform_limbs(seed + 1, qs, n, 2 * count).reshape(count, 2, len(qs), n)
+    return a, b
+
+
+@pytest.mark.parametrize("log_n,qs", [(5, Q45[:2]), (12, Q50[:4]), (14, Q45)])
+def test_tensor(sg, oracle, log_n, qs):
+    n, count = 1 << log_n, 2
+    a, b = _ct_pair(oracle, qs, n, count, 40)
+    rns = oracle.Rns(log_n, qs)
+    want = np.stack([rns.tensor(a[i], b[i]) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    da, db = _dev(sg, a), _dev(sg, b)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_ct_tensor, ctx.h, out.ptr, da.ptr, db.ptr, count, len(qs), None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+KS_CASES = [
+    (4, Q45[:2], [20, 20]),
+    (10, Q45[:3], [20, 20, 20]),
+    (12, Q50[:4], [20, 20, 20, 20]),
+    (11, Q50[:2], [50, 16]),        # a full-width digit exercises the balanced lift
+    (14, Q45, [20] * 6),           # the ct-mult+relin workload's parameters
+]
+
+
+@pytest.mark.parametrize("log_n,qs,log_bs", KS_CASES)
+def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs):
+    n, L = 1 << log_n, len(qs)
+    count = 2 if log_n < 14 else 1
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    kb = oracle.uniform_limbs(50, qs, n, k)
+    ka = oracle.uniform_limbs(51, qs, n, k)
+    a, b = _ct_pair(oracle, qs, n, count, 52)
+    ct3 = np.stack([rns.tensor(a[i], b[i]) for i in range(count)])
+    want = np.stack([rns.relin(ct3[i], kb, ka, log_bs) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, log_bs, 1, kb, ka)
+    assert key.dimension == k
+    lib = sg.lib()
+    d3 = _dev(sg, ct3)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, lib.shg_relin_apply, ctx.h, key.h, out.ptr, d3.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want)
+    da, db = _dev(sg, a), _dev(sg, b)
+    out2 = sg.DeviceBuffer(want.nbytes)
+    _run(sg, lib.shg_bgv_mul_relin, ctx.h, key.h, out2.ptr, da.ptr, db.ptr, count, None)
+    assert np.array_equal(out2.download(want.shape), want)
+
+
+@pytest.mark.parametrize("log_n,qs,log_bs,power", [
+    (4, Q45[:2], [20, 20], 5), (12, Q50[:3], [20, 20, 20], 5 ** 3 % 8192),
+    (13, Q50[:2], [50, 50], 8191), (14, Q45, [20] * 6, 5)])
+def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power):
+    n, L, count = 1 << log_n, len(qs), 2
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    kb = oracle.uniform_limbs(60, qs, n, k)
+    ka = oracle.uniform_limbs(61, qs, n, k)
+    ct = oracle.uniform_limbs(62, qs, n, 2 * count).reshape(count, 2, L, n)
+    want = np.stack([rns.galois(ct[i], kb, ka, log_bs) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, log_bs, power, kb, ka)
+    lib = sg.lib()
+    d = _dev(sg, ct)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, lib.shg_galois_apply, ctx.h, key.h, out.ptr, d.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want)
+    # rotate = Substitute(power) then Galois key switch
+    sub = np.stack([np.stack([rns.substitute(ct[i, c], power) for c in range(2)])
+                    for i in range(count)])
+    want_rot = np.stack([rns.galois(sub[i], kb, ka, log_bs) for i in range(count)])
+    _run(sg, lib.shg_bgv_rotate, ctx.h, key.h, out.ptr, d.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want_rot)
+
+
+def test_relin_rejects_galois_key(sg, oracle):
+    qs, log_n = Q45[:2], 4
+    n = 1 << log_n
+    kb = oracle.uniform_limbs(1, qs, n, 6)
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, [20, 20], 5, kb, kb)
+    d = sg.DeviceBuffer(3 * 2 * n * 8)
+    out = sg.DeviceBuffer(2 * 2 * n * 8)
+    with pytest.raises(sg.ShgError, match="power 1"):
+        sg.check(sg.lib().shg_relin_apply(ctx.h, key.h, out.ptr, d.ptr, 1, None))
+
+
+# --------------------------------------------------------------------------
+# ModReduceLsb
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("log_n,qs,is_ntt", [(4, Q45[:2], 1), (12, Q50[:5], 1),
+                                             (14, Q45, 1), (10, Q50[:4], 0), (14, Q45, 0)])
+def test_modreduce_lsb(sg, oracle, log_n, qs, is_ntt):
+    n, L, count, t = 1 << log_n, len(qs), 3, 65537
+    x = oracle.uniform_limbs(70, qs, n, count)
+    rns = oracle.Rns(log_n, qs)
+    want = np.stack([rns.modreduce_lsb(x[i], t, bool(is_ntt)) for i in range(count)])
+    ctx = sg.Context(log_n, qs, t)
+    ql_inv = ctx.ql_inv(L - 1)
+    assert np.array_equal(ql_inv, rns.ql_inv(L - 1))
+    d = _dev(sg, x)
+    out = sg.DeviceBuffer(want.nbytes)
+    import ctypes
+    _run(sg, sg.lib().shg_poly_modreduce_lsb, ctx.h, out.ptr, d.ptr, t,
+         ql_inv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), is_ntt, count, L, None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+# --------------------------------------------------------------------------
+# Single-modulus key switching, oblivious expansion, absorb
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("q,log_n,log_b", [(Q60, 7, 10), (Q60, 12, 8), (Q59, 9, 16)])
+def test_single_modulus_galois(sg, oracle, q, log_n, log_b):
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    dim = p.gadget_size(log_b)
+    k0 = oracle.uniform_limbs(80, [q], n, dim).reshape(dim, n)
+    k1 = oracle.uniform_limbs(81, [q], n, dim).reshape(dim, n)
+    ct = oracle.uniform_limbs(82, [q], n, 2).reshape(2, n)
+    want = p.galois_apply(log_b, ct, k0, k1)
+    ctx = sg.Context(log_n, [q])
+    key = sg.Key(ctx, [log_b], (n >> 1) + 1, k0, k1)
+    d = _dev(sg, ct)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_galois_apply, ctx.h, key.h, out.ptr, d.ptr, 1, None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+@pytest.mark.parametrize("q,log_n,levels,log_b,count", [(Q60, 7, 3, 10, 2), (Q60, 8, 8, 8, 1),
+                                                        (Q60, 12, 4, 8, 2)])
+def test_oblivious_expand(sg, oracle, q, log_n, levels, log_b, count):
+    import ctypes
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    dim = p.gadget_size(log_b)
+    keys = oracle.uniform_limbs(90, [q], n, levels * 2 * dim).reshape(levels, 2, dim, n)
+    cts = oracle.uniform_limbs(91, [q], n, 2 * count).reshape(count, 2, n)
+    want = np.stack([p.oblivious_expand(levels, log_b, keys, cts[i]) for i in range(count)])
+    ctx = sg.Context(log_n, [q])
+    gkeys = [sg.Key(ctx, [log_b], (n >> j) + 1, keys[j, 0], keys[j, 1]) for j in range(levels)]
+    arr = (ctypes.c_void_p * levels)(*[k.h for k in gkeys])
+    d = _dev(sg, cts)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_oblivious_expand, ctx.h, arr, levels, out.ptr, d.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+def test_absorb_sum(sg, oracle):
+    q, log_n, items, count = Q60, 10, 37, 2
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    cts = oracle.uniform_limbs(95, [q], n, count * items * 2).reshape(count, items, 2, n)
+    db = oracle.uniform_limbs(96, [q], n, items).reshape(items, n)
+    want = np.stack([p.absorb_sum(cts[i], db) for i in range(count)])
+    ctx = sg.Context(log_n, [q])
+    dc, dd = _dev(sg, cts), _dev(sg, db)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_absorb_sum, ctx.h, out.ptr, dc.ptr, dd.ptr, items, count, None)
+    assert np.array_equal(out.download(want.shape), want)
