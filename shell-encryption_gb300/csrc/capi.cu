@@ -800,9 +800,12 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
   // 197-200), built on the device from a coefficient vector.
   const size_t per_member = ((size_t)n + (size_t)kmax * n + 2 * (size_t)n) *
                             sizeof(uint64_t);
+  // A chunk holds whole queries, so it must fit the 2^(levels-1) members one
+  // query contributes at the last level.
   const int members_max = std::max(1, count << (levels - 1));
-  const int C = std::max(1, (int)std::min<size_t>((size_t)members_max,
-                                                  ((size_t)256 << 20) / per_member));
+  const int C = std::max(
+      1 << (levels - 1),
+      (int)std::min<size_t>((size_t)members_max, ((size_t)256 << 20) / per_member));
   std::lock_guard<std::mutex> lock(ctx->mu);
   const size_t mono_bytes = (size_t)levels * n * sizeof(uint64_t);
   if ((st = ctx->ensure_ws(mono_bytes + per_member * C))) return st;
