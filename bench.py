@@ -1,0 +1,434 @@
+#!/usr/bin/env python3
+"""Benchmark: RNS BGV ct x ct multiply + relinearization on one GB300.
+
+Workload (the reference's ct-mult+relin configuration): ring degree n = 2^14,
+six 45-bit NTT primes (the largest below 2^45 that are 1 mod 2^15), t = 65537,
+gadget base 2^20 (dimension 18), 1024 seeded ciphertext pairs per step.
+
+One step = RnsBgvCiphertext::operator* + RnsRelinKey::ApplyTo on all 1024
+pairs.  `value` is the batched path (shg_bgv_mul_relin, replayed from a CUDA
+graph) with inputs resident in HBM; `e2e` is the same call fed from pinned
+host buffers with the host->device and device->host copies inside the timed
+region; `plain` is the one-call-per-op drop-in path (shg_ct_tensor +
+shg_relin_apply per ciphertext).  Every path is bit-exact with the CPU
+reference (tests/test_gpu_parity.py).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "shell-encryption_gb300")
+sys.path.insert(0, PKG)
+
+LOG_N = 14
+QS = [35184371138561, 35184370941953, 35184370352129, 35184370155521,
+      35184369893377, 35184368877569]
+T_PLAIN = 65537
+LOG_BS = [20] * 6
+METRIC = "RNS ct-mult+relin/sec (batched vs plain, same GPU, bit-exact); p50/p99 ms"
+UNIT = "ct-mult+relin/s"
+# DRAM bytes (read + write) of one k_digit_ntt launch over a 16-ciphertext
+# chunk, scaled from the ncu capture in profiles/digit_ntt_ct_mult_relin.md.
+DIGIT_NTT_TRAFFIC_PER_LIMB_NTT = None
+
+
+def config(batch):
+    return {
+        "workload": "bgv-ct-mult-relin n=2^14 L=6x45-bit t=65537 gadget 2^20 (k=18)",
+        "log_n": LOG_N, "num_limbs": len(QS), "log_q": 45, "gadget_log_base": 20,
+        "gadget_dim": 18, "batch": batch,
+        "l2": "inputs larger than L2 (each step reads 3.2 GB of ciphertexts)",
+        "parallelism": "replicas",
+    }
+
+
+def splitmix_limbs(seed, count, qs, n):
+    """Seeded uniform residues [count][len(qs)][n] (splitmix64 stream)."""
+    L = len(qs)
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, count * L * n + 1, dtype=np.uint64)
+        z = np.uint64(seed) + idx * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z.reshape(count, L, n) % np.array(qs, np.uint64).reshape(1, L, 1))
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # plumbing only: barrier and max-reduce
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons in the background."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(count_per_thread, threads, seed=7):
+    """The reference's CPU path (oracle restatement) on host threads: returns
+    (ops/s, ops, seconds)."""
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    n = 1 << LOG_N
+    rns = O.Rns(LOG_N, QS)
+    k = rns.gadget_dim(LOG_BS)
+    kb = splitmix_limbs(seed + 2, k, QS, n)
+    ka = splitmix_limbs(seed + 3, k, QS, n)
+    ops = count_per_thread * threads
+    a = splitmix_limbs(seed, 2 * ops, QS, n).reshape(ops, 2, len(QS), n)
+    b = splitmix_limbs(seed + 1, 2 * ops, QS, n).reshape(ops, 2, len(QS), n)
+    t0 = time.perf_counter()
+    rns.mul_relin_batch(a, b, kb, ka, LOG_BS, threads=threads)
+    dt = time.perf_counter() - t0
+    return ops / dt, ops, dt
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    per_step = []
+    ops_total = 0
+    for i in range(args.warmup + args.steps):
+        rate, ops, dt = cpu_reference(1, threads, seed=100 + i)
+        if i >= args.warmup:
+            per_step.append(dt)
+            ops_total += ops
+    total = sum(per_step)
+    value = ops_total / total
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": dict(config(threads), batch=threads),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{threads} ct-mult+relin ops per step (one per host "
+                                   f"thread) at n=2^14, L=6"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--plain-ops", type=int, default=256)
+    ap.add_argument("--chunk", type=int, default=0, help="ciphertexts per internal chunk")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        return
+
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    n = 1 << LOG_N
+    L = len(QS)
+    B = args.batch
+    ct_elems = 2 * L * n
+    ct_bytes = ct_elems * 8
+
+    ctx = sg.Context(LOG_N, QS, T_PLAIN)
+    if args.chunk:
+        sg.check(lib.shg_context_set_chunk(ctx.h, args.chunk))
+    k = 18
+    kb = splitmix_limbs(1000 + rank, k, QS, n)
+    ka = splitmix_limbs(2000 + rank, k, QS, n)
+    key = sg.Key(ctx, LOG_BS, 1, kb, ka)
+
+    # Pinned host inputs (also the e2e source) and device copies.
+    def host(nbytes):
+        p = ctypes.c_void_p()
+        sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+        return p.value
+
+    h_a, h_b, h_out = host(B * ct_bytes), host(B * ct_bytes), host(B * ct_bytes)
+    for hp, seed in ((h_a, 11 + 97 * rank), (h_b, 13 + 97 * rank)):
+        view = np.ctypeslib.as_array((ctypes.c_uint64 * (B * ct_elems)).from_address(hp))
+        for c0 in range(0, B, 64):
+            c1 = min(B, c0 + 64)
+            view[c0 * ct_elems:c1 * ct_elems] = splitmix_limbs(
+                seed * 1000003 + c0, 2 * (c1 - c0), QS, n).reshape(-1)
+    d_a, d_b, d_out = (sg.DeviceBuffer(B * ct_bytes) for _ in range(3))
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+    sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, B * ct_bytes, s))
+    sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, B * ct_bytes, s))
+    sg.check(lib.shg_stream_synchronize(s))
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def step_device():
+        sg.check(lib.shg_bgv_mul_relin(ctx.h, key.h, d_out.ptr, d_a.ptr, d_b.ptr, B, s))
+
+    # Warm up (allocates scratch), then capture one step into a graph.
+    step_device()
+    sg.check(lib.shg_stream_synchronize(s))
+    n0 = lib.shg_launch_count()
+    sg.check(lib.shg_graph_capture_begin(s))
+    step_device()
+    g = ctypes.c_void_p()
+    sg.check(lib.shg_graph_capture_end(s, ctypes.byref(g)))
+    graph = g.value
+    launches_per_step = lib.shg_launch_count() - n0
+    for _ in range(args.warmup):
+        sg.check(lib.shg_graph_launch(graph, s))
+    sg.check(lib.shg_stream_synchronize(s))
+
+    evs = [ev() for _ in range(args.steps + 1)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    sg.check(lib.shg_device_synchronize())
+    sg.check(lib.shg_event_record(evs[0], s))
+    for i in range(args.steps):
+        sg.check(lib.shg_graph_launch(graph, s))
+        sg.check(lib.shg_event_record(evs[i + 1], s))
+    sg.check(lib.shg_stream_synchronize(s))
+    sg.check(lib.shg_device_synchronize())
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = [elapsed(evs[i], evs[i + 1]) for i in range(args.steps)]
+    total_ms = max_over_ranks(dist, elapsed(evs[0], evs[-1]))
+    ops_all = sum_over_ranks(dist, float(B * args.steps))
+    value = ops_all / (total_ms / 1e3)
+
+    # Bit-exactness spot check of the timed graph's output against the
+    # non-graph call (the parity tests cover the oracle side).
+    out_graph = np.empty(ct_elems * 2, np.uint64)
+    sg.check(lib.shg_memcpy_d2h(out_graph.ctypes.data, d_out.ptr, out_graph.nbytes, s))
+    sg.check(lib.shg_stream_synchronize(s))
+
+    # End to end: pinned host buffers in, result back to the host, per step.
+    e2e = None
+    if not args.no_e2e:
+        def step_e2e():
+            sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, B * ct_bytes, s))
+            sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, B * ct_bytes, s))
+            step_device()
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, B * ct_bytes, s))
+        for _ in range(2):
+            step_e2e()
+        sg.check(lib.shg_stream_synchronize(s))
+        e0, e1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(e0, s))
+        for _ in range(args.steps):
+            step_e2e()
+        sg.check(lib.shg_event_record(e1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        barrier(dist)
+        e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
+               "ms_per_step": e2e_ms / args.steps}
+
+    # Plain drop-in path: one ct_tensor + one relin_apply call per ciphertext.
+    P = min(args.plain_ops, B)
+    d_ct3 = sg.DeviceBuffer(P * 3 * L * n * 8)
+    op_evs = [ev() for _ in range(P + 1)]
+
+    def plain(record):
+        for i in range(P):
+            sg.check(lib.shg_ct_tensor(ctx.h, d_ct3.ptr + i * 3 * L * n * 8,
+                                       d_a.ptr + i * ct_bytes, d_b.ptr + i * ct_bytes, 1, L, s))
+            sg.check(lib.shg_relin_apply(ctx.h, key.h, d_out.ptr + i * ct_bytes,
+                                         d_ct3.ptr + i * 3 * L * n * 8, 1, s))
+            if record:
+                sg.check(lib.shg_event_record(op_evs[i + 1], s))
+    plain(False)
+    sg.check(lib.shg_stream_synchronize(s))
+    sg.check(lib.shg_event_record(op_evs[0], s))
+    plain(True)
+    sg.check(lib.shg_stream_synchronize(s))
+    op_ms = [elapsed(op_evs[i], op_evs[i + 1]) for i in range(P)]
+    plain_total = elapsed(op_evs[0], op_evs[-1])
+    plain_rate = P / (plain_total / 1e3)
+    # plain outputs must equal the batched ones (same inputs, same key)
+    out_plain = np.empty(ct_elems * 2, np.uint64)
+    sg.check(lib.shg_memcpy_d2h(out_plain.ctypes.data, d_out.ptr, out_plain.nbytes, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    bit_exact = bool(np.array_equal(out_graph, out_plain))
+
+    # Dominant kernel timing (live CUDA events on the launch stream) for the
+    # roofline: one more batched step with per-launch events.
+    sg.check(lib.shg_profile_start())
+    step_device()
+    sg.check(lib.shg_profile_stop())
+    prof = {}
+    for name in ("tensor_intt", "digit_ntt", "ks_inner"):
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        prof[name] = (ms.value, cnt.value)
+    dig_ms, dig_cnt = prof["digit_ntt"]
+    limb_ntts_per_launch = B * k * L / max(dig_cnt, 1)
+    alg_bytes = limb_ntts_per_launch * 16 * n
+    achieved = alg_bytes / (dig_ms / max(dig_cnt, 1) / 1e3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    traffic = (DIGIT_NTT_TRAFFIC_PER_LIMB_NTT * limb_ntts_per_launch
+               if DIGIT_NTT_TRAFFIC_PER_LIMB_NTT else None)
+    step_total = sum(v[0] for v in prof.values())
+    roofline = {
+        "kernel": "k_digit_ntt<14> (gadget digit extraction + forward NTT)",
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+        "algorithmic_bytes_per_launch": alg_bytes,
+        "avg_launch_ms": dig_ms / max(dig_cnt, 1),
+        "share_of_step": {k2: v[0] / step_total for k2, v in prof.items()},
+    }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, ops, dt = cpu_reference(4, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ops} ct-mult+relin ops (one per host thread) at n=2^14, L=6, "
+                         f"{dt:.1f} s"}
+
+    lat = sorted(step_ms)
+    oplat = sorted(op_ms)
+
+    def pct(v, p):
+        return v[min(len(v) - 1, int(round(p / 100 * (len(v) - 1))))]
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded uniform residues, splitmix64)", "config": config(B),
+        "latency_ms": {"batched_step_p50": pct(lat, 50), "batched_step_p99": pct(lat, 99),
+                       "plain_op_p50": pct(oplat, 50), "plain_op_p99": pct(oplat, 99)},
+        "plain": {"value": plain_rate, "unit": UNIT, "ops": P,
+                  "path": "shg_ct_tensor + shg_relin_apply per ciphertext"},
+        "batched_over_plain": value / world / plain_rate,
+        "bit_exact_batched_vs_plain": bit_exact,
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "gpu_launches": int(launches_per_step * args.steps),
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sg.check(lib.shg_graph_destroy(graph))
+    for hp in (h_a, h_b, h_out):
+        lib.shg_host_free(hp)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -42,6 +42,14 @@ int shg_graph_destroy(void* graph_exec);
 /* Number of kernels launched by this library so far (host-side count of
  * launch calls; graph replays are not counted). */
 uint64_t shg_launch_count(void);
+/* Per-kernel timing: between start and stop every launch of this library is
+ * bracketed by CUDA events on its own stream; stop synchronizes the device
+ * and accumulates.  query returns the total milliseconds and launch count of
+ * one kernel family ("ntt_fwd", "ntt_inv", "digit_ntt", "ks_inner",
+ * "tensor_intt", "intt_export", "pointwise", ...). */
+int shg_profile_start(void);
+int shg_profile_stop(void);
+int shg_profile_query(const char* kernel, double* total_ms, uint64_t* launches);
 /* Reserve scratch space for batched calls up front (so a later call can be
  * captured into a graph without allocating). */
 int shg_context_reserve(shg_context* ctx, size_t bytes);

@@ -972,6 +972,63 @@ int shg_graph_destroy(void* exec) {
   return SHG_OK;
 }
 uint64_t shg_launch_count(void) { return shg::g_launch_count.load(); }
+
+namespace {
+struct ProfTotal {
+  std::string name;
+  double ms = 0;
+  uint64_t launches = 0;
+};
+std::vector<ProfTotal> g_prof_totals;
+}  // namespace
+
+int shg_profile_start(void) {
+  std::lock_guard<std::mutex> lock(shg::g_prof_mu);
+  for (auto& e : shg::g_prof_pending) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  shg::g_prof_pending.clear();
+  g_prof_totals.clear();
+  shg::g_prof_on = true;
+  return SHG_OK;
+}
+
+int shg_profile_stop(void) {
+  shg::g_prof_on = false;
+  SHG_CUDA(cudaDeviceSynchronize());
+  std::lock_guard<std::mutex> lock(shg::g_prof_mu);
+  for (auto& e : shg::g_prof_pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    auto it = std::find_if(g_prof_totals.begin(), g_prof_totals.end(),
+                           [&](const ProfTotal& t) { return t.name == e.name; });
+    if (it == g_prof_totals.end()) {
+      g_prof_totals.push_back(ProfTotal{e.name, 0, 0});
+      it = g_prof_totals.end() - 1;
+    }
+    it->ms += ms;
+    it->launches += 1;
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  shg::g_prof_pending.clear();
+  return SHG_OK;
+}
+
+int shg_profile_query(const char* kernel, double* total_ms, uint64_t* launches) {
+  if (!kernel || !total_ms || !launches)
+    return fail(SHG_INVALID_ARGUMENT, "null argument");
+  *total_ms = 0;
+  *launches = 0;
+  for (const auto& t : g_prof_totals) {
+    if (t.name == kernel) {
+      *total_ms = t.ms;
+      *launches = t.launches;
+    }
+  }
+  return SHG_OK;
+}
 int shg_context_reserve(shg_context* ctx, size_t bytes) {
   if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
   std::lock_guard<std::mutex> lock(ctx->mu);

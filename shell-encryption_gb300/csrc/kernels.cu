@@ -9,8 +9,34 @@
 namespace shg {
 
 std::atomic<uint64_t> g_launch_count{0};
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+std::vector<ProfEntry> g_prof_pending;
 
 namespace {
+
+// Counts every launch; with profiling on, brackets it with CUDA events on the
+// launch stream (these also work inside stream capture).
+struct LaunchScope {
+  const char* name;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LaunchScope(const char* n, cudaStream_t st) : name(n), s(st) {
+    g_launch_count++;
+    if (g_prof_on.load()) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~LaunchScope() {
+    if (a) {
+      cudaEventRecord(b, s);
+      std::lock_guard<std::mutex> lock(g_prof_mu);
+      g_prof_pending.push_back(ProfEntry{name, a, b});
+    }
+  }
+};
 
 template <int LOG_N>
 struct Cfg {
@@ -581,6 +607,7 @@ int blocks_for(int num) {
 void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                     int L, cudaStream_t s) {
   if (num <= 0) return;
+  LaunchScope scope_("ntt_fwd", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_ntt_fwd<LN>;                                                \
@@ -590,7 +617,6 @@ void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
@@ -598,6 +624,7 @@ static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
                                   int in_stride, int mode, uint64_t sw,
                                   uint64_t swp, cudaStream_t s) {
   if (num <= 0) return;
+  LaunchScope scope_("ntt_inv", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_ntt_inv<LN>;                                                \
@@ -607,7 +634,6 @@ static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 void launch_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
@@ -621,27 +647,27 @@ void launch_pointwise(const CtxDev& c, PwOp op, uint64_t* out, const uint64_t* a
                       cudaStream_t s) {
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
+  LaunchScope scope_("pointwise", s);
   k_pointwise<<<grid_for(total / 2, 256), 256, 0, s>>>(op, out, a, b, sc, total,
                                                        c.log_n, L, c);
-  g_launch_count++;
 }
 
 void launch_substitute(const CtxDev& c, uint64_t* out, const uint64_t* in,
                        int power, int count, int L, cudaStream_t s) {
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
+  LaunchScope scope_("substitute", s);
   k_substitute<<<grid_for(total, 256), 256, 0, s>>>(out, in, power, total,
                                                     c.log_n);
-  g_launch_count++;
 }
 
 void launch_tensor(const CtxDev& c, uint64_t* out, const uint64_t* a,
                    const uint64_t* b, int count, int L, cudaStream_t s) {
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
+  LaunchScope scope_("tensor", s);
   k_tensor<<<grid_for(total, 256), 256, 0, s>>>(out, a, b, total, c.log_n, L,
                                                 c);
-  g_launch_count++;
 }
 
 void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
@@ -649,6 +675,7 @@ void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
                         cudaStream_t s) {
   const int num = count * L;
   if (num <= 0) return;
+  LaunchScope scope_("tensor_intt", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_tensor_intt<LN>;                                            \
@@ -658,7 +685,6 @@ void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
@@ -666,6 +692,7 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
                         int count, int L, cudaStream_t s) {
   const int num = count * L;
   if (num <= 0) return;
+  LaunchScope scope_("intt_export", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_intt_export<LN>;                                            \
@@ -675,7 +702,6 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
@@ -683,6 +709,7 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       int L, cudaStream_t s) {
   const int num = count * k * L;
   if (num <= 0) return;
+  LaunchScope scope_("digit_ntt", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_digit_ntt<LN>;                                              \
@@ -692,7 +719,6 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
@@ -702,10 +728,10 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
                      cudaStream_t s) {
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
+  LaunchScope scope_("ks_inner", s);
   k_ks_inner<<<grid_for(total, 256), 256, 0, s>>>(
       out, D, kb, ka, k, chunk, base, base_ct_elems, map, base1_zero,
       subst_power, total, c.log_n, L, c);
-  g_launch_count++;
 }
 
 void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
@@ -718,6 +744,7 @@ void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
   // folded into one scale k * n^{-1} * 2^-64 -> Y [count][n] plain.
   launch_ntt_inv_scaled(c, in, Y, count, L, L - 1, L, 2, k_plain, k_shoup, s);
   // Stage 2: lift, forward NTT, combine.
+  LaunchScope scope_("modreduce_lift", s);
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_modreduce_lift<LN>;                                         \
@@ -728,7 +755,6 @@ void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
   }
   SHG_DISPATCH_LOGN(c.log_n, F)
 #undef F
-  g_launch_count++;
 }
 
 void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
@@ -737,9 +763,9 @@ void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
                             cudaStream_t s) {
   const size_t total = (size_t)count * (L - 1) * c.n;
   if (total == 0) return;
+  LaunchScope scope_("modreduce_coeff", s);
   k_modreduce_coeff<<<grid_for(total, 256), 256, 0, s>>>(
       out, in, k_plain, k_shoup, sc, total, c.log_n, L, c);
-  g_launch_count++;
 }
 
 void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
@@ -747,9 +773,9 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            int count, cudaStream_t s) {
   const size_t total = (size_t)count * 2 * c.n;
   if (total == 0) return;
+  LaunchScope scope_("expand_combine", s);
   k_expand_combine<<<grid_for(total, 256), 256, 0, s>>>(base, ks, mono, map,
                                                         half, total, c.log_n, c);
-  g_launch_count++;
 }
 
 void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
@@ -757,9 +783,9 @@ void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
                        cudaStream_t s) {
   const size_t total = (size_t)count * 2 * c.n;
   if (total == 0) return;
+  LaunchScope scope_("absorb_sum", s);
   k_absorb_sum<<<grid_for(total, 256), 256, 0, s>>>(out, cts, db, num_items,
                                                     chunk, total, c.log_n, c);
-  g_launch_count++;
 }
 
 }  // namespace shg

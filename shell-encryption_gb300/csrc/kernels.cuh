@@ -4,6 +4,8 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <mutex>
+#include <vector>
 
 #include "modarith.cuh"
 #include "ntt.cuh"
@@ -50,6 +52,16 @@ struct CtMap {
 
 // Number of kernels this library has launched (host-side counter).
 extern std::atomic<uint64_t> g_launch_count;
+
+// Optional per-kernel timing: while g_prof_on is set every launch is
+// bracketed by a pair of CUDA events recorded on its stream.
+struct ProfEntry {
+  const char* name;
+  cudaEvent_t a, b;
+};
+extern std::atomic<bool> g_prof_on;
+extern std::mutex g_prof_mu;
+extern std::vector<ProfEntry> g_prof_pending;
 
 // `num` limb transforms; limb index of transform g is g % L.
 void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
@@ -101,7 +113,8 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
 // Key inner product, per ciphertext p and limb:
 //   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
 // kb/ka hold the key premultiplied by 2^64 mod q (so REDC lands in Montgomery
-// form); `chunk` products are summed per REDC (chunk * q < 2^64).  out [count][2][L][n]; base component c of member p lives at
+// form); `chunk` products are summed per REDC (chunk * q < 2^64).
+// out [count][2][L][n]; base component c of member p lives at
 // base + map(p) * base_ct_elems + c * L * n; base1_zero drops base1.  If
 // subst_power > 0, base0 is read through that substitution.
 void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,

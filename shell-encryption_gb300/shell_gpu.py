@@ -81,6 +81,10 @@ SIGNATURES = {
     "shg_graph_launch": (ctypes.c_int, [_vp, _vp]),
     "shg_graph_destroy": (ctypes.c_int, [_vp]),
     "shg_launch_count": (ctypes.c_uint64, []),
+    "shg_profile_start": (ctypes.c_int, []),
+    "shg_profile_stop": (ctypes.c_int, []),
+    "shg_profile_query": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_uint64)]),
     "shg_context_reserve": (ctypes.c_int, [_vp, _sz]),
     "shg_context_set_chunk": (ctypes.c_int, [_vp, ctypes.c_int]),
 }
