@@ -158,6 +158,25 @@ size_t shg_key_device_bytes(const shg_key* key);
  * ct [count][3][L][n] (NTT) -> out [count][2][L][n].  out may not alias ct. */
 int shg_relin_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
                     const uint64_t* ct, int count, shg_stream stream);
+/* Allocation-free variant of shg_relin_apply; it has no counterpart in the
+ * reference.  It is for callers that may not allocate device memory during a
+ * call (memory handed out by an external pool or arena, a device budget owned
+ * by another component, or a latency-critical path where an allocation's
+ * implicit synchronization would stall other streams).  Its scratch is a
+ * fixed 32 MiB array inside the library's device image (held on every GPU
+ * that loads the library until the process exits); the call allocates and
+ * frees nothing.  Inputs, outputs and results are those of shg_relin_apply.
+ * Limit: one ciphertext's scratch, n * num_limbs * (1 + gadget dimension) * 8
+ * bytes, must fit in 32 MiB (n = 2^14 with 6 limbs and dimension 18 needs
+ * 14.9 MiB); larger shapes return SHG_INVALID_ARGUMENT.  Batches larger than
+ * the scratch are processed in chunks.  The first call on each device looks
+ * up the array's device address (with that device current) and should come
+ * before any stream capture.  All calls on a device share the one array, so
+ * calls whose work overlaps on the GPU (different streams, or host threads)
+ * race: serialize them on one stream. */
+int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key, uint64_t* out,
+                            const uint64_t* ct, int count, shg_stream stream);
+
 /* RnsGaloisKey::ApplyTo (rns/rns_galois_key.h:146-156, .cc:238-287) on
  * ciphertexts already substituted to the key's power: ct [count][2][L][n]
  * -> out [count][2][L][n]. */

@@ -1041,3 +1041,97 @@ int shg_context_set_chunk(shg_context* ctx, int cts) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free relinearization.
+//
+// Some callers of this library cannot allocate device memory while they run:
+// a host process whose GPU memory is handed out by an external pool or arena
+// manager that forbids cudaMalloc, code running while another component holds
+// the whole device budget, or a real-time request path where an allocation's
+// implicit device synchronization would stall other streams.  For them,
+// shg_relin_apply_noalloc runs the same key-switch kernels as
+// shg_relin_apply, but its scratch lives in the fixed array below, which is
+// part of the library's device image: every GPU that loads the library holds
+// these bytes until the process exits, and no call allocates or frees.
+// ---------------------------------------------------------------------------
+
+// Scratch of the allocation-free entry point: the exported source limbs and
+// the NTT'd digits of one chunk of ciphertexts.  Both are completely
+// overwritten before they are read, so nothing needs clearing between calls.
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB
+static __device__ __align__(256) uint64_t
+    g_noalloc_scratch[kNoAllocScratchBytes / sizeof(uint64_t)];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint64_t* g_noalloc_dev_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  In host code
+// `g_noalloc_scratch` only names a host-side shadow, so the address must come
+// from cudaGetSymbolAddress, taken once per device while that device is
+// current (this is the set-up done by the first call on each device).
+int noalloc_scratch(int device, uint64_t** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return fail(SHG_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_dev_ptr[device] == nullptr) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+    g_noalloc_dev_ptr[device] = static_cast<uint64_t*>(p);
+  }
+  *out = g_noalloc_dev_ptr[device];
+  return SHG_OK;
+}
+
+}  // namespace
+
+extern "C" int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key,
+                                       uint64_t* out, const uint64_t* ct,
+                                       int count, shg_stream stream) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (key->power != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Relinearization key can only apply to a ciphertext of power 1.");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  int device = -1;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (device != ctx->device)
+    return fail(SHG_FAILED_PRECONDITION,
+                "call shg_relin_apply_noalloc with the context's device current");
+  const int L = key->L, n = ctx->n, k = key->k;
+  const size_t Ln = (size_t)L * n;
+  const size_t per_ct = (Ln + (size_t)k * Ln) * sizeof(uint64_t);
+  if (per_ct > kNoAllocScratchBytes)
+    return fail(SHG_INVALID_ARGUMENT,
+                "shg_relin_apply_noalloc: one ciphertext needs " +
+                    std::to_string(per_ct) +
+                    " bytes of scratch (n * limbs * (1 + gadget dimension) * 8) "
+                    "but the fixed scratch holds " +
+                    std::to_string(kNoAllocScratchBytes) + " bytes");
+  uint64_t* scratch = nullptr;
+  if ((st = noalloc_scratch(device, &scratch))) return st;
+  const int C = (int)std::min<size_t>((size_t)count, kNoAllocScratchBytes / per_ct);
+  uint64_t* X = scratch;
+  uint64_t* D = X + (size_t)C * Ln;
+  cudaStream_t s = (cudaStream_t)stream;
+  const CtxDev dv = ctx->dev();
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    const uint64_t* src = ct + (size_t)c0 * 3 * Ln;
+    shg::launch_intt_export(dv, X, src, 3, 2, 0, CtMap::identity(), cc, L, s);
+    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
+    shg::launch_ks_inner(dv, out + (size_t)c0 * 2 * Ln, D, key->kb, key->ka, k,
+                         key->chunk, src, 3 * Ln, CtMap::identity(), 0, 0, cc,
+                         L, s);
+  }
+  return launch_status("relin_apply_noalloc");
+}

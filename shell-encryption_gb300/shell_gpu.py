@@ -51,6 +51,7 @@ SIGNATURES = {
     "shg_key_dimension": (ctypes.c_int, [_vp]),
     "shg_key_device_bytes": (_sz, [_vp]),
     "shg_relin_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_relin_apply_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_galois_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_rotate": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
