@@ -1,0 +1,336 @@
+// Test infrastructure: a C interface over google/shell-encryption's own
+// hot-path classes, compiled in place from the reference sources (see
+// oracle/ref/Makefile).  It lets the golden-vector generator run the real
+// reference on seeded inputs; the product never links it.
+//
+// Keys are built from given components (key data, not key generation), which
+// needs the private constructors of RnsRelinKey / RelinearizationKey /
+// GaloisKey; the reference headers are therefore included with class
+// member access opened up for this translation unit only.
+
+// Standard headers first, with normal access control.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <iomanip>
+#include <iostream>
+#include <iterator>
+#include <limits>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <optional>
+#include <random>
+#include <sstream>
+#include <string>
+#include <string_view>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "absl/numeric/int128.h"
+#include "absl/status/status.h"
+#include "absl/status/statusor.h"
+#include "absl/strings/str_cat.h"
+#include "absl/types/span.h"
+
+#define private public
+#define protected public
+#include "shell_encryption/dft_transformations.h"
+#include "shell_encryption/gadget.h"
+#include "shell_encryption/galois_key.h"
+#include "shell_encryption/montgomery.h"
+#include "shell_encryption/ntt_parameters.h"
+#include "shell_encryption/oblivious_expand.h"
+#include "shell_encryption/polynomial.h"
+#include "shell_encryption/relinearization_key.h"
+#include "shell_encryption/rns/rns_bgv_ciphertext.h"
+#include "shell_encryption/rns/rns_context.h"
+#include "shell_encryption/rns/rns_error_params.h"
+#include "shell_encryption/rns/rns_gadget.h"
+#include "shell_encryption/rns/rns_galois_key.h"
+#include "shell_encryption/rns/rns_polynomial.h"
+#include "shell_encryption/rns/rns_relinearization_key.h"
+#include "shell_encryption/symmetric_encryption.h"
+#undef private
+#undef protected
+
+using M = rlwe::MontgomeryInt<uint64_t>;
+using Params = M::Params;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(const absl::Status& s) {
+  g_err = std::string(s.message());
+  return s.code() == absl::StatusCode::kOk ? 0 : (int)s.code();
+}
+
+struct Prime {
+  std::unique_ptr<const Params> params;
+  rlwe::NttParameters<M> ntt;
+};
+
+int make_prime(uint64_t q, int log_n, Prime* p) {
+  auto params = Params::Create(q);
+  if (!params.ok()) return fail(params.status());
+  p->params = std::move(*params);
+  auto ntt = rlwe::InitializeNttParameters<M>(log_n, p->params.get());
+  if (!ntt.ok()) return fail(ntt.status());
+  p->ntt = std::move(*ntt);
+  return 0;
+}
+
+std::vector<M> to_vec(const uint64_t* a, size_t n) {
+  std::vector<M> v;
+  v.reserve(n);
+  for (size_t i = 0; i < n; ++i) v.push_back(M(a[i]));
+  return v;
+}
+
+void from_vec(const std::vector<M>& v, uint64_t* out) {
+  for (size_t i = 0; i < v.size(); ++i) out[i] = v[i].GetMontgomeryRepresentation();
+}
+
+using Ctx = rlwe::RnsContext<M>;
+
+std::unique_ptr<Ctx> make_ctx(int log_n, const uint64_t* qs, int L, uint64_t t,
+                              int* st) {
+  auto ctx = Ctx::Create(log_n, std::vector<uint64_t>(qs, qs + L), {}, t);
+  if (!ctx.ok()) {
+    *st = fail(ctx.status());
+    return nullptr;
+  }
+  *st = 0;
+  return std::make_unique<Ctx>(std::move(*ctx));
+}
+
+rlwe::RnsPolynomial<M> make_poly(const uint64_t* data, int L, int n, bool is_ntt) {
+  std::vector<std::vector<M>> cv;
+  for (int l = 0; l < L; ++l) cv.push_back(to_vec(data + (size_t)l * n, n));
+  return rlwe::RnsPolynomial<M>(rlwe::RnsPolynomial<M>::Create(std::move(cv), is_ntt).value());
+}
+
+void store_poly(const rlwe::RnsPolynomial<M>& p, uint64_t* out) {
+  const auto& cv = p.Coeffs();
+  size_t n = cv[0].size();
+  for (size_t l = 0; l < cv.size(); ++l) from_vec(cv[l], out + l * n);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error(void) { return g_err.c_str(); }
+
+// NttParameters tables (Montgomery reps) and constants of one prime.
+int ref_prime_tables(uint64_t q, int log_n, uint64_t* fwd, uint64_t* inv,
+                     uint64_t* n_inv) {
+  Prime p;
+  int st = make_prime(q, log_n, &p);
+  if (st) return st;
+  from_vec(p.ntt.psis_bitrev, fwd);
+  from_vec(p.ntt.psis_inv_bitrev, inv);
+  *n_inv = p.ntt.n_inv_ptr->GetMontgomeryRepresentation();
+  return 0;
+}
+
+// ForwardNumberTheoreticTransform / InverseNumberTheoreticTransform on
+// `count` vectors of n Montgomery residues, in place.
+int ref_ntt(uint64_t q, int log_n, uint64_t* data, int count, int inverse) {
+  Prime p;
+  int st = make_prime(q, log_n, &p);
+  if (st) return st;
+  const int n = 1 << log_n;
+  for (int c = 0; c < count; ++c) {
+    std::vector<M> v = to_vec(data + (size_t)c * n, n);
+    absl::Status s = inverse
+                         ? rlwe::InverseNumberTheoreticTransform(v, p.ntt, *p.params)
+                         : rlwe::ForwardNumberTheoreticTransform(v, p.ntt, *p.params);
+    if (!s.ok()) return fail(s);
+    from_vec(v, data + (size_t)c * n);
+  }
+  return 0;
+}
+
+// RnsPolynomial::Substitute.
+int ref_rns_substitute(int log_n, const uint64_t* qs, int L, int power,
+                       const uint64_t* in, uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  auto p = make_poly(in, L, 1 << log_n, true);
+  auto r = p.Substitute(power, ctx->MainPrimeModuli());
+  if (!r.ok()) return fail(r.status());
+  store_poly(*r, out);
+  return 0;
+}
+
+// RnsPolynomial::ModReduceLsb with ql_inv from MainPrimeModulusInverseResidues.
+int ref_rns_modreduce_lsb(int log_n, const uint64_t* qs, int L, uint64_t t,
+                          int is_ntt, const uint64_t* in, uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, t, &st);
+  if (!ctx) return st;
+  auto p = make_poly(in, L, 1 << log_n, is_ntt != 0);
+  auto ql_inv = ctx->MainPrimeModulusInverseResidues()[L - 1].Prefix(L - 1);
+  absl::Status s = p.ModReduceLsb(t, ql_inv, ctx->MainPrimeModuli());
+  if (!s.ok()) return fail(s);
+  store_poly(p, out);
+  return 0;
+}
+
+// RnsBgvCiphertext::operator* followed by RnsRelinKey::ApplyTo, on `count`
+// pairs a, b [count][2][L][n] with key components [k][L][n]; also returns the
+// degree-2 product in prod [count][3][L][n] when prod is not null.
+int ref_bgv_mul_relin(int log_n, const uint64_t* qs, int L, uint64_t t,
+                      const int* log_bs, const uint64_t* key_b,
+                      const uint64_t* key_a, const uint64_t* a,
+                      const uint64_t* b, int count, uint64_t* prod,
+                      uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, t, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto q_hats = ctx->MainPrimeModulusComplements(L - 1).value();
+  auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(L - 1).value();
+  auto gadget = rlwe::RnsGadget<M>::Create(
+      log_n, std::vector<size_t>(log_bs, log_bs + L), q_hats, q_hat_invs, moduli);
+  if (!gadget.ok()) return fail(gadget.status());
+  const int k = gadget->Dimension();
+  std::vector<rlwe::RnsPolynomial<M>> kas, kbs;
+  for (int j = 0; j < k; ++j) {
+    kbs.push_back(make_poly(key_b + (size_t)j * P, L, n, true));
+    kas.push_back(make_poly(key_a + (size_t)j * P, L, n, true));
+  }
+  rlwe::RnsRelinKey<M> key(std::move(kas), std::move(kbs), &*gadget,
+                           /*degree=*/2, moduli, "", rlwe::PRNG_TYPE_HKDF);
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, {}, 16, 3.19);
+  if (!ep.ok()) return fail(ep.status());
+  for (int c = 0; c < count; ++c) {
+    std::vector<rlwe::RnsPolynomial<M>> ca, cb;
+    for (int i = 0; i < 2; ++i) {
+      ca.push_back(make_poly(a + ((size_t)c * 2 + i) * P, L, n, true));
+      cb.push_back(make_poly(b + ((size_t)c * 2 + i) * P, L, n, true));
+    }
+    rlwe::RnsBgvCiphertext<M> x(std::move(ca), moduli, 1, 1.0, &*ep);
+    rlwe::RnsBgvCiphertext<M> y(std::move(cb), moduli, 1, 1.0, &*ep);
+    auto xy = x * y;
+    if (!xy.ok()) return fail(xy.status());
+    if (prod)
+      for (int i = 0; i < 3; ++i)
+        store_poly(xy->Component(i).value(), prod + ((size_t)c * 3 + i) * P);
+    auto r = key.ApplyTo(*xy);
+    if (!r.ok()) return fail(r.status());
+    for (int i = 0; i < 2; ++i)
+      store_poly(r->Component(i).value(), out + ((size_t)c * 2 + i) * P);
+  }
+  return 0;
+}
+
+// RnsBgvCiphertext::Substitute(power) then RnsGaloisKey::ApplyTo, with a key
+// built by RnsGaloisKey::CreateFromKeyComponents.
+int ref_bgv_rotate(int log_n, const uint64_t* qs, int L, const int* log_bs,
+                   int power, const uint64_t* key_b, const uint64_t* key_a,
+                   const uint64_t* ct, int count, uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto q_hats = ctx->MainPrimeModulusComplements(L - 1).value();
+  auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(L - 1).value();
+  auto gadget = rlwe::RnsGadget<M>::Create(
+      log_n, std::vector<size_t>(log_bs, log_bs + L), q_hats, q_hat_invs, moduli);
+  if (!gadget.ok()) return fail(gadget.status());
+  const int k = gadget->Dimension();
+  std::vector<rlwe::RnsPolynomial<M>> kas, kbs;
+  for (int j = 0; j < k; ++j) {
+    kbs.push_back(make_poly(key_b + (size_t)j * P, L, n, true));
+    kas.push_back(make_poly(key_a + (size_t)j * P, L, n, true));
+  }
+  auto key = rlwe::RnsGaloisKey<M>::CreateFromKeyComponents(
+      std::move(kas), std::move(kbs), power, &*gadget, moduli, "",
+      rlwe::PRNG_TYPE_HKDF);
+  if (!key.ok()) return fail(key.status());
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, {}, 16, 3.19);
+  if (!ep.ok()) return fail(ep.status());
+  for (int c = 0; c < count; ++c) {
+    std::vector<rlwe::RnsPolynomial<M>> comps;
+    for (int i = 0; i < 2; ++i)
+      comps.push_back(make_poly(ct + ((size_t)c * 2 + i) * P, L, n, true));
+    rlwe::RnsBgvCiphertext<M> x(std::move(comps), moduli, 1, 1.0, &*ep);
+    auto sub = x.Substitute(power);
+    if (!sub.ok()) return fail(sub.status());
+    auto r = key->ApplyTo(*sub);
+    if (!r.ok()) return fail(r.status());
+    for (int i = 0; i < 2; ++i)
+      store_poly(r->Component(i).value(), out + ((size_t)c * 2 + i) * P);
+  }
+  return 0;
+}
+
+// GaloisKeysObliviousExpander::ObliviousExpand of `count` ciphertexts [2][n]
+// with keys[levels][2][dim][n] (row 0 = the "b" row, row 1 = the random row)
+// for the substitution powers n/2^i + 1; out [count][2^levels][2][n].
+int ref_oblivious_expand(uint64_t q, int log_n, int log_t, int levels, int log_b,
+                         const uint64_t* keys, const uint64_t* ct, int count,
+                         uint64_t* out) {
+  Prime p;
+  int st = make_prime(q, log_n, &p);
+  if (st) return st;
+  const int n = 1 << log_n;
+  const int dim = rlwe::GadgetSize<M>(log_b, p.params.get());
+  auto ep = rlwe::ErrorParams<M>::Create(log_t, 8, p.params.get(), &p.ntt);
+  if (!ep.ok()) return fail(ep.status());
+  auto dm = M::ImportInt((uint64_t)1 << log_b, p.params.get()).value();
+  std::vector<rlwe::GaloisKey<M>> gks;
+  for (int j = 0; j < levels; ++j) {
+    std::vector<std::vector<rlwe::Polynomial<M>>> matrix(2);
+    for (int row = 0; row < 2; ++row)
+      for (int d = 0; d < dim; ++d)
+        matrix[row].push_back(rlwe::Polynomial<M>(to_vec(
+            keys + (((size_t)j * 2 + row) * dim + d) * n, n)));
+    typename rlwe::RelinearizationKey<M>::RelinearizationKeyPart part(
+        std::move(matrix), (uint64_t)log_b);
+    rlwe::RelinearizationKey<M> rk((uint64_t)log_b, dm, p.params.get(), &p.ntt);
+    rk.dimension_ = dim;
+    rk.num_parts_ = 2;
+    rk.substitution_power_ = (n >> j) + 1;
+    rk.relinearization_key_.push_back(std::move(part));
+    gks.push_back(rlwe::GaloisKey<M>(std::move(rk)));
+  }
+  auto exp = rlwe::GaloisKeysObliviousExpander<M>::Create(std::move(gks), log_t,
+                                                          p.params.get(), &p.ntt);
+  if (!exp.ok()) return fail(exp.status());
+  for (int c = 0; c < count; ++c) {
+    std::vector<rlwe::Polynomial<M>> comps;
+    for (int i = 0; i < 2; ++i)
+      comps.push_back(rlwe::Polynomial<M>(to_vec(ct + ((size_t)c * 2 + i) * n, n)));
+    std::vector<rlwe::SymmetricRlweCiphertext<M>> in;
+    in.emplace_back(std::move(comps), 1, 1.0, p.params.get(), &*ep);
+    auto r = (*exp)->ObliviousExpand(std::move(in), levels, 1 << levels);
+    if (!r.ok()) return fail(r.status());
+    for (int i = 0; i < (1 << levels); ++i)
+      for (int comp = 0; comp < 2; ++comp)
+        from_vec((*r)[i].Component(comp).value().Coeffs(),
+                 out + (((size_t)c << levels) + i) * 2 * n + (size_t)comp * n);
+  }
+  return 0;
+}
+
+// ObliviousExpander::ComputeNormalizer.
+uint64_t ref_compute_normalizer(int k, int log_t) {
+  return rlwe::ObliviousExpander<M>::ComputeNormalizer(k, log_t);
+}
+
+}  // extern "C"

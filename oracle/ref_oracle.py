@@ -1,0 +1,132 @@
+"""ctypes wrapper around oracle/_ref/libshellref.so — TEST INFRASTRUCTURE ONLY.
+
+libshellref.so is google/shell-encryption's own hot-path C++ code, compiled in
+place from the reference sources by oracle/ref/Makefile (only where those
+sources exist; the GPU machine has only the committed golden fixtures).  It is
+used to generate the golden vectors in tests/golden/ and to check the C
+restatement (oracle/shell_oracle.c) against the real reference.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libshellref.so")
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+_IP = ctypes.POINTER(ctypes.c_int)
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(LIB_PATH)
+        L.ref_last_error.restype = ctypes.c_char_p
+        L.ref_prime_tables.argtypes = [ctypes.c_uint64, ctypes.c_int, _U64P, _U64P, _U64P]
+        L.ref_ntt.argtypes = [ctypes.c_uint64, ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_int]
+        L.ref_rns_substitute.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_int,
+                                         _U64P, _U64P]
+        L.ref_rns_modreduce_lsb.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_uint64,
+                                            ctypes.c_int, _U64P, _U64P]
+        L.ref_bgv_mul_relin.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_uint64, _IP,
+                                        _U64P, _U64P, _U64P, _U64P, ctypes.c_int, _U64P, _U64P]
+        L.ref_bgv_rotate.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _IP, ctypes.c_int,
+                                     _U64P, _U64P, _U64P, ctypes.c_int, _U64P]
+        L.ref_oblivious_expand.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, _U64P, _U64P,
+                                           ctypes.c_int, _U64P]
+        L.ref_compute_normalizer.restype = ctypes.c_uint64
+        L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    assert a.dtype == np.uint64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_U64P)
+
+
+def _check(code):
+    if code != 0:
+        raise RuntimeError(f"reference returned {code}: {lib().ref_last_error().decode()}")
+
+
+def _qs(qs):
+    return np.array([int(q) for q in qs], dtype=np.uint64)
+
+
+def prime_tables(q, log_n):
+    n = 1 << log_n
+    f = np.zeros(n, np.uint64)
+    i = np.zeros(n, np.uint64)
+    ninv = np.zeros(1, np.uint64)
+    _check(lib().ref_prime_tables(q, log_n, _p(f), _p(i), _p(ninv)))
+    return f, i, int(ninv[0])
+
+
+def ntt(q, log_n, data, inverse=False):
+    d = np.array(data, dtype=np.uint64, copy=True).reshape(-1, 1 << log_n)
+    _check(lib().ref_ntt(q, log_n, _p(d), d.shape[0], int(inverse)))
+    return d.reshape(np.shape(data))
+
+
+def rns_substitute(log_n, qs, poly, power):
+    q = _qs(qs)
+    poly = np.ascontiguousarray(poly, dtype=np.uint64)
+    out = np.empty_like(poly)
+    _check(lib().ref_rns_substitute(log_n, _p(q), len(q), power, _p(poly), _p(out)))
+    return out
+
+
+def rns_modreduce_lsb(log_n, qs, poly, t, is_ntt=True):
+    q = _qs(qs)
+    poly = np.ascontiguousarray(poly, dtype=np.uint64)
+    out = np.empty((len(q) - 1, 1 << log_n), np.uint64)
+    _check(lib().ref_rns_modreduce_lsb(log_n, _p(q), len(q), t, int(is_ntt), _p(poly), _p(out)))
+    return out
+
+
+def bgv_mul_relin(log_n, qs, t, log_bs, key_b, key_a, a, b):
+    q = _qs(qs)
+    lb = np.ascontiguousarray(log_bs, dtype=np.int32)
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    count = a.shape[0]
+    L, n = len(q), 1 << log_n
+    prod = np.empty((count, 3, L, n), np.uint64)
+    out = np.empty((count, 2, L, n), np.uint64)
+    _check(lib().ref_bgv_mul_relin(log_n, _p(q), L, t, lb.ctypes.data_as(_IP),
+                                   _p(np.ascontiguousarray(key_b)),
+                                   _p(np.ascontiguousarray(key_a)), _p(a), _p(b), count,
+                                   _p(prod), _p(out)))
+    return prod, out
+
+
+def bgv_rotate(log_n, qs, log_bs, power, key_b, key_a, ct):
+    q = _qs(qs)
+    lb = np.ascontiguousarray(log_bs, dtype=np.int32)
+    ct = np.ascontiguousarray(ct, dtype=np.uint64)
+    out = np.empty_like(ct)
+    _check(lib().ref_bgv_rotate(log_n, _p(q), len(q), lb.ctypes.data_as(_IP), power,
+                                _p(np.ascontiguousarray(key_b)),
+                                _p(np.ascontiguousarray(key_a)), _p(ct), ct.shape[0], _p(out)))
+    return out
+
+
+def oblivious_expand(q, log_n, log_t, levels, log_b, keys, cts):
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    cts = np.ascontiguousarray(cts, dtype=np.uint64)
+    count = cts.shape[0]
+    out = np.empty((count, 1 << levels, 2, 1 << log_n), np.uint64)
+    _check(lib().ref_oblivious_expand(q, log_n, log_t, levels, log_b, _p(keys), _p(cts), count,
+                                      _p(out)))
+    return out
+
+
+def compute_normalizer(k, log_t):
+    return int(lib().ref_compute_normalizer(k, log_t))

@@ -168,10 +168,11 @@ struct shg_context {
   uint64_t* ws = nullptr;      // scratch for batched pipelines
   size_t ws_bytes = 0;
   int chunk_cts = 0;
+  int small_q = 0;  // all moduli below 2^58
   std::mutex mu;
 
   CtxDev dev() const {
-    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod};
+    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -307,6 +308,9 @@ int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
       twi[(size_t)i * n + j] = Tw{h.inv[j], shoup_of(h.inv[j], h.q)};
     }
   }
+  ctx->small_q = 1;
+  for (int i = 0; i < L; ++i)
+    if ((qs[i] >> 58) != 0) ctx->small_q = 0;
   ctx->qmod.resize((size_t)L * L);
   for (int i = 0; i < L; ++i)
     for (int j = 0; j < L; ++j) ctx->qmod[(size_t)i * L + j] = qs[i] % qs[j];
@@ -745,19 +749,26 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
   cudaStream_t s = (cudaStream_t)stream;
   const int L = key->L, n = ctx->n, k = key->k;
   const size_t Ln = (size_t)L * n;
-  const size_t per_ct = (Ln + (size_t)k * Ln) * sizeof(uint64_t);
-  const int C = chunk_for(ctx, per_ct, count);
+  // Phase 1 over the whole batch (one launch fills the GPU): tensor product
+  // and the exported coefficients X of every degree-2 component.  Phase 2 in
+  // chunks small enough that the digit NTTs D stay in L2 between the digit
+  // kernel and the key inner product.
+  const size_t x_bytes = (size_t)count * Ln * sizeof(uint64_t);
+  const size_t d_per_ct = (size_t)k * Ln * sizeof(uint64_t);
+  int C = ctx->chunk_cts > 0 ? ctx->chunk_cts
+                             : (int)std::max<size_t>(1, ((size_t)56 << 20) / d_per_ct);
+  C = std::max(1, std::min(C, count));
   std::lock_guard<std::mutex> lock(ctx->mu);
-  if ((st = ctx->ensure_ws(per_ct * C))) return st;
+  if ((st = ctx->ensure_ws(x_bytes + d_per_ct * C))) return st;
   uint64_t* X = ctx->ws;
-  uint64_t* D = X + (size_t)C * Ln;
+  uint64_t* D = X + (size_t)count * Ln;
   const CtxDev dv = ctx->dev();
+  shg::launch_tensor_intt(dv, out, X, a, b, count, L, s);
   for (int c0 = 0; c0 < count; c0 += C) {
     const int cc = std::min(C, count - c0);
     uint64_t* o = out + (size_t)c0 * 2 * Ln;
-    shg::launch_tensor_intt(dv, o, X, a + (size_t)c0 * 2 * Ln,
-                            b + (size_t)c0 * 2 * Ln, cc, L, s);
-    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
+    shg::launch_digit_ntt(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
+                          key->need_lift, cc, L, s);
     shg::launch_ks_inner(dv, o, D, key->kb, key->ka, k, key->chunk, o, 2 * Ln,
                          CtMap::identity(), 0, 0, cc, L, s);
   }

@@ -95,12 +95,21 @@ __device__ __forceinline__ int subst_src_rt(int pos, int power, int log_n) {
   return (int)(__brev(t) >> (32 - log_n));
 }
 
+// Canonical residues at the end of a forward transform.
+template <bool LAZY, int E>
+__device__ __forceinline__ void finish_forward(uint64_t (&x)[E], uint64_t q,
+                                               uint64_t two_q, uint64_t bar) {
+#pragma unroll
+  for (int k = 0; k < E; ++k)
+    x[k] = LAZY ? reduce_full(x[k], q, bar) : reduce_4q(x[k], q, two_q);
+}
+
 // --------------------------------------------------------------------------
 // Forward / inverse NTT (ForwardNumberTheoreticTransform /
 // InverseNumberTheoreticTransform, dft_transformations.h:158-201).
 // --------------------------------------------------------------------------
 
-template <int LOG_N>
+template <int LOG_N, bool LAZY>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_ntt_fwd(const uint64_t* in, uint64_t* out, int num, int L, CtxDev c) {
   using C = NttCore<LOG_N>;
@@ -116,10 +125,9 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   uint64_t x[C::E];
 #pragma unroll
   for (int k = 0; k < C::E; ++k) x[k] = src[C::fwd_in_idx(tid, k)];
-  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)l * C::N, 1, q,
-             two_q);
-#pragma unroll
-  for (int k = 0; k < C::E; ++k) x[k] = reduce_4q(x[k], q, two_q);
+  C::template forward<LAZY>(x, tid, smem + sub * C::N,
+                            c.tw_fwd + (size_t)l * C::N, 1, q, two_q);
+  finish_forward<LAZY, C::E>(x, q, two_q, c.primes[l].barrett);
   if (active) store_contig(out + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
 }
 
@@ -265,7 +273,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
 // (rns_relinearization_key.cc:219-226).  One CTA per (ct, digit, out limb).
 // The NTT runs on the plain digits; the key is premultiplied by 2^64 so the
 // inner product's REDC restores Montgomery form.
-template <int LOG_N>
+template <int LOG_N, bool LAZY>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_digit_ntt(uint64_t* D, const uint64_t* X, const DigitDesc* digits, int k,
                 int need_lift, int num, int L, CtxDev c) {
@@ -302,17 +310,16 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
       x[kk] = v;
     }
   }
-  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)j * C::N, 1, q,
-             two_q);
-#pragma unroll
-  for (int kk = 0; kk < C::E; ++kk) x[kk] = reduce_4q(x[kk], q, two_q);
+  C::template forward<LAZY>(x, tid, smem + sub * C::N,
+                            c.tw_fwd + (size_t)j * C::N, 1, q, two_q);
+  finish_forward<LAZY, C::E>(x, q, two_q, P->barrett);
   if (active) store_contig(D + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
 }
 
 // RnsPolynomial::ModReduceLsb, NTT form, second half (rns/rns_polynomial.cc:
 // 302-323): balanced lift of the top limb's plain coefficients Y to q_i,
 // forward NTT, and out_i = in_i * c1_i + delta_i * c2_i.
-template <int LOG_N>
+template <int LOG_N, bool LAZY>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_modreduce_lift(uint64_t* out, const uint64_t* Y, const uint64_t* in,
                      ScalarPack sc, int num, int L, CtxDev c) {
@@ -341,8 +348,9 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     if (neg) y += q - ql_mod_qi;
     x[k] = y;
   }
-  C::forward(x, tid, smem + sub * C::N, c.tw_fwd + (size_t)i * C::N, 1, q,
-             two_q);
+  C::template forward<LAZY>(x, tid, smem + sub * C::N,
+                            c.tw_fwd + (size_t)i * C::N, 1, q, two_q);
+  finish_forward<LAZY, C::E>(x, q, two_q, bar);
   const uint64_t c1 = sc.v[4 * i], c1p = sc.v[4 * i + 1];
   const uint64_t c2 = sc.v[4 * i + 2], c2p = sc.v[4 * i + 3];
   const size_t off = ((size_t)p * L + i) * C::N + C::fwd_out_idx(tid, 0);
@@ -350,8 +358,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   load_contig(a, in + off);
 #pragma unroll
   for (int k = 0; k < C::E; ++k) {
-    const uint64_t d = reduce_4q(x[k], q, two_q);
-    x[k] = reduce_2q_full(shoup(a[k], c1, c1p, q) + shoup(d, c2, c2p, q), q);
+    x[k] = reduce_2q_full(shoup(a[k], c1, c1p, q) + shoup(x[k], c2, c2p, q), q);
   }
   if (active)
     store_contig(out + ((size_t)p * Lr + i) * C::N + C::fwd_out_idx(tid, 0), x);
@@ -610,7 +617,7 @@ void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
   LaunchScope scope_("ntt_fwd", s);
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_ntt_fwd<LN>;                                                \
+    auto kern = c.small_q ? k_ntt_fwd<LN, true> : k_ntt_fwd<LN, false>;  \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         in, out, num, L, c);                                                  \
@@ -712,7 +719,7 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
   LaunchScope scope_("digit_ntt", s);
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_digit_ntt<LN>;                                              \
+    auto kern = c.small_q ? k_digit_ntt<LN, true> : k_digit_ntt<LN, false>;  \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         D, X, digits, k, need_lift, num, L, c);                               \
@@ -747,7 +754,7 @@ void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
   LaunchScope scope_("modreduce_lift", s);
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_modreduce_lift<LN>;                                         \
+    auto kern = c.small_q ? k_modreduce_lift<LN, true> : k_modreduce_lift<LN, false>;  \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     const int num = count * (L - 1);                                          \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \

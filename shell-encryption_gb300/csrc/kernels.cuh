@@ -23,6 +23,7 @@ struct CtxDev {
   const Tw* tw_fwd;           // [L][n]  plain psi^{brv(i)} + Shoup constant
   const Tw* tw_inv;           // [L][n]  plain psis_inv_bitrev + Shoup constant
   const uint64_t* qmod;       // [L][L]  q_i mod q_j (plain), row i
+  int small_q;                // every q < 2^58: forward NTTs skip per-level reductions
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,

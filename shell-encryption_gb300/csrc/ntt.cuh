@@ -48,6 +48,24 @@ __device__ __forceinline__ void bf_ct(uint64_t& X, uint64_t& Y, Tw w,
   Y = x - t + two_q;
 }
 
+// Cooley-Tukey butterfly without any per-level reduction.  The Shoup product
+// is below 2q for every 64-bit input, so each level grows the bound by 2q:
+// after the 14 levels of n = 2^14 values stay below 29q, which fits 64 bits
+// for q < 2^58 (the path's 45- and 50-bit primes); the final pass reduces.
+__device__ __forceinline__ void bf_ct_lazy(uint64_t& X, uint64_t& Y, Tw w,
+                                           uint64_t q, uint64_t two_q) {
+  uint64_t t = shoup_lazy(Y, w.w, w.wp, q);
+  uint64_t x = X;
+  X = x + t;
+  Y = x - t + two_q;
+}
+
+// x mod q for any x < 2^64 with bar = floor(2^64 / q).
+__device__ __forceinline__ uint64_t reduce_full(uint64_t x, uint64_t q,
+                                                uint64_t bar) {
+  return reduce_2q(x - mulhi64(x, bar) * q, q);
+}
+
 // Gentleman-Sande butterfly, inputs/outputs in [0, 2q).
 __device__ __forceinline__ void bf_gs(uint64_t& X, uint64_t& Y, Tw w,
                                       uint64_t q, uint64_t two_q) {
@@ -58,15 +76,24 @@ __device__ __forceinline__ void bf_gs(uint64_t& X, uint64_t& Y, Tw w,
   Y = shoup_lazy(d, w.w, w.wp, q);
 }
 
-// Shared-memory swizzle: XOR the low 4 index bits with bits 4..7 so that every
-// pass's per-register access pattern is bank-conflict free.
-__device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
+// Coefficients per thread: 16, or 32 at n = 2^14 (512 threads, so a thread
+// may use 128 registers and the transform needs one exchange less).
+__host__ __device__ constexpr int default_elog(int log_n) {
+  return log_n < 4 ? log_n : (log_n == 14 ? 5 : 4);
+}
 
-template <int LOG_N>
+template <int LOG_N, int ELOG_ = default_elog(LOG_N)>
 struct NttCore {
   static_assert(LOG_N >= 1 && LOG_N <= 14, "CTA-resident NTT handles n <= 2^14");
   static constexpr int N = 1 << LOG_N;
-  static constexpr int ELOG = LOG_N < 4 ? LOG_N : 4;
+  static constexpr int ELOG = ELOG_;
+
+  // Shared-memory swizzle: XOR the low 4 index bits with bits ELOG..ELOG+3,
+  // which makes every pass's per-register access pattern bank-conflict free
+  // (each half-warp of 8-byte accesses hits 16 distinct bank pairs).
+  __device__ __forceinline__ static int swz(int i) {
+    return i ^ ((i >> ELOG) & 15);
+  }
   static constexpr int E = 1 << ELOG;
   static constexpr int T = N / E;  // threads per limb
   static constexpr int P = (LOG_N + ELOG - 1) / ELOG;  // passes
@@ -112,7 +139,8 @@ struct NttCore {
   // One forward pass on registers.  tw is the limb's psi_bitrev table; stage s
   // reads tw[tw_mult * 2^s + (i >> (b+1))] (tw_mult = 1 for a full transform;
   // 2 + h for half h of a 2n transform whose first level ran elsewhere).
-  template <int p>
+  // LAZY selects bf_ct_lazy (valid when q < 2^58, see above).
+  template <int p, bool LAZY>
   __device__ __forceinline__ static void fwd_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
                                                   int tw_mult, uint64_t q,
@@ -132,7 +160,11 @@ struct NttCore {
         static_for<0, (1 << lb)>([&](auto ll) {
           constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
           constexpr int k1 = k0 | (1 << lb);
-          bf_ct(x[k0], x[k1], w, q, two_q);
+          if constexpr (LAZY) {
+            bf_ct_lazy(x[k0], x[k1], w, q, two_q);
+          } else {
+            bf_ct(x[k0], x[k1], w, q, two_q);
+          }
         });
       });
     });
@@ -181,7 +213,9 @@ struct NttCore {
   }
 
   // Full forward transform on registers (input in fwd_in layout, values in
-  // [0, 4q); output in fwd_out layout, values in [0, 4q)).
+  // [0, 4q) -- below q for LAZY; output in fwd_out layout, values in [0, 4q),
+  // or below (2 LOG_N + 1) q for LAZY).
+  template <bool LAZY = false>
   __device__ __forceinline__ static void forward(uint64_t (&x)[E], int tid,
                                                  uint64_t* sm,
                                                  const Tw* __restrict__ tw,
@@ -189,7 +223,7 @@ struct NttCore {
                                                  uint64_t two_q) {
     static_for<0, P>([&](auto pp) {
       constexpr int p = decltype(pp)::value;
-      fwd_pass<p>(x, tid, tw, tw_mult, q, two_q);
+      fwd_pass<p, LAZY>(x, tid, tw, tw_mult, q, two_q);
       if constexpr (p + 1 < P) exchange(x, tid, sm, fwd_clo(p), fwd_clo(p + 1));
     });
   }

@@ -1,0 +1,134 @@
+#!/usr/bin/env python3
+"""Generates tests/golden/*.npz and digests.json by running google/shell-encryption's
+own code (oracle/_ref/libshellref.so, built from the reference sources in place by
+oracle/ref/Makefile) on seeded inputs.
+
+  make -C oracle/ref && python tests/golden/make_golden.py
+
+Small cases are stored whole (inputs and outputs).  Full-size workloads are
+stored as SHA-256 digests of the reference's outputs; their inputs are
+regenerated from the recorded splitmix64 seeds (oracle.uniform_limbs).
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import oracle as O  # noqa: E402
+from oracle import ref_oracle as R  # noqa: E402
+
+Q45 = [35184371138561, 35184370941953, 35184370352129, 35184370155521,
+       35184369893377, 35184368877569]
+Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073]
+Q59 = 576460752303415297
+Q60 = 1152921504606830593
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.uint64).tobytes()).hexdigest()
+
+
+def main():
+    if not R.available():
+        sys.exit("oracle/_ref/libshellref.so is missing: run `make -C oracle/ref` first")
+    g = {}
+    # NTT tables and transforms (ntt_parameters.h, dft_transformations.h).
+    for q, log_n in [(Q45[0], 1), (Q45[1], 4), (Q50[0], 7), (Q59, 12), (Q60, 12),
+                     (Q45[2], 10), (Q45[0], 14)]:
+        tag = f"ntt_{q}_{log_n}"
+        f, i, ninv = R.prime_tables(q, log_n)
+        x = O.uniform_limbs(1000 + log_n, [q], 1 << log_n, 2).reshape(2, -1)
+        g[tag + "_psis_bitrev"] = f
+        g[tag + "_psis_inv_bitrev"] = i
+        g[tag + "_n_inv"] = np.array([ninv], np.uint64)
+        g[tag + "_in"] = x
+        g[tag + "_fwd"] = R.ntt(q, log_n, x)
+        g[tag + "_inv"] = R.ntt(q, log_n, x, inverse=True)
+    # RnsPolynomial::Substitute and ModReduceLsb.
+    for log_n, qs, power in [(6, Q45[:3], 5), (10, Q50[:4], 1023)]:
+        tag = f"subst_{log_n}_{power}"
+        x = O.uniform_limbs(2000 + log_n, qs, 1 << log_n).reshape(len(qs), -1)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_in"] = x
+        g[tag + "_out"] = R.rns_substitute(log_n, qs, x, power)
+    for log_n, qs, is_ntt in [(5, Q45[:2], 1), (9, Q50[:4], 1), (9, Q50[:4], 0)]:
+        tag = f"modreduce_{log_n}_{len(qs)}_{is_ntt}"
+        x = O.uniform_limbs(3000 + log_n + is_ntt, qs, 1 << log_n).reshape(len(qs), -1)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_in"] = x
+        g[tag + "_out"] = R.rns_modreduce_lsb(log_n, qs, x, 65537, bool(is_ntt))
+    # BGV ct x ct + relinearization, and rotation (Substitute + Galois key).
+    for log_n, qs, log_bs in [(5, Q45[:2], [20, 20]), (8, Q45[:3], [20, 20, 20]),
+                              (7, Q50[:2], [50, 16])]:
+        tag = f"mulrelin_{log_n}_{len(qs)}_{log_bs[-1]}"
+        n = 1 << log_n
+        k = O.Rns(log_n, qs).gadget_dim(log_bs)
+        kb = O.uniform_limbs(4000 + log_n, qs, n, k)
+        ka = O.uniform_limbs(4100 + log_n, qs, n, k)
+        a = O.uniform_limbs(4200 + log_n, qs, n, 4).reshape(2, 2, len(qs), n)
+        b = O.uniform_limbs(4300 + log_n, qs, n, 4).reshape(2, 2, len(qs), n)
+        prod, out = R.bgv_mul_relin(log_n, qs, 65537, log_bs, kb, ka, a, b)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_log_bs"] = np.array(log_bs, np.int32)
+        for nm, v in (("kb", kb), ("ka", ka), ("a", a), ("b", b), ("prod", prod), ("out", out)):
+            g[f"{tag}_{nm}"] = v
+        rtag = f"rotate_{log_n}_{len(qs)}_{log_bs[-1]}"
+        power = 5
+        g[rtag + "_power"] = np.array([power], np.int32)
+        g[rtag + "_out"] = R.bgv_rotate(log_n, qs, log_bs, power, kb, ka, a)
+    # Oblivious expansion (n = 128, 60-bit q, base 2^10, 3 levels).
+    q, log_n, levels, log_b = Q60, 7, 3, 10
+    n = 1 << log_n
+    dim = O.Prime(q, log_n).gadget_size(log_b)
+    keys = O.uniform_limbs(5000, [q], n, levels * 2 * dim).reshape(levels, 2, dim, n)
+    cts = O.uniform_limbs(5001, [q], n, 4).reshape(2, 2, n)
+    g["expand_keys"] = keys
+    g["expand_cts"] = cts
+    g["expand_out"] = R.oblivious_expand(q, log_n, 16, levels, log_b, keys, cts)
+    g["normalizer_10_16"] = np.array([R.compute_normalizer(10, 16)], np.uint64)
+    np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **g)
+
+    # Full-size workloads: digests of the reference's outputs on seeded inputs.
+    d = {}
+    log_n, qs, log_bs = 14, Q45, [20] * 6
+    n, k = 1 << log_n, 18
+    kb = O.uniform_limbs(7001, qs, n, k)
+    ka = O.uniform_limbs(7002, qs, n, k)
+    a = O.uniform_limbs(7003, qs, n, 4).reshape(2, 2, 6, n)
+    b = O.uniform_limbs(7004, qs, n, 4).reshape(2, 2, 6, n)
+    prod, out = R.bgv_mul_relin(log_n, qs, 65537, log_bs, kb, ka, a, b)
+    d["mul_relin_n14_L6"] = {
+        "log_n": 14, "qs": qs, "t": 65537, "log_bs": log_bs, "count": 2,
+        "seeds": {"key_b": 7001, "key_a": 7002, "a": 7003, "b": 7004},
+        "prod_sha256": digest(prod), "out_sha256": digest(out)}
+    rot = R.bgv_rotate(log_n, qs, log_bs, 5, kb, ka, a)
+    d["rotate_n14_L6_p5"] = {"power": 5, "note": "key and ct as in mul_relin_n14_L6 (ct = a)",
+                             "out_sha256": digest(rot)}
+    x = O.uniform_limbs(7005, qs, n).reshape(6, n)
+    d["modreduce_n14_L6"] = {"seed": 7005, "t": 65537,
+                             "ntt_sha256": digest(R.rns_modreduce_lsb(log_n, qs, x, 65537, True)),
+                             "coeff_sha256": digest(R.rns_modreduce_lsb(log_n, qs, x, 65537,
+                                                                        False))}
+    q, log_n, levels, log_b = Q60, 12, 10, 8
+    n, dim = 1 << log_n, 8
+    keys = O.uniform_limbs(7010, [q], n, levels * 2 * dim).reshape(levels, 2, dim, n)
+    cts = O.uniform_limbs(7011, [q], n, 2).reshape(1, 2, n)
+    d["expand_n12_levels10_b8"] = {"q": q, "log_n": 12, "levels": 10, "log_b": 8,
+                                   "seeds": {"keys": 7010, "ct": 7011},
+                                   "out_sha256": digest(R.oblivious_expand(q, log_n, 16, levels,
+                                                                           log_b, keys, cts))}
+    x = O.uniform_limbs(7020, [Q59], 1 << 12, 64).reshape(64, -1)
+    d["ntt_q59_n12_x64"] = {"seed": 7020, "fwd_sha256": digest(R.ntt(Q59, 12, x)),
+                            "inv_sha256": digest(R.ntt(Q59, 12, x, inverse=True))}
+    with open(os.path.join(HERE, "digests.json"), "w") as fh:
+        json.dump(d, fh, indent=1)
+    print("wrote", os.path.join(HERE, "reference_small.npz"), "and digests.json")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,308 @@
+"""Golden vectors produced by google/shell-encryption's own code (compiled in
+place by oracle/ref/Makefile; generator: tests/golden/make_golden.py).
+
+CPU tests pin the C restatement (oracle/shell_oracle.c) to the reference;
+the gpu-marked tests check the CUDA library against the same vectors
+through the C ABI.  Full-size workloads are compared as SHA-256 digests of
+outputs on seeded inputs.
+"""
+import ctypes
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+SMALL = np.load(os.path.join(GOLDEN, "reference_small.npz"))
+DIGESTS = json.load(open(os.path.join(GOLDEN, "digests.json")))
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.uint64).tobytes()).hexdigest()
+
+
+def tags(prefix):
+    return sorted({k.rsplit("_", 1)[0] for k in SMALL.files if k.startswith(prefix) and
+                   k.endswith("_in")})
+
+
+NTT_TAGS = sorted({k[:-3] for k in SMALL.files if k.startswith("ntt_") and k.endswith("_in")})
+
+
+def _ntt_params(tag):
+    _, q, log_n = tag.split("_")
+    return int(q), int(log_n)
+
+
+# --------------------------------------------------------------------------
+# The oracle restatement against the reference (CPU)
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("tag", NTT_TAGS)
+def test_oracle_ntt_golden(oracle, tag):
+    q, log_n = _ntt_params(tag)
+    p = oracle.Prime(q, log_n)
+    f, i = p.tables()
+    assert np.array_equal(f, SMALL[tag + "_psis_bitrev"])
+    assert np.array_equal(i, SMALL[tag + "_psis_inv_bitrev"])
+    assert p.info()["n_inv"] == int(SMALL[tag + "_n_inv"][0])
+    x = SMALL[tag + "_in"]
+    assert np.array_equal(np.stack([p.ntt_fwd(r) for r in x]), SMALL[tag + "_fwd"])
+    assert np.array_equal(np.stack([p.ntt_inv(r) for r in x]), SMALL[tag + "_inv"])
+
+
+def _cases(prefix):
+    return sorted({k[:k.index("_qs")] for k in SMALL.files if k.startswith(prefix) and
+                   k.endswith("_qs")})
+
+
+@pytest.mark.parametrize("tag", _cases("subst_"))
+def test_oracle_substitute_golden(oracle, tag):
+    log_n, power = int(tag.split("_")[1]), int(tag.split("_")[2])
+    rns = oracle.Rns(log_n, SMALL[tag + "_qs"])
+    assert np.array_equal(rns.substitute(SMALL[tag + "_in"], power), SMALL[tag + "_out"])
+
+
+@pytest.mark.parametrize("tag", _cases("modreduce_"))
+def test_oracle_modreduce_golden(oracle, tag):
+    log_n, is_ntt = int(tag.split("_")[1]), int(tag.split("_")[3])
+    rns = oracle.Rns(log_n, SMALL[tag + "_qs"])
+    got = rns.modreduce_lsb(SMALL[tag + "_in"], 65537, bool(is_ntt))
+    assert np.array_equal(got, SMALL[tag + "_out"])
+
+
+@pytest.mark.parametrize("tag", _cases("mulrelin_"))
+def test_oracle_mul_relin_and_rotate_golden(oracle, tag):
+    log_n = int(tag.split("_")[1])
+    qs = SMALL[tag + "_qs"]
+    lb = SMALL[tag + "_log_bs"]
+    rns = oracle.Rns(log_n, qs)
+    a, b, kb, ka = (SMALL[f"{tag}_{x}"] for x in ("a", "b", "kb", "ka"))
+    prod = np.stack([rns.tensor(a[i], b[i]) for i in range(a.shape[0])])
+    assert np.array_equal(prod, SMALL[tag + "_prod"])
+    assert np.array_equal(rns.mul_relin_batch(a, b, kb, ka, lb), SMALL[tag + "_out"])
+    rtag = tag.replace("mulrelin_", "rotate_")
+    power = int(SMALL[rtag + "_power"][0])
+    sub = np.stack([np.stack([rns.substitute(a[i, c], power) for c in range(2)])
+                    for i in range(a.shape[0])])
+    rot = np.stack([rns.galois(sub[i], kb, ka, lb) for i in range(a.shape[0])])
+    assert np.array_equal(rot, SMALL[rtag + "_out"])
+
+
+def test_oracle_expand_golden(oracle):
+    from conftest import Q60
+    p = oracle.Prime(Q60, 7)
+    keys, cts = SMALL["expand_keys"], SMALL["expand_cts"]
+    got = np.stack([p.oblivious_expand(3, 10, keys, cts[i]) for i in range(cts.shape[0])])
+    assert np.array_equal(got, SMALL["expand_out"])
+    assert oracle.compute_normalizer(10, 16) == int(SMALL["normalizer_10_16"][0])
+
+
+def test_oracle_full_size_digests(oracle):
+    d = DIGESTS["mul_relin_n14_L6"]
+    qs, n = d["qs"], 1 << d["log_n"]
+    rns = oracle.Rns(d["log_n"], qs)
+    s = d["seeds"]
+    kb = oracle.uniform_limbs(s["key_b"], qs, n, 18)
+    ka = oracle.uniform_limbs(s["key_a"], qs, n, 18)
+    a = oracle.uniform_limbs(s["a"], qs, n, 4).reshape(2, 2, 6, n)
+    b = oracle.uniform_limbs(s["b"], qs, n, 4).reshape(2, 2, 6, n)
+    prod = np.stack([rns.tensor(a[i], b[i]) for i in range(2)])
+    assert digest(prod) == d["prod_sha256"]
+    assert digest(rns.mul_relin_batch(a, b, kb, ka, d["log_bs"], threads=2)) == d["out_sha256"]
+    sub = np.stack([np.stack([rns.substitute(a[i, c], 5) for c in range(2)]) for i in range(2)])
+    rot = np.stack([rns.galois(sub[i], kb, ka, d["log_bs"]) for i in range(2)])
+    assert digest(rot) == DIGESTS["rotate_n14_L6_p5"]["out_sha256"]
+    m = DIGESTS["modreduce_n14_L6"]
+    x = oracle.uniform_limbs(m["seed"], qs, n).reshape(6, n)
+    assert digest(rns.modreduce_lsb(x, 65537, True)) == m["ntt_sha256"]
+    assert digest(rns.modreduce_lsb(x, 65537, False)) == m["coeff_sha256"]
+
+
+def test_oracle_expand_full_size_digest(oracle):
+    d = DIGESTS["expand_n12_levels10_b8"]
+    n = 1 << d["log_n"]
+    p = oracle.Prime(d["q"], d["log_n"])
+    keys = oracle.uniform_limbs(d["seeds"]["keys"], [d["q"]], n, d["levels"] * 2 * 8).reshape(
+        d["levels"], 2, 8, n)
+    ct = oracle.uniform_limbs(d["seeds"]["ct"], [d["q"]], n, 2).reshape(2, n)
+    out = p.oblivious_expand(d["levels"], d["log_b"], keys, ct)
+    assert digest(out[None]) == d["out_sha256"]
+
+
+def test_oracle_matches_reference_library_when_built(oracle):
+    """Where the reference sources are present (this build container), also
+    compare directly with the shim-built reference on fresh inputs."""
+    from oracle import ref_oracle as R
+    if not R.available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    from conftest import Q45
+    qs, log_n, log_bs = Q45[:4], 9, [20] * 4
+    rns = oracle.Rns(log_n, qs)
+    n = 1 << log_n
+    k = rns.gadget_dim(log_bs)
+    kb, ka = oracle.uniform_limbs(31, qs, n, k), oracle.uniform_limbs(32, qs, n, k)
+    a = oracle.uniform_limbs(33, qs, n, 6).reshape(3, 2, 4, n)
+    b = oracle.uniform_limbs(34, qs, n, 6).reshape(3, 2, 4, n)
+    _, ref_out = R.bgv_mul_relin(log_n, qs, 65537, log_bs, kb, ka, a, b)
+    assert np.array_equal(rns.mul_relin_batch(a, b, kb, ka, log_bs), ref_out)
+
+
+# --------------------------------------------------------------------------
+# The CUDA library against the reference's vectors (GPU)
+# --------------------------------------------------------------------------
+
+def _run(sg, fn, *args):
+    sg.check(fn(*args))
+    sg.synchronize()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", NTT_TAGS)
+def test_gpu_ntt_golden(sg, tag):
+    q, log_n = _ntt_params(tag)
+    ctx = sg.Context(log_n, [q])
+    f, i = ctx.ntt_tables(0)
+    assert np.array_equal(f, SMALL[tag + "_psis_bitrev"])
+    assert np.array_equal(i, SMALL[tag + "_psis_inv_bitrev"])
+    x = SMALL[tag + "_in"]
+    d = sg.DeviceBuffer.from_array(x)
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, d.ptr, x.shape[0], 1, None)
+    assert np.array_equal(d.download(x.shape), SMALL[tag + "_fwd"])
+    d.upload(x)
+    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, d.ptr, x.shape[0], 1, None)
+    assert np.array_equal(d.download(x.shape), SMALL[tag + "_inv"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", _cases("subst_"))
+def test_gpu_substitute_golden(sg, tag):
+    log_n, power = int(tag.split("_")[1]), int(tag.split("_")[2])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    ctx = sg.Context(log_n, qs)
+    x = SMALL[tag + "_in"]
+    d, out = sg.DeviceBuffer.from_array(x), sg.DeviceBuffer(x.nbytes)
+    _run(sg, sg.lib().shg_poly_substitute, ctx.h, out.ptr, d.ptr, power, 1, len(qs), None)
+    assert np.array_equal(out.download(x.shape), SMALL[tag + "_out"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", _cases("modreduce_"))
+def test_gpu_modreduce_golden(sg, tag):
+    log_n, is_ntt = int(tag.split("_")[1]), int(tag.split("_")[3])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    ctx = sg.Context(log_n, qs, 65537)
+    ql_inv = ctx.ql_inv(len(qs) - 1)
+    x = SMALL[tag + "_in"]
+    want = SMALL[tag + "_out"]
+    d, out = sg.DeviceBuffer.from_array(x), sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_poly_modreduce_lsb, ctx.h, out.ptr, d.ptr, 65537,
+         ql_inv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), is_ntt, 1, len(qs), None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", _cases("mulrelin_"))
+def test_gpu_mul_relin_and_rotate_golden(sg, tag):
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    lb = [int(x) for x in SMALL[tag + "_log_bs"]]
+    a, b, kb, ka = (SMALL[f"{tag}_{x}"] for x in ("a", "b", "kb", "ka"))
+    count = a.shape[0]
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, lb, 1, kb, ka)
+    lib = sg.lib()
+    da, db = sg.DeviceBuffer.from_array(a), sg.DeviceBuffer.from_array(b)
+    prod = sg.DeviceBuffer(SMALL[tag + "_prod"].nbytes)
+    out = sg.DeviceBuffer(a.nbytes)
+    _run(sg, lib.shg_ct_tensor, ctx.h, prod.ptr, da.ptr, db.ptr, count, len(qs), None)
+    assert np.array_equal(prod.download(SMALL[tag + "_prod"].shape), SMALL[tag + "_prod"])
+    _run(sg, lib.shg_relin_apply, ctx.h, key.h, out.ptr, prod.ptr, count, None)
+    assert np.array_equal(out.download(a.shape), SMALL[tag + "_out"])
+    _run(sg, lib.shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, count, None)
+    assert np.array_equal(out.download(a.shape), SMALL[tag + "_out"])
+    rtag = tag.replace("mulrelin_", "rotate_")
+    power = int(SMALL[rtag + "_power"][0])
+    gkey = sg.Key(ctx, lb, power, kb, ka)
+    _run(sg, lib.shg_bgv_rotate, ctx.h, gkey.h, out.ptr, da.ptr, count, None)
+    assert np.array_equal(out.download(a.shape), SMALL[rtag + "_out"])
+
+
+@pytest.mark.gpu
+def test_gpu_expand_golden(sg):
+    from conftest import Q60
+    keys, cts, want = SMALL["expand_keys"], SMALL["expand_cts"], SMALL["expand_out"]
+    ctx = sg.Context(7, [Q60])
+    gk = [sg.Key(ctx, [10], (128 >> j) + 1, keys[j, 0], keys[j, 1]) for j in range(3)]
+    arr = (ctypes.c_void_p * 3)(*[k.h for k in gk])
+    d, out = sg.DeviceBuffer.from_array(cts), sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_oblivious_expand, ctx.h, arr, 3, out.ptr, d.ptr, cts.shape[0], None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+@pytest.mark.gpu
+def test_gpu_full_size_digests(sg, oracle):
+    d = DIGESTS["mul_relin_n14_L6"]
+    qs, n = d["qs"], 1 << d["log_n"]
+    s = d["seeds"]
+    kb = oracle.uniform_limbs(s["key_b"], qs, n, 18)
+    ka = oracle.uniform_limbs(s["key_a"], qs, n, 18)
+    a = oracle.uniform_limbs(s["a"], qs, n, 4).reshape(2, 2, 6, n)
+    b = oracle.uniform_limbs(s["b"], qs, n, 4).reshape(2, 2, 6, n)
+    ctx = sg.Context(d["log_n"], qs, d["t"])
+    key = sg.Key(ctx, d["log_bs"], 1, kb, ka)
+    lib = sg.lib()
+    da, db = sg.DeviceBuffer.from_array(a), sg.DeviceBuffer.from_array(b)
+    out = sg.DeviceBuffer(a.nbytes)
+    prod = sg.DeviceBuffer(3 * 6 * n * 8 * 2)
+    _run(sg, lib.shg_ct_tensor, ctx.h, prod.ptr, da.ptr, db.ptr, 2, 6, None)
+    assert digest(prod.download((2, 3, 6, n))) == d["prod_sha256"]
+    _run(sg, lib.shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, 2, None)
+    assert digest(out.download(a.shape)) == d["out_sha256"]
+    gkey = sg.Key(ctx, d["log_bs"], 5, kb, ka)
+    _run(sg, lib.shg_bgv_rotate, ctx.h, gkey.h, out.ptr, da.ptr, 2, None)
+    assert digest(out.download(a.shape)) == DIGESTS["rotate_n14_L6_p5"]["out_sha256"]
+    m = DIGESTS["modreduce_n14_L6"]
+    x = oracle.uniform_limbs(m["seed"], qs, n).reshape(1, 6, n)
+    dx, dout = sg.DeviceBuffer.from_array(x), sg.DeviceBuffer(5 * n * 8)
+    ql_inv = ctx.ql_inv(5)
+    for is_ntt, key_name in ((1, "ntt_sha256"), (0, "coeff_sha256")):
+        _run(sg, lib.shg_poly_modreduce_lsb, ctx.h, dout.ptr, dx.ptr, 65537,
+             ql_inv.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), is_ntt, 1, 6, None)
+        assert digest(dout.download((5, n))) == m[key_name]
+
+
+@pytest.mark.gpu
+def test_gpu_expand_full_size_digest(sg, oracle):
+    d = DIGESTS["expand_n12_levels10_b8"]
+    q, log_n, levels = d["q"], d["log_n"], d["levels"]
+    n = 1 << log_n
+    keys = oracle.uniform_limbs(d["seeds"]["keys"], [q], n, levels * 2 * 8).reshape(
+        levels, 2, 8, n)
+    ct = oracle.uniform_limbs(d["seeds"]["ct"], [q], n, 2).reshape(1, 2, n)
+    ctx = sg.Context(log_n, [q])
+    gk = [sg.Key(ctx, [d["log_b"]], (n >> j) + 1, keys[j, 0], keys[j, 1])
+          for j in range(levels)]
+    arr = (ctypes.c_void_p * levels)(*[k.h for k in gk])
+    dct = sg.DeviceBuffer.from_array(ct)
+    out = sg.DeviceBuffer(2 * n * 8 << levels)
+    _run(sg, sg.lib().shg_oblivious_expand, ctx.h, arr, levels, out.ptr, dct.ptr, 1, None)
+    assert digest(out.download((1, 1 << levels, 2, n))) == d["out_sha256"]
+
+
+@pytest.mark.gpu
+def test_gpu_ntt_q59_digest(sg, oracle):
+    from conftest import Q59
+    d = DIGESTS["ntt_q59_n12_x64"]
+    x = oracle.uniform_limbs(d["seed"], [Q59], 1 << 12, 64).reshape(64, 1, -1)
+    ctx = sg.Context(12, [Q59])
+    buf = sg.DeviceBuffer.from_array(x)
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, buf.ptr, 64, 1, None)
+    assert digest(buf.download((64, 1 << 12))) == d["fwd_sha256"]
+    buf.upload(x)
+    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, buf.ptr, 64, 1, None)
+    assert digest(buf.download((64, 1 << 12))) == d["inv_sha256"]
