@@ -56,6 +56,10 @@ int shg_context_reserve(shg_context* ctx, size_t bytes);
 /* Ciphertexts per internal chunk of the batched key-switch pipeline
  * (0 = default). */
 int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
+/* Transforms of n >= 2^log_n use the two-kernel four-step NTT (14 = default;
+ * 15 keeps n = 2^14 on the one-CTA-per-limb kernel; n = 2^15 always uses the
+ * four-step kernels). */
+int shg_context_set_four_step_min(shg_context* ctx, int log_n);
 
 #ifdef __cplusplus
 }

@@ -169,10 +169,11 @@ struct shg_context {
   size_t ws_bytes = 0;
   int chunk_cts = 0;
   int small_q = 0;  // all moduli below 2^58
+  int ntt4_min = 14;  // four-step transforms from this log_n up
   std::mutex mu;
 
   CtxDev dev() const {
-    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q};
+    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -261,9 +262,6 @@ int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
   if (log_n > 15)
     return fail(SHG_INVALID_ARGUMENT,
                 "log_n, " + std::to_string(log_n) + ", must be less than 15.");
-  if (log_n > 14)
-    return fail(SHG_INVALID_ARGUMENT,
-                "log_n = 15 is not supported by this build of the GPU library");
   if (qs == nullptr || num_qs <= 0 || num_qs > shg::kMaxLimbs)
     return fail(SHG_INVALID_ARGUMENT,
                 "`qs` must hold between 1 and " + std::to_string(shg::kMaxLimbs) +
@@ -514,6 +512,13 @@ int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
   if (t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
   if (count == 0) return SHG_OK;
   if ((st = check_ptrs({out, in}))) return st;
+  {
+    const size_t in_bytes = (size_t)count * num_limbs * ctx->n * sizeof(uint64_t);
+    const size_t out_bytes = (size_t)count * (num_limbs - 1) * ctx->n * sizeof(uint64_t);
+    const uintptr_t i0 = (uintptr_t)in, o0 = (uintptr_t)out;
+    if (o0 < i0 + in_bytes && i0 < o0 + out_bytes)
+      return fail(SHG_INVALID_ARGUMENT, "`out` must not overlap `in`");
+  }
   const int Lr = num_limbs - 1;
   const HostPrime& hl = ctx->hp[Lr];
   const uint64_t r = hl.q % t;
@@ -1048,6 +1053,12 @@ int shg_context_reserve(shg_context* ctx, size_t bytes) {
 int shg_context_set_chunk(shg_context* ctx, int cts) {
   if (!ctx || cts < 0) return fail(SHG_INVALID_ARGUMENT, "bad chunk size");
   ctx->chunk_cts = cts;
+  return SHG_OK;
+}
+int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
+  if (!ctx || log_n < 14 || log_n > 16)
+    return fail(SHG_INVALID_ARGUMENT, "four-step threshold must be 14, 15 or 16");
+  ctx->ntt4_min = log_n;
   return SHG_OK;
 }
 

@@ -604,6 +604,10 @@ int grid_for(size_t work, int threads) {
     default: break;                                                  \
   }
 
+// Transforms of n >= 2^ntt4_min (always n = 2^15) run as two four-step
+// phase kernels (ntt4.cu); smaller ones as one CTA-resident kernel.
+bool use_ntt4(const CtxDev& c) { return c.log_n >= c.ntt4_min || c.log_n > 14; }
+
 template <int LOG_N>
 int blocks_for(int num) {
   return (num + Cfg<LOG_N>::LPC - 1) / Cfg<LOG_N>::LPC;
@@ -615,6 +619,10 @@ void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                     int L, cudaStream_t s) {
   if (num <= 0) return;
   LaunchScope scope_("ntt_fwd", s);
+  if (use_ntt4(c)) {
+    launch4_ntt_fwd(c, in, out, num, L, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = c.small_q ? k_ntt_fwd<LN, true> : k_ntt_fwd<LN, false>;  \
@@ -632,6 +640,10 @@ static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
                                   uint64_t swp, cudaStream_t s) {
   if (num <= 0) return;
   LaunchScope scope_("ntt_inv", s);
+  if (use_ntt4(c)) {
+    launch4_ntt_inv(c, in, out, num, L, in_first, in_stride, mode, sw, swp, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_ntt_inv<LN>;                                                \
@@ -683,6 +695,10 @@ void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
   const int num = count * L;
   if (num <= 0) return;
   LaunchScope scope_("tensor_intt", s);
+  if (use_ntt4(c)) {
+    launch4_tensor_intt(c, out01, X, a, b, count, L, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_tensor_intt<LN>;                                            \
@@ -700,6 +716,10 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
   const int num = count * L;
   if (num <= 0) return;
   LaunchScope scope_("intt_export", s);
+  if (use_ntt4(c)) {
+    launch4_intt_export(c, X, ct, ncomp, comp, subst_power, map, count, L, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = k_intt_export<LN>;                                            \
@@ -717,6 +737,10 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
   const int num = count * k * L;
   if (num <= 0) return;
   LaunchScope scope_("digit_ntt", s);
+  if (use_ntt4(c)) {
+    launch4_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = c.small_q ? k_digit_ntt<LN, true> : k_digit_ntt<LN, false>;  \
@@ -752,6 +776,10 @@ void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,
   launch_ntt_inv_scaled(c, in, Y, count, L, L - 1, L, 2, k_plain, k_shoup, s);
   // Stage 2: lift, forward NTT, combine.
   LaunchScope scope_("modreduce_lift", s);
+  if (use_ntt4(c)) {
+    launch4_modreduce_lift(c, out, Y, in, sc, count, L, s);
+    return;
+  }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = c.small_q ? k_modreduce_lift<LN, true> : k_modreduce_lift<LN, false>;  \

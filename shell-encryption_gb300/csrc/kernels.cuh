@@ -24,6 +24,7 @@ struct CtxDev {
   const Tw* tw_inv;           // [L][n]  plain psis_inv_bitrev + Shoup constant
   const uint64_t* qmod;       // [L][L]  q_i mod q_j (plain), row i
   int small_q;                // every q < 2^58: forward NTTs skip per-level reductions
+  int ntt4_min;               // log_n from which transforms use the four-step kernels
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,
@@ -146,5 +147,25 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
 void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
                        const uint64_t* db, int num_items, int chunk, int count,
                        cudaStream_t s);
+
+// Four-step variants (ntt4.cu), n = 2^14 and 2^15; same semantics as the
+// launchers above.
+void launch4_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                     int L, cudaStream_t s);
+void launch4_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                     int L, int in_first, int in_stride, int mode, uint64_t sw,
+                     uint64_t swp, cudaStream_t s);
+void launch4_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
+                         const uint64_t* a, const uint64_t* b, int count, int L,
+                         cudaStream_t s);
+void launch4_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
+                         int ncomp, int comp, int subst_power, CtMap map,
+                         int count, int L, cudaStream_t s);
+void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                       const DigitDesc* digits, int k, int need_lift, int count,
+                       int L, cudaStream_t s);
+void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
+                            const uint64_t* in, const ScalarPack& sc, int count,
+                            int L, cudaStream_t s);
 
 }  // namespace shg

@@ -170,13 +170,17 @@ struct NttCore {
     });
   }
 
-  // One inverse pass.  Layer b reads tw[inv_base(b) + (i >> (b+1))] where
-  // inv_base(b) = Nfull - Nfull/2^b + h * Nfull/2^(b+2) (h = 0, Nfull = N for a
-  // full transform).
+  // One inverse pass.  Layer b (local bit) reads
+  //   tw[nfull - nfull / 2^(b + bit_off) + (row << (LOG_N - b - 1)) + (i >> (b+1))]
+  // which is the reference's IterativeGentlemanSande order for a full
+  // transform (bit_off = 0, row = 0), for row r of a transform whose low
+  // LOG_N bits form the rows (bit_off = 0, row = r), and for the columns of
+  // one whose low bit_off bits were done first (row = 0).
   template <int p>
   __device__ __forceinline__ static void inv_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
-                                                  int nfull, int h, uint64_t q,
+                                                  int nfull, int bit_off,
+                                                  int row, uint64_t q,
                                                   uint64_t two_q) {
     constexpr int clo = inv_clo(p);
     constexpr int plo = inv_plo(p);
@@ -185,8 +189,8 @@ struct NttCore {
     static_for<0, RR>([&](auto ii) {
       constexpr int lb = plo + decltype(ii)::value;  // low to high
       constexpr int b = clo + lb;
-      const int base = nfull - (nfull >> b) + h * (nfull >> (b + 2)) +
-                       (tid_high << (ELOG - lb - 1));
+      const int base = nfull - (nfull >> (b + bit_off)) +
+                       (row << (LOG_N - b - 1)) + (tid_high << (ELOG - lb - 1));
       static_for<0, (E >> (lb + 1))>([&](auto uu) {
         constexpr int u = decltype(uu)::value;
         const Tw w = load_tw(tw + base + u);
@@ -199,47 +203,77 @@ struct NttCore {
     });
   }
 
+  // Shared-memory position maps for the register exchanges: one transform
+  // per shared tile (swizzled), or CB interleaved column transforms (element
+  // i of column j at i * CB + j, conflict-free without a swizzle).
+  struct SwzMap {
+    uint64_t* sm;
+    __device__ __forceinline__ uint64_t& operator()(int i) const { return sm[swz(i)]; }
+  };
+  struct ColMap {
+    uint64_t* sm;
+    int cb, j;
+    __device__ __forceinline__ uint64_t& operator()(int i) const { return sm[i * cb + j]; }
+  };
+
   // Register exchange through shared memory from layout clo_a to clo_b.
-  // Caller guarantees sm is not being read by a previous exchange.
+  template <class Map>
   __device__ __forceinline__ static void exchange(uint64_t (&x)[E], int tid,
-                                                  uint64_t* sm, int clo_a,
+                                                  const Map& m, int clo_a,
                                                   int clo_b) {
 #pragma unroll
-    for (int k = 0; k < E; ++k) sm[swz(idx(tid, k, clo_a))] = x[k];
+    for (int k = 0; k < E; ++k) m(idx(tid, k, clo_a)) = x[k];
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < E; ++k) x[k] = sm[swz(idx(tid, k, clo_b))];
+    for (int k = 0; k < E; ++k) x[k] = m(idx(tid, k, clo_b));
     __syncthreads();
   }
 
   // Full forward transform on registers (input in fwd_in layout, values in
   // [0, 4q) -- below q for LAZY; output in fwd_out layout, values in [0, 4q),
   // or below (2 LOG_N + 1) q for LAZY).
+  template <bool LAZY = false, class Map = SwzMap>
+  __device__ __forceinline__ static void forward_m(uint64_t (&x)[E], int tid,
+                                                   const Map& m,
+                                                   const Tw* __restrict__ tw,
+                                                   int tw_mult, uint64_t q,
+                                                   uint64_t two_q) {
+    static_for<0, P>([&](auto pp) {
+      constexpr int p = decltype(pp)::value;
+      fwd_pass<p, LAZY>(x, tid, tw, tw_mult, q, two_q);
+      if constexpr (p + 1 < P) exchange(x, tid, m, fwd_clo(p), fwd_clo(p + 1));
+    });
+  }
   template <bool LAZY = false>
   __device__ __forceinline__ static void forward(uint64_t (&x)[E], int tid,
                                                  uint64_t* sm,
                                                  const Tw* __restrict__ tw,
                                                  int tw_mult, uint64_t q,
                                                  uint64_t two_q) {
-    static_for<0, P>([&](auto pp) {
-      constexpr int p = decltype(pp)::value;
-      fwd_pass<p, LAZY>(x, tid, tw, tw_mult, q, two_q);
-      if constexpr (p + 1 < P) exchange(x, tid, sm, fwd_clo(p), fwd_clo(p + 1));
-    });
+    forward_m<LAZY>(x, tid, SwzMap{sm}, tw, tw_mult, q, two_q);
   }
 
   // Full inverse transform without the n^{-1} scaling (input in inv_in
   // layout, values in [0, 2q); output in inv_out layout, values in [0, 2q)).
+  template <class Map = SwzMap>
+  __device__ __forceinline__ static void inverse_m(uint64_t (&x)[E], int tid,
+                                                   const Map& m,
+                                                   const Tw* __restrict__ tw,
+                                                   int nfull, int bit_off,
+                                                   int row, uint64_t q,
+                                                   uint64_t two_q) {
+    static_for<0, P>([&](auto pp) {
+      constexpr int p = decltype(pp)::value;
+      inv_pass<p>(x, tid, tw, nfull, bit_off, row, q, two_q);
+      if constexpr (p + 1 < P) exchange(x, tid, m, inv_clo(p), inv_clo(p + 1));
+    });
+  }
   __device__ __forceinline__ static void inverse(uint64_t (&x)[E], int tid,
                                                  uint64_t* sm,
                                                  const Tw* __restrict__ tw,
-                                                 int nfull, int h, uint64_t q,
+                                                 int nfull, int row, uint64_t q,
                                                  uint64_t two_q) {
-    static_for<0, P>([&](auto pp) {
-      constexpr int p = decltype(pp)::value;
-      inv_pass<p>(x, tid, tw, nfull, h, q, two_q);
-      if constexpr (p + 1 < P) exchange(x, tid, sm, inv_clo(p), inv_clo(p + 1));
-    });
+    inverse_m(x, tid, SwzMap{sm}, tw, nfull, 0, row, q, two_q);
   }
 };
 

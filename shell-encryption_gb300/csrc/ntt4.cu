@@ -1,0 +1,492 @@
+// Four-step NTT kernels (n = 2^14, 2^15) and the fused operations built on
+// them.  Phase kernels take a source policy (how transform g's inputs are
+// produced) and a sink policy (where its outputs go); see ntt4.cuh.
+#include "ntt4.cuh"
+
+namespace shg {
+namespace {
+
+template <class K>
+void set_smem4(K kernel, int smem) {
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+template <bool LAZY, int E>
+__device__ __forceinline__ void finish_fwd(uint64_t (&x)[E], uint64_t q,
+                                           uint64_t two_q, uint64_t bar) {
+#pragma unroll
+  for (int k = 0; k < E; ++k)
+    x[k] = LAZY ? reduce_full(x[k], q, bar) : reduce_4q(x[k], q, two_q);
+}
+
+// ---------------------------------------------------------------------------
+// Forward phase-1 sources: element `idx` of transform g (column loads).
+// ---------------------------------------------------------------------------
+
+template <int LOG_N>
+struct FwdSrcPlain {
+  const uint64_t* p;
+  struct H {
+    const uint64_t* base;
+    __device__ __forceinline__ uint64_t operator()(int i) const { return base[i]; }
+  };
+  __device__ H bind(int g, int, const CtxDev&) const {
+    return H{p + ((size_t)g << LOG_N)};
+  }
+};
+
+// RnsGadget::Decompose's digit of the exported source limb, balanced-lifted
+// to the output limb when needed (rns/rns_gadget.cc:108-153).
+template <int LOG_N>
+struct FwdSrcDigit {
+  const uint64_t* X;
+  const DigitDesc* digits;
+  int k, L, need_lift;
+  struct H {
+    const uint64_t* base;
+    int shift, lift;
+    uint64_t mask, half_qi, q, bar, add;
+    __device__ __forceinline__ uint64_t operator()(int i) const {
+      uint64_t v = (base[i] >> shift) & mask;
+      if (lift) {
+        const bool neg = v > half_qi;
+        v = reduce_2q(v - mulhi64(v, bar) * q, q);
+        if (neg) v += add;
+      }
+      return v;
+    }
+  };
+  __device__ H bind(int g, int j, const CtxDev& c) const {
+    const int pd = g / L;
+    const int di = pd % k, p = pd / k;
+    const DigitDesc dd = digits[di];
+    H h;
+    h.base = X + (((size_t)p * L + dd.src_limb) << LOG_N);
+    h.shift = dd.shift;
+    h.mask = dd.mask;
+    h.lift = need_lift;
+    h.half_qi = c.primes[dd.src_limb].half_q;
+    h.q = c.primes[j].q;
+    h.bar = c.primes[j].barrett;
+    h.add = dd.src_limb != j ? h.q - c.qmod[dd.src_limb * c.L + j] : 0;
+    return h;
+  }
+};
+
+// ModReduceLsb: balanced lift of the top limb's plain coefficients to q_i
+// (rns/rns_polynomial.cc:307-313).
+template <int LOG_N>
+struct FwdSrcModLift {
+  const uint64_t* Y;
+  int Lr;
+  struct H {
+    const uint64_t* base;
+    uint64_t half_ql, q, bar, add;
+    __device__ __forceinline__ uint64_t operator()(int i) const {
+      uint64_t y = base[i];
+      const bool neg = y > half_ql;
+      y = reduce_2q(y - mulhi64(y, bar) * q, q);
+      if (neg) y += add;
+      return y;
+    }
+  };
+  __device__ H bind(int g, int i, const CtxDev& c) const {
+    H h;
+    h.base = Y + ((size_t)(g / Lr) << LOG_N);
+    h.half_ql = c.primes[Lr].half_q;
+    h.q = c.primes[i].q;
+    h.bar = c.primes[i].barrett;
+    h.add = h.q - c.qmod[Lr * c.L + i];
+    return h;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Forward phase-2 sinks: 16 canonical values at idx0..idx0+15 of transform g.
+// ---------------------------------------------------------------------------
+
+template <int LOG_N>
+struct FwdDstPlain {
+  uint64_t* p;
+  struct H {
+    uint64_t* base;
+    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
+#pragma unroll
+      for (int k = 0; k < 16; k += 2)
+        *reinterpret_cast<ulonglong2*>(base + i0 + k) = make_ulonglong2(x[k], x[k + 1]);
+    }
+  };
+  __device__ H bind(int g, int, const CtxDev&) const { return H{p + ((size_t)g << LOG_N)}; }
+};
+
+// ModReduceLsb combine: out_i = in_i * c1 + delta_i * c2
+// (rns/rns_polynomial.cc:314-323).
+template <int LOG_N>
+struct FwdDstModCombine {
+  uint64_t* out;
+  const uint64_t* in;
+  int L;
+  ScalarPack sc;
+  struct H {
+    uint64_t* o;
+    const uint64_t* a;
+    uint64_t q, c1, c1p, c2, c2p;
+    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
+#pragma unroll
+      for (int k = 0; k < 16; k += 2) {
+        const ulonglong2 av = *reinterpret_cast<const ulonglong2*>(a + i0 + k);
+        ulonglong2 r;
+        r.x = reduce_2q_full(shoup(av.x, c1, c1p, q) + shoup(x[k], c2, c2p, q), q);
+        r.y = reduce_2q_full(shoup(av.y, c1, c1p, q) + shoup(x[k + 1], c2, c2p, q), q);
+        *reinterpret_cast<ulonglong2*>(o + i0 + k) = r;
+      }
+    }
+  };
+  __device__ H bind(int g, int i, const CtxDev& c) const {
+    const int Lr = L - 1;
+    const int p = g / Lr;
+    H h;
+    h.o = out + ((size_t)g << LOG_N);
+    h.a = in + (((size_t)p * L + i) << LOG_N);
+    h.q = c.primes[i].q;
+    h.c1 = sc.v[4 * i];
+    h.c1p = sc.v[4 * i + 1];
+    h.c2 = sc.v[4 * i + 2];
+    h.c2p = sc.v[4 * i + 3];
+    return h;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Inverse phase-1 sources: 16 values at idx0..idx0+15 of transform g (rows).
+// ---------------------------------------------------------------------------
+
+template <int LOG_N>
+struct InvSrcPlain {
+  const uint64_t* p;
+  int first, stride;  // source limb of transform g: first + g * stride
+  struct H {
+    const uint64_t* base;
+    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
+#pragma unroll
+      for (int k = 0; k < 16; k += 2) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(base + i0 + k);
+        x[k] = v.x;
+        x[k + 1] = v.y;
+      }
+    }
+  };
+  __device__ H bind(int g, int, const CtxDev&) const {
+    return H{p + (((size_t)first + (size_t)g * stride) << LOG_N)};
+  }
+};
+
+// One component of ciphertext map(p), optionally read through the NTT-domain
+// substitution X -> X^power (rns/rns_polynomial.cc:236-256).
+template <int LOG_N>
+struct InvSrcComponent {
+  const uint64_t* ct;
+  int ncomp, comp, power, L;
+  CtMap map;
+  struct H {
+    const uint64_t* base;
+    int power;
+    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
+      if (power > 0) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const unsigned j = __brev((unsigned)(i0 + k)) >> (32 - LOG_N);
+          const unsigned t = ((unsigned)((power - 1) >> 1) + j * (unsigned)power) &
+                             ((1u << LOG_N) - 1);
+          x[k] = base[__brev(t) >> (32 - LOG_N)];
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 16; k += 2) {
+          const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(base + i0 + k);
+          x[k] = v.x;
+          x[k + 1] = v.y;
+        }
+      }
+    }
+  };
+  __device__ H bind(int g, int l, const CtxDev&) const {
+    const int p = g / L;
+    return H{ct + (((map(p) * ncomp + comp) * (size_t)L + l) << LOG_N), power};
+  }
+};
+
+// RnsRlweCiphertext::Mul for degree-1 inputs (rns/rns_ciphertext.h:501-524):
+// writes (c0, c1) of the product and yields its degree-2 component.
+template <int LOG_N>
+struct InvSrcTensor {
+  const uint64_t* a;
+  const uint64_t* b;
+  uint64_t* out01;
+  int L;
+  struct H {
+    const uint64_t *a0, *b0;
+    uint64_t* o0;
+    size_t Ln;
+    uint64_t q, qinv;
+    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
+#pragma unroll
+      for (int k = 0; k < 16; k += 2) {
+        const ulonglong2 va0 = *reinterpret_cast<const ulonglong2*>(a0 + i0 + k);
+        const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a0 + Ln + i0 + k);
+        const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b0 + i0 + k);
+        const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b0 + Ln + i0 + k);
+        ulonglong2 r0, r1;
+        r0.x = mont_mul(va0.x, vb0.x, q, qinv);
+        r0.y = mont_mul(va0.y, vb0.y, q, qinv);
+        uint64_t lo = 0, hi = 0;
+        mac128(lo, hi, va0.x, vb1.x);
+        mac128(lo, hi, va1.x, vb0.x);
+        r1.x = redc128(lo, hi, q, qinv);
+        lo = 0;
+        hi = 0;
+        mac128(lo, hi, va0.y, vb1.y);
+        mac128(lo, hi, va1.y, vb0.y);
+        r1.y = redc128(lo, hi, q, qinv);
+        x[k] = mont_mul(va1.x, vb1.x, q, qinv);
+        x[k + 1] = mont_mul(va1.y, vb1.y, q, qinv);
+        *reinterpret_cast<ulonglong2*>(o0 + i0 + k) = r0;
+        *reinterpret_cast<ulonglong2*>(o0 + Ln + i0 + k) = r1;
+      }
+    }
+  };
+  __device__ H bind(int g, int l, const CtxDev& c) const {
+    const int ct = g / L;
+    H h;
+    h.Ln = (size_t)L << LOG_N;
+    const size_t off = (size_t)ct * 2 * h.Ln + ((size_t)l << LOG_N);
+    h.a0 = a + off;
+    h.b0 = b + off;
+    h.o0 = out01 + off;
+    h.q = c.primes[l].q;
+    h.qinv = c.primes[l].inv_modulus;
+    return h;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Inverse phase-2 sink: scaled value at idx of transform g (column stores).
+// mode 0: x n^{-1}; 1: x n^{-1} 2^-64 (ExportInt folded); 2: x (sw, swp).
+// ---------------------------------------------------------------------------
+
+template <int LOG_N>
+struct InvDstScale {
+  uint64_t* p;
+  int mode;
+  uint64_t sw, swp;
+  struct H {
+    uint64_t* base;
+    uint64_t w, wp, q;
+    __device__ __forceinline__ void operator()(int i, uint64_t x) const {
+      base[i] = shoup(x, w, wp, q);
+    }
+  };
+  __device__ H bind(int g, int l, const CtxDev& c) const {
+    const PrimeDev* P = c.primes + l;
+    H h;
+    h.base = p + ((size_t)g << LOG_N);
+    h.q = P->q;
+    h.w = mode == 0 ? P->n_inv : (mode == 1 ? P->n_inv_r : sw);
+    h.wp = mode == 0 ? P->n_inv_shoup : (mode == 1 ? P->n_inv_r_shoup : swp);
+    return h;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Phase kernels.
+// ---------------------------------------------------------------------------
+
+template <int LOG_N, bool LAZY, class Src>
+__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
+    k4_fwd_cols(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::CC;
+  extern __shared__ uint64_t smem[];
+  const int g = blockIdx.x / S::COL_TILES, tile = blockIdx.x % S::COL_TILES;
+  const int j = threadIdx.x % S::COLS, t = threadIdx.x / S::COLS;
+  const int col = tile * S::COLS + j;
+  const int l = pm(g);
+  const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
+  const auto h = src.bind(g, l, c);
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) x[k] = h((C::fwd_in_idx(t, k) << S::B) | col);
+  C::template forward_m<LAZY>(x, t, typename C::ColMap{smem, S::COLS, j},
+                              c.tw_fwd + ((size_t)l << LOG_N), 1, q, two_q);
+  uint64_t* dst = buf + ((size_t)g << LOG_N);
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) dst[(C::fwd_out_idx(t, k) << S::B) | col] = x[k];
+}
+
+template <int LOG_N, bool LAZY, class Dst>
+__global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
+    k4_fwd_rows(const uint64_t* buf, Dst dst, PrimeMap pm, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::RC;
+  extern __shared__ uint64_t smem[];
+  const int g = blockIdx.x / S::ROW_TILES, tile = blockIdx.x % S::ROW_TILES;
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  const int row = tile * S::ROWS + sub;
+  const int l = pm(g);
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t* src = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) x[k] = src[C::fwd_in_idx(tid, k)];
+  C::template forward_m<LAZY>(x, tid, RowMap<S::B>{smem, sub},
+                              c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
+                              two_q);
+  finish_fwd<LAZY>(x, q, two_q, P->barrett);
+  dst.bind(g, l, c)((row << S::B) | C::fwd_out_idx(tid, 0), x);
+}
+
+template <int LOG_N, class Src>
+__global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
+    k4_inv_rows(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::RC;
+  extern __shared__ uint64_t smem[];
+  const int g = blockIdx.x / S::ROW_TILES, tile = blockIdx.x % S::ROW_TILES;
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  const int row = tile * S::ROWS + sub;
+  const int l = pm(g);
+  const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
+  uint64_t x[C::E];
+  src.bind(g, l, c)((row << S::B) | C::inv_in_idx(tid, 0), x);
+  C::inverse_m(x, tid, RowMap<S::B>{smem, sub}, c.tw_inv + ((size_t)l << LOG_N),
+               S::N, 0, row, q, two_q);
+  uint64_t* dst = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) dst[C::inv_out_idx(tid, k)] = x[k];
+}
+
+template <int LOG_N, class Dst>
+__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
+    k4_inv_cols(const uint64_t* buf, Dst dst, PrimeMap pm, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::CC;
+  extern __shared__ uint64_t smem[];
+  const int g = blockIdx.x / S::COL_TILES, tile = blockIdx.x % S::COL_TILES;
+  const int j = threadIdx.x % S::COLS, t = threadIdx.x / S::COLS;
+  const int col = tile * S::COLS + j;
+  const int l = pm(g);
+  const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
+  const uint64_t* src = buf + ((size_t)g << LOG_N);
+  uint64_t x[C::E];
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) x[k] = src[(C::inv_in_idx(t, k) << S::B) | col];
+  C::inverse_m(x, t, typename C::ColMap{smem, S::COLS, j},
+               c.tw_inv + ((size_t)l << LOG_N), S::N, S::B, 0, q, two_q);
+  const auto h = dst.bind(g, l, c);
+#pragma unroll
+  for (int k = 0; k < C::E; ++k) h((C::inv_out_idx(t, k) << S::B) | col, x[k]);
+}
+
+template <int LOG_N, class Src, class Dst>
+void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
+          uint64_t* buf, int num, cudaStream_t s) {
+  using S = Ntt4<LOG_N>;
+  if (c.small_q) {
+    auto k1 = k4_fwd_cols<LOG_N, true, Src>;
+    auto k2 = k4_fwd_rows<LOG_N, true, Dst>;
+    set_smem4(k1, S::COL_SMEM);
+    set_smem4(k2, S::ROW_SMEM);
+    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
+    k2<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm, c);
+  } else {
+    auto k1 = k4_fwd_cols<LOG_N, false, Src>;
+    auto k2 = k4_fwd_rows<LOG_N, false, Dst>;
+    set_smem4(k1, S::COL_SMEM);
+    set_smem4(k2, S::ROW_SMEM);
+    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
+    k2<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm, c);
+  }
+}
+
+template <int LOG_N, class Src, class Dst>
+void inv4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
+          uint64_t* buf, int num, cudaStream_t s) {
+  using S = Ntt4<LOG_N>;
+  auto k1 = k4_inv_rows<LOG_N, Src>;
+  auto k2 = k4_inv_cols<LOG_N, Dst>;
+  set_smem4(k1, S::ROW_SMEM);
+  set_smem4(k2, S::COL_SMEM);
+  k1<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(src, pm, buf, c);
+  k2<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(buf, dst, pm, c);
+}
+
+#define SHG_DISPATCH4(log_n, F) \
+  switch (log_n) {              \
+    case 14: F(14); break;      \
+    case 15: F(15); break;      \
+    default: break;             \
+  }
+
+}  // namespace
+
+void launch4_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                     int L, cudaStream_t s) {
+#define F(LN) fwd4<LN>(c, FwdSrcPlain<LN>{in}, FwdDstPlain<LN>{out}, PrimeMap{0, 1, L}, out, num, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
+                     int L, int in_first, int in_stride, int mode, uint64_t sw,
+                     uint64_t swp, cudaStream_t s) {
+#define F(LN)                                                                    \
+  inv4<LN>(c, InvSrcPlain<LN>{in, in_first, in_stride},                         \
+           InvDstScale<LN>{out, mode, sw, swp}, PrimeMap{in_first, in_stride, L}, \
+           out, num, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
+                         const uint64_t* a, const uint64_t* b, int count, int L,
+                         cudaStream_t s) {
+#define F(LN)                                                                  \
+  inv4<LN>(c, InvSrcTensor<LN>{a, b, out01, L}, InvDstScale<LN>{X, 1, 0, 0},  \
+           PrimeMap{0, 1, L}, X, count * L, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
+                         int ncomp, int comp, int subst_power, CtMap map,
+                         int count, int L, cudaStream_t s) {
+#define F(LN)                                                                  \
+  inv4<LN>(c, InvSrcComponent<LN>{ct, ncomp, comp, subst_power, L, map},      \
+           InvDstScale<LN>{X, 1, 0, 0}, PrimeMap{0, 1, L}, X, count * L, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                       const DigitDesc* digits, int k, int need_lift, int count,
+                       int L, cudaStream_t s) {
+#define F(LN)                                                                  \
+  fwd4<LN>(c, FwdSrcDigit<LN>{X, digits, k, L, need_lift}, FwdDstPlain<LN>{D}, \
+           PrimeMap{0, 1, L}, D, count * k * L, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
+                            const uint64_t* in, const ScalarPack& sc, int count,
+                            int L, cudaStream_t s) {
+#define F(LN)                                                                  \
+  fwd4<LN>(c, FwdSrcModLift<LN>{Y, L - 1}, FwdDstModCombine<LN>{out, in, L, sc}, \
+           PrimeMap{0, 1, L - 1}, out, count * (L - 1), s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+}  // namespace shg

@@ -88,6 +88,7 @@ SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_uint64)]),
     "shg_context_reserve": (ctypes.c_int, [_vp, _sz]),
     "shg_context_set_chunk": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "shg_context_set_four_step_min": (ctypes.c_int, [_vp, ctypes.c_int]),
 }
 
 _lib = None

@@ -66,7 +66,32 @@ def test_context_validation(sg):
 # --------------------------------------------------------------------------
 
 NTT_CASES = [(log_n, qs) for log_n in range(1, 15) for qs in ([Q45[0], Q45[1]],)] + [
-    (12, [Q59]), (12, [Q60]), (11, Q50[:4]), (13, Q50[:3]), (14, Q45)]
+    (12, [Q59]), (12, [Q60]), (11, Q50[:4]), (13, Q50[:3]), (14, Q45), (15, Q50[:2]),
+    (15, [Q50[5]])]
+
+
+@pytest.mark.parametrize("four_step_min", [14, 15])
+def test_ntt_2_14_both_kernels(sg, oracle, four_step_min):
+    """n = 2^14 runs on the four-step kernels by default and on the
+    one-CTA-per-limb kernel when the threshold is raised; both are exact."""
+    log_n, qs, n = 14, Q45[:3], 1 << 14
+    x = oracle.uniform_limbs(77, qs, n, 2)
+    rns = oracle.Rns(log_n, qs)
+    ctx = sg.Context(log_n, qs)
+    sg.check(sg.lib().shg_context_set_four_step_min(ctx.h, four_step_min))
+    d = _dev(sg, x)
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, d.ptr, 2, 3, None)
+    assert np.array_equal(d.download(x.shape), np.stack([rns.ntt_fwd(x[i]) for i in range(2)]))
+    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, d.ptr, 2, 3, None)
+    assert np.array_equal(d.download(x.shape), x)
+    k = rns.gadget_dim([20] * 3)
+    kb, ka = oracle.uniform_limbs(78, qs, n, k), oracle.uniform_limbs(79, qs, n, k)
+    a, b = _ct_pair(oracle, qs, n, 1, 80)
+    want = rns.relin(rns.tensor(a[0], b[0]), kb, ka, [20] * 3)
+    key = sg.Key(ctx, [20] * 3, 1, kb, ka)
+    da, db, out = _dev(sg, a), _dev(sg, b), sg.DeviceBuffer(a.nbytes)
+    _run(sg, sg.lib().shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, 1, None)
+    assert np.array_equal(out.download(want.shape), want)
 
 
 @pytest.mark.parametrize("log_n,qs", NTT_CASES)
@@ -199,9 +224,9 @@ def test_pointwise_ops(sg, oracle, log_n, qs):
 # --------------------------------------------------------------------------
 
 @pytest.mark.parametrize("log_n,power", [(3, 3), (6, 5), (10, 1023), (12, 4097), (14, 5),
-                                         (14, 2 * 16384 - 1), (13, 1)])
+                                         (14, 2 * 16384 - 1), (13, 1), (15, 5)])
 def test_substitute(sg, oracle, log_n, power):
-    qs = Q45[:3]
+    qs = Q45[:3] if log_n < 15 else Q50[:3]
     n = 1 << log_n
     x = oracle.uniform_limbs(31, qs, n, 2)
     rns = oracle.Rns(log_n, qs)
@@ -230,7 +255,7 @@ def _ct_pair(oracle, qs, n, count, seed):
     return a, b
 
 
-@pytest.mark.parametrize("log_n,qs", [(5, Q45[:2]), (12, Q50[:4]), (14, Q45)])
+@pytest.mark.parametrize("log_n,qs", [(5, Q45[:2]), (12, Q50[:4]), (14, Q45), (15, Q50[:2])])
 def test_tensor(sg, oracle, log_n, qs):
     n, count = 1 << log_n, 2
     a, b = _ct_pair(oracle, qs, n, count, 40)
@@ -249,6 +274,8 @@ KS_CASES = [
     (12, Q50[:4], [20, 20, 20, 20]),
     (11, Q50[:2], [50, 16]),        # a full-width digit exercises the balanced lift
     (14, Q45, [20] * 6),           # the ct-mult+relin workload's parameters
+    (15, Q50[:3], [20] * 3),
+    (15, Q50[:2], [50, 16]),
 ]
 
 
@@ -279,7 +306,7 @@ def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs):
 
 @pytest.mark.parametrize("log_n,qs,log_bs,power", [
     (4, Q45[:2], [20, 20], 5), (12, Q50[:3], [20, 20, 20], 5 ** 3 % 8192),
-    (13, Q50[:2], [50, 50], 8191), (14, Q45, [20] * 6, 5)])
+    (13, Q50[:2], [50, 50], 8191), (14, Q45, [20] * 6, 5), (15, Q50[:2], [20, 20], 25)])
 def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power):
     n, L, count = 1 << log_n, len(qs), 2
     rns = oracle.Rns(log_n, qs)
@@ -320,7 +347,8 @@ def test_relin_rejects_galois_key(sg, oracle):
 # --------------------------------------------------------------------------
 
 @pytest.mark.parametrize("log_n,qs,is_ntt", [(4, Q45[:2], 1), (12, Q50[:5], 1),
-                                             (14, Q45, 1), (10, Q50[:4], 0), (14, Q45, 0)])
+                                             (14, Q45, 1), (10, Q50[:4], 0), (14, Q45, 0),
+                                             (15, Q50[:3], 1), (15, Q50[:3], 0)])
 def test_modreduce_lsb(sg, oracle, log_n, qs, is_ntt):
     n, L, count, t = 1 << log_n, len(qs), 3, 65537
     x = oracle.uniform_limbs(70, qs, n, count)
