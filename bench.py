@@ -209,6 +209,8 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain-ops", type=int, default=256)
     ap.add_argument("--chunk", type=int, default=0, help="ciphertexts per internal chunk")
+    ap.add_argument("--four-step-min", type=int, default=0,
+                    help="log n from which NTTs use the four-step kernels (default 14)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -231,6 +233,8 @@ def main():
     ctx = sg.Context(LOG_N, QS, T_PLAIN)
     if args.chunk:
         sg.check(lib.shg_context_set_chunk(ctx.h, args.chunk))
+    if args.four_step_min:
+        sg.check(lib.shg_context_set_four_step_min(ctx.h, args.four_step_min))
     k = 18
     kb = splitmix_limbs(1000 + rank, k, QS, n)
     ka = splitmix_limbs(2000 + rank, k, QS, n)
@@ -371,9 +375,11 @@ def main():
         sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
         prof[name] = (ms.value, cnt.value)
     dig_ms, dig_cnt = prof["digit_ntt"]
-    limb_ntts_per_launch = B * k * L / max(dig_cnt, 1)
+    if dig_cnt == 0 or dig_ms <= 0:
+        raise RuntimeError("no k_digit_ntt launch was timed in the profiled step")
+    limb_ntts_per_launch = B * k * L / dig_cnt
     alg_bytes = limb_ntts_per_launch * 16 * n
-    achieved = alg_bytes / (dig_ms / max(dig_cnt, 1) / 1e3) / 1e9
+    achieved = alg_bytes / (dig_ms / dig_cnt / 1e3) / 1e9
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))

@@ -684,10 +684,10 @@ int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
     const uint64_t* src = a.ct + (size_t)c0 * a.ncomp * Ln;
     shg::launch_intt_export(dv, X, src, a.ncomp, a.comp, a.subst_power,
                             CtMap::identity(), cc, L, s);
-    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
-    shg::launch_ks_inner(dv, out + (size_t)c0 * 2 * Ln, D, key->kb, key->ka, k,
-                         key->chunk, src, (size_t)a.ncomp * Ln, CtMap::identity(),
-                         a.base1_zero, a.subst_power, cc, L, s);
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk,
+                          key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src,
+                          (size_t)a.ncomp * Ln, CtMap::identity(), a.base1_zero,
+                          a.subst_power, cc, L, s);
   }
   return launch_status("keyswitch");
 }
@@ -760,8 +760,12 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
   // kernel and the key inner product.
   const size_t x_bytes = (size_t)count * Ln * sizeof(uint64_t);
   const size_t d_per_ct = (size_t)k * Ln * sizeof(uint64_t);
+  // 16 ciphertexts per chunk measured fastest at n = 2^14, L = 6 (the digit
+  // kernel's grid is then ~13.8 K CTAs; smaller chunks that keep D in L2 lose
+  // more to the shorter grids than they gain in the inner product).
   int C = ctx->chunk_cts > 0 ? ctx->chunk_cts
-                             : (int)std::max<size_t>(1, ((size_t)56 << 20) / d_per_ct);
+                             : (int)std::max<size_t>(1, ((size_t)256 << 20) / d_per_ct);
+  C = std::min(C, 16);
   C = std::max(1, std::min(C, count));
   std::lock_guard<std::mutex> lock(ctx->mu);
   if ((st = ctx->ensure_ws(x_bytes + d_per_ct * C))) return st;
@@ -772,10 +776,9 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
   for (int c0 = 0; c0 < count; c0 += C) {
     const int cc = std::min(C, count - c0);
     uint64_t* o = out + (size_t)c0 * 2 * Ln;
-    shg::launch_digit_ntt(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
-                          key->need_lift, cc, L, s);
-    shg::launch_ks_inner(dv, o, D, key->kb, key->ka, k, key->chunk, o, 2 * Ln,
-                         CtMap::identity(), 0, 0, cc, L, s);
+    shg::launch_keyswitch(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
+                          key->need_lift, key->chunk, key->kb, key->ka, o, o,
+                          2 * Ln, CtMap::identity(), 0, 0, cc, L, s);
   }
   return launch_status("bgv_mul_relin");
 }
@@ -850,10 +853,9 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
       const int mc = qc << j;
       uint64_t* blk = out + (size_t)q0 * per_query;
       shg::launch_intt_export(dv, X, blk, 2, 1, power, map, mc, 1, s);
-      shg::launch_digit_ntt(dv, D, X, key->d_digits, key->k, key->need_lift, mc,
-                            1, s);
-      shg::launch_ks_inner(dv, KS, D, key->kb, key->ka, key->k, key->chunk, blk,
-                           2 * (size_t)n, map, 1, power, mc, 1, s);
+      shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->need_lift,
+                            key->chunk, key->kb, key->ka, KS, blk, 2 * (size_t)n,
+                            map, 1, power, mc, 1, s);
       shg::launch_expand_combine(dv, blk, KS, mono + (size_t)j * n, map, 1 << j,
                                  mc, s);
     }
@@ -1150,10 +1152,9 @@ extern "C" int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key,
     const int cc = std::min(C, count - c0);
     const uint64_t* src = ct + (size_t)c0 * 3 * Ln;
     shg::launch_intt_export(dv, X, src, 3, 2, 0, CtMap::identity(), cc, L, s);
-    shg::launch_digit_ntt(dv, D, X, key->d_digits, k, key->need_lift, cc, L, s);
-    shg::launch_ks_inner(dv, out + (size_t)c0 * 2 * Ln, D, key->kb, key->ka, k,
-                         key->chunk, src, 3 * Ln, CtMap::identity(), 0, 0, cc,
-                         L, s);
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk,
+                          key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src, 3 * Ln,
+                          CtMap::identity(), 0, 0, cc, L, s);
   }
   return launch_status("relin_apply_noalloc");
 }

@@ -125,6 +125,16 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
                      int base1_zero, int subst_power, int count, int L,
                      cudaStream_t s);
 
+// Gadget key switch core: digit decomposition + NTT of every digit + key
+// inner product + base add (launch_digit_ntt then launch_ks_inner).
+// D: [count][k][L][n] scratch.
+void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                      const DigitDesc* digits, int k, int need_lift, int chunk,
+                      const uint64_t* kb, const uint64_t* ka, uint64_t* out,
+                      const uint64_t* base, size_t base_ct_elems, CtMap map,
+                      int base1_zero, int subst_power, int count, int L,
+                      cudaStream_t s);
+
 // ModReduceLsb (NTT form): Y [count][n] scratch; out [count][L-1][n].
 // sc.v[4i..4i+3] = (c1, Shoup(c1), c2, Shoup(c2)) for output limb i with
 // out = in_i * c1 + delta_i * c2.  (k_plain, k_shoup) multiply the top limb.
