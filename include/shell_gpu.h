@@ -190,6 +190,15 @@ int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
 int shg_bgv_mul_relin(shg_context* ctx, const shg_key* relin_key, uint64_t* out,
                       const uint64_t* a, const uint64_t* b, int count,
                       shg_stream stream);
+/* shg_bgv_mul_relin on HOST buffers (a, b, out in host memory, page-locked
+ * for full speed): the batch is split into pieces whose host->device copy,
+ * ct-mult+relin and device->host copy run on three streams so transfers
+ * overlap computation.  Ordered after prior work on `stream`; `stream` is
+ * ordered after the last copy back (synchronize it before reading out). */
+int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* relin_key,
+                           uint64_t* out, const uint64_t* a, const uint64_t* b,
+                           int count, shg_stream stream);
+
 /* RnsBgvCiphertext::Substitute(power) then RnsGaloisKey::ApplyTo
  * (rns/rns_bgv_ciphertext.h:161-174): ct [count][2][L][n] -> out. */
 int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,

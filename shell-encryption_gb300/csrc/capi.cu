@@ -171,6 +171,11 @@ struct shg_context {
   int small_q = 0;  // all moduli below 2^58
   int ntt4_min = 14;  // four-step transforms from this log_n up
   std::mutex mu;
+  // Host-buffer pipeline: device staging slots and three streams.
+  uint64_t* io = nullptr;
+  size_t io_bytes = 0;
+  cudaStream_t io_streams[3] = {nullptr, nullptr, nullptr};
+  std::mutex io_mu;
 
   CtxDev dev() const {
     return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min};
@@ -344,6 +349,9 @@ void shg_context_destroy(shg_context* ctx) {
   cudaFree(ctx->d_tw_inv);
   cudaFree(ctx->d_qmod);
   cudaFree(ctx->ws);
+  cudaFree(ctx->io);
+  for (cudaStream_t s : ctx->io_streams)
+    if (s) cudaStreamDestroy(s);
   delete ctx;
 }
 
@@ -726,6 +734,83 @@ int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
   if ((st = check_ptrs({out, ct}))) return st;
   if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
   return keyswitch(ctx, key, out, KsArgs{ct, 2, 1, 0, 1}, count, (cudaStream_t)s);
+}
+
+int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
+                           const uint64_t* a, const uint64_t* b, int count,
+                           shg_stream stream) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if (!out || !a || !b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  const size_t ct_elems = 2 * (size_t)key->L * ctx->n;
+  const size_t ct_bytes = ct_elems * sizeof(uint64_t);
+  // Pieces of 64 ciphertexts, two staging slots of (a, b, out) each.
+  const int P = std::min(count, 64);
+  const size_t slot = 3 * (size_t)P * ct_bytes;
+  std::lock_guard<std::mutex> io_lock(ctx->io_mu);
+  if (ctx->io_bytes < 2 * slot) {
+    SHG_CUDA(cudaDeviceSynchronize());
+    cudaFree(ctx->io);
+    ctx->io = nullptr;
+    ctx->io_bytes = 0;
+    cudaError_t e = cudaMalloc(&ctx->io, 2 * slot);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(SHG_RESOURCE_EXHAUSTED, "cannot reserve host-pipeline staging");
+    }
+    ctx->io_bytes = 2 * slot;
+  }
+  for (cudaStream_t& s : ctx->io_streams)
+    if (!s) SHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  cudaStream_t s_in = ctx->io_streams[0], s_comp = ctx->io_streams[1],
+               s_out = ctx->io_streams[2];
+  cudaStream_t user = (cudaStream_t)stream;
+  const int pieces = (count + P - 1) / P;
+  std::vector<cudaEvent_t> evs;
+  auto event = [&](cudaEvent_t* e) -> int {
+    SHG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    evs.push_back(*e);
+    return SHG_OK;
+  };
+  cudaEvent_t start;
+  if ((st = event(&start))) return st;
+  SHG_CUDA(cudaEventRecord(start, user));
+  SHG_CUDA(cudaStreamWaitEvent(s_in, start, 0));
+  std::vector<cudaEvent_t> loaded(pieces), computed(pieces), stored(pieces);
+  for (int i = 0; i < pieces; ++i) {
+    if ((st = event(&loaded[i])) || (st = event(&computed[i])) || (st = event(&stored[i])))
+      break;
+  }
+  int rc = st;
+  for (int i = 0; i < pieces && rc == SHG_OK; ++i) {
+    const int c0 = i * P, cc = std::min(P, count - c0);
+    uint64_t* da = ctx->io + (size_t)(i & 1) * (slot / sizeof(uint64_t));
+    uint64_t* db = da + (size_t)P * ct_elems;
+    uint64_t* dout = db + (size_t)P * ct_elems;
+    // Slot reuse: piece i-2 must have been copied back (its compute also
+    // finished reading a, b before that).
+    if (i >= 2) SHG_CUDA(cudaStreamWaitEvent(s_in, stored[i - 2], 0));
+    SHG_CUDA(cudaMemcpyAsync(da, a + (size_t)c0 * ct_elems, cc * ct_bytes,
+                             cudaMemcpyHostToDevice, s_in));
+    SHG_CUDA(cudaMemcpyAsync(db, b + (size_t)c0 * ct_elems, cc * ct_bytes,
+                             cudaMemcpyHostToDevice, s_in));
+    SHG_CUDA(cudaEventRecord(loaded[i], s_in));
+    SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded[i], 0));
+    rc = shg_bgv_mul_relin(ctx, key, dout, da, db, cc, (shg_stream)s_comp);
+    if (rc) break;
+    SHG_CUDA(cudaEventRecord(computed[i], s_comp));
+    SHG_CUDA(cudaStreamWaitEvent(s_out, computed[i], 0));
+    SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * ct_elems, dout, cc * ct_bytes,
+                             cudaMemcpyDeviceToHost, s_out));
+    SHG_CUDA(cudaEventRecord(stored[i], s_out));
+  }
+  if (rc == SHG_OK) {
+    SHG_CUDA(cudaStreamWaitEvent(user, stored[pieces - 1], 0));
+  }
+  for (cudaEvent_t e : evs) cudaEventDestroy(e);
+  return rc;
 }
 
 int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,

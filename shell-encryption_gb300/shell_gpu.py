@@ -54,6 +54,7 @@ SIGNATURES = {
     "shg_relin_apply_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_galois_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_bgv_mul_relin_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_rotate": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_oblivious_expand": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp, _vp,
                                             ctypes.c_int, _vp]),
