@@ -38,9 +38,36 @@ T_PLAIN = 65537
 LOG_BS = [20] * 6
 METRIC = "RNS ct-mult+relin/sec (batched vs plain, same GPU, bit-exact); p50/p99 ms"
 UNIT = "ct-mult+relin/s"
-# DRAM bytes (read + write) of one k_digit_ntt launch over a 16-ciphertext
-# chunk, scaled from the ncu capture in profiles/digit_ntt_ct_mult_relin.md.
-DIGIT_NTT_TRAFFIC_PER_LIMB_NTT = None
+# DRAM bytes (read + write) per ciphertext of each kernel scope, from ncu
+# captures of the same kernels (profiles/); None where not captured.
+TRAFFIC_PER_CT = {}
+# Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
+# step; the four-step key switch runs digit_cols + ks_rows, the unfused one
+# digit_ntt + ks_inner.
+SCOPES = ("tensor_intt", "digit_cols", "ks_rows", "digit_ntt", "ks_inner")
+
+
+def scope_model(name, n, L, k, cts):
+    """(algorithmic DRAM bytes, butterflies) of one launch over `cts` ciphertexts.
+
+    Bytes count each operand once: tensor_intt reads both inputs and writes
+    (c0, c1) and the plain c2 (7 polys); the digit kernels read c2 and write
+    the k digit transforms; the inner-product kernels read the digit
+    transforms, the base and write the result (k + 4 polys) plus the key once.
+    """
+    poly = L * n * 8
+    bfly_ntt = n // 2 * (n.bit_length() - 1)
+    if name == "tensor_intt":
+        return 7 * poly * cts, L * bfly_ntt * cts
+    if name == "digit_ntt":
+        return (1 + k) * poly * cts, k * L * bfly_ntt * cts
+    if name == "digit_cols":
+        return (1 + k) * poly * cts, k * L * (n // 2) * (n.bit_length() - 1 - 7) * cts
+    if name == "ks_rows":
+        return (k + 4) * poly * cts + 2 * k * poly, k * L * (n // 2) * 7 * cts
+    if name == "ks_inner":
+        return (k + 4) * poly * cts + 2 * k * poly, 0
+    raise KeyError(name)
 
 
 def config(batch):
@@ -216,6 +243,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=0, help="ciphertexts per internal chunk")
     ap.add_argument("--four-step-min", type=int, default=0,
                     help="log n from which NTTs use the four-step kernels (default 14)")
+    ap.add_argument("--ks-unfused", action="store_true",
+                    help="separate digit row phase and key inner product kernels")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -240,6 +269,8 @@ def main():
         sg.check(lib.shg_context_set_chunk(ctx.h, args.chunk))
     if args.four_step_min:
         sg.check(lib.shg_context_set_four_step_min(ctx.h, args.four_step_min))
+    if args.ks_unfused:
+        sg.check(lib.shg_context_set_ks_fused(ctx.h, 0))
     k = 18
     kb = splitmix_limbs(1000 + rank, k, QS, n)
     ka = splitmix_limbs(2000 + rank, k, QS, n)
@@ -374,32 +405,51 @@ def main():
     step_device()
     sg.check(lib.shg_profile_stop())
     prof = {}
-    for name in ("tensor_intt", "digit_ntt", "ks_inner"):
+    for name in SCOPES:
         ms, cnt = ctypes.c_double(), ctypes.c_uint64()
         sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
-        prof[name] = (ms.value, cnt.value)
-    dig_ms, dig_cnt = prof["digit_ntt"]
-    if dig_cnt == 0 or dig_ms <= 0:
-        raise RuntimeError("no k_digit_ntt launch was timed in the profiled step")
-    limb_ntts_per_launch = B * k * L / dig_cnt
-    alg_bytes = limb_ntts_per_launch * 16 * n
-    achieved = alg_bytes / (dig_ms / dig_cnt / 1e3) / 1e9
-    peaks = {}
+        if cnt.value:
+            prof[name] = (ms.value, cnt.value)
+    if not prof:
+        raise RuntimeError("no kernel launch was timed in the profiled step")
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
-    traffic = (DIGIT_NTT_TRAFFIC_PER_LIMB_NTT * limb_ntts_per_launch
-               if DIGIT_NTT_TRAFFIC_PER_LIMB_NTT else None)
+    bfly_peak = ctypes.c_double()
+    sg.check(lib.shg_measure_butterfly_rate(ctypes.byref(bfly_peak)))
     step_total = sum(v[0] for v in prof.values())
+    kernels = {}
+    bfly_step, bfly_ms = 0.0, 0.0
+    for name, (ms, cnt) in prof.items():
+        nbytes, bfly = scope_model(name, n, L, k, B / cnt)
+        launch_s = ms / cnt / 1e3
+        kernels[name] = {
+            "share_of_step": ms / step_total, "launches": cnt, "avg_launch_ms": ms / cnt,
+            "algorithmic_bytes_per_launch": nbytes, "achieved_gbs": nbytes / launch_s / 1e9,
+            "butterflies_per_launch": bfly,
+            "int_frac": (bfly / launch_s / bfly_peak.value) if bfly else None,
+        }
+        if bfly:
+            bfly_step += bfly * cnt
+            bfly_ms += ms
+    top = max(prof, key=lambda nm: prof[nm][0])
+    tk = kernels[top]
+    traffic = (TRAFFIC_PER_CT[top] * B / prof[top][1]) if top in TRAFFIC_PER_CT else None
     roofline = {
-        "kernel": "k_digit_ntt<14> (gadget digit extraction + forward NTT)",
-        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-        "algorithmic_bytes_per_launch": alg_bytes,
-        "avg_launch_ms": dig_ms / max(dig_cnt, 1),
-        "share_of_step": {k2: v[0] / step_total for k2, v in prof.items()},
+        "kernel": top, "bound": "hbm", "achieved": tk["achieved_gbs"], "peak": peak,
+        "unit": "GB/s", "frac": tk["achieved_gbs"] / peak, "peak_source": peak_src,
+        "traffic": traffic,
+        "algorithmic_bytes_per_launch": tk["algorithmic_bytes_per_launch"],
+        "avg_launch_ms": tk["avg_launch_ms"],
+        # The transforms are bound by 64-bit integer multiply issue, not HBM:
+        # butterflies/s of the NTT-bearing kernels against the live probe.
+        "integer": {"peak_butterflies_per_s": bfly_peak.value,
+                    "achieved_butterflies_per_s": bfly_step / (bfly_ms / 1e3),
+                    "frac": bfly_step / (bfly_ms / 1e3) / bfly_peak.value,
+                    "peak_source": "shg_measure_butterfly_rate (register-only lazy butterflies)"},
+        "kernels": kernels,
     }
 
     cpu = None

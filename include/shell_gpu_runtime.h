@@ -47,6 +47,10 @@ uint64_t shg_launch_count(void);
  * and accumulates.  query returns the total milliseconds and launch count of
  * one kernel family ("ntt_fwd", "ntt_inv", "digit_ntt", "ks_inner",
  * "tensor_intt", "intt_export", "pointwise", ...). */
+/* Butterflies per second of the NTT's lazy Cooley-Tukey butterfly on
+ * register-resident values, measured on the current device (about 0.1 s of
+ * GPU time): the integer-pipe ceiling of every transform kernel. */
+int shg_measure_butterfly_rate(double* per_second);
 int shg_profile_start(void);
 int shg_profile_stop(void);
 int shg_profile_query(const char* kernel, double* total_ms, uint64_t* launches);
@@ -60,6 +64,10 @@ int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
  * 15 keeps n = 2^14 on the one-CTA-per-limb kernel; n = 2^15 always uses the
  * four-step kernels). */
 int shg_context_set_four_step_min(shg_context* ctx, int log_n);
+/* 1 (default): four-step key switches run the digit row phase and the key
+ * inner product as one kernel; 0: separate row phase, digit NTTs written to
+ * scratch, then the inner product.  Results are identical. */
+int shg_context_set_ks_fused(shg_context* ctx, int on);
 
 #ifdef __cplusplus
 }

@@ -170,6 +170,7 @@ struct shg_context {
   int chunk_cts = 0;
   int small_q = 0;  // all moduli below 2^58
   int ntt4_min = 14;  // four-step transforms from this log_n up
+  int ks_fused = 1;   // fused digit row phase + key inner product
   std::mutex mu;
   // Host-buffer pipeline: device staging slots and three streams.
   uint64_t* io = nullptr;
@@ -178,7 +179,8 @@ struct shg_context {
   std::mutex io_mu;
 
   CtxDev dev() const {
-    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min};
+    return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min,
+                  ks_fused};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -1076,6 +1078,14 @@ int shg_graph_destroy(void* exec) {
 }
 uint64_t shg_launch_count(void) { return shg::g_launch_count.load(); }
 
+int shg_measure_butterfly_rate(double* per_second) {
+  if (!per_second) return fail(SHG_INVALID_ARGUMENT, "null argument");
+  if (shg::measure_butterfly_rate(per_second) != 0)
+    return fail(SHG_INTERNAL, std::string("butterfly probe failed: ") +
+                                  cudaGetErrorString(cudaGetLastError()));
+  return SHG_OK;
+}
+
 namespace {
 struct ProfTotal {
   std::string name;
@@ -1146,6 +1156,12 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
   if (!ctx || log_n < 14 || log_n > 16)
     return fail(SHG_INVALID_ARGUMENT, "four-step threshold must be 14, 15 or 16");
   ctx->ntt4_min = log_n;
+  return SHG_OK;
+}
+int shg_context_set_ks_fused(shg_context* ctx, int on) {
+  if (!ctx || (on != 0 && on != 1))
+    return fail(SHG_INVALID_ARGUMENT, "fused key switch switch must be 0 or 1");
+  ctx->ks_fused = on;
   return SHG_OK;
 }
 

@@ -463,69 +463,44 @@ __global__ void k_tensor(uint64_t* out, const uint64_t* a, const uint64_t* b,
 
 // Key inner product of the gadget key switch (rns_relinearization_key.cc:
 // 219-226, rns_galois_key.cc:265-283, relinearization_key.cc:76-96): 128-bit
-// lazy accumulation of raw products, one REDC per `chunk` terms.  Each thread
-// serves CTB ciphertexts at one (limb, position), so every key element read
-// from L2 is used CTB times.
-template <int CTB>
+// lazy accumulation of raw products, one REDC per `chunk` terms.
 __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
                            const uint64_t* ka, int k, int chunk,
                            const uint64_t* base, size_t base_ct_elems,
                            CtMap map, int base1_zero, int subst_power,
-                           int count, int log_n, int L, CtxDev c) {
+                           size_t total /* count*L*n */, int log_n, int L,
+                           CtxDev c) {
   const size_t n = (size_t)1 << log_n;
   const size_t Ln = (size_t)L * n;
-  const size_t groups = ((size_t)count + CTB - 1) / CTB;
-  const size_t total = groups * Ln;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += stride) {
-    const size_t gp = e / Ln, r = e % Ln;
+    const size_t p = e / Ln, r = e % Ln;
     const int l = (int)(r >> log_n);
     const size_t pos = r & (n - 1);
     const PrimeDev* P = c.primes + l;
     const uint64_t q = P->q, qinv = P->inv_modulus;
-    const size_t p0 = gp * CTB;
-    const int nb = (int)min((size_t)CTB, (size_t)count - p0);
-    uint64_t s0[CTB], s1[CTB];
-#pragma unroll
-    for (int b = 0; b < CTB; ++b) s0[b] = s1[b] = 0;
+    const uint64_t* dp = D + p * (size_t)k * Ln + r;
+    uint64_t s0 = 0, s1 = 0;
     for (int j0 = 0; j0 < k; j0 += chunk) {
       const int j1 = min(k, j0 + chunk);
-      uint64_t lo0[CTB], hi0[CTB], lo1[CTB], hi1[CTB];
-#pragma unroll
-      for (int b = 0; b < CTB; ++b) lo0[b] = hi0[b] = lo1[b] = hi1[b] = 0;
+      uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
       for (int j = j0; j < j1; ++j) {
-        const uint64_t vb = __ldg(kb + (size_t)j * Ln + r);
-        const uint64_t va = __ldg(ka + (size_t)j * Ln + r);
-#pragma unroll
-        for (int b = 0; b < CTB; ++b) {
-          if (b < nb) {
-            const uint64_t d = D[((p0 + b) * (size_t)k + j) * Ln + r];
-            mac128(lo0[b], hi0[b], d, vb);
-            mac128(lo1[b], hi1[b], d, va);
-          }
-        }
+        const uint64_t d = dp[(size_t)j * Ln];
+        mac128(lo0, hi0, d, __ldg(kb + (size_t)j * Ln + r));
+        mac128(lo1, hi1, d, __ldg(ka + (size_t)j * Ln + r));
       }
-#pragma unroll
-      for (int b = 0; b < CTB; ++b) {
-        s0[b] = add_mod(s0[b], redc128(lo0[b], hi0[b], q, qinv), q);
-        s1[b] = add_mod(s1[b], redc128(lo1[b], hi1[b], q, qinv), q);
-      }
+      s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
+      s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
     }
+    const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
     const size_t pos0 =
         subst_power > 0 ? (size_t)subst_src_rt((int)pos, subst_power, log_n)
                         : pos;
-#pragma unroll
-    for (int b = 0; b < CTB; ++b) {
-      if (b < nb) {
-        const size_t p = p0 + b;
-        const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
-        const uint64_t b0 = bp[pos0];
-        const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
-        out[p * 2 * Ln + r] = add_mod(b0, s0[b], q);
-        out[p * 2 * Ln + Ln + r] = add_mod(b1, s1[b], q);
-      }
-    }
+    const uint64_t b0 = bp[pos0];
+    const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
+    out[p * 2 * Ln + r] = add_mod(b0, s0, q);
+    out[p * 2 * Ln + Ln + r] = add_mod(b1, s1, q);
   }
 }
 
@@ -792,9 +767,9 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
   LaunchScope scope_("ks_inner", s);
   // One ciphertext per thread: blocking several ciphertexts per thread to
   // reuse key loads measured slower (lower occupancy, fewer loads in flight).
-  k_ks_inner<1><<<grid_for(total, 256), 256, 0, s>>>(
+  k_ks_inner<<<grid_for(total, 256), 256, 0, s>>>(
       out, D, kb, ka, k, chunk, base, base_ct_elems, map, base1_zero,
-      subst_power, count, c.log_n, L, c);
+      subst_power, total, c.log_n, L, c);
 }
 
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
@@ -804,6 +779,16 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       int base1_zero, int subst_power, int count, int L,
                       cudaStream_t s) {
   if (count <= 0) return;
+  if (use_ntt4(c) && c.ks_fused && ks4_rows_per_cta(k) > 0) {
+    {
+      LaunchScope scope_("digit_cols", s);
+      launch4_digit_cols(c, D, X, digits, k, need_lift, count, L, s);
+    }
+    LaunchScope scope_("ks_rows", s);
+    launch4_ks_rows(c, D, k, chunk, kb, ka, out, base, base_ct_elems, map,
+                    base1_zero, subst_power, count, L, s);
+    return;
+  }
   launch_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
   launch_ks_inner(c, out, D, kb, ka, k, chunk, base, base_ct_elems, map,
                   base1_zero, subst_power, count, L, s);
@@ -866,6 +851,61 @@ void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
   LaunchScope scope_("absorb_sum", s);
   k_absorb_sum<<<grid_for(total, 256), 256, 0, s>>>(out, cts, db, num_items,
                                                     chunk, total, c.log_n, c);
+}
+
+// Integer ceiling of the transforms: the NTT's lazy Cooley-Tukey butterfly
+// (bf_ct_lazy) on register-resident values with one fixed twiddle, ILP
+// independent pairs per thread, no memory traffic.  The values wrap mod 2^64;
+// only the instruction stream matters.
+namespace {
+template <int ILP>
+__global__ void __launch_bounds__(256)
+    k_butterfly_probe(uint64_t* sink, Tw w, uint64_t q, int iters) {
+  const uint64_t two_q = 2 * q;
+  uint64_t x[2 * ILP];
+#pragma unroll
+  for (int i = 0; i < 2 * ILP; ++i)
+    x[i] = (uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u + i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < ILP; ++i) bf_ct_lazy(x[2 * i], x[2 * i + 1], w, q, two_q);
+  }
+  uint64_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < 2 * ILP; ++i) acc ^= x[i];
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+}  // namespace
+
+int measure_butterfly_rate(double* per_second) {
+  constexpr int kIlp = 8, kThreads = 256, kIters = 8192;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return -1;
+  const int blocks = sms * 8;
+  uint64_t* sink = nullptr;
+  if (cudaMalloc(&sink, (size_t)blocks * kThreads * 8) != cudaSuccess) return -1;
+  // 45-bit prime of the ct-mult workload and an arbitrary twiddle below it.
+  const uint64_t q = 35184371138561ull, wv = 1234567890123ull;
+  const Tw w{wv, (uint64_t)(((unsigned __int128)wv << 64) / q)};
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_butterfly_probe<kIlp><<<blocks, kThreads>>>(sink, w, q, 64);
+  cudaEventRecord(a);
+  k_butterfly_probe<kIlp><<<blocks, kThreads>>>(sink, w, q, kIters);
+  cudaEventRecord(b);
+  g_launch_count += 2;
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  if (e != cudaSuccess || ms <= 0) return -1;
+  *per_second = (double)blocks * kThreads * kIlp * kIters / (ms * 1e-3);
+  return 0;
 }
 
 }  // namespace shg

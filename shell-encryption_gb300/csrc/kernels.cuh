@@ -25,6 +25,7 @@ struct CtxDev {
   const uint64_t* qmod;       // [L][L]  q_i mod q_j (plain), row i
   int small_q;                // every q < 2^58: forward NTTs skip per-level reductions
   int ntt4_min;               // log_n from which transforms use the four-step kernels
+  int ks_fused;               // four-step key switch: digit row phase fused with the inner product
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,
@@ -158,6 +159,11 @@ void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
                        const uint64_t* db, int num_items, int chunk, int count,
                        cudaStream_t s);
 
+// Butterflies per second of the NTT's lazy butterfly on register-resident
+// values (the integer ceiling of every transform kernel) on the current
+// device; 0 on success.
+int measure_butterfly_rate(double* per_second);
+
 // Four-step variants (ntt4.cu), n = 2^14 and 2^15; same semantics as the
 // launchers above.
 void launch4_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
@@ -177,5 +183,21 @@ void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
 void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
                             const uint64_t* in, const ScalarPack& sc, int count,
                             int L, cudaStream_t s);
+
+// Fused four-step key switch: launch4_digit_cols runs the digit extraction and
+// column phase of every digit transform into D [count][k][L][n];
+// launch4_ks_rows runs the row phase of all digits of each (ciphertext, limb)
+// together with the key inner product and base add (launch_ks_inner's
+// arguments and output).  ks4_rows_per_cta(k) is the number of rows one CTA
+// of launch4_ks_rows takes, 0 if k digits do not fit one CTA.
+int ks4_rows_per_cta(int k);
+void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                        const DigitDesc* digits, int k, int need_lift, int count,
+                        int L, cudaStream_t s);
+void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
+                     const uint64_t* kb, const uint64_t* ka, uint64_t* out,
+                     const uint64_t* base, size_t base_ct_elems, CtMap map,
+                     int base1_zero, int subst_power, int count, int L,
+                     cudaStream_t s);
 
 }  // namespace shg

@@ -324,16 +324,25 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
   for (int k = 0; k < C::E; ++k) dst[(C::fwd_out_idx(t, k) << S::B) | col] = x[k];
 }
 
+// The CTA takes row `row` of ROWS transforms that share a prime (transform g
+// has limb g mod pm.L for every forward use), so the sub-rows read the same
+// twiddles and the loads hit in L1.
 template <int LOG_N, bool LAZY, class Dst>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
-    k4_fwd_rows(const uint64_t* buf, Dst dst, PrimeMap pm, CtxDev c) {
+    k4_fwd_rows(const uint64_t* buf, Dst dst, PrimeMap pm, int num, CtxDev c) {
   using S = Ntt4<LOG_N>;
   using C = typename S::RC;
   extern __shared__ uint64_t smem[];
-  const int g = blockIdx.x / S::ROW_TILES, tile = blockIdx.x % S::ROW_TILES;
+  const int rows = 1 << S::A;
+  const int per_class = num / pm.L;
+  const int groups = (per_class + S::ROWS - 1) / S::ROWS;
+  const int row = blockIdx.x % rows;
+  const int cg = blockIdx.x / rows;
+  const int l = cg / groups, grp = cg % groups;
   const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
-  const int row = tile * S::ROWS + sub;
-  const int l = pm(g);
+  const int m = grp * S::ROWS + sub;
+  const bool active = m < per_class;
+  const int g = l + pm.L * (active ? m : per_class - 1);
   const PrimeDev* P = c.primes + l;
   const uint64_t q = P->q, two_q = P->two_q;
   const uint64_t* src = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
@@ -344,7 +353,88 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
                               c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
                               two_q);
   finish_fwd<LAZY>(x, q, two_q, P->barrett);
-  dst.bind(g, l, c)((row << S::B) | C::fwd_out_idx(tid, 0), x);
+  if (active) dst.bind(g, l, c)((row << S::B) | C::fwd_out_idx(tid, 0), x);
+}
+
+// Forward row phase of all k gadget digits of (ciphertext p, limb l), fused
+// with the key inner product and base add of the key switch
+// (rns_relinearization_key.cc:219-226, rns_galois_key.cc:265-283,
+// relinearization_key.cc:76-96).  The CTA runs rows tile*R .. tile*R+R-1 of
+// the k digit transforms (sub-row r*k + j: row r, digit j; they share the
+// prime and the row, so they read the same twiddles), parks the canonical NTT
+// values in shared memory, and then each thread produces output slots:
+//   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
+// with 128-bit lazy accumulation, one REDC per `chunk` digits.  The digit
+// transforms never go back to memory.  Arguments as in launch_ks_inner.
+constexpr int kKsRowsMaxThreads = 512;
+
+template <int LOG_N, bool LAZY>
+__global__ void __maxnreg__(96)
+    k4_ks_rows(const uint64_t* buf, int k, int R, int chunk, const uint64_t* kb,
+               const uint64_t* ka, uint64_t* out, const uint64_t* base,
+               size_t base_ct_elems, CtMap map, int base1_zero, int subst_power,
+               int L, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::RC;
+  extern __shared__ uint64_t smem[];
+  const int tiles = (1 << S::A) / R;
+  const int tile = blockIdx.x % tiles;
+  const int pl = blockIdx.x / tiles;
+  const int l = pl % L;
+  const size_t p = (size_t)(pl / L);
+  const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  const int r = sub / k, j = sub % k;
+  const int row = tile * R + r;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t* src =
+      buf + (((p * k + j) * L + l) << LOG_N) + ((size_t)row << S::B);
+  uint64_t x[C::E];
+#pragma unroll
+  for (int e = 0; e < C::E; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
+  C::template forward_m<LAZY>(x, tid, RowMap<S::B>{smem, sub},
+                              c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
+                              two_q);
+  finish_fwd<LAZY>(x, q, two_q, P->barrett);
+  __syncthreads();  // every sub-row is done with its exchange tile
+  {
+    const RowMap<S::B> park{smem, sub};
+    const int i0 = C::fwd_out_idx(tid, 0);
+#pragma unroll
+    for (int e = 0; e < C::E; ++e) park(i0 + e) = x[e];
+  }
+  __syncthreads();
+  const size_t n = (size_t)1 << LOG_N, Ln = (size_t)L * n;
+  const uint64_t qinv = P->inv_modulus;
+  for (int o = threadIdx.x; o < (R << S::B); o += blockDim.x) {
+    const int rr = o >> S::B, e = o & ((1 << S::B) - 1);
+    const int pos = ((tile * R + rr) << S::B) | e;
+    const size_t kr = (size_t)l * n + pos;
+    uint64_t s0 = 0, s1 = 0;
+    for (int j0 = 0; j0 < k; j0 += chunk) {
+      const int j1 = min(k, j0 + chunk);
+      uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+      for (int jj = j0; jj < j1; ++jj) {
+        const uint64_t d = RowMap<S::B>{smem, rr * k + jj}(e);
+        mac128(lo0, hi0, d, __ldg(kb + (size_t)jj * Ln + kr));
+        mac128(lo1, hi1, d, __ldg(ka + (size_t)jj * Ln + kr));
+      }
+      s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
+      s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
+    }
+    const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
+    int pos0 = pos;
+    if (subst_power > 0) {
+      const unsigned jb = __brev((unsigned)pos) >> (32 - LOG_N);
+      const unsigned t = ((unsigned)((subst_power - 1) >> 1) + jb * (unsigned)subst_power) &
+                         ((1u << LOG_N) - 1);
+      pos0 = (int)(__brev(t) >> (32 - LOG_N));
+    }
+    const uint64_t b0 = bp[pos0];
+    const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
+    out[p * 2 * Ln + kr] = add_mod(b0, s0, q);
+    out[p * 2 * Ln + Ln + kr] = add_mod(b1, s1, q);
+  }
 }
 
 template <int LOG_N, class Src>
@@ -389,6 +479,16 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
   for (int k = 0; k < C::E; ++k) h((C::inv_out_idx(t, k) << S::B) | col, x[k]);
 }
 
+// Forward row phase grid: (prime class, group of ROWS transforms, row).
+// Every forward caller passes PrimeMap{0, 1, L} with num a multiple of L.
+template <int LOG_N>
+int row_blocks(int num, PrimeMap pm) {
+  using S = Ntt4<LOG_N>;
+  const int per_class = num / pm.L;
+  const int groups = (per_class + S::ROWS - 1) / S::ROWS;
+  return pm.L * groups * (1 << S::A);
+}
+
 template <int LOG_N, class Src, class Dst>
 void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s) {
@@ -399,14 +499,16 @@ void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
     set_smem4(k1, S::COL_SMEM);
     set_smem4(k2, S::ROW_SMEM);
     k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
-    k2<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm, c);
+    k2<<<row_blocks<LOG_N>(num, pm), S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm,
+                                                                      num, c);
   } else {
     auto k1 = k4_fwd_cols<LOG_N, false, Src>;
     auto k2 = k4_fwd_rows<LOG_N, false, Dst>;
     set_smem4(k1, S::COL_SMEM);
     set_smem4(k2, S::ROW_SMEM);
     k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
-    k2<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm, c);
+    k2<<<row_blocks<LOG_N>(num, pm), S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm,
+                                                                      num, c);
   }
 }
 
@@ -475,6 +577,51 @@ void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
 #define F(LN)                                                                  \
   fwd4<LN>(c, FwdSrcDigit<LN>{X, digits, k, L, need_lift}, FwdDstPlain<LN>{D}, \
            PrimeMap{0, 1, L}, D, count * k * L, s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+int ks4_rows_per_cta(int k) {
+  constexpr int T = NttCore<kNtt4RowBits, 4>::T;
+  for (int R = 1; R <= 4; R *= 2)
+    if ((R * k * T) % 32 == 0 && R * k * T <= kKsRowsMaxThreads) return R;
+  return k >= 1 && k * T <= kKsRowsMaxThreads ? 1 : 0;
+}
+
+void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
+                        const DigitDesc* digits, int k, int need_lift, int count,
+                        int L, cudaStream_t s) {
+#define F(LN)                                                                   \
+  {                                                                             \
+    using S = Ntt4<LN>;                                                         \
+    const FwdSrcDigit<LN> src{X, digits, k, L, need_lift};                      \
+    auto k1 = c.small_q ? k4_fwd_cols<LN, true, FwdSrcDigit<LN>>                \
+                        : k4_fwd_cols<LN, false, FwdSrcDigit<LN>>;              \
+    set_smem4(k1, S::COL_SMEM);                                                 \
+    k1<<<count * k * L * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(       \
+        src, PrimeMap{0, 1, L}, D, c);                                          \
+  }
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
+                     const uint64_t* kb, const uint64_t* ka, uint64_t* out,
+                     const uint64_t* base, size_t base_ct_elems, CtMap map,
+                     int base1_zero, int subst_power, int count, int L,
+                     cudaStream_t s) {
+  const int R = ks4_rows_per_cta(k);
+#define F(LN)                                                                   \
+  {                                                                             \
+    using S = Ntt4<LN>;                                                         \
+    auto kern = c.small_q ? k4_ks_rows<LN, true> : k4_ks_rows<LN, false>;       \
+    const int threads = R * k * S::RC::T;                                       \
+    const int smem = R * k * (1 << S::B) * 8;                                   \
+    set_smem4(kern, smem);                                                      \
+    kern<<<count * L * ((1 << S::A) / R), threads, smem, s>>>(                  \
+        D, k, R, chunk, kb, ka, out, base, base_ct_elems, map, base1_zero,      \
+        subst_power, L, c);                                                     \
+  }
   SHG_DISPATCH4(c.log_n, F)
 #undef F
 }

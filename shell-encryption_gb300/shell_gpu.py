@@ -83,6 +83,7 @@ SIGNATURES = {
     "shg_graph_launch": (ctypes.c_int, [_vp, _vp]),
     "shg_graph_destroy": (ctypes.c_int, [_vp]),
     "shg_launch_count": (ctypes.c_uint64, []),
+    "shg_measure_butterfly_rate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "shg_profile_start": (ctypes.c_int, []),
     "shg_profile_stop": (ctypes.c_int, []),
     "shg_profile_query": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
@@ -90,6 +91,7 @@ SIGNATURES = {
     "shg_context_reserve": (ctypes.c_int, [_vp, _sz]),
     "shg_context_set_chunk": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_set_four_step_min": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "shg_context_set_ks_fused": (ctypes.c_int, [_vp, ctypes.c_int]),
 }
 
 _lib = None

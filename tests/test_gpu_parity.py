@@ -276,11 +276,16 @@ KS_CASES = [
     (14, Q45, [20] * 6),           # the ct-mult+relin workload's parameters
     (15, Q50[:3], [20] * 3),
     (15, Q50[:2], [50, 16]),
+    (14, Q45[:2], [2, 2]),          # 46 digits: one row per CTA, partial last warp
+    (14, Q45[:2], [1, 1]),          # 90 digits: too many for one CTA, unfused path
 ]
 
 
+@pytest.mark.parametrize("ks_fused", [1, 0])
 @pytest.mark.parametrize("log_n,qs,log_bs", KS_CASES)
-def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs):
+def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs, ks_fused):
+    if log_n < 14 and not ks_fused:
+        pytest.skip("the fused key-switch row phase exists for n >= 2^14 only")
     n, L = 1 << log_n, len(qs)
     count = 2 if log_n < 14 else 1
     rns = oracle.Rns(log_n, qs)
@@ -291,9 +296,10 @@ def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs):
     ct3 = np.stack([rns.tensor(a[i], b[i]) for i in range(count)])
     want = np.stack([rns.relin(ct3[i], kb, ka, log_bs) for i in range(count)])
     ctx = sg.Context(log_n, qs)
+    lib = sg.lib()
+    sg.check(lib.shg_context_set_ks_fused(ctx.h, ks_fused))
     key = sg.Key(ctx, log_bs, 1, kb, ka)
     assert key.dimension == k
-    lib = sg.lib()
     d3 = _dev(sg, ct3)
     out = sg.DeviceBuffer(want.nbytes)
     _run(sg, lib.shg_relin_apply, ctx.h, key.h, out.ptr, d3.ptr, count, None)
@@ -307,7 +313,10 @@ def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs):
 @pytest.mark.parametrize("log_n,qs,log_bs,power", [
     (4, Q45[:2], [20, 20], 5), (12, Q50[:3], [20, 20, 20], 5 ** 3 % 8192),
     (13, Q50[:2], [50, 50], 8191), (14, Q45, [20] * 6, 5), (15, Q50[:2], [20, 20], 25)])
-def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power):
+@pytest.mark.parametrize("ks_fused", [1, 0])
+def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power, ks_fused):
+    if log_n < 14 and not ks_fused:
+        pytest.skip("the fused key-switch row phase exists for n >= 2^14 only")
     n, L, count = 1 << log_n, len(qs), 2
     rns = oracle.Rns(log_n, qs)
     k = rns.gadget_dim(log_bs)
@@ -316,8 +325,9 @@ def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power):
     ct = oracle.uniform_limbs(62, qs, n, 2 * count).reshape(count, 2, L, n)
     want = np.stack([rns.galois(ct[i], kb, ka, log_bs) for i in range(count)])
     ctx = sg.Context(log_n, qs)
-    key = sg.Key(ctx, log_bs, power, kb, ka)
     lib = sg.lib()
+    sg.check(lib.shg_context_set_ks_fused(ctx.h, ks_fused))
+    key = sg.Key(ctx, log_bs, power, kb, ka)
     d = _dev(sg, ct)
     out = sg.DeviceBuffer(want.nbytes)
     _run(sg, lib.shg_galois_apply, ctx.h, key.h, out.ptr, d.ptr, count, None)
