@@ -122,6 +122,15 @@ int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
                            uint64_t t, const uint64_t* ql_inv, int is_ntt,
                            int count, int num_limbs, shg_stream stream);
 
+/* RnsGadget::Decompose (rns/rns_gadget.cc:108-153) with the gadget of
+ * log_bs[num_limbs] (rns/rns_gadget.cc:42-102): in [count][num_limbs][n]
+ * (coefficient form) -> out [count][k][num_limbs][n] (coefficient form),
+ * k = sum_i GadgetSize(log q_i, log_bs[i]) (gadget.h:43-47).  out must not
+ * alias in. */
+int shg_gadget_decompose(shg_context* ctx, int num_limbs, const int* log_bs,
+                         uint64_t* out, const uint64_t* in, int count,
+                         shg_stream stream);
+
 /* ---------------------------------------------------------------------------
  * Ciphertexts
  * ------------------------------------------------------------------------- */

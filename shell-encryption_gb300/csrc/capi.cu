@@ -507,6 +507,30 @@ int shg_poly_substitute(shg_context* ctx, uint64_t* out, const uint64_t* in,
   return launch_status("substitute");
 }
 
+int shg_gadget_decompose(shg_context* ctx, int num_limbs, const int* log_bs,
+                         uint64_t* out, const uint64_t* in, int count,
+                         shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (!log_bs)
+    return fail(SHG_INVALID_ARGUMENT,
+                "`log_bs` must contain " + std::to_string(num_limbs) + " elements.");
+  shg::GadgetBases gb{};
+  int k = 0;
+  for (int i = 0; i < num_limbs; ++i) {
+    if (log_bs[i] <= 0 || log_bs[i] >= 63)
+      return fail(SHG_INVALID_ARGUMENT, "log_b must lie in [1, 62]");
+    gb.log_b[i] = log_bs[i];
+    k += (ctx->hp[i].log_q + log_bs[i] - 1) / log_bs[i];  // GadgetSize (gadget.h:43-47)
+  }
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  if (out == in) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `in`");
+  shg::launch_decompose(ctx->dev(), out, in, gb, k, count, num_limbs,
+                        (cudaStream_t)s);
+  return launch_status("gadget decompose");
+}
+
 int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
                            uint64_t t, const uint64_t* ql_inv, int is_ntt,
                            int count, int num_limbs, shg_stream s) {

@@ -504,6 +504,45 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
   }
 }
 
+// RnsGadget::Decompose (rns/rns_gadget.cc:108-153) of coefficient-form
+// polys: digit d of limb i's exported residue (BaseDecompose, gadget.h:
+// 50-79), imported to limb i as is and to every other limb l through
+// ConvertModulusBalanced (modulus_conversion.h:30-157: values above
+// floor(q_i/2) stand for value - q_i).  out [count][k][L][n], Montgomery
+// form, coefficient domain.
+__global__ void k_decompose(uint64_t* out, const uint64_t* in, GadgetBases gb,
+                            int k, size_t total /* count*k*L*n */, int log_n,
+                            int L, CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t Ln = (size_t)L * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e / ((size_t)k * Ln), r = e % ((size_t)k * Ln);
+    const int di = (int)(r / Ln);
+    const size_t rem = r % Ln;
+    const int l = (int)(rem >> log_n);
+    const size_t pos = rem & (n - 1);
+    int i = 0, d = di;
+    for (; i < L; ++i) {
+      const int dims = ((int)c.primes[i].log_q + gb.log_b[i] - 1) / gb.log_b[i];
+      if (d < dims) break;
+      d -= dims;
+    }
+    const PrimeDev* Pi = c.primes + i;
+    const PrimeDev* Pl = c.primes + l;
+    const int b = gb.log_b[i];
+    const uint64_t x = shoup(in[(p * L + i) * n + pos], Pi->inv_r, Pi->inv_r_shoup, Pi->q);
+    uint64_t v = (x >> (d * b)) & ((uint64_t(1) << b) - 1);
+    if (l != i) {
+      const bool neg = v > Pi->half_q;
+      v = reduce_full(v, Pl->q, Pl->barrett);
+      if (neg) v = reduce_2q(v + (Pl->q - c.qmod[i * c.L + l]), Pl->q);
+    }
+    out[e] = shoup(v, Pl->r_mod_q, Pl->r_mod_q_shoup, Pl->q);
+  }
+}
+
 // ModReduceLsb, coefficient form (rns/rns_polynomial.cc:324-342).
 __global__ void k_modreduce_coeff(uint64_t* out, const uint64_t* in,
                                   uint64_t k_plain, uint64_t k_shoup,
@@ -831,6 +870,16 @@ void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
   LaunchScope scope_("modreduce_coeff", s);
   k_modreduce_coeff<<<grid_for(total, 256), 256, 0, s>>>(
       out, in, k_plain, k_shoup, sc, total, c.log_n, L, c);
+}
+
+void launch_decompose(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                      const GadgetBases& gb, int k, int count, int L,
+                      cudaStream_t s) {
+  const size_t total = (size_t)count * k * L * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("decompose", s);
+  k_decompose<<<grid_for(total, 256), 256, 0, s>>>(out, in, gb, k, total,
+                                                   c.log_n, L, c);
 }
 
 void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,

@@ -36,6 +36,11 @@ struct DigitDesc {
   uint64_t mask;  // 2^log_b_i - 1
 };
 
+// Gadget base exponents per limb (RnsGadget log_bs), passed by value.
+struct GadgetBases {
+  int log_b[kMaxLimbs];
+};
+
 // Small per-limb constant arrays passed by value.
 struct ScalarPack {
   uint64_t v[4 * kMaxLimbs];
@@ -147,6 +152,12 @@ void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
                             uint64_t k_plain, uint64_t k_shoup,
                             const ScalarPack& sc, int count, int L,
                             cudaStream_t s);
+
+// RnsGadget::Decompose: in [count][L][n] coefficient form -> out
+// [count][k][L][n] coefficient form (k = sum_i GadgetSize(log q_i, log_b_i)).
+void launch_decompose(const CtxDev& c, uint64_t* out, const uint64_t* in,
+                      const GadgetBases& gb, int k, int count, int L,
+                      cudaStream_t s);
 
 // Oblivious-expand level combine for members p (ciphertext at map(p) of
 // `base`, partner at map(p) + half): hi = (c - ks[p]) * mono; c = c + ks[p].

@@ -44,6 +44,8 @@ SIGNATURES = {
                                            ctypes.c_int, _vp]),
     "shg_poly_modreduce_lsb": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_uint64, _u64p,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_gadget_decompose": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _vp, _vp, ctypes.c_int,
+                                            _vp]),
     "shg_ct_tensor": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "shg_key_create": (ctypes.c_int, [_vp, ctypes.c_int, _ip, ctypes.c_int, _u64p, _u64p,
                                       ctypes.POINTER(_vp)]),

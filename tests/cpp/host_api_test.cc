@@ -1,0 +1,383 @@
+// Parity test of the C++ host classes (rlwe_gpu.h) on the GPU against the C
+// oracle (oracle/shell_oracle.h, a restatement of the reference's CPU code
+// pinned to it by tests/golden).  Written like the reference's own tests:
+// rns/rns_polynomial_test.cc (NTT round trip, arithmetic, Substitute,
+// ModReduceLsb), rns/rns_gadget_test.cc (Decompose),
+// rns/rns_relinearization_key_test.cc, rns/rns_galois_key_test.cc,
+// rns/rns_bgv_ciphertext_test.cc and oblivious_expand_test.cc, plus the
+// reference's status messages on invalid calls.  Prints "ALL OK" and exits 0
+// when every check passes.
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rlwe_gpu.h"
+#include "shell_oracle.h"
+
+using namespace rlwe_gpu;
+
+namespace {
+
+int g_failures = 0;
+int g_checks = 0;
+
+#define EXPECT(cond, what)                                            \
+  do {                                                                \
+    ++g_checks;                                                       \
+    if (!(cond)) {                                                    \
+      ++g_failures;                                                   \
+      std::printf("FAIL %s:%d %s\n", __FILE__, __LINE__, what);       \
+    }                                                                 \
+  } while (0)
+
+#define ASSERT_OK_AND_ASSIGN(lhs, expr)                                          \
+  auto RLWE_GPU_CONCAT_(_r_, __LINE__) = (expr);                                 \
+  if (!RLWE_GPU_CONCAT_(_r_, __LINE__).ok()) {                                   \
+    std::printf("FAIL %s:%d %s\n", __FILE__, __LINE__,                           \
+                RLWE_GPU_CONCAT_(_r_, __LINE__).status().ToString().c_str());    \
+    ++g_failures;                                                                \
+    return;                                                                      \
+  }                                                                              \
+  lhs = std::move(RLWE_GPU_CONCAT_(_r_, __LINE__)).value()
+
+#define EXPECT_OK(expr)                                                    \
+  do {                                                                     \
+    Status _s = (expr);                                                    \
+    ++g_checks;                                                            \
+    if (!_s.ok()) {                                                        \
+      ++g_failures;                                                        \
+      std::printf("FAIL %s:%d %s\n", __FILE__, __LINE__, _s.ToString().c_str()); \
+    }                                                                      \
+  } while (0)
+
+void ExpectError(const Status& s, const std::string& msg, int line) {
+  ++g_checks;
+  if (s.ok() || s.code() != StatusCode::kInvalidArgument || s.message() != msg) {
+    ++g_failures;
+    std::printf("FAIL line %d: expected InvalidArgument \"%s\", got %s\n", line, msg.c_str(),
+                s.ToString().c_str());
+  }
+}
+#define EXPECT_ERROR(expr, msg) ExpectError((expr), (msg), __LINE__)
+
+uint64_t SplitMix(uint64_t& s) {
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// `count` polynomials of uniform residues over qs, flat [count][L][n].
+std::vector<uint64_t> Uniform(uint64_t seed, const std::vector<uint64_t>& qs, int n,
+                              int count) {
+  std::vector<uint64_t> out((size_t)count * qs.size() * n);
+  uint64_t s = seed;
+  for (int c = 0; c < count; ++c)
+    for (size_t l = 0; l < qs.size(); ++l)
+      for (int i = 0; i < n; ++i)
+        out[((size_t)c * qs.size() + l) * n + i] = SplitMix(s) % qs[l];
+  return out;
+}
+
+std::vector<std::vector<uint64_t>> Limbs(const uint64_t* flat, int L, int n) {
+  std::vector<std::vector<uint64_t>> v(L);
+  for (int l = 0; l < L; ++l) v[l].assign(flat + (size_t)l * n, flat + (size_t)(l + 1) * n);
+  return v;
+}
+
+std::vector<uint64_t> Flat(const std::vector<std::vector<uint64_t>>& limbs) {
+  std::vector<uint64_t> out;
+  for (const auto& l : limbs) out.insert(out.end(), l.begin(), l.end());
+  return out;
+}
+
+std::vector<uint64_t> FlatCt(const RnsBgvCiphertext& ct) {
+  std::vector<uint64_t> out;
+  for (int c = 0; c < ct.Len(); ++c) {
+    auto comp = ct.Component(c);
+    auto f = Flat(comp->Coeffs());
+    out.insert(out.end(), f.begin(), f.end());
+  }
+  return out;
+}
+
+const std::vector<uint64_t> kQ45 = {35184371138561ull, 35184370941953ull, 35184370352129ull,
+                                    35184370155521ull, 35184369893377ull, 35184368877569ull};
+const std::vector<uint64_t> kQ50 = {1125899904679937ull, 1125899903827969ull,
+                                    1125899903500289ull};
+const uint64_t kQ60 = 1152921504606830593ull;
+
+void TestContextErrors() {
+  auto bad = RnsContext::Create(10, {35184371138560ull}, {}, 65537);  // even
+  EXPECT(!bad.ok(), "even modulus must be rejected");
+  auto aux = RnsContext::Create(10, kQ45, {kQ50[0]}, 65537);
+  EXPECT(!aux.ok(), "auxiliary primes are rejected");
+}
+
+void TestPolynomial(int log_n, const std::vector<uint64_t>& qs) {
+  const int n = 1 << log_n, L = (int)qs.size();
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, qs, {}, 65537));
+  const Moduli moduli = ctx->MainPrimeModuli();
+  so_rns* orc = so_rns_create(log_n, qs.data(), L);
+  auto a = Uniform(100 + log_n, qs, n, 1), b = Uniform(200 + log_n, qs, n, 1);
+
+  // ConvertToNttForm / ConvertToCoeffForm (rns_polynomial_test.cc NTT round trip)
+  RnsPolynomial pa;
+  ASSERT_OK_AND_ASSIGN(pa, RnsPolynomial::Create(Limbs(a.data(), L, n), false));
+  EXPECT_OK(pa.ConvertToNttForm(moduli));
+  std::vector<uint64_t> want = a;
+  so_rns_ntt_fwd(orc, want.data(), L);
+  EXPECT(Flat(pa.Coeffs()) == want, "ConvertToNttForm equals the oracle");
+  EXPECT_ERROR(pa.ConvertToNttForm(moduli), "Polynomial already in NTT form");
+  EXPECT_OK(pa.ConvertToCoeffForm(moduli));
+  EXPECT(Flat(pa.Coeffs()) == a, "NTT round trip");
+  EXPECT_ERROR(pa.ConvertToCoeffForm(moduli), "Polynomial already in Coefficient form");
+  EXPECT_OK(pa.ConvertToNttForm(moduli));
+
+  RnsPolynomial pb;
+  ASSERT_OK_AND_ASSIGN(pb, RnsPolynomial::Create(Limbs(b.data(), L, n), true));
+  std::vector<uint64_t> wa = want, wb = b, w(a.size());
+  // Add / Sub / Negate / Mul / FusedMulAdd against the per-prime oracle ops.
+  auto per_limb = [&](auto fn) {
+    for (int l = 0; l < L; ++l) fn(so_rns_prime(orc, l), (size_t)l * n);
+  };
+  RnsPolynomial r;
+  ASSERT_OK_AND_ASSIGN(r, pa.Add(pb, moduli));
+  per_limb([&](const so_prime* p, size_t o) { so_add(p, &wa[o], &wb[o], &w[o], n); });
+  EXPECT(Flat(r.Coeffs()) == w, "Add");
+  ASSERT_OK_AND_ASSIGN(r, pa.Sub(pb, moduli));
+  per_limb([&](const so_prime* p, size_t o) { so_sub(p, &wa[o], &wb[o], &w[o], n); });
+  EXPECT(Flat(r.Coeffs()) == w, "Sub");
+  ASSERT_OK_AND_ASSIGN(r, pa.Negate(moduli));
+  per_limb([&](const so_prime* p, size_t o) { so_neg(p, &wa[o], &w[o], n); });
+  EXPECT(Flat(r.Coeffs()) == w, "Negate");
+  ASSERT_OK_AND_ASSIGN(r, pa.Mul(pb, moduli));
+  per_limb([&](const so_prime* p, size_t o) { so_mul(p, &wa[o], &wb[o], &w[o], n); });
+  EXPECT(Flat(r.Coeffs()) == w, "Mul");
+  std::vector<uint64_t> acc = w;
+  EXPECT_OK(r.FusedMulAddInPlace(pa, pb, moduli));
+  per_limb([&](const so_prime* p, size_t o) { so_fma(p, &acc[o], &wa[o], &wb[o], n); });
+  EXPECT(Flat(r.Coeffs()) == acc, "FusedMulAddInPlace");
+
+  // Invalid arguments keep the reference's messages.
+  Moduli fewer(moduli.begin(), moduli.end() - 1);
+  if (L > 1)
+    EXPECT_ERROR(r.AddInPlace(pb, fewer),
+                 "`moduli` must contain " + std::to_string(L) + " RNS moduli.");
+  RnsPolynomial coeff;
+  ASSERT_OK_AND_ASSIGN(coeff, RnsPolynomial::Create(Limbs(a.data(), L, n), false));
+  EXPECT_ERROR(coeff.MulInPlace(pb, moduli), "RNS polynomial `this` must be in NTT form.");
+  EXPECT_ERROR(pa.Substitute(4, moduli).status(),
+               "Substitution power must be a non-negative odd integer less than 2*n.");
+
+  // Substitute (rns_polynomial_test.cc Substitute in NTT form).
+  for (int power : {3, 2 * n - 1}) {
+    ASSERT_OK_AND_ASSIGN(r, pa.Substitute(power, moduli));
+    so_rns_substitute(orc, L, power, wa.data(), w.data());
+    EXPECT(Flat(r.Coeffs()) == w, "Substitute");
+  }
+
+  // ModReduceLsb in NTT and coefficient form.
+  if (L > 1) {
+    std::vector<uint64_t> ql_inv;
+    ASSERT_OK_AND_ASSIGN(ql_inv, ctx->MainPrimeModulusInverseResidues(L - 1));
+    for (int is_ntt : {1, 0}) {
+      const std::vector<uint64_t>& src = is_ntt ? wa : a;
+      RnsPolynomial m;
+      ASSERT_OK_AND_ASSIGN(m, RnsPolynomial::Create(Limbs(src.data(), L, n), is_ntt));
+      EXPECT_OK(m.ModReduceLsb(65537, ql_inv, moduli));
+      std::vector<uint64_t> wm((size_t)(L - 1) * n);
+      so_rns_modreduce_lsb(orc, L, 65537, is_ntt, src.data(), wm.data());
+      EXPECT(m.NumModuli() == L - 1 && Flat(m.Coeffs()) == wm, "ModReduceLsb");
+    }
+    RnsPolynomial m;
+    ASSERT_OK_AND_ASSIGN(m, RnsPolynomial::Create(Limbs(wa.data(), L, n), true));
+    EXPECT_ERROR(m.ModReduceLsb(65537, std::vector<uint64_t>(L), moduli),
+                 "`ql_inv` must be defined with respect to " + std::to_string(L - 1) +
+                     " moduli.");
+  }
+  so_rns_destroy(orc);
+}
+
+void TestGadgetAndKeys(int log_n, const std::vector<uint64_t>& qs, std::vector<int> log_bs) {
+  const int n = 1 << log_n, L = (int)qs.size();
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, qs, {}, 65537));
+  const Moduli moduli = ctx->MainPrimeModuli();
+  so_rns* orc = so_rns_create(log_n, qs.data(), L);
+  RnsGadget gadget;
+  ASSERT_OK_AND_ASSIGN(gadget, RnsGadget::Create(log_n, log_bs, moduli));
+  const int k = gadget.Dimension();
+  EXPECT(k == so_rns_gadget_dim(orc, L, log_bs.data()), "gadget dimension");
+
+  // Decompose (rns_gadget_test.cc).
+  auto x = Uniform(300 + log_n, qs, n, 1);
+  RnsPolynomial px;
+  ASSERT_OK_AND_ASSIGN(px, RnsPolynomial::Create(Limbs(x.data(), L, n), false));
+  std::vector<RnsPolynomial> digits;
+  ASSERT_OK_AND_ASSIGN(digits, gadget.Decompose(px, moduli));
+  std::vector<uint64_t> wd((size_t)k * L * n);
+  so_rns_decompose(orc, L, log_bs.data(), x.data(), wd.data());
+  bool same = (int)digits.size() == k;
+  for (int j = 0; same && j < k; ++j)
+    same = Flat(digits[j].Coeffs()) ==
+           std::vector<uint64_t>(wd.begin() + (size_t)j * L * n,
+                                 wd.begin() + (size_t)(j + 1) * L * n);
+  EXPECT(same, "Decompose");
+  EXPECT_OK(px.ConvertToNttForm(moduli));
+  EXPECT_ERROR(gadget.Decompose(px, moduli).status(), "`a` must be in coefficient form");
+
+  // Keys from components; ct * ct then relinearize (rns_bgv_ciphertext_test.cc
+  // + rns_relinearization_key_test.cc).
+  auto kb = Uniform(400 + log_n, qs, n, k), ka = Uniform(500 + log_n, qs, n, k);
+  std::vector<RnsPolynomial> key_bs, key_as;
+  for (int j = 0; j < k; ++j) {
+    RnsPolynomial pb, pa;
+    ASSERT_OK_AND_ASSIGN(pb, RnsPolynomial::Create(Limbs(&kb[(size_t)j * L * n], L, n), true));
+    ASSERT_OK_AND_ASSIGN(pa, RnsPolynomial::Create(Limbs(&ka[(size_t)j * L * n], L, n), true));
+    key_bs.push_back(std::move(pb));
+    key_as.push_back(std::move(pa));
+  }
+  RnsRelinKey relin;
+  ASSERT_OK_AND_ASSIGN(relin, RnsRelinKey::CreateFromKeyComponents(key_bs, key_as, &gadget,
+                                                                   moduli));
+  EXPECT(relin.Dimension() == k, "relin key dimension");
+  auto c = Uniform(600 + log_n, qs, n, 2), d = Uniform(700 + log_n, qs, n, 2);
+  auto make_ct = [&](const std::vector<uint64_t>& flat, int power) {
+    std::vector<RnsPolynomial> comps;
+    for (int i = 0; i < 2; ++i)
+      comps.push_back(*RnsPolynomial::Create(Limbs(&flat[(size_t)i * L * n], L, n), true));
+    return RnsBgvCiphertext(std::move(comps), moduli, power, 1.0);
+  };
+  RnsBgvCiphertext ct1 = make_ct(c, 1), ct2 = make_ct(d, 1);
+  RnsBgvCiphertext prod = ct1;
+  ASSERT_OK_AND_ASSIGN(prod, ct1 * ct2);
+  std::vector<uint64_t> w3((size_t)3 * L * n);
+  so_rns_tensor(orc, L, c.data(), d.data(), w3.data());
+  EXPECT(prod.Degree() == 2 && FlatCt(prod) == w3, "RnsBgvCiphertext operator*");
+  RnsBgvCiphertext relined = prod;
+  ASSERT_OK_AND_ASSIGN(relined, relin.ApplyTo(prod));
+  std::vector<uint64_t> w2((size_t)2 * L * n);
+  so_rns_relin(orc, L, log_bs.data(), w3.data(), kb.data(), ka.data(), w2.data());
+  EXPECT(relined.Degree() == 1 && FlatCt(relined) == w2, "RnsRelinKey::ApplyTo");
+
+  // Degree-3 product goes through the general FMA path.
+  RnsBgvCiphertext cube = prod;
+  ASSERT_OK_AND_ASSIGN(cube, prod * ct1);
+  EXPECT(cube.Degree() == 3, "degree-3 product");
+  EXPECT_ERROR(relin.ApplyTo(cube).status(),
+               "`ciphertext` degree is larger than degree of this relinearization key, 2.");
+
+  // Rotation: Substitute then the Galois key (rns_galois_key_test.cc).
+  const int power = 5;
+  RnsGaloisKey galois;
+  ASSERT_OK_AND_ASSIGN(galois, RnsGaloisKey::CreateFromKeyComponents(key_as, key_bs, power,
+                                                                     &gadget, moduli));
+  EXPECT_ERROR(galois.ApplyTo(ct1).status(),
+               "`ciphertext` does not have a matching substitution power.");
+  RnsBgvCiphertext sub = ct1;
+  ASSERT_OK_AND_ASSIGN(sub, ct1.Substitute(power));
+  EXPECT(sub.PowerOfS() == power, "power of s after Substitute");
+  RnsBgvCiphertext rot = sub;
+  ASSERT_OK_AND_ASSIGN(rot, galois.ApplyTo(sub));
+  std::vector<uint64_t> sc((size_t)2 * L * n), wr((size_t)2 * L * n);
+  for (int i = 0; i < 2; ++i)
+    so_rns_substitute(orc, L, power, &c[(size_t)i * L * n], &sc[(size_t)i * L * n]);
+  so_rns_galois(orc, L, log_bs.data(), sc.data(), kb.data(), ka.data(), wr.data());
+  EXPECT(rot.PowerOfS() == 1 && FlatCt(rot) == wr, "RnsGaloisKey::ApplyTo");
+
+  // ModReduce drops the top prime of every component.
+  if (L > 1) {
+    std::vector<uint64_t> ql_inv;
+    ASSERT_OK_AND_ASSIGN(ql_inv, ctx->MainPrimeModulusInverseResidues(L - 1));
+    RnsBgvCiphertext m = relined;
+    EXPECT_OK(m.ModReduce(65537, ql_inv));
+    std::vector<uint64_t> wm((size_t)2 * (L - 1) * n);
+    for (int i = 0; i < 2; ++i)
+      so_rns_modreduce_lsb(orc, L, 65537, 1, &w2[(size_t)i * L * n],
+                           &wm[(size_t)i * (L - 1) * n]);
+    EXPECT(m.NumModuli() == L - 1 && FlatCt(m) == wm, "RnsBgvCiphertext::ModReduce");
+  }
+  so_rns_destroy(orc);
+}
+
+void TestSingleModulus(int log_n, int levels, int log_b) {
+  const int n = 1 << log_n;
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, {kQ60}, {}, 65537));
+  const PrimeModulus* m = ctx->MainPrimeModuli()[0];
+  so_prime* p = so_prime_create(kQ60, log_n);
+  const int dim = so_gadget_size(p, log_b);
+  auto keys = Uniform(800 + log_n, {kQ60}, n, levels * 2 * dim);  // [levels][2][dim][n]
+  std::vector<GaloisKey> gks;
+  for (int j = 0; j < levels; ++j) {
+    std::vector<Polynomial> k0, k1;
+    for (int i = 0; i < dim; ++i) {
+      const uint64_t* r0 = &keys[((size_t)(j * 2 + 0) * dim + i) * n];
+      const uint64_t* r1 = &keys[((size_t)(j * 2 + 1) * dim + i) * n];
+      k0.push_back(*RnsPolynomial::Create({std::vector<uint64_t>(r0, r0 + n)}, true));
+      k1.push_back(*RnsPolynomial::Create({std::vector<uint64_t>(r1, r1 + n)}, true));
+    }
+    GaloisKey gk = *GaloisKey::CreateFromKeyComponents(k0, k1, (n >> j) + 1, log_b, m);
+    gks.push_back(std::move(gk));
+  }
+  auto c = Uniform(900 + log_n, {kQ60}, n, 2);
+  std::vector<Polynomial> comps;
+  for (int i = 0; i < 2; ++i)
+    comps.push_back(*RnsPolynomial::Create({std::vector<uint64_t>(c.begin() + i * n,
+                                                                  c.begin() + (i + 1) * n)},
+                                           true));
+  SymmetricRlweCiphertext ct(std::move(comps), m, 1, 1.0);
+
+  // GaloisKey::ApplyTo after Substitute (galois_key_test.cc).
+  const int power = n + 1;
+  SymmetricRlweCiphertext sub = ct;
+  ASSERT_OK_AND_ASSIGN(sub, ct.Substitute(power));
+  SymmetricRlweCiphertext sw = sub;
+  ASSERT_OK_AND_ASSIGN(sw, gks[0].ApplyTo(sub));
+  std::vector<uint64_t> sc(2 * (size_t)n), w(2 * (size_t)n);
+  for (int i = 0; i < 2; ++i) so_substitute(p, power, &c[(size_t)i * n], &sc[(size_t)i * n]);
+  so_galois_apply(p, log_b, dim, sc.data(), &keys[0], &keys[(size_t)dim * n], w.data());
+  EXPECT(FlatCt(sw.rns()) == w, "GaloisKey::ApplyTo");
+  EXPECT_ERROR(gks[0].ApplyTo(ct).status(),
+               "Ciphertext PowerOfS: 1 doesn't match the key substitution power: " +
+                   std::to_string(power));
+
+  // ObliviousExpand (oblivious_expand_test.cc) with a truncated output.
+  std::unique_ptr<GaloisKeysObliviousExpander> ex;
+  ASSERT_OK_AND_ASSIGN(ex, GaloisKeysObliviousExpander::Create(gks, 16, m));
+  const int out_len = (1 << levels) - 1;
+  std::vector<SymmetricRlweCiphertext> expanded;
+  ASSERT_OK_AND_ASSIGN(expanded, ex->ObliviousExpand({ct}, levels, out_len));
+  std::vector<uint64_t> we(((size_t)2 << levels) * n);
+  so_oblivious_expand(p, levels, log_b, keys.data(), c.data(), we.data());
+  bool same = (int)expanded.size() == out_len;
+  for (int i = 0; same && i < out_len; ++i)
+    same = FlatCt(expanded[i].rns()) ==
+           std::vector<uint64_t>(we.begin() + (size_t)i * 2 * n,
+                                 we.begin() + (size_t)(i + 1) * 2 * n);
+  EXPECT(same, "ObliviousExpand");
+  EXPECT_ERROR(ex->ObliviousExpand({ct}, levels, (1 << levels) + 1).status(),
+               "Output length must be at most " + std::to_string(1 << levels));
+  so_prime_destroy(p);
+}
+
+}  // namespace
+
+int main() {
+  TestContextErrors();
+  TestPolynomial(4, {kQ45[0], kQ45[1]});
+  TestPolynomial(11, kQ50);
+  TestPolynomial(14, kQ45);
+  TestPolynomial(15, {kQ50[0], kQ50[1]});
+  TestGadgetAndKeys(10, {kQ45[0], kQ45[1], kQ45[2]}, {20, 20, 20});
+  TestGadgetAndKeys(12, {kQ50[0], kQ50[1]}, {50, 16});
+  TestGadgetAndKeys(14, kQ45, {20, 20, 20, 20, 20, 20});
+  TestSingleModulus(8, 4, 8);
+  TestSingleModulus(12, 3, 10);
+  std::printf("%d checks, %d failures\n", g_checks, g_failures);
+  if (g_failures == 0) std::printf("ALL OK\n");
+  return g_failures == 0 ? 0 : 1;
+}

@@ -268,6 +268,26 @@ def test_tensor(sg, oracle, log_n, qs):
     assert np.array_equal(out.download(want.shape), want)
 
 
+@pytest.mark.parametrize("log_n,qs,log_bs", [
+    (4, Q45[:2], [20, 20]), (10, Q45, [20] * 6), (11, Q50[:2], [50, 16]),
+    (12, Q50[:3], [7, 13, 62]), (14, Q45[:3], [20, 20, 20])])
+def test_gadget_decompose(sg, oracle, log_n, qs, log_bs):
+    n, L, count = 1 << log_n, len(qs), 2
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    a = oracle.uniform_limbs(45, qs, n, count).reshape(count, L, n)
+    want = np.stack([rns.decompose(a[i], log_bs) for i in range(count)])
+    assert want.shape == (count, k, L, n)
+    ctx = sg.Context(log_n, qs)
+    lib = sg.lib()
+    lb = np.array(log_bs, np.int32)
+    d = _dev(sg, a)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, lib.shg_gadget_decompose, ctx.h, L, lb.ctypes.data_as(sg._ip), out.ptr, d.ptr,
+         count, None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
 KS_CASES = [
     (4, Q45[:2], [20, 20]),
     (10, Q45[:3], [20, 20, 20]),
