@@ -232,6 +232,282 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# PIR workload: oblivious expansion + database absorb (n = 2^12, one 60-bit
+# prime, 10 levels, gadget base 2^8, 256 queries, 2^10-item database).
+# ---------------------------------------------------------------------------
+
+PIR_LOG_N, PIR_Q, PIR_LEVELS, PIR_LOG_B = 12, 1152921504606830593, 10, 8
+PIR_QUERIES, PIR_ITEMS, PIR_LOG_T = 256, 1024, 16
+PIR_METRIC = "PIR oblivious expansion + absorb queries/sec (n=2^12, 10 levels, 2^10 items)"
+PIR_UNIT = "queries/s"
+PIR_SCOPES = ("monomials", "ntt_fwd", "intt_export", "digit_ntt", "ks_inner",
+              "expand_combine", "absorb_sum")
+
+
+def pir_config(queries):
+    return {
+        "workload": "pir-expand-absorb n=2^12 q=60-bit gadget 2^8 (dim 8) 10 levels, "
+                    "2^10-item database",
+        "log_n": PIR_LOG_N, "log_q": 60, "levels": PIR_LEVELS, "gadget_log_base": PIR_LOG_B,
+        "gadget_dim": 8, "queries": queries, "db_items": PIR_ITEMS,
+        "l2": "expanded ciphertexts per step (16 GiB) exceed L2",
+        "parallelism": "replicas",
+    }
+
+
+def pir_scope_model(name, n, dim, members, queries, levels):
+    """(algorithmic DRAM bytes, butterflies) of one whole step of a scope:
+    members = key switches (every non-root node of every query's tree)."""
+    poly = n * 8
+    bfly = n // 2 * (n.bit_length() - 1)
+    if name == "monomials":
+        return levels * poly, 0
+    if name == "ntt_fwd":
+        return 2 * levels * poly, levels * bfly
+    if name == "intt_export":
+        return 2 * poly * members, bfly * members
+    if name == "digit_ntt":
+        return (1 + dim) * poly * members, dim * bfly * members
+    if name == "ks_inner":
+        return (dim + 3) * poly * members, 0
+    if name == "expand_combine":
+        return 8 * poly * members, 0
+    if name == "absorb_sum":
+        return (PIR_ITEMS * 2 + 2) * poly * queries + PIR_ITEMS * poly, 0
+    raise KeyError(name)
+
+
+def pir_keys_db_queries(seed, n, queries):
+    dim = -(-60 // PIR_LOG_B)
+    keys = np.stack([np.stack([splitmix_limbs(seed + 10 * j + c, dim, [PIR_Q], n).reshape(dim, n)
+                               for c in (0, 1)]) for j in range(PIR_LEVELS)])
+    with np.errstate(over="ignore"):
+        db_plain = (splitmix_limbs(seed + 999, PIR_ITEMS, [1 << 62], n).reshape(PIR_ITEMS, n)
+                    & np.uint64((1 << PIR_LOG_T) - 1))
+    q = splitmix_limbs(seed + 555, 2 * queries, [PIR_Q], n).reshape(queries, 2, n)
+    return dim, keys, db_plain, q
+
+
+def cpu_pir(seconds, threads, seed=7):
+    """The reference's CPU path for one PIR query (oracle restatement of
+    GaloisKeysObliviousExpander::ObliviousExpand + FusedAbsorbAddInPlace),
+    one query per host thread per round, for about `seconds`."""
+    import concurrent.futures
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    n = 1 << PIR_LOG_N
+    p = O.Prime(PIR_Q, PIR_LOG_N)
+    dim, keys, db_plain, q = pir_keys_db_queries(seed, n, threads)
+    db = np.stack([p.ntt_fwd(p.import_(row)) for row in db_plain])
+
+    def one(i):
+        return p.absorb_sum(p.oblivious_expand(PIR_LEVELS, PIR_LOG_B, keys, q[i]), db)
+
+    ops = 0
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        while True:
+            list(ex.map(one, range(threads)))
+            ops += threads
+            dt = time.perf_counter() - t0
+            if dt >= seconds:
+                break
+    return ops / dt, ops, dt
+
+
+def run_pir_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    per_step, ops_total = [], 0
+    for i in range(args.warmup + args.steps):
+        _, ops, dt = cpu_pir(2.0, threads, seed=100 + i)
+        if i >= args.warmup:
+            per_step.append(dt)
+            ops_total += ops
+    total = sum(per_step)
+    value = ops_total / total
+    print(json.dumps({
+        "metric": PIR_METRIC, "value": value, "unit": PIR_UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": pir_config(threads),
+        "cpu_baseline": {"value": value, "unit": PIR_UNIT, "cores": threads, "kind": "port",
+                         "sample": "each step: about 2 s of whole queries, one per host "
+                                   "thread per round"},
+        "e2e": {"value": value, "unit": PIR_UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_pir(args, world, rank, local, dist):
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    n = 1 << PIR_LOG_N
+    Qn = args.queries
+    ctx = sg.Context(PIR_LOG_N, [PIR_Q], (1 << PIR_LOG_T) + 1)
+    dim, keys, db_plain, queries = pir_keys_db_queries(3000 + 97 * rank, n, Qn)
+    gkeys = [sg.Key(ctx, [PIR_LOG_B], (n >> j) + 1, keys[j, 0], keys[j, 1])
+             for j in range(PIR_LEVELS)]
+    karr = (ctypes.c_void_p * PIR_LEVELS)(*[k.h for k in gkeys])
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+    # Database rows: plaintexts in [0, 2^16) imported to Montgomery form
+    # (times R^2 mod q through a Montgomery multiply) and put in NTT form.
+    d_db = sg.DeviceBuffer.from_array(db_plain)
+    r2 = np.array([pow(2, 128, PIR_Q)], np.uint64)
+    sg.check(lib.shg_poly_mul_rns_scalar(ctx.h, d_db.ptr, d_db.ptr,
+                                         r2.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                         PIR_ITEMS, 1, s))
+    sg.check(lib.shg_ntt_forward(ctx.h, d_db.ptr, PIR_ITEMS, 1, s))
+    q_bytes = Qn * 2 * n * 8
+
+    def host(nbytes):
+        p = ctypes.c_void_p()
+        sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+        return p.value
+
+    h_q, h_out = host(q_bytes), host(q_bytes)
+    np.ctypeslib.as_array((ctypes.c_uint64 * (Qn * 2 * n)).from_address(h_q))[:] = queries.reshape(-1)
+    d_q, d_out = sg.DeviceBuffer(q_bytes), sg.DeviceBuffer(q_bytes)
+    sg.check(lib.shg_memcpy_h2d(d_q.ptr, h_q, q_bytes, s))
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def step_device():
+        sg.check(lib.shg_pir_expand_absorb(ctx.h, karr, PIR_LEVELS, d_db.ptr, PIR_ITEMS,
+                                           d_out.ptr, d_q.ptr, Qn, s))
+
+    step_device()
+    sg.check(lib.shg_stream_synchronize(s))
+    n0 = lib.shg_launch_count()
+    sg.check(lib.shg_graph_capture_begin(s))
+    step_device()
+    g = ctypes.c_void_p()
+    sg.check(lib.shg_graph_capture_end(s, ctypes.byref(g)))
+    graph = g.value
+    launches_per_step = lib.shg_launch_count() - n0
+    for _ in range(args.warmup):
+        sg.check(lib.shg_graph_launch(graph, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    evs = [ev() for _ in range(args.steps + 1)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    sg.check(lib.shg_event_record(evs[0], s))
+    for i in range(args.steps):
+        sg.check(lib.shg_graph_launch(graph, s))
+        sg.check(lib.shg_event_record(evs[i + 1], s))
+    sg.check(lib.shg_stream_synchronize(s))
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = [elapsed(evs[i], evs[i + 1]) for i in range(args.steps)]
+    total_ms = max_over_ranks(dist, elapsed(evs[0], evs[-1]))
+    ops_all = sum_over_ranks(dist, float(Qn * args.steps))
+    value = ops_all / (total_ms / 1e3)
+
+    # End to end: queries in from pinned host memory, results back, per step.
+    e2e = None
+    if not args.no_e2e:
+        def step_e2e():
+            sg.check(lib.shg_memcpy_h2d(d_q.ptr, h_q, q_bytes, s))
+            step_device()
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, q_bytes, s))
+        step_e2e()
+        sg.check(lib.shg_stream_synchronize(s))
+        e0, e1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(e0, s))
+        for _ in range(args.steps):
+            step_e2e()
+        sg.check(lib.shg_event_record(e1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": PIR_UNIT,
+               "h2d_bytes_per_step": q_bytes, "d2h_bytes_per_step": q_bytes,
+               "ms_per_step": e2e_ms / args.steps}
+
+    sg.check(lib.shg_profile_start())
+    step_device()
+    sg.check(lib.shg_profile_stop())
+    prof = {}
+    for name in PIR_SCOPES:
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        if cnt.value:
+            prof[name] = (ms.value, cnt.value)
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    bfly_peak = ctypes.c_double()
+    sg.check(lib.shg_measure_butterfly_rate(ctypes.byref(bfly_peak)))
+    members = Qn * ((1 << PIR_LEVELS) - 1)
+    step_total = sum(v[0] for v in prof.values())
+    kernels, bfly_step, bfly_ms = {}, 0.0, 0.0
+    for name, (ms, cnt) in prof.items():
+        nbytes, bfly = pir_scope_model(name, n, dim, members, Qn, PIR_LEVELS)
+        kernels[name] = {"share_of_step": ms / step_total, "launches": cnt,
+                         "avg_launch_ms": ms / cnt,
+                         "algorithmic_bytes_per_launch": nbytes / cnt,
+                         "achieved_gbs": nbytes / (ms / 1e3) / 1e9,
+                         "int_frac": (bfly / (ms / 1e3) / bfly_peak.value) if bfly else None}
+        if bfly:
+            bfly_step += bfly
+            bfly_ms += ms
+    top = max(prof, key=lambda nm: prof[nm][0])
+    tk = kernels[top]
+    roofline = {
+        "kernel": top, "bound": "hbm", "achieved": tk["achieved_gbs"], "peak": peak,
+        "unit": "GB/s", "frac": tk["achieved_gbs"] / peak, "peak_source": peak_src,
+        "traffic": None, "algorithmic_bytes_per_launch": tk["algorithmic_bytes_per_launch"],
+        "avg_launch_ms": tk["avg_launch_ms"],
+        "integer": {"peak_butterflies_per_s": bfly_peak.value,
+                    "achieved_butterflies_per_s": bfly_step / (bfly_ms / 1e3),
+                    "frac": bfly_step / (bfly_ms / 1e3) / bfly_peak.value},
+        "kernels": kernels,
+    }
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, ops, dt = cpu_pir(10.0, threads)
+        cpu = {"value": rate, "unit": PIR_UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ops} queries (expand to 2^10 + absorb) in {dt:.1f} s, "
+                         f"one query per host thread per round"}
+    lat = sorted(step_ms)
+    line = {
+        "metric": PIR_METRIC, "value": value, "unit": PIR_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded uniform keys, queries and a 2^16-valued database)",
+        "config": pir_config(Qn),
+        "expanded_ciphertexts_per_s": value * (1 << PIR_LEVELS),
+        "key_switches_per_s": value * ((1 << PIR_LEVELS) - 1),
+        "latency_ms": {"step_p50": lat[len(lat) // 2], "step_p99": lat[-1]},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "gpu_launches": int(launches_per_step * args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sg.check(lib.shg_graph_destroy(graph))
+    for hp in (h_q, h_out):
+        lib.shg_host_free(hp)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -245,12 +521,22 @@ def main():
                     help="log n from which NTTs use the four-step kernels (default 14)")
     ap.add_argument("--ks-unfused", action="store_true",
                     help="separate digit row phase and key inner product kernels")
+    ap.add_argument("--workload", default="ct-mult-relin", choices=["ct-mult-relin", "pir"],
+                    help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
+                         "pir: oblivious expansion + database absorb (n=2^12, one prime)")
+    ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
 
     world, rank, local, dist = dist_setup(args)
+    if args.workload == "pir":
+        if args.impl == "reference":
+            run_pir_reference(args, world, rank)
+        else:
+            run_pir(args, world, rank, local, dist)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         return

@@ -223,6 +223,19 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,
 int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
                          int levels, uint64_t* out, const uint64_t* ct,
                          int count, shg_stream stream);
+/* PIR server step: GaloisKeysObliviousExpander::ObliviousExpand of every
+ * query to num_items ciphertexts (oblivious_expand.h:95-138, 173-227), then
+ * sum_i expanded_i * db[i] with SymmetricRlweCiphertext::FusedAbsorbAddInPlace
+ * (symmetric_encryption.h:250-275).  keys as for shg_oblivious_expand,
+ * db [num_items][n] (NTT form, device), 1 <= num_items <= 2^levels,
+ * ct [count][2][n] -> out [count][2][n].  Equals shg_oblivious_expand
+ * followed by shg_absorb_sum over each query's first num_items ciphertexts,
+ * without holding all expanded ciphertexts at once (queries go through in
+ * groups that share 1 GiB of scratch). */
+int shg_pir_expand_absorb(shg_context* ctx, const shg_key* const* keys,
+                          int levels, const uint64_t* db, int num_items,
+                          uint64_t* out, const uint64_t* ct, int count,
+                          shg_stream stream);
 /* Sum_i cts[i] * db[i] via SymmetricRlweCiphertext::FusedAbsorbAddInPlace
  * (symmetric_encryption.h:250-275): cts [count][num_items][2][n],
  * db [num_items][n] -> out [count][2][n]. */

@@ -894,9 +894,14 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
   return launch_status("bgv_mul_relin");
 }
 
-int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
-                         int levels, uint64_t* out, const uint64_t* ct,
-                         int count, shg_stream stream) {
+}  // extern "C"
+
+namespace {
+
+// Argument checks shared by the expansion entry points
+// (oblivious_expand.h:95-138, 237-258).
+int check_expand(const shg_context* ctx, const shg_key* const* keys, int levels,
+                 int count) {
   if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
   if (levels < 0 || levels >= 32)
     return fail(SHG_INVALID_ARGUMENT,
@@ -904,9 +909,6 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
   if ((1 << std::min(levels, 30)) > ctx->n)
     return fail(SHG_INVALID_ARGUMENT, "levels of expansion exceed log n");
   if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
-  int st;
-  if (count == 0) return SHG_OK;
-  if ((st = check_ptrs({out, ct}))) return st;
   for (int j = 0; j < levels; ++j) {
     if (!keys || !keys[j]) return fail(SHG_INVALID_ARGUMENT, "null Galois key");
     if (keys[j]->ctx != ctx || keys[j]->L != 1)
@@ -916,42 +918,51 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
                   "Substitution power of the i'th GaloisKey must be (N / (2 ^ "
                   "i)) + 1");
   }
-  cudaStream_t s = (cudaStream_t)stream;
+  return SHG_OK;
+}
+
+// Scratch of one expansion pass: the level monomials, then X, D and KS for
+// C members at a time.  A chunk holds whole queries, so it must fit the
+// 2^(levels-1) members one query contributes at the last level.
+struct ExpandPlan {
+  int C = 1;
+  size_t mono_bytes = 0, per_member = 0;
+  size_t bytes() const { return mono_bytes + per_member * C; }
+};
+
+ExpandPlan plan_expand(const shg_context* ctx, const shg_key* const* keys, int levels,
+                       int count) {
+  ExpandPlan p;
   const int n = ctx->n;
-  const size_t per_query = ((size_t)2 * n) << levels;
-  // Place each query at slot 0 of its output block.
-  for (int qi = 0; qi < count; ++qi) {
-    SHG_CUDA(cudaMemcpyAsync(out + (size_t)qi * per_query, ct + (size_t)qi * 2 * n,
-                             2 * n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
-  }
-  if (levels == 0) return SHG_OK;
+  const int kmax = levels ? keys[0]->k : 0;
+  p.per_member = ((size_t)n + (size_t)kmax * n + 2 * (size_t)n) * sizeof(uint64_t);
+  p.mono_bytes = (size_t)levels * n * sizeof(uint64_t);
+  const int members_max = std::max(1, count << std::max(levels - 1, 0));
+  p.C = std::max(1 << std::max(levels - 1, 0),
+                 (int)std::min<size_t>((size_t)members_max, ((size_t)256 << 20) / p.per_member));
+  return p;
+}
+
+// ExpandCiphertext over `count` queries already placed at slot 0 of their
+// [2^levels][2][n] blocks in `out` (oblivious_expand.h:173-227): level j
+// substitutes every member by n/2^j + 1, key-switches it and combines
+// (c + ks, (c - ks) * -x^{n - 2^j}) into slots p and p + 2^j.  `ws` is the
+// plan's scratch, the monomials first.
+int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_t* out,
+               int count, const ExpandPlan& plan, uint64_t* ws, cudaStream_t s) {
+  if (levels == 0 || count == 0) return SHG_OK;
+  const int n = ctx->n;
+  const int C = plan.C;
   const int kmax = keys[0]->k;
-  // Monomials -x^{n - 2^j} in NTT form (ExpandCiphertext, oblivious_expand.h:
-  // 197-200), built on the device from a coefficient vector.
-  const size_t per_member = ((size_t)n + (size_t)kmax * n + 2 * (size_t)n) *
-                            sizeof(uint64_t);
-  // A chunk holds whole queries, so it must fit the 2^(levels-1) members one
-  // query contributes at the last level.
-  const int members_max = std::max(1, count << (levels - 1));
-  const int C = std::max(
-      1 << (levels - 1),
-      (int)std::min<size_t>((size_t)members_max, ((size_t)256 << 20) / per_member));
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  const size_t mono_bytes = (size_t)levels * n * sizeof(uint64_t);
-  if ((st = ctx->ensure_ws(mono_bytes + per_member * C))) return st;
-  uint64_t* mono = ctx->ws;
+  const size_t per_query = ((size_t)2 * n) << levels;
+  uint64_t* mono = ws;
   uint64_t* X = mono + (size_t)levels * n;
   uint64_t* D = X + (size_t)C * n;
   uint64_t* KS = D + (size_t)C * kmax * n;
-  {
-    std::vector<uint64_t> h((size_t)levels * n, 0);
-    const HostPrime& hp = ctx->hp[0];
-    for (int j = 0; j < levels; ++j)
-      h[(size_t)j * n + (n - (1 << j))] = hp.q - hp.r_mod_q;  // -1 (Montgomery)
-    SHG_CUDA(cudaMemcpyAsync(mono, h.data(), mono_bytes, cudaMemcpyHostToDevice, s));
-    SHG_CUDA(cudaStreamSynchronize(s));
-    shg::launch_ntt_fwd(ctx->dev(), mono, mono, levels, 1, s);
-  }
+  // Monomials -x^{n - 2^j} in NTT form (oblivious_expand.h:197-200), built
+  // on the stream so the whole expansion can be captured in a graph.
+  shg::launch_monomials(ctx->dev(), mono, levels, ctx->hp[0].q - ctx->hp[0].r_mod_q, s);
+  shg::launch_ntt_fwd(ctx->dev(), mono, mono, levels, 1, s);
   const CtxDev dv = ctx->dev();
   for (int j = 0; j < levels; ++j) {
     const shg_key* key = keys[j];
@@ -971,7 +982,74 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
                                  mc, s);
     }
   }
+  return SHG_OK;
+}
+
+int absorb_chunk(const shg_context* ctx) {
+  const uint64_t q = ctx->hp[0].q;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(1u << 20, (~(uint64_t)0) / q));
+}
+
+}  // namespace
+
+extern "C" {
+
+int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
+                         int levels, uint64_t* out, const uint64_t* ct,
+                         int count, shg_stream stream) {
+  int st = check_expand(ctx, keys, levels, count);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = ctx->n;
+  const size_t per_query = ((size_t)2 * n) << levels;
+  // Place each query at slot 0 of its output block.
+  for (int qi = 0; qi < count; ++qi) {
+    SHG_CUDA(cudaMemcpyAsync(out + (size_t)qi * per_query, ct + (size_t)qi * 2 * n,
+                             2 * n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  }
+  if (levels == 0) return SHG_OK;
+  const ExpandPlan plan = plan_expand(ctx, keys, levels, count);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(plan.bytes()))) return st;
+  if ((st = run_expand(ctx, keys, levels, out, count, plan, ctx->ws, s))) return st;
   return launch_status("oblivious_expand");
+}
+
+int shg_pir_expand_absorb(shg_context* ctx, const shg_key* const* keys, int levels,
+                          const uint64_t* db, int num_items, uint64_t* out,
+                          const uint64_t* ct, int count, shg_stream stream) {
+  int st = check_expand(ctx, keys, levels, count);
+  if (st) return st;
+  if (num_items < 1 || num_items > (1 << levels))
+    return fail(SHG_INVALID_ARGUMENT,
+                "Output length must be at most " + std::to_string(1 << levels));
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct, db}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = ctx->n;
+  const size_t per_query_elems = ((size_t)2 * n) << levels;
+  // Queries per group: their expanded blocks (2^levels ciphertexts each) share
+  // a 1 GiB scratch region and are absorbed before the next group starts.
+  const int group = (int)std::max<size_t>(
+      1, std::min<size_t>((size_t)count, ((size_t)1 << 30) / (per_query_elems * 8)));
+  const ExpandPlan plan = plan_expand(ctx, keys, levels, group);
+  const size_t blocks_bytes = (size_t)group * per_query_elems * sizeof(uint64_t);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(plan.bytes() + blocks_bytes))) return st;
+  uint64_t* blocks = ctx->ws + plan.bytes() / sizeof(uint64_t);
+  for (int g0 = 0; g0 < count; g0 += group) {
+    const int gc = std::min(group, count - g0);
+    // Slot 0 of every block <- its query; the strided copy is one call.
+    SHG_CUDA(cudaMemcpy2DAsync(blocks, per_query_elems * sizeof(uint64_t),
+                               ct + (size_t)g0 * 2 * n, 2 * n * sizeof(uint64_t),
+                               2 * n * sizeof(uint64_t), gc, cudaMemcpyDeviceToDevice, s));
+    if ((st = run_expand(ctx, keys, levels, blocks, gc, plan, ctx->ws, s))) return st;
+    shg::launch_absorb_sum(ctx->dev(), out + (size_t)g0 * 2 * n, blocks, db, num_items,
+                           (size_t)1 << levels, absorb_chunk(ctx), gc, s);
+  }
+  return launch_status("pir_expand_absorb");
 }
 
 int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,
@@ -983,10 +1061,8 @@ int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,
   if (count == 0) return SHG_OK;
   int st = check_ptrs({out, cts, db});
   if (st) return st;
-  const uint64_t q = ctx->hp[0].q;
-  const int chunk = (int)std::max<uint64_t>(1, std::min<uint64_t>(1u << 20, (~(uint64_t)0) / q));
-  shg::launch_absorb_sum(ctx->dev(), out, cts, db, num_items, chunk, count,
-                         (cudaStream_t)stream);
+  shg::launch_absorb_sum(ctx->dev(), out, cts, db, num_items, (size_t)num_items,
+                         absorb_chunk(ctx), count, (cudaStream_t)stream);
   return launch_status("absorb_sum");
 }
 

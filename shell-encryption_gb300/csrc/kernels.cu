@@ -590,9 +590,26 @@ __global__ void k_expand_combine(uint64_t* base, const uint64_t* ks,
   }
 }
 
+// Monomials -x^{n - 2^j}, j < levels, in coefficient form
+// (oblivious_expand.h:197-200): row j is zero but for coefficient n - 2^j,
+// which is `minus_one` (the Montgomery form of -1).
+__global__ void k_monomials(uint64_t* mono, int levels, int log_n,
+                            uint64_t minus_one) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t total = (size_t)levels * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const int j = (int)(e >> log_n);
+    const size_t i = e & (n - 1);
+    mono[e] = i == n - ((size_t)1 << j) ? minus_one : 0;
+  }
+}
+
 // FusedAbsorbAddInPlace chain (symmetric_encryption.h:250-275).
 __global__ void k_absorb_sum(uint64_t* out, const uint64_t* cts,
-                             const uint64_t* db, int num_items, int chunk,
+                             const uint64_t* db, int num_items,
+                             size_t item_stride, int chunk,
                              size_t total /* count*2*n */, int log_n,
                              CtxDev c) {
   const size_t n = (size_t)1 << log_n;
@@ -602,7 +619,7 @@ __global__ void k_absorb_sum(uint64_t* out, const uint64_t* cts,
        e += stride) {
     const size_t qi = e / (2 * n), r = e % (2 * n);
     const size_t pos = r & (n - 1);
-    const uint64_t* cp = cts + qi * (size_t)num_items * 2 * n + r;
+    const uint64_t* cp = cts + qi * item_stride * 2 * n + r;
     uint64_t s = 0;
     for (int i0 = 0; i0 < num_items; i0 += chunk) {
       const int i1 = min(num_items, i0 + chunk);
@@ -892,14 +909,22 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                                                         half, total, c.log_n, c);
 }
 
+void launch_monomials(const CtxDev& c, uint64_t* mono, int levels,
+                      uint64_t minus_one, cudaStream_t s) {
+  const size_t total = (size_t)levels * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("monomials", s);
+  k_monomials<<<grid_for(total, 256), 256, 0, s>>>(mono, levels, c.log_n, minus_one);
+}
+
 void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
-                       const uint64_t* db, int num_items, int chunk, int count,
-                       cudaStream_t s) {
+                       const uint64_t* db, int num_items, size_t item_stride,
+                       int chunk, int count, cudaStream_t s) {
   const size_t total = (size_t)count * 2 * c.n;
   if (total == 0) return;
   LaunchScope scope_("absorb_sum", s);
-  k_absorb_sum<<<grid_for(total, 256), 256, 0, s>>>(out, cts, db, num_items,
-                                                    chunk, total, c.log_n, c);
+  k_absorb_sum<<<grid_for(total, 256), 256, 0, s>>>(
+      out, cts, db, num_items, item_stride, chunk, total, c.log_n, c);
 }
 
 // Integer ceiling of the transforms: the NTT's lazy Cooley-Tukey butterfly

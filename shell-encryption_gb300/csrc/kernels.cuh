@@ -165,10 +165,16 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            const uint64_t* mono, CtMap map, int half,
                            int count, cudaStream_t s);
 
-// out [count][2][n] = sum_i cts[count][i][2][n] * db[i][n].
+// mono [levels][n] <- -x^{n - 2^j} in coefficient form (minus_one = the
+// Montgomery form of -1).
+void launch_monomials(const CtxDev& c, uint64_t* mono, int levels,
+                      uint64_t minus_one, cudaStream_t s);
+
+// out [count][2][n] = sum_{i < num_items} cts[count][i][2][n] * db[i][n],
+// query p's items starting at cts + p * item_stride * 2n.
 void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
-                       const uint64_t* db, int num_items, int chunk, int count,
-                       cudaStream_t s);
+                       const uint64_t* db, int num_items, size_t item_stride,
+                       int chunk, int count, cudaStream_t s);
 
 // Butterflies per second of the NTT's lazy butterfly on register-resident
 // values (the integer ceiling of every transform kernel) on the current

@@ -447,3 +447,31 @@ def test_absorb_sum(sg, oracle):
     out = sg.DeviceBuffer(want.nbytes)
     _run(sg, sg.lib().shg_absorb_sum, ctx.h, out.ptr, dc.ptr, dd.ptr, items, count, None)
     assert np.array_equal(out.download(want.shape), want)
+
+
+@pytest.mark.parametrize("log_n,levels,log_b,items,count", [
+    (7, 3, 10, 8, 3), (9, 5, 8, 27, 2), (12, 4, 8, 16, 33), (12, 10, 8, 1024, 17)])
+def test_pir_expand_absorb(sg, oracle, log_n, levels, log_b, items, count):
+    """Expansion to `items` ciphertexts then the database absorb-sum, in one
+    call.  At n=2^12 with 10 levels (the PIR workload's shape) a query's
+    expansion is 64 MiB, so 17 queries take two groups of the 1 GiB scratch."""
+    import ctypes
+    q, n = Q60, 1 << log_n
+    p = oracle.Prime(q, log_n)
+    dim = p.gadget_size(log_b)
+    keys = oracle.uniform_limbs(97, [q], n, levels * 2 * dim).reshape(levels, 2, dim, n)
+    cts = oracle.uniform_limbs(98, [q], n, 2 * count).reshape(count, 2, n)
+    db = oracle.uniform_limbs(99, [q], n, items).reshape(items, n)
+    want = np.stack([p.absorb_sum(p.oblivious_expand(levels, log_b, keys, cts[i])[:items], db)
+                     for i in range(count)])
+    ctx = sg.Context(log_n, [q])
+    gkeys = [sg.Key(ctx, [log_b], (n >> j) + 1, keys[j, 0], keys[j, 1]) for j in range(levels)]
+    arr = (ctypes.c_void_p * levels)(*[k.h for k in gkeys])
+    dc, dd = _dev(sg, cts), _dev(sg, db)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_pir_expand_absorb, ctx.h, arr, levels, dd.ptr, items, out.ptr,
+         dc.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want)
+    with pytest.raises(sg.ShgError, match="Output length must be at most"):
+        sg.check(sg.lib().shg_pir_expand_absorb(ctx.h, arr, levels, dd.ptr, (1 << levels) + 1,
+                                                out.ptr, dc.ptr, count, None))
