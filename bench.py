@@ -508,6 +508,237 @@ def run_pir(args, world, rank, local, dist):
         lib.shg_host_free(hp)
 
 
+# ---------------------------------------------------------------------------
+# Uneven batch: 4096 instances, n in {2^11..2^15}, 1..12 limbs of 50-bit
+# primes, 70% ct-mult+relin / 20% rotation / 10% modulus switch, run through
+# the batch executor (autotuned, graph-replayed) vs one call per operation.
+# ---------------------------------------------------------------------------
+
+Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,
+       1125899902124033, 1125899901665281, 1125899899174913, 1125899896160257,
+       1125899887312897, 1125899886395393, 1125899885740033, 1125899885412353]
+UNEVEN_METRIC = "uneven batch ops/sec (n 2^11..2^15, 1..12 limbs; 70% ct-mult+relin, " \
+                "20% rotation, 10% ModReduce)"
+UNEVEN_UNIT = "ops/s"
+UNEVEN_LOG_B = 20
+
+
+def uneven_instances(count, seed):
+    """Seeded instance list: (log_n, limbs, kind, galois exponent j)."""
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(count):
+        log_n = rng.randint(11, 15)
+        L = rng.randint(1, 12)
+        r = rng.random()
+        kind = 0 if r < 0.7 else (1 if r < 0.9 else 2)
+        while kind == 2 and L == 1:
+            L = rng.randint(1, 12)
+        out.append((log_n, L, kind, rng.randint(1, 8)))
+    return out
+
+
+def uneven_config(count):
+    return {"workload": "uneven-batch n=2^11..2^15 L=1..12 x 50-bit, gadget 2^20, "
+                        "70/20/10 ct-mult+relin/rotation/ModReduce, Galois powers 5^j mod 2n, "
+                        "j in 1..8",
+            "instances": count, "gadget_log_base": UNEVEN_LOG_B,
+            "l2": "operands per step exceed L2 by far", "parallelism": "replicas"}
+
+
+def run_uneven(args, world, rank, local, dist):
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    inst = uneven_instances(args.instances, 4242 + rank)
+    shapes = sorted({(ln, L) for ln, L, _, _ in inst})
+    ctxs, relin, galois = {}, {}, {}
+    pools = {}
+    for ln, L in shapes:
+        n = 1 << ln
+        if ln not in pools:
+            Lmax = max(l2 for l1, l2 in shapes if l1 == ln)
+            kmax = 3 * Lmax
+            pools[ln] = (splitmix_limbs(9000 + ln, kmax, Q50[:Lmax], n),
+                         splitmix_limbs(9100 + ln, kmax, Q50[:Lmax], n))
+        pb, pa = pools[ln]
+        ctx = sg.Context(ln, Q50[:L])
+        ctxs[(ln, L)] = ctx
+        k = 3 * L
+        kb = np.ascontiguousarray(pb[:k, :L])
+        ka = np.ascontiguousarray(pa[:k, :L])
+        used = {(kind, j) for l1, l2, kind, j in inst if (l1, l2) == (ln, L)}
+        if any(kind == 0 for kind, _ in used):
+            relin[(ln, L)] = sg.Key(ctx, [UNEVEN_LOG_B] * L, 1, kb, ka)
+        for kind, j in used:
+            if kind == 1 and (ln, L, j) not in galois:
+                galois[(ln, L, j)] = sg.Key(ctx, [UNEVEN_LOG_B] * L, pow(5, j, 2 * n), kb, ka)
+    # Operands: inputs in one region, outputs in another, each instance at a
+    # shuffled position (a group's operands are not adjacent).
+    import random
+    rng = random.Random(77 + rank)
+    order = list(range(len(inst)))
+    rng.shuffle(order)
+    in_off, out_off, pos_in, pos_out = 0, 0, {}, {}
+    for i in order:
+        ln, L, kind, _ = inst[i]
+        ct = 2 * L * (1 << ln) * 8
+        pos_in[i] = in_off
+        in_off += ct * (2 if kind == 0 else 1)
+        pos_out[i] = out_off
+        out_off += ct
+    d_in, d_out = sg.DeviceBuffer(in_off), sg.DeviceBuffer(out_off)
+    for i, (ln, L, kind, _) in enumerate(inst):
+        cts = 2 if kind == 0 else 1
+        sg.check(lib.shg_poly_fill_uniform(ctxs[(ln, L)].h, d_in.ptr + pos_in[i], 2 * cts, L,
+                                           500000 + i, None))
+    ql = {key: ctxs[key].ql_inv(key[1] - 1) for key in ctxs if key[1] > 1}
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+    b = ctypes.c_void_p()
+    sg.check(lib.shg_batch_create(ctypes.byref(b)))
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+
+    def per_op(i):
+        ln, L, kind, j = inst[i]
+        ctx = ctxs[(ln, L)]
+        a = d_in.ptr + pos_in[i]
+        o = d_out.ptr + pos_out[i]
+        ct = 2 * L * (1 << ln) * 8
+        if kind == 0:
+            return lib.shg_bgv_mul_relin(ctx.h, relin[(ln, L)].h, o, a, a + ct, 1, s)
+        if kind == 1:
+            return lib.shg_bgv_rotate(ctx.h, galois[(ln, L, j)].h, o, a, 1, s)
+        return lib.shg_poly_modreduce_lsb(ctx.h, o, a, 65537, ql[(ln, L)].ctypes.data_as(u64p),
+                                          1, 2, L, s)
+
+    for i, (ln, L, kind, j) in enumerate(inst):
+        ctx = ctxs[(ln, L)]
+        a = d_in.ptr + pos_in[i]
+        o = d_out.ptr + pos_out[i]
+        ct = 2 * L * (1 << ln) * 8
+        if kind == 0:
+            sg.check(lib.shg_batch_add_mul_relin(b, ctx.h, relin[(ln, L)].h, o, a, a + ct))
+        elif kind == 1:
+            sg.check(lib.shg_batch_add_rotate(b, ctx.h, galois[(ln, L, j)].h, o, a))
+        else:
+            sg.check(lib.shg_batch_add_modreduce(b, ctx.h, o, a, 2, L, 65537,
+                                                 ql[(ln, L)].ctypes.data_as(u64p)))
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b2):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b2, ctypes.byref(ms)))
+        return ms.value
+
+    # Plain: one call per operation (also the reference result).
+    for i in range(len(inst)):
+        sg.check(per_op(i))
+    sg.check(lib.shg_stream_synchronize(s))
+    e0, e1 = ev(), ev()
+    sg.check(lib.shg_event_record(e0, s))
+    for i in range(len(inst)):
+        sg.check(per_op(i))
+    sg.check(lib.shg_event_record(e1, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    plain_ms = elapsed(e0, e1)
+    ref_out = np.empty(out_off // 8, np.uint64)
+    sg.check(lib.shg_memcpy_d2h(ref_out.ctypes.data, d_out.ptr, out_off, s))
+    sg.check(lib.shg_memset_device(d_out.ptr, 0, out_off, s))
+
+    # Batched: plan + autotune (untimed), capture, replay.
+    sg.check(lib.shg_batch_run(b, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    t0 = time.perf_counter()
+    if not args.no_autotune:
+        sg.check(lib.shg_batch_autotune(b, 2, s))
+    tune_s = time.perf_counter() - t0
+    sg.check(lib.shg_batch_run(b, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    n0 = lib.shg_launch_count()
+    sg.check(lib.shg_graph_capture_begin(s))
+    sg.check(lib.shg_batch_run(b, s))
+    g = ctypes.c_void_p()
+    sg.check(lib.shg_graph_capture_end(s, ctypes.byref(g)))
+    graph = g.value
+    launches_per_step = lib.shg_launch_count() - n0
+    for _ in range(args.warmup):
+        sg.check(lib.shg_graph_launch(graph, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    evs = [ev() for _ in range(args.steps + 1)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    sg.check(lib.shg_event_record(evs[0], s))
+    for i in range(args.steps):
+        sg.check(lib.shg_graph_launch(graph, s))
+        sg.check(lib.shg_event_record(evs[i + 1], s))
+    sg.check(lib.shg_stream_synchronize(s))
+    barrier(dist)
+    clk = clocks.stop()
+    total_ms = max_over_ranks(dist, elapsed(evs[0], evs[-1]))
+    ops_all = sum_over_ranks(dist, float(len(inst) * args.steps))
+    value = ops_all / (total_ms / 1e3)
+    got = np.empty(out_off // 8, np.uint64)
+    sg.check(lib.shg_memcpy_d2h(got.ctypes.data, d_out.ptr, out_off, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    bit_exact = bool(np.array_equal(got, ref_out))
+
+    e2e = None
+    if not args.no_e2e:
+        def host(nbytes):
+            p = ctypes.c_void_p()
+            sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+            return p.value
+        h_in, h_out = host(in_off), host(out_off)
+        sg.check(lib.shg_memcpy_d2h(h_in, d_in.ptr, in_off, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        x0, x1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(x0, s))
+        for _ in range(args.steps):
+            sg.check(lib.shg_memcpy_h2d(d_in.ptr, h_in, in_off, s))
+            sg.check(lib.shg_graph_launch(graph, s))
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, out_off, s))
+        sg.check(lib.shg_event_record(x1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        e2e_ms = max_over_ranks(dist, elapsed(x0, x1))
+        e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNEVEN_UNIT,
+               "h2d_bytes_per_step": in_off, "d2h_bytes_per_step": out_off,
+               "ms_per_step": e2e_ms / args.steps}
+        lib.shg_host_free(h_in)
+        lib.shg_host_free(h_out)
+    kinds = [x[2] for x in inst]
+    line = {
+        "metric": UNEVEN_METRIC, "value": value, "unit": UNEVEN_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded instances, uniform residues, keys from seeded pools)",
+        "config": uneven_config(len(inst)),
+        "mix": {"ct_mult_relin": kinds.count(0), "rotation": kinds.count(1),
+                "modreduce": kinds.count(2), "contexts": len(ctxs),
+                "galois_keys": len(galois), "groups": lib.shg_batch_num_groups(b)},
+        "plain": {"value": len(inst) / (plain_ms / 1e3), "unit": UNEVEN_UNIT,
+                  "path": "one per-op C ABI call per instance"},
+        "batched_over_plain": (value / world) / (len(inst) / (plain_ms / 1e3)),
+        "bit_exact_batched_vs_plain": bit_exact,
+        "autotune": {"seconds": tune_s, "entries": lib.shg_tuning_size(),
+                     "enabled": not args.no_autotune},
+        "e2e": e2e, "gpu_launches": int(launches_per_step * args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sg.check(lib.shg_graph_destroy(graph))
+    lib.shg_batch_destroy(b)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,9 +752,13 @@ def main():
                     help="log n from which NTTs use the four-step kernels (default 14)")
     ap.add_argument("--ks-unfused", action="store_true",
                     help="separate digit row phase and key inner product kernels")
-    ap.add_argument("--workload", default="ct-mult-relin", choices=["ct-mult-relin", "pir"],
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--workload", default="ct-mult-relin",
+                    choices=["ct-mult-relin", "pir", "uneven"],
                     help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
-                         "pir: oblivious expansion + database absorb (n=2^12, one prime)")
+                         "pir: oblivious expansion + database absorb (n=2^12, one prime); "
+                         "uneven: 4096 mixed instances through the batch executor")
     ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -531,6 +766,15 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
 
     world, rank, local, dist = dist_setup(args)
+    if args.workload == "uneven":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": UNEVEN_METRIC,
+                                  "unavailable": "timed only for the ct-mult-relin and pir "
+                                                 "workloads"}), flush=True)
+        else:
+            run_uneven(args, world, rank, local, dist)
+        return
     if args.workload == "pir":
         if args.impl == "reference":
             run_pir_reference(args, world, rank)

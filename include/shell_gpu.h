@@ -159,6 +159,11 @@ int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
                    shg_key** out);
 void shg_key_destroy(shg_key* key);
 int shg_key_dimension(const shg_key* key);
+/* Number of limbs, substitution power (1 = relinearization key) and owning
+ * context of a key. */
+int shg_key_num_limbs(const shg_key* key);
+int shg_key_power(const shg_key* key);
+shg_context* shg_key_context(const shg_key* key);
 /* Device bytes held by the key. */
 size_t shg_key_device_bytes(const shg_key* key);
 

@@ -60,14 +60,23 @@ int shg_context_reserve(shg_context* ctx, size_t bytes);
 /* Ciphertexts per internal chunk of the batched key-switch pipeline
  * (0 = default). */
 int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
-/* Transforms of n >= 2^log_n use the two-kernel four-step NTT (14 = default;
- * 15 keeps n = 2^14 on the one-CTA-per-limb kernel; n = 2^15 always uses the
- * four-step kernels). */
+/* Transforms of n >= 2^log_n use the two-kernel four-step NTT, log_n in
+ * [12, 16] (14 = default; 12 or 13 also move n = 2^12 / 2^13 off the
+ * one-CTA-per-limb kernels; 15 keeps n = 2^14 on them; n = 2^15 always uses
+ * the four-step kernels). */
 int shg_context_set_four_step_min(shg_context* ctx, int log_n);
 /* 1 (default): four-step key switches run the digit row phase and the key
  * inner product as one kernel; 0: separate row phase, digit NTTs written to
  * scratch, then the inner product.  Results are identical. */
 int shg_context_set_ks_fused(shg_context* ctx, int on);
+/* Current values of the three settings above (chunk 0 = default). */
+int shg_context_get_tuning(const shg_context* ctx, int* chunk_cts, int* four_step_min,
+                           int* ks_fused);
+/* Seeded synthetic data: polys [count][num_limbs][n] <- uniform residues,
+ * element e = splitmix64 output e + 1 of state `seed` mod its limb's prime
+ * (the generator of the test suite's oracle.uniform_limbs). */
+int shg_poly_fill_uniform(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                          uint64_t seed, shg_stream stream);
 
 #ifdef __cplusplus
 }

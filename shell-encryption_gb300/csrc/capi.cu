@@ -151,6 +151,10 @@ int make_prime(uint64_t q, int log_n, HostPrime* hp) {
 
 }  // namespace
 
+namespace shg {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace shg
+
 // ---------------------------------------------------------------------------
 // Context and key objects
 // ---------------------------------------------------------------------------
@@ -686,6 +690,9 @@ void shg_key_destroy(shg_key* key) {
   delete key;
 }
 
+int shg_key_num_limbs(const shg_key* key) { return key ? key->L : 0; }
+int shg_key_power(const shg_key* key) { return key ? key->power : 0; }
+shg_context* shg_key_context(const shg_key* key) { return key ? key->ctx : nullptr; }
 int shg_key_dimension(const shg_key* key) { return key ? key->k : -1; }
 size_t shg_key_device_bytes(const shg_key* key) { return key ? key->bytes : 0; }
 
@@ -1253,10 +1260,28 @@ int shg_context_set_chunk(shg_context* ctx, int cts) {
   return SHG_OK;
 }
 int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
-  if (!ctx || log_n < 14 || log_n > 16)
-    return fail(SHG_INVALID_ARGUMENT, "four-step threshold must be 14, 15 or 16");
+  if (!ctx || log_n < 12 || log_n > 16)
+    return fail(SHG_INVALID_ARGUMENT, "four-step threshold must lie in [12, 16]");
   ctx->ntt4_min = log_n;
   return SHG_OK;
+}
+int shg_context_get_tuning(const shg_context* ctx, int* chunk, int* four_step_min,
+                           int* ks_fused) {
+  if (!ctx || !chunk || !four_step_min || !ks_fused)
+    return fail(SHG_INVALID_ARGUMENT, "null argument");
+  *chunk = ctx->chunk_cts;
+  *four_step_min = ctx->ntt4_min;
+  *ks_fused = ctx->ks_fused;
+  return SHG_OK;
+}
+int shg_poly_fill_uniform(shg_context* ctx, uint64_t* polys, int count, int num_limbs,
+                          uint64_t seed, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({polys}))) return st;
+  shg::launch_fill_uniform(ctx->dev(), polys, seed, count, num_limbs, (cudaStream_t)s);
+  return launch_status("fill_uniform");
 }
 int shg_context_set_ks_fused(shg_context* ctx, int on) {
   if (!ctx || (on != 0 && on != 1))

@@ -606,6 +606,49 @@ __global__ void k_monomials(uint64_t* mono, int levels, int log_n,
   }
 }
 
+// Seeded uniform residues: element e of [count][L][n] is splitmix64 output
+// e + 1 of state `seed`, reduced mod its limb's prime.
+__global__ void k_fill_uniform(uint64_t* out, uint64_t seed, size_t total,
+                               int log_n, int L, CtxDev c) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    uint64_t z = seed + (uint64_t)(e + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const int l = (int)((e >> log_n) % (size_t)L);
+    out[e] = z % c.primes[l].q;
+  }
+}
+
+// Operand gather / result scatter of the batch executor: `count` blocks of
+// `elems` uint64 (a multiple of 2, 16-byte aligned) between a contiguous
+// buffer and a device table of block pointers.
+__global__ void k_gather(uint64_t* dst, const uint64_t* const* srcs, size_t elems,
+                         size_t total /* count*elems/2 */) {
+  const size_t half = elems / 2;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t b = e / half, i = e % half;
+    reinterpret_cast<ulonglong2*>(dst)[e] =
+        reinterpret_cast<const ulonglong2*>(srcs[b])[i];
+  }
+}
+
+__global__ void k_scatter(uint64_t* const* dsts, const uint64_t* src, size_t elems,
+                          size_t total /* count*elems/2 */) {
+  const size_t half = elems / 2;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t b = e / half, i = e % half;
+    reinterpret_cast<ulonglong2*>(dsts[b])[i] =
+        reinterpret_cast<const ulonglong2*>(src)[e];
+  }
+}
+
 // FusedAbsorbAddInPlace chain (symmetric_encryption.h:250-275).
 __global__ void k_absorb_sum(uint64_t* out, const uint64_t* cts,
                              const uint64_t* db, int num_items,
@@ -907,6 +950,30 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
   LaunchScope scope_("expand_combine", s);
   k_expand_combine<<<grid_for(total, 256), 256, 0, s>>>(base, ks, mono, map,
                                                         half, total, c.log_n, c);
+}
+
+void launch_fill_uniform(const CtxDev& c, uint64_t* out, uint64_t seed, int count,
+                         int L, cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("fill_uniform", s);
+  k_fill_uniform<<<grid_for(total, 256), 256, 0, s>>>(out, seed, total, c.log_n, L, c);
+}
+
+void launch_gather(uint64_t* dst, const uint64_t* const* srcs, size_t elems, int count,
+                   cudaStream_t s) {
+  const size_t total = (size_t)count * (elems / 2);
+  if (total == 0) return;
+  LaunchScope scope_("gather", s);
+  k_gather<<<grid_for(total, 256), 256, 0, s>>>(dst, srcs, elems, total);
+}
+
+void launch_scatter(uint64_t* const* dsts, const uint64_t* src, size_t elems, int count,
+                    cudaStream_t s) {
+  const size_t total = (size_t)count * (elems / 2);
+  if (total == 0) return;
+  LaunchScope scope_("scatter", s);
+  k_scatter<<<grid_for(total, 256), 256, 0, s>>>(dsts, src, elems, total);
 }
 
 void launch_monomials(const CtxDev& c, uint64_t* mono, int levels,

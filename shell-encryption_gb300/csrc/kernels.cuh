@@ -5,6 +5,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "modarith.cuh"
@@ -165,6 +166,19 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            const uint64_t* mono, CtMap map, int half,
                            int count, cudaStream_t s);
 
+// Seeded uniform residues [count][L][n] (splitmix64, reduced per limb).
+void launch_fill_uniform(const CtxDev& c, uint64_t* out, uint64_t seed, int count,
+                         int L, cudaStream_t s);
+// dst [count][elems] <- srcs[b][elems]; dsts[b][elems] <- src [count][elems].
+// elems even, every block 16-byte aligned; srcs / dsts are device tables.
+void launch_gather(uint64_t* dst, const uint64_t* const* srcs, size_t elems, int count,
+                   cudaStream_t s);
+void launch_scatter(uint64_t* const* dsts, const uint64_t* src, size_t elems, int count,
+                    cudaStream_t s);
+// Sets this thread's last-error message (the C ABI's shg_last_error) and
+// returns `code`.
+int set_error(int code, const std::string& msg);
+
 // mono [levels][n] <- -x^{n - 2^j} in coefficient form (minus_one = the
 // Montgomery form of -1).
 void launch_monomials(const CtxDev& c, uint64_t* mono, int levels,
@@ -181,7 +195,7 @@ void launch_absorb_sum(const CtxDev& c, uint64_t* out, const uint64_t* cts,
 // device; 0 on success.
 int measure_butterfly_rate(double* per_second);
 
-// Four-step variants (ntt4.cu), n = 2^14 and 2^15; same semantics as the
+// Four-step variants (ntt4.cu), n = 2^12 .. 2^15; same semantics as the
 // launchers above.
 void launch4_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                      int L, cudaStream_t s);

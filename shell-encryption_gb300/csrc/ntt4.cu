@@ -1,4 +1,4 @@
-// Four-step NTT kernels (n = 2^14, 2^15) and the fused operations built on
+// Four-step NTT kernels (n = 2^12 .. 2^15) and the fused operations built on
 // them.  Phase kernels take a source policy (how transform g's inputs are
 // produced) and a sink policy (where its outputs go); see ntt4.cuh.
 #include "ntt4.cuh"
@@ -526,6 +526,8 @@ void inv4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
 
 #define SHG_DISPATCH4(log_n, F) \
   switch (log_n) {              \
+    case 12: F(12); break;      \
+    case 13: F(13); break;      \
     case 14: F(14); break;      \
     case 15: F(15); break;      \
     default: break;             \

@@ -1,4 +1,4 @@
-// Four-step organisation of the negacyclic NTT for n = 2^14 and 2^15.
+// Four-step organisation of the negacyclic NTT for n = 2^12 .. 2^15.
 //
 // The transform index splits into A high "row" bits and B = 7 low "column"
 // bits.  The forward transform's first A levels pair elements that differ

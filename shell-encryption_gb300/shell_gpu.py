@@ -51,6 +51,9 @@ SIGNATURES = {
                                       ctypes.POINTER(_vp)]),
     "shg_key_destroy": (None, [_vp]),
     "shg_key_dimension": (ctypes.c_int, [_vp]),
+    "shg_key_num_limbs": (ctypes.c_int, [_vp]),
+    "shg_key_power": (ctypes.c_int, [_vp]),
+    "shg_key_context": (_vp, [_vp]),
     "shg_key_device_bytes": (_sz, [_vp]),
     "shg_relin_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_relin_apply_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
@@ -96,6 +99,27 @@ SIGNATURES = {
     "shg_context_set_chunk": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_set_four_step_min": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_set_ks_fused": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "shg_context_get_tuning": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
+    "shg_poly_fill_uniform": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_uint64, _vp]),
+    # uneven-batch executor and autotuner (include/shell_gpu_batch.h)
+    "shg_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp)]),
+    "shg_batch_destroy": (None, [_vp]),
+    "shg_batch_clear": (ctypes.c_int, [_vp]),
+    "shg_batch_size": (ctypes.c_int, [_vp]),
+    "shg_batch_add_mul_relin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "shg_batch_add_rotate": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "shg_batch_add_modreduce": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_uint64, _u64p]),
+    "shg_batch_run": (ctypes.c_int, [_vp, _vp]),
+    "shg_batch_num_groups": (ctypes.c_int, [_vp]),
+    "shg_batch_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "shg_tuning_clear": (ctypes.c_int, []),
+    "shg_tuning_size": (ctypes.c_int, []),
+    "shg_tuning_save": (ctypes.c_int, [ctypes.c_char_p]),
+    "shg_tuning_load": (ctypes.c_int, [ctypes.c_char_p]),
+    "shg_tuning_lookup": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, _ip, _ip, _ip]),
 }
 
 _lib = None

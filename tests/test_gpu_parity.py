@@ -70,28 +70,45 @@ NTT_CASES = [(log_n, qs) for log_n in range(1, 15) for qs in ([Q45[0], Q45[1]],)
     (15, [Q50[5]])]
 
 
-@pytest.mark.parametrize("four_step_min", [14, 15])
-def test_ntt_2_14_both_kernels(sg, oracle, four_step_min):
-    """n = 2^14 runs on the four-step kernels by default and on the
-    one-CTA-per-limb kernel when the threshold is raised; both are exact."""
-    log_n, qs, n = 14, Q45[:3], 1 << 14
+@pytest.mark.parametrize("log_n,four_step_min", [(12, 12), (12, 16), (13, 13), (13, 16),
+                                                   (14, 14), (14, 15)])
+def test_ntt_both_kernels(sg, oracle, log_n, four_step_min):
+    """n = 2^12 .. 2^14 run either on the one-CTA-per-limb kernels or on the
+    two-phase four-step kernels (the threshold picks); every fused operation
+    is exact on both: NTT round trip, ct-mult+relin, rotation, ModReduceLsb."""
+    qs, n = Q45[:3], 1 << log_n
     x = oracle.uniform_limbs(77, qs, n, 2)
     rns = oracle.Rns(log_n, qs)
     ctx = sg.Context(log_n, qs)
-    sg.check(sg.lib().shg_context_set_four_step_min(ctx.h, four_step_min))
+    lib = sg.lib()
+    sg.check(lib.shg_context_set_four_step_min(ctx.h, four_step_min))
     d = _dev(sg, x)
-    _run(sg, sg.lib().shg_ntt_forward, ctx.h, d.ptr, 2, 3, None)
+    _run(sg, lib.shg_ntt_forward, ctx.h, d.ptr, 2, 3, None)
     assert np.array_equal(d.download(x.shape), np.stack([rns.ntt_fwd(x[i]) for i in range(2)]))
-    _run(sg, sg.lib().shg_ntt_inverse, ctx.h, d.ptr, 2, 3, None)
+    _run(sg, lib.shg_ntt_inverse, ctx.h, d.ptr, 2, 3, None)
     assert np.array_equal(d.download(x.shape), x)
     k = rns.gadget_dim([20] * 3)
     kb, ka = oracle.uniform_limbs(78, qs, n, k), oracle.uniform_limbs(79, qs, n, k)
-    a, b = _ct_pair(oracle, qs, n, 1, 80)
-    want = rns.relin(rns.tensor(a[0], b[0]), kb, ka, [20] * 3)
+    a, b = _ct_pair(oracle, qs, n, 2, 80)
+    want = np.stack([rns.relin(rns.tensor(a[i], b[i]), kb, ka, [20] * 3) for i in range(2)])
     key = sg.Key(ctx, [20] * 3, 1, kb, ka)
     da, db, out = _dev(sg, a), _dev(sg, b), sg.DeviceBuffer(a.nbytes)
-    _run(sg, sg.lib().shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, 1, None)
+    _run(sg, lib.shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, 2, None)
     assert np.array_equal(out.download(want.shape), want)
+    power = 5
+    gkey = sg.Key(ctx, [20] * 3, power, kb, ka)
+    sub = np.stack([np.stack([rns.substitute(a[i, c], power) for c in range(2)])
+                    for i in range(2)])
+    want_rot = np.stack([rns.galois(sub[i], kb, ka, [20] * 3) for i in range(2)])
+    _run(sg, lib.shg_bgv_rotate, ctx.h, gkey.h, out.ptr, da.ptr, 2, None)
+    assert np.array_equal(out.download(want_rot.shape), want_rot)
+    ql_inv = ctx.ql_inv(2)
+    want_mr = np.stack([rns.modreduce_lsb(a[i, c], 65537, True) for i in range(2)
+                        for c in range(2)])
+    mr = sg.DeviceBuffer(want_mr.nbytes)
+    _run(sg, lib.shg_poly_modreduce_lsb, ctx.h, mr.ptr, da.ptr, 65537,
+         ql_inv.ctypes.data_as(sg._u64p), 1, 4, 3, None)
+    assert np.array_equal(mr.download(want_mr.shape), want_mr)
 
 
 @pytest.mark.parametrize("log_n,qs", NTT_CASES)
