@@ -739,6 +739,167 @@ def run_uneven(args, world, rank, local, dist):
     lib.shg_batch_destroy(b)
 
 
+# ---------------------------------------------------------------------------
+# Serving: Poisson arrivals from 64 clients with resident keys; parameter sets
+# (n, limbs) in {(2^12, 2), (2^13, 3), (2^14, 6), (2^15, 12)} of 50-bit primes;
+# 70% ct-mult+relin, 20% rotation, 10% PIR expand+absorb; served with
+# continuous batching vs one call per request.
+# ---------------------------------------------------------------------------
+
+SERVE_PARAMS = [(12, 2), (13, 3), (14, 6), (15, 12)]
+SERVE_METRIC = "served requests/sec (continuous batching, Poisson arrivals; p50/p99/p999 ms)"
+SERVE_UNIT = "req/s"
+
+
+def serve_config(clients, rates, seconds):
+    return {"workload": "serving: Poisson arrivals, 64 clients, (n, limbs) in "
+                        "{(2^12,2),(2^13,3),(2^14,6),(2^15,12)} x 50-bit, 70% ct-mult+relin, "
+                        "20% rotation, 10% PIR expand+absorb (n=2^12, 10 levels)",
+            "clients": clients, "rates_req_s": rates, "arrival_seconds": seconds,
+            "parallelism": "replicas"}
+
+
+def run_serve(args, world, rank, local, dist):
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    rates = [int(r) for r in args.rates.split(",")]
+    clients = args.clients
+    ctxs, keys = {}, {}
+    for ln, L in SERVE_PARAMS:
+        n = 1 << ln
+        ctx = sg.Context(ln, Q50[:L])
+        ctxs[(ln, L)] = ctx
+        k = 3 * L
+        kb = splitmix_limbs(9300 + ln, k, Q50[:L], n)
+        ka = splitmix_limbs(9400 + ln, k, Q50[:L], n)
+        for c in range(clients):
+            keys[(c, ln, L, 0)] = sg.Key(ctx, [UNEVEN_LOG_B] * L, 1, kb, ka)
+            keys[(c, ln, L, 1)] = sg.Key(ctx, [UNEVEN_LOG_B] * L, 5, kb, ka)
+    # PIR: one context, a shared database, per-client expansion keys.
+    pn = 1 << PIR_LOG_N
+    pctx = sg.Context(PIR_LOG_N, [PIR_Q], (1 << PIR_LOG_T) + 1)
+    dim, pkeys, db_plain, _ = pir_keys_db_queries(3000, pn, 1)
+    d_db = sg.DeviceBuffer.from_array(db_plain)
+    r2 = np.array([pow(2, 128, PIR_Q)], np.uint64)
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    sg.check(lib.shg_poly_mul_rns_scalar(pctx.h, d_db.ptr, d_db.ptr, r2.ctypes.data_as(u64p),
+                                         PIR_ITEMS, 1, None))
+    sg.check(lib.shg_ntt_forward(pctx.h, d_db.ptr, PIR_ITEMS, 1, None))
+    pir_keys, pir_arr = {}, {}
+    for c in range(clients):
+        pir_keys[c] = [sg.Key(pctx, [PIR_LOG_B], (pn >> j) + 1, pkeys[j, 0], pkeys[j, 1])
+                       for j in range(PIR_LEVELS)]
+        pir_arr[c] = (ctypes.c_void_p * PIR_LEVELS)(*[kk.h for kk in pir_keys[c]])
+
+    def host(nbytes):
+        p = ctypes.c_void_p()
+        sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+        return p.value
+
+    # Pinned host operands: two input ciphertexts per parameter set (read
+    # only, shared) and a ring of output slots per parameter set.
+    RING = 64
+    bufs = {}
+    for ln, L in SERVE_PARAMS:
+        ct = 2 * L * (1 << ln) * 8
+        a, b = host(ct), host(ct)
+        for hp, seed in ((a, 11), (b, 12)):
+            view = np.ctypeslib.as_array((ctypes.c_uint64 * (ct // 8)).from_address(hp))
+            view[:] = splitmix_limbs(seed + ln, 2, Q50[:L], 1 << ln).reshape(-1)
+        bufs[(ln, L)] = (a, b, [host(ct) for _ in range(RING)])
+    pq = host(2 * pn * 8)
+    np.ctypeslib.as_array((ctypes.c_uint64 * (2 * pn)).from_address(pq))[:] = \
+        splitmix_limbs(555, 2, [PIR_Q], pn).reshape(-1)
+    pouts = [host(2 * pn * 8) for _ in range(RING)]
+
+    def requests(rate, seed):
+        rng = np.random.default_rng(seed)
+        count = max(1, int(rate * args.seconds))
+        gaps = rng.exponential(1e6 / rate, count)
+        arrival = np.cumsum(gaps) - gaps[0]
+        arr = (sg.Request * count)()
+        kinds = np.zeros(count, np.int32)
+        for i in range(count):
+            c = int(rng.integers(clients))
+            r = rng.random()
+            kind = 0 if r < 0.7 else (1 if r < 0.9 else 2)
+            kinds[i] = kind
+            q = arr[i]
+            if kind == 2:
+                q.kind, q.ctx, q.keys, q.levels = 2, pctx.h, pir_arr[c], PIR_LEVELS
+                q.db, q.num_items, q.in_a, q.out = d_db.ptr, PIR_ITEMS, pq, pouts[i % RING]
+                continue
+            ln, L = SERVE_PARAMS[int(rng.integers(len(SERVE_PARAMS)))]
+            a, b, outs = bufs[(ln, L)]
+            q.kind, q.ctx, q.key = kind, ctxs[(ln, L)].h, keys[(c, ln, L, kind)].h
+            q.in_a, q.in_b, q.out = a, b, outs[i % RING]
+        return arr, (ctypes.c_double * count)(*arrival.tolist()), kinds
+
+    def serve(rate, max_batch, streams, seed):
+        cfg = sg.ServerConfig(args.hbm_budget_gb << 30, max_batch, args.max_wait_us, streams)
+        sv = ctypes.c_void_p()
+        sg.check(lib.shg_server_create(ctypes.byref(cfg), ctypes.byref(sv)))
+        reqs, arrival, kinds = requests(rate, seed)
+        count = len(reqs)
+        tickets = (ctypes.c_uint64 * count)()
+        t0 = time.perf_counter()
+        sg.check(lib.shg_server_replay(sv, reqs, arrival, count, tickets))
+        for i in range(count):
+            sg.check(lib.shg_server_wait(sv, tickets[i], 600_000_000))
+        wall = time.perf_counter() - t0
+        lat = np.empty(count)
+        a_, l_, d_ = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        end = 0.0
+        for i in range(count):
+            sg.check(lib.shg_server_latency(sv, tickets[i], ctypes.byref(a_), ctypes.byref(l_),
+                                            ctypes.byref(d_)))
+            lat[i] = d_.value
+            end = max(end, arrival[i] + d_.value)
+        st = sg.ServerStats()
+        sg.check(lib.shg_server_get_stats(sv, ctypes.byref(st)))
+        lib.shg_server_destroy(sv)
+        ms = lat / 1e3
+
+        def pct(p):
+            return float(np.percentile(ms, p))
+        res = {"offered_req_s": rate, "requests": count,
+               "throughput_req_s": count / (end / 1e6), "wall_s": wall,
+               "p50_ms": pct(50), "p99_ms": pct(99), "p999_ms": pct(99.9),
+               "by_kind_p50_ms": {k: float(np.percentile(ms[kinds == i], 50))
+                                  for i, k in enumerate(["ct_mult_relin", "rotation", "pir"])
+                                  if np.any(kinds == i)},
+               "mean_batch": st.mean_batch, "batches": st.batches,
+               "peak_gb_in_flight": st.peak_bytes_in_flight / 2**30,
+               "admission_waits": st.admission_waits, "failed": st.failed}
+        return res
+
+    serve(1000, 16, args.streams, 1)  # warm-up: scratch, pools, code paths
+    sweep, plain = [], []
+    for i, rate in enumerate(rates):
+        sweep.append(serve(rate, args.max_batch, args.streams, 100 + i))
+        plain.append(serve(rate, 1, 1, 100 + i))
+    clk = {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled for the serving sweep"]}
+    top = sweep[-1]
+    line = {
+        "metric": SERVE_METRIC, "value": top["throughput_req_s"], "unit": SERVE_UNIT,
+        "n_gpus": world, "steps": len(rates), "warmup": 1,
+        "ms_per_step": 1e3 * top["wall_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded Poisson arrivals, uniform ciphertexts, pooled key material)",
+        "config": serve_config(clients, rates, args.seconds),
+        "latency_ms": {"p50": top["p50_ms"], "p99": top["p99_ms"], "p999": top["p999_ms"]},
+        "sweep": sweep, "plain_per_request": plain,
+        "served_over_plain_at_top_rate": top["throughput_req_s"] / plain[-1]["throughput_req_s"],
+        "e2e": {"value": top["throughput_req_s"], "unit": SERVE_UNIT,
+                "note": "requests carry host buffers; copies in and out are inside every "
+                        "request's latency"},
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -753,9 +914,16 @@ def main():
     ap.add_argument("--ks-unfused", action="store_true",
                     help="separate digit row phase and key inner product kernels")
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--rates", default="1000,5000,20000,50000")
+    ap.add_argument("--seconds", type=float, default=1.0, help="arrival window per rate")
+    ap.add_argument("--clients", type=int, default=64)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--max-wait-us", type=int, default=500)
+    ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
-                    choices=["ct-mult-relin", "pir", "uneven"],
+                    choices=["ct-mult-relin", "pir", "uneven", "serve"],
                     help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
                          "pir: oblivious expansion + database absorb (n=2^12, one prime); "
                          "uneven: 4096 mixed instances through the batch executor")
@@ -766,6 +934,15 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
 
     world, rank, local, dist = dist_setup(args)
+    if args.workload == "serve":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": SERVE_METRIC,
+                                  "unavailable": "timed only for the ct-mult-relin and pir "
+                                                 "workloads"}), flush=True)
+        else:
+            run_serve(args, world, rank, local, dist)
+        return
     if args.workload == "uneven":
         if args.impl == "reference":
             if rank == 0:

@@ -122,6 +122,45 @@ SIGNATURES = {
                                          ctypes.c_int, _ip, _ip, _ip]),
 }
 
+
+
+class ServerConfig(ctypes.Structure):
+    """shg_server_config (include/shell_gpu_serve.h)."""
+    _fields_ = [("hbm_budget_bytes", _sz), ("max_batch", ctypes.c_int),
+                ("max_wait_us", ctypes.c_int), ("num_streams", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    """shg_request (include/shell_gpu_serve.h)."""
+    _fields_ = [("kind", ctypes.c_int), ("ctx", _vp), ("key", _vp),
+                ("keys", ctypes.POINTER(_vp)), ("levels", ctypes.c_int), ("db", _vp),
+                ("num_items", ctypes.c_int), ("in_a", _vp), ("in_b", _vp), ("out", _vp)]
+
+
+class ServerStats(ctypes.Structure):
+    """shg_server_stats (include/shell_gpu_serve.h)."""
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("mean_batch", ctypes.c_double), ("peak_bytes_in_flight", _sz),
+                ("admission_waits", ctypes.c_uint64)]
+
+
+SIGNATURES.update({
+    "shg_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "shg_server_destroy": (None, [_vp]),
+    "shg_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(Request),
+                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "shg_server_poll": (ctypes.c_int, [_vp, ctypes.c_uint64, _ip]),
+    "shg_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int64]),
+    "shg_server_latency": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
+    "shg_server_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "shg_server_replay": (ctypes.c_int, [_vp, ctypes.POINTER(Request),
+                                         ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_uint64)]),
+})
+
 _lib = None
 
 
