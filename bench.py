@@ -40,7 +40,11 @@ METRIC = "RNS ct-mult+relin/sec (batched vs plain, same GPU, bit-exact); p50/p99
 UNIT = "ct-mult+relin/s"
 # DRAM bytes (read + write) per ciphertext of each kernel scope, from ncu
 # captures of the same kernels (profiles/); None where not captured.
-TRAFFIC_PER_CT = {}
+TRAFFIC_PER_CT = {
+    # profiles/ks_rows_ct_mult_relin_n14.md: one 16-ciphertext launch
+    "ks_rows": (303.4e6 + 22.6e6) / 16,
+    "digit_cols": (12.7e6 + 165.3e6) / 16,
+}
 # Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
 # step; the four-step key switch runs digit_cols + ks_rows, the unfused one
 # digit_ntt + ks_inner.
