@@ -205,9 +205,10 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* relin_key, uint64_t* out,
                       const uint64_t* a, const uint64_t* b, int count,
                       shg_stream stream);
 /* shg_bgv_mul_relin on HOST buffers (a, b, out in host memory, page-locked
- * for full speed): the batch is split into pieces whose host->device copy,
- * ct-mult+relin and device->host copy run on three streams so transfers
- * overlap computation.  Ordered after prior work on `stream`; `stream` is
+ * for full speed): the batch is split into pieces whose host->device copies
+ * (a and b on two streams), ct-mult+relin and device->host copy run on four
+ * streams through a ring of device staging slots, so transfers overlap
+ * computation (shape: shg_context_set_host_pipeline).  Ordered after prior work on `stream`; `stream` is
  * ordered after the last copy back (synchronize it before reading out). */
 int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* relin_key,
                            uint64_t* out, const uint64_t* a, const uint64_t* b,

@@ -69,6 +69,9 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n);
  * inner product as one kernel; 0: separate row phase, digit NTTs written to
  * scratch, then the inner product.  Results are identical. */
 int shg_context_set_ks_fused(shg_context* ctx, int on);
+/* shg_bgv_mul_relin_host pipeline shape: ciphertexts per piece (default 128)
+ * and device staging slots in flight (default 4, at most 8). */
+int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots);
 /* Current values of the three settings above (chunk 0 = default). */
 int shg_context_get_tuning(const shg_context* ctx, int* chunk_cts, int* four_step_min,
                            int* ks_fused);

@@ -175,11 +175,13 @@ struct shg_context {
   int small_q = 0;  // all moduli below 2^58
   int ntt4_min = 14;  // four-step transforms from this log_n up
   int ks_fused = 1;   // fused digit row phase + key inner product
+  int host_piece = 128;  // host pipeline: ciphertexts per piece
+  int host_slots = 4;    // host pipeline: device staging slots in flight
   std::mutex mu;
   // Host-buffer pipeline: device staging slots and three streams.
   uint64_t* io = nullptr;
   size_t io_bytes = 0;
-  cudaStream_t io_streams[3] = {nullptr, nullptr, nullptr};
+  cudaStream_t io_streams[4] = {nullptr, nullptr, nullptr, nullptr};
   std::mutex io_mu;
 
   CtxDev dev() const {
@@ -779,26 +781,28 @@ int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
   if (!out || !a || !b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
   const size_t ct_elems = 2 * (size_t)key->L * ctx->n;
   const size_t ct_bytes = ct_elems * sizeof(uint64_t);
-  // Pieces of 64 ciphertexts, two staging slots of (a, b, out) each.
-  const int P = std::min(count, 64);
+  // Pieces of host_piece ciphertexts through host_slots staging slots of
+  // (a, b, out); a and b come in on two copy streams.
+  const int P = std::min(count, ctx->host_piece);
+  const int S = ctx->host_slots;
   const size_t slot = 3 * (size_t)P * ct_bytes;
   std::lock_guard<std::mutex> io_lock(ctx->io_mu);
-  if (ctx->io_bytes < 2 * slot) {
+  if (ctx->io_bytes < S * slot) {
     SHG_CUDA(cudaDeviceSynchronize());
     cudaFree(ctx->io);
     ctx->io = nullptr;
     ctx->io_bytes = 0;
-    cudaError_t e = cudaMalloc(&ctx->io, 2 * slot);
+    cudaError_t e = cudaMalloc(&ctx->io, S * slot);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(SHG_RESOURCE_EXHAUSTED, "cannot reserve host-pipeline staging");
     }
-    ctx->io_bytes = 2 * slot;
+    ctx->io_bytes = S * slot;
   }
   for (cudaStream_t& s : ctx->io_streams)
     if (!s) SHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   cudaStream_t s_in = ctx->io_streams[0], s_comp = ctx->io_streams[1],
-               s_out = ctx->io_streams[2];
+               s_out = ctx->io_streams[2], s_in2 = ctx->io_streams[3];
   cudaStream_t user = (cudaStream_t)stream;
   const int pieces = (count + P - 1) / P;
   std::vector<cudaEvent_t> evs;
@@ -811,26 +815,33 @@ int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
   if ((st = event(&start))) return st;
   SHG_CUDA(cudaEventRecord(start, user));
   SHG_CUDA(cudaStreamWaitEvent(s_in, start, 0));
-  std::vector<cudaEvent_t> loaded(pieces), computed(pieces), stored(pieces);
+  SHG_CUDA(cudaStreamWaitEvent(s_in2, start, 0));
+  std::vector<cudaEvent_t> loaded(pieces), loaded2(pieces), computed(pieces), stored(pieces);
   for (int i = 0; i < pieces; ++i) {
-    if ((st = event(&loaded[i])) || (st = event(&computed[i])) || (st = event(&stored[i])))
+    if ((st = event(&loaded[i])) || (st = event(&loaded2[i])) || (st = event(&computed[i])) ||
+        (st = event(&stored[i])))
       break;
   }
   int rc = st;
   for (int i = 0; i < pieces && rc == SHG_OK; ++i) {
     const int c0 = i * P, cc = std::min(P, count - c0);
-    uint64_t* da = ctx->io + (size_t)(i & 1) * (slot / sizeof(uint64_t));
+    uint64_t* da = ctx->io + (size_t)(i % S) * (slot / sizeof(uint64_t));
     uint64_t* db = da + (size_t)P * ct_elems;
     uint64_t* dout = db + (size_t)P * ct_elems;
-    // Slot reuse: piece i-2 must have been copied back (its compute also
+    // Slot reuse: piece i-S must have been copied back (its compute also
     // finished reading a, b before that).
-    if (i >= 2) SHG_CUDA(cudaStreamWaitEvent(s_in, stored[i - 2], 0));
+    if (i >= S) {
+      SHG_CUDA(cudaStreamWaitEvent(s_in, stored[i - S], 0));
+      SHG_CUDA(cudaStreamWaitEvent(s_in2, stored[i - S], 0));
+    }
     SHG_CUDA(cudaMemcpyAsync(da, a + (size_t)c0 * ct_elems, cc * ct_bytes,
                              cudaMemcpyHostToDevice, s_in));
     SHG_CUDA(cudaMemcpyAsync(db, b + (size_t)c0 * ct_elems, cc * ct_bytes,
-                             cudaMemcpyHostToDevice, s_in));
+                             cudaMemcpyHostToDevice, s_in2));
     SHG_CUDA(cudaEventRecord(loaded[i], s_in));
+    SHG_CUDA(cudaEventRecord(loaded2[i], s_in2));
     SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded[i], 0));
+    SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded2[i], 0));
     rc = shg_bgv_mul_relin(ctx, key, dout, da, db, cc, (shg_stream)s_comp);
     if (rc) break;
     SHG_CUDA(cudaEventRecord(computed[i], s_comp));
@@ -1263,6 +1274,13 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
   if (!ctx || log_n < 12 || log_n > 16)
     return fail(SHG_INVALID_ARGUMENT, "four-step threshold must lie in [12, 16]");
   ctx->ntt4_min = log_n;
+  return SHG_OK;
+}
+int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots) {
+  if (!ctx || piece_cts < 1 || slots < 2 || slots > 8)
+    return fail(SHG_INVALID_ARGUMENT, "piece must be positive and slots in [2, 8]");
+  ctx->host_piece = piece_cts;
+  ctx->host_slots = slots;
   return SHG_OK;
 }
 int shg_context_get_tuning(const shg_context* ctx, int* chunk, int* four_step_min,

@@ -468,40 +468,41 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
                            const uint64_t* ka, int k, int chunk,
                            const uint64_t* base, size_t base_ct_elems,
                            CtMap map, int base1_zero, int subst_power,
-                           size_t total /* count*L*n */, int log_n, int L,
-                           CtxDev c) {
-  const size_t n = (size_t)1 << log_n;
-  const size_t Ln = (size_t)L * n;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += stride) {
-    const size_t p = e / Ln, r = e % Ln;
-    const int l = (int)(r >> log_n);
-    const size_t pos = r & (n - 1);
-    const PrimeDev* P = c.primes + l;
-    const uint64_t q = P->q, qinv = P->inv_modulus;
-    const uint64_t* dp = D + p * (size_t)k * Ln + r;
-    uint64_t s0 = 0, s1 = 0;
-    for (int j0 = 0; j0 < k; j0 += chunk) {
-      const int j1 = min(k, j0 + chunk);
-      uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
-      for (int j = j0; j < j1; ++j) {
-        const uint64_t d = dp[(size_t)j * Ln];
-        mac128(lo0, hi0, d, __ldg(kb + (size_t)j * Ln + r));
-        mac128(lo1, hi1, d, __ldg(ka + (size_t)j * Ln + r));
-      }
-      s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
-      s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
+                           int p0, int log_n, int L, CtxDev c) {
+  // blockIdx.y: ciphertext p0 + y; x covers its L * n slots.
+  const int Ln = L << log_n;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= Ln) return;
+  const size_t p = (size_t)p0 + blockIdx.y;
+  const int l = r >> log_n;
+  const int pos = r & ((1 << log_n) - 1);
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, qinv = P->inv_modulus;
+  const uint64_t* dp = D + p * (size_t)k * Ln + r;
+  const uint64_t* pb = kb + r;
+  const uint64_t* pa = ka + r;
+  uint64_t s0 = 0, s1 = 0;
+  for (int j0 = 0; j0 < k; j0 += chunk) {
+    const int j1 = min(k, j0 + chunk);
+    uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+#pragma unroll 4
+    for (int j = j0; j < j1; ++j) {
+      const uint64_t d = *dp;
+      mac128(lo0, hi0, d, __ldg(pb));
+      mac128(lo1, hi1, d, __ldg(pa));
+      dp += Ln;
+      pb += Ln;
+      pa += Ln;
     }
-    const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
-    const size_t pos0 =
-        subst_power > 0 ? (size_t)subst_src_rt((int)pos, subst_power, log_n)
-                        : pos;
-    const uint64_t b0 = bp[pos0];
-    const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
-    out[p * 2 * Ln + r] = add_mod(b0, s0, q);
-    out[p * 2 * Ln + Ln + r] = add_mod(b1, s1, q);
+    s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
+    s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
   }
+  const uint64_t* bp = base + map(p) * base_ct_elems + ((size_t)l << log_n);
+  const int pos0 = subst_power > 0 ? subst_src_rt(pos, subst_power, log_n) : pos;
+  const uint64_t b0 = bp[pos0];
+  const uint64_t b1 = base1_zero ? 0 : bp[(size_t)Ln + pos];
+  out[p * 2 * Ln + r] = add_mod(b0, s0, q);
+  out[p * 2 * Ln + Ln + r] = add_mod(b1, s1, q);
 }
 
 // RnsGadget::Decompose (rns/rns_gadget.cc:108-153) of coefficient-form
@@ -864,11 +865,16 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
   LaunchScope scope_("ks_inner", s);
-  // One ciphertext per thread: blocking several ciphertexts per thread to
-  // reuse key loads measured slower (lower occupancy, fewer loads in flight).
-  k_ks_inner<<<grid_for(total, 256), 256, 0, s>>>(
-      out, D, kb, ka, k, chunk, base, base_ct_elems, map, base1_zero,
-      subst_power, total, c.log_n, L, c);
+  // One slot of one ciphertext per thread: blocking several ciphertexts per
+  // thread to reuse key loads measured slower (lower occupancy, fewer loads
+  // in flight).  Grid: x over the L * n slots, y over ciphertexts.
+  const int Ln = L << c.log_n;
+  const dim3 block(256);
+  for (int p0 = 0; p0 < count; p0 += 65535) {
+    const dim3 grid((Ln + 255) / 256, std::min(count - p0, 65535));
+    k_ks_inner<<<grid, block, 0, s>>>(out, D, kb, ka, k, chunk, base, base_ct_elems,
+                                      map, base1_zero, subst_power, p0, c.log_n, L, c);
+  }
 }
 
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,

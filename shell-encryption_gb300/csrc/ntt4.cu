@@ -410,14 +410,23 @@ __global__ void __maxnreg__(96)
     const int rr = o >> S::B, e = o & ((1 << S::B) - 1);
     const int pos = ((tile * R + rr) << S::B) | e;
     const size_t kr = (size_t)l * n + pos;
+    // Digit jj of this slot sits in sub-row rr*k + jj at RowMap's swizzled
+    // column: the 16-element swizzle of e, flipped on bit 3 for odd rows.
+    const uint64_t* drow = smem + ((size_t)(rr * k) << S::B);
+    const int col_even = (e ^ ((e >> 4) & 15)) ^ (((rr * k) & 1) << 3);
+    const uint64_t* pb = kb + kr;
+    const uint64_t* pa = ka + kr;
     uint64_t s0 = 0, s1 = 0;
     for (int j0 = 0; j0 < k; j0 += chunk) {
       const int j1 = min(k, j0 + chunk);
       uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+#pragma unroll 6
       for (int jj = j0; jj < j1; ++jj) {
-        const uint64_t d = RowMap<S::B>{smem, rr * k + jj}(e);
-        mac128(lo0, hi0, d, __ldg(kb + (size_t)jj * Ln + kr));
-        mac128(lo1, hi1, d, __ldg(ka + (size_t)jj * Ln + kr));
+        const uint64_t d = drow[(jj << S::B) + (col_even ^ ((jj & 1) << 3))];
+        mac128(lo0, hi0, d, __ldg(pb));
+        mac128(lo1, hi1, d, __ldg(pa));
+        pb += Ln;
+        pa += Ln;
       }
       s0 = add_mod(s0, redc128(lo0, hi0, q, qinv), q);
       s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
