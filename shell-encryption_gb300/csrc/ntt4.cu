@@ -366,10 +366,12 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
 //   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
 // with 128-bit lazy accumulation, one REDC per `chunk` digits.  The digit
 // transforms never go back to memory.  Arguments as in launch_ks_inner.
+// 72 registers let three 288-thread CTAs (k = 18 digits, 2 rows) share an
+// SM; 96 allowed only two.
 constexpr int kKsRowsMaxThreads = 512;
 
 template <int LOG_N, bool LAZY>
-__global__ void __maxnreg__(96)
+__global__ void __maxnreg__(72)
     k4_ks_rows(const uint64_t* buf, int k, int R, int chunk, const uint64_t* kb,
                const uint64_t* ka, uint64_t* out, const uint64_t* base,
                size_t base_ct_elems, CtMap map, int base1_zero, int subst_power,
