@@ -162,6 +162,8 @@ int shg_key_dimension(const shg_key* key);
 /* Number of limbs, substitution power (1 = relinearization key) and owning
  * context of a key. */
 int shg_key_num_limbs(const shg_key* key);
+/* The key's gadget base exponents (num_limbs entries into log_bs[max]). */
+int shg_key_log_bs(const shg_key* key, int* log_bs, int max);
 int shg_key_power(const shg_key* key);
 shg_context* shg_key_context(const shg_key* key);
 /* Device bytes held by the key. */
@@ -204,6 +206,24 @@ int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
 int shg_bgv_mul_relin(shg_context* ctx, const shg_key* relin_key, uint64_t* out,
                       const uint64_t* a, const uint64_t* b, int count,
                       shg_stream stream);
+/* Batches whose members bring their own keys (different clients): member i
+ * of shg_bgv_mul_relin_multikey / shg_bgv_rotate_multikey uses keys[i], and
+ * query q of shg_pir_expand_absorb_multikey uses keys[q * levels + j] at
+ * level j.  All keys of one call share the context, limbs, gadget and
+ * substitution power (per level for the expansion); results equal one call
+ * per key.  The key tables are staged from host memory, so these calls are
+ * not for stream capture. */
+int shg_bgv_mul_relin_multikey(shg_context* ctx, const shg_key* const* relin_keys,
+                               uint64_t* out, const uint64_t* a, const uint64_t* b,
+                               int count, shg_stream stream);
+int shg_bgv_rotate_multikey(shg_context* ctx, const shg_key* const* galois_keys,
+                            uint64_t* out, const uint64_t* ct, int count,
+                            shg_stream stream);
+int shg_pir_expand_absorb_multikey(shg_context* ctx, const shg_key* const* keys,
+                                   int levels, const uint64_t* db, int num_items,
+                                   uint64_t* out, const uint64_t* ct, int count,
+                                   shg_stream stream);
+
 /* shg_bgv_mul_relin on HOST buffers (a, b, out in host memory, page-locked
  * for full speed): the batch is split into pieces whose host->device copies
  * (a and b on two streams), ct-mult+relin and device->host copy run on four

@@ -693,6 +693,12 @@ void shg_key_destroy(shg_key* key) {
 }
 
 int shg_key_num_limbs(const shg_key* key) { return key ? key->L : 0; }
+int shg_key_log_bs(const shg_key* key, int* log_bs, int max) {
+  if (!key || !log_bs) return fail(SHG_INVALID_ARGUMENT, "null argument");
+  if (max < key->L) return fail(SHG_INVALID_ARGUMENT, "`log_bs` array too short");
+  for (int i = 0; i < key->L; ++i) log_bs[i] = key->log_bs[i];
+  return SHG_OK;
+}
 int shg_key_power(const shg_key* key) { return key ? key->power : 0; }
 shg_context* shg_key_context(const shg_key* key) { return key ? key->ctx : nullptr; }
 int shg_key_dimension(const shg_key* key) { return key ? key->k : -1; }
@@ -710,27 +716,42 @@ struct KsArgs {
   int base1_zero;      // Galois: c1' has no base term
 };
 
+int upload_key_table(const shg_key* const* keys, int count, int stride, int offset,
+                     const uint64_t** dst, shg::KeyTable* out, cudaStream_t s);
+
+// Gadget key switch of component a.comp of `count` ciphertexts; with `keys`,
+// member i uses keys[i] (same gadget shape as `key`).
 int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
-              const KsArgs& a, int count, cudaStream_t s) {
+              const KsArgs& a, int count, cudaStream_t s,
+              const shg_key* const* keys = nullptr) {
   const int L = key->L, n = ctx->n, k = key->k;
   const size_t Ln = (size_t)L * n;
   const size_t per_ct = (Ln + (size_t)k * Ln) * sizeof(uint64_t);
   const int C = chunk_for(ctx, per_ct, count);
+  const size_t tab_bytes = keys ? 2 * (size_t)count * sizeof(void*) : 0;
   std::lock_guard<std::mutex> lock(ctx->mu);
-  int st = ctx->ensure_ws(per_ct * C);
+  int st = ctx->ensure_ws(per_ct * C + tab_bytes);
   if (st) return st;
   uint64_t* X = ctx->ws;
   uint64_t* D = X + (size_t)C * Ln;
+  shg::KeyTable table;
+  if (keys &&
+      (st = upload_key_table(keys, count, 1, 0,
+                             reinterpret_cast<const uint64_t**>(D + (size_t)C * k * Ln),
+                             &table, s)))
+    return st;
   const CtxDev dv = ctx->dev();
   for (int c0 = 0; c0 < count; c0 += C) {
     const int cc = std::min(C, count - c0);
     const uint64_t* src = a.ct + (size_t)c0 * a.ncomp * Ln;
     shg::launch_intt_export(dv, X, src, a.ncomp, a.comp, a.subst_power,
                             CtMap::identity(), cc, L, s);
+    shg::KeyTable kt;
+    if (keys) kt = shg::KeyTable{table.kb + c0, table.ka + c0, 0};
     shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src,
                           (size_t)a.ncomp * Ln, CtMap::identity(), a.base1_zero,
-                          a.subst_power, cc, L, s);
+                          a.subst_power, cc, L, s, kt);
   }
   return launch_status("keyswitch");
 }
@@ -742,6 +763,85 @@ int check_key(const shg_context* ctx, const shg_key* key) {
     return fail(SHG_INVALID_ARGUMENT,
                 "`ciphertext` does not have a matching RNS moduli set.");
   return SHG_OK;
+}
+
+// keys[i * stride] for i < count must share the first key's context, limbs,
+// gadget (log_bs) and substitution power.
+int check_same_shape(const shg_context* ctx, const shg_key* const* keys, int count,
+                     int stride) {
+  if (!keys) return fail(SHG_INVALID_ARGUMENT, "null key list");
+  int st = check_key(ctx, keys[0]);
+  if (st) return st;
+  const shg_key* k0 = keys[0];
+  for (int i = 1; i < count; ++i) {
+    const shg_key* k = keys[(size_t)i * stride];
+    if ((st = check_key(ctx, k))) return st;
+    if (k->L != k0->L || k->log_bs != k0->log_bs || k->power != k0->power)
+      return fail(SHG_INVALID_ARGUMENT,
+                  "keys of one batch must share their moduli, gadget and power");
+  }
+  return SHG_OK;
+}
+
+// Device tables of kb / ka pointers for keys[i * stride + offset], i < count,
+// written into `dst` (2 * count pointers of device scratch).  The source is
+// pageable host memory, so the call is not graph-capturable.
+int upload_key_table(const shg_key* const* keys, int count, int stride, int offset,
+                     const uint64_t** dst, shg::KeyTable* out, cudaStream_t s) {
+  std::vector<const uint64_t*> h(2 * (size_t)count);
+  for (int i = 0; i < count; ++i) {
+    const shg_key* k = keys[(size_t)i * stride + offset];
+    h[i] = k->kb;
+    h[count + i] = k->ka;
+  }
+  SHG_CUDA(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(void*), cudaMemcpyHostToDevice,
+                           s));
+  *out = shg::KeyTable{dst, dst + count, 0};
+  return SHG_OK;
+}
+
+// RnsBgvCiphertext::operator* then RnsRelinKey::ApplyTo over a batch; with
+// `keys`, member i uses keys[i] (same gadget shape as `key`).
+int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* keys,
+                   uint64_t* out, const uint64_t* a, const uint64_t* b, int count,
+                   cudaStream_t s) {
+  int st;
+  const int L = key->L, n = ctx->n, k = key->k;
+  const size_t Ln = (size_t)L * n;
+  // Phase 1 over the whole batch (one launch fills the GPU): tensor product
+  // and the exported coefficients X of every degree-2 component.  Phase 2 in
+  // chunks of the digit NTTs D and the key inner product.
+  const size_t x_bytes = (size_t)count * Ln * sizeof(uint64_t);
+  const size_t d_per_ct = (size_t)k * Ln * sizeof(uint64_t);
+  // 16 ciphertexts per chunk measured fastest at n = 2^14, L = 6 (the digit
+  // kernel's grid is then ~13.8 K CTAs).
+  int C = ctx->chunk_cts > 0 ? ctx->chunk_cts
+                             : (int)std::max<size_t>(1, ((size_t)256 << 20) / d_per_ct);
+  C = std::min(C, 16);
+  C = std::max(1, std::min(C, count));
+  const size_t tab_bytes = keys ? 2 * (size_t)count * sizeof(void*) : 0;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(x_bytes + d_per_ct * C + tab_bytes))) return st;
+  uint64_t* X = ctx->ws;
+  uint64_t* D = X + (size_t)count * Ln;
+  shg::KeyTable kt;
+  if (keys &&
+      (st = upload_key_table(keys, count, 1, 0,
+                             reinterpret_cast<const uint64_t**>(D + (size_t)C * k * Ln),
+                             &kt, s)))
+    return st;
+  const CtxDev dv = ctx->dev();
+  shg::launch_tensor_intt(dv, out, X, a, b, count, L, s);
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    uint64_t* o = out + (size_t)c0 * 2 * Ln;
+    shg::KeyTable kc;
+    if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0};
+    shg::launch_keyswitch(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
+                          key->need_lift, key->chunk, key->kb, key->ka, o, o,
+                          2 * Ln, CtMap::identity(), 0, 0, cc, L, s, kc);
+  }
+  return launch_status("bgv_mul_relin");
 }
 
 }  // namespace
@@ -869,6 +969,18 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,
                    (cudaStream_t)s);
 }
 
+int shg_bgv_rotate_multikey(shg_context* ctx, const shg_key* const* keys, uint64_t* out,
+                            const uint64_t* ct, int count, shg_stream s) {
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  int st = check_same_shape(ctx, keys, count, 1);
+  if (st) return st;
+  if ((st = check_ptrs({out, ct}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  return keyswitch(ctx, keys[0], out, KsArgs{ct, 2, 1, keys[0]->power, 1}, count,
+                   (cudaStream_t)s, keys);
+}
+
 int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
                       const uint64_t* a, const uint64_t* b, int count,
                       shg_stream stream) {
@@ -880,36 +992,21 @@ int shg_bgv_mul_relin(shg_context* ctx, const shg_key* key, uint64_t* out,
   if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
   if (count == 0) return SHG_OK;
   if ((st = check_ptrs({out, a, b}))) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int L = key->L, n = ctx->n, k = key->k;
-  const size_t Ln = (size_t)L * n;
-  // Phase 1 over the whole batch (one launch fills the GPU): tensor product
-  // and the exported coefficients X of every degree-2 component.  Phase 2 in
-  // chunks small enough that the digit NTTs D stay in L2 between the digit
-  // kernel and the key inner product.
-  const size_t x_bytes = (size_t)count * Ln * sizeof(uint64_t);
-  const size_t d_per_ct = (size_t)k * Ln * sizeof(uint64_t);
-  // 16 ciphertexts per chunk measured fastest at n = 2^14, L = 6 (the digit
-  // kernel's grid is then ~13.8 K CTAs; smaller chunks that keep D in L2 lose
-  // more to the shorter grids than they gain in the inner product).
-  int C = ctx->chunk_cts > 0 ? ctx->chunk_cts
-                             : (int)std::max<size_t>(1, ((size_t)256 << 20) / d_per_ct);
-  C = std::min(C, 16);
-  C = std::max(1, std::min(C, count));
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  if ((st = ctx->ensure_ws(x_bytes + d_per_ct * C))) return st;
-  uint64_t* X = ctx->ws;
-  uint64_t* D = X + (size_t)count * Ln;
-  const CtxDev dv = ctx->dev();
-  shg::launch_tensor_intt(dv, out, X, a, b, count, L, s);
-  for (int c0 = 0; c0 < count; c0 += C) {
-    const int cc = std::min(C, count - c0);
-    uint64_t* o = out + (size_t)c0 * 2 * Ln;
-    shg::launch_keyswitch(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
-                          key->need_lift, key->chunk, key->kb, key->ka, o, o,
-                          2 * Ln, CtMap::identity(), 0, 0, cc, L, s);
-  }
-  return launch_status("bgv_mul_relin");
+  return mul_relin_impl(ctx, key, nullptr, out, a, b, count, (cudaStream_t)stream);
+}
+
+int shg_bgv_mul_relin_multikey(shg_context* ctx, const shg_key* const* keys,
+                               uint64_t* out, const uint64_t* a, const uint64_t* b,
+                               int count, shg_stream stream) {
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  int st = check_same_shape(ctx, keys, count, 1);
+  if (st) return st;
+  if (keys[0]->power != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Relinearization key can only apply to a ciphertext of power 1.");
+  if ((st = check_ptrs({out, a, b}))) return st;
+  return mul_relin_impl(ctx, keys[0], keys, out, a, b, count, (cudaStream_t)stream);
 }
 
 }  // extern "C"
@@ -966,8 +1063,11 @@ ExpandPlan plan_expand(const shg_context* ctx, const shg_key* const* keys, int l
 // substitutes every member by n/2^j + 1, key-switches it and combines
 // (c + ks, (c - ks) * -x^{n - 2^j}) into slots p and p + 2^j.  `ws` is the
 // plan's scratch, the monomials first.
+// `tables` (optional): per level j, device tables of the count queries' key
+// pointers (query q uses entry q): every query brings its own keys.
 int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_t* out,
-               int count, const ExpandPlan& plan, uint64_t* ws, cudaStream_t s) {
+               int count, const ExpandPlan& plan, uint64_t* ws, cudaStream_t s,
+               const shg::KeyTable* tables = nullptr) {
   if (levels == 0 || count == 0) return SHG_OK;
   const int n = ctx->n;
   const int C = plan.C;
@@ -993,9 +1093,11 @@ int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_
       const int mc = qc << j;
       uint64_t* blk = out + (size_t)q0 * per_query;
       shg::launch_intt_export(dv, X, blk, 2, 1, power, map, mc, 1, s);
+      shg::KeyTable kt;
+      if (tables) kt = shg::KeyTable{tables[j].kb + q0, tables[j].ka + q0, j};
       shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->need_lift,
                             key->chunk, key->kb, key->ka, KS, blk, 2 * (size_t)n,
-                            map, 1, power, mc, 1, s);
+                            map, 1, power, mc, 1, s, kt);
       shg::launch_expand_combine(dv, blk, KS, mono + (size_t)j * n, map, 1 << j,
                                  mc, s);
     }
@@ -1006,6 +1108,62 @@ int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_
 int absorb_chunk(const shg_context* ctx) {
   const uint64_t q = ctx->hp[0].q;
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(1u << 20, (~(uint64_t)0) / q));
+}
+
+// PIR server step over `count` queries; per_query_keys: keys is
+// [count][levels] (query q's level-j key at keys[q * levels + j]), else one
+// key list [levels] for every query.
+int pir_impl(shg_context* ctx, const shg_key* const* keys, bool per_query_keys, int levels,
+             const uint64_t* db, int num_items, uint64_t* out, const uint64_t* ct, int count,
+             cudaStream_t s) {
+  int st = check_expand(ctx, keys, levels, count);
+  if (st) return st;
+  if (num_items < 1 || num_items > (1 << levels))
+    return fail(SHG_INVALID_ARGUMENT,
+                "Output length must be at most " + std::to_string(1 << levels));
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct, db}))) return st;
+  if (per_query_keys)
+    for (int j = 0; j < levels; ++j)
+      if ((st = check_same_shape(ctx, keys + j, count, levels))) return st;
+  const int n = ctx->n;
+  const size_t per_query_elems = ((size_t)2 * n) << levels;
+  // Queries per group: their expanded blocks (2^levels ciphertexts each) share
+  // a 1 GiB scratch region and are absorbed before the next group starts.
+  const int group = (int)std::max<size_t>(
+      1, std::min<size_t>((size_t)count, ((size_t)1 << 30) / (per_query_elems * 8)));
+  const ExpandPlan plan = plan_expand(ctx, keys, levels, group);
+  const size_t blocks_bytes = (size_t)group * per_query_elems * sizeof(uint64_t);
+  const size_t tab_bytes = per_query_keys ? 2 * (size_t)levels * count * sizeof(void*) : 0;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(plan.bytes() + blocks_bytes + tab_bytes))) return st;
+  uint64_t* blocks = ctx->ws + plan.bytes() / sizeof(uint64_t);
+  std::vector<shg::KeyTable> tables(per_query_keys ? levels : 0);
+  if (per_query_keys) {
+    const uint64_t** tab = reinterpret_cast<const uint64_t**>(
+        blocks + (size_t)group * per_query_elems);
+    for (int j = 0; j < levels; ++j)
+      if ((st = upload_key_table(keys, count, levels, j, tab + 2 * (size_t)j * count,
+                                 &tables[j], s)))
+        return st;
+  }
+  const shg_key* const* level_keys = keys;  // per-level shape (first query's keys)
+  for (int g0 = 0; g0 < count; g0 += group) {
+    const int gc = std::min(group, count - g0);
+    // Slot 0 of every block <- its query; the strided copy is one call.
+    SHG_CUDA(cudaMemcpy2DAsync(blocks, per_query_elems * sizeof(uint64_t),
+                               ct + (size_t)g0 * 2 * n, 2 * n * sizeof(uint64_t),
+                               2 * n * sizeof(uint64_t), gc, cudaMemcpyDeviceToDevice, s));
+    std::vector<shg::KeyTable> gt(tables.size());
+    for (size_t j = 0; j < tables.size(); ++j)
+      gt[j] = shg::KeyTable{tables[j].kb + g0, tables[j].ka + g0, 0};
+    if ((st = run_expand(ctx, level_keys, levels, blocks, gc, plan, ctx->ws, s,
+                         per_query_keys ? gt.data() : nullptr)))
+      return st;
+    shg::launch_absorb_sum(ctx->dev(), out + (size_t)g0 * 2 * n, blocks, db, num_items,
+                           (size_t)1 << levels, absorb_chunk(ctx), gc, s);
+  }
+  return launch_status("pir_expand_absorb");
 }
 
 }  // namespace
@@ -1038,36 +1196,15 @@ int shg_oblivious_expand(shg_context* ctx, const shg_key* const* keys,
 int shg_pir_expand_absorb(shg_context* ctx, const shg_key* const* keys, int levels,
                           const uint64_t* db, int num_items, uint64_t* out,
                           const uint64_t* ct, int count, shg_stream stream) {
-  int st = check_expand(ctx, keys, levels, count);
-  if (st) return st;
-  if (num_items < 1 || num_items > (1 << levels))
-    return fail(SHG_INVALID_ARGUMENT,
-                "Output length must be at most " + std::to_string(1 << levels));
-  if (count == 0) return SHG_OK;
-  if ((st = check_ptrs({out, ct, db}))) return st;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int n = ctx->n;
-  const size_t per_query_elems = ((size_t)2 * n) << levels;
-  // Queries per group: their expanded blocks (2^levels ciphertexts each) share
-  // a 1 GiB scratch region and are absorbed before the next group starts.
-  const int group = (int)std::max<size_t>(
-      1, std::min<size_t>((size_t)count, ((size_t)1 << 30) / (per_query_elems * 8)));
-  const ExpandPlan plan = plan_expand(ctx, keys, levels, group);
-  const size_t blocks_bytes = (size_t)group * per_query_elems * sizeof(uint64_t);
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  if ((st = ctx->ensure_ws(plan.bytes() + blocks_bytes))) return st;
-  uint64_t* blocks = ctx->ws + plan.bytes() / sizeof(uint64_t);
-  for (int g0 = 0; g0 < count; g0 += group) {
-    const int gc = std::min(group, count - g0);
-    // Slot 0 of every block <- its query; the strided copy is one call.
-    SHG_CUDA(cudaMemcpy2DAsync(blocks, per_query_elems * sizeof(uint64_t),
-                               ct + (size_t)g0 * 2 * n, 2 * n * sizeof(uint64_t),
-                               2 * n * sizeof(uint64_t), gc, cudaMemcpyDeviceToDevice, s));
-    if ((st = run_expand(ctx, keys, levels, blocks, gc, plan, ctx->ws, s))) return st;
-    shg::launch_absorb_sum(ctx->dev(), out + (size_t)g0 * 2 * n, blocks, db, num_items,
-                           (size_t)1 << levels, absorb_chunk(ctx), gc, s);
-  }
-  return launch_status("pir_expand_absorb");
+  return pir_impl(ctx, keys, false, levels, db, num_items, out, ct, count,
+                  (cudaStream_t)stream);
+}
+
+int shg_pir_expand_absorb_multikey(shg_context* ctx, const shg_key* const* keys, int levels,
+                                   const uint64_t* db, int num_items, uint64_t* out,
+                                   const uint64_t* ct, int count, shg_stream stream) {
+  return pir_impl(ctx, keys, true, levels, db, num_items, out, ct, count,
+                  (cudaStream_t)stream);
 }
 
 int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,

@@ -468,12 +468,16 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
                            const uint64_t* ka, int k, int chunk,
                            const uint64_t* base, size_t base_ct_elems,
                            CtMap map, int base1_zero, int subst_power,
-                           int p0, int log_n, int L, CtxDev c) {
+                           int p0, int log_n, int L, KeyTable kt, CtxDev c) {
   // blockIdx.y: ciphertext p0 + y; x covers its L * n slots.
   const int Ln = L << log_n;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= Ln) return;
   const size_t p = (size_t)p0 + blockIdx.y;
+  if (kt.kb) {
+    kb = kt.kb[p >> kt.shift];
+    ka = kt.ka[p >> kt.shift];
+  }
   const int l = r >> log_n;
   const int pos = r & ((1 << log_n) - 1);
   const PrimeDev* P = c.primes + l;
@@ -861,7 +865,7 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
                      const uint64_t* kb, const uint64_t* ka, int k, int chunk,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
-                     cudaStream_t s) {
+                     cudaStream_t s, const KeyTable& kt) {
   const size_t total = (size_t)count * L * c.n;
   if (total == 0) return;
   LaunchScope scope_("ks_inner", s);
@@ -873,7 +877,8 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
   for (int p0 = 0; p0 < count; p0 += 65535) {
     const dim3 grid((Ln + 255) / 256, std::min(count - p0, 65535));
     k_ks_inner<<<grid, block, 0, s>>>(out, D, kb, ka, k, chunk, base, base_ct_elems,
-                                      map, base1_zero, subst_power, p0, c.log_n, L, c);
+                                      map, base1_zero, subst_power, p0, c.log_n, L, kt,
+                                      c);
   }
 }
 
@@ -882,7 +887,7 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
                       int base1_zero, int subst_power, int count, int L,
-                      cudaStream_t s) {
+                      cudaStream_t s, const KeyTable& kt) {
   if (count <= 0) return;
   if (use_ntt4(c) && c.ks_fused && ks4_rows_per_cta(k) > 0) {
     {
@@ -891,12 +896,12 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
     }
     LaunchScope scope_("ks_rows", s);
     launch4_ks_rows(c, D, k, chunk, kb, ka, out, base, base_ct_elems, map,
-                    base1_zero, subst_power, count, L, s);
+                    base1_zero, subst_power, count, L, s, kt);
     return;
   }
   launch_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
   launch_ks_inner(c, out, D, kb, ka, k, chunk, base, base_ct_elems, map,
-                  base1_zero, subst_power, count, L, s);
+                  base1_zero, subst_power, count, L, s, kt);
 }
 
 void launch_modreduce_ntt(const CtxDev& c, uint64_t* out, uint64_t* Y,

@@ -37,6 +37,16 @@ struct DigitDesc {
   uint64_t mask;  // 2^log_b_i - 1
 };
 
+// Per-member keys of a batched key switch: member p of a launch uses the key
+// at kb[p >> shift], ka[p >> shift] (device tables of key base pointers, all
+// keys of one gadget shape).  kb == nullptr: every member uses the launch's
+// single key.
+struct KeyTable {
+  const uint64_t* const* kb = nullptr;
+  const uint64_t* const* ka = nullptr;
+  int shift = 0;
+};
+
 // Gadget base exponents per limb (RnsGadget log_bs), passed by value.
 struct GadgetBases {
   int log_b[kMaxLimbs];
@@ -130,7 +140,7 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
                      const uint64_t* kb, const uint64_t* ka, int k, int chunk,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
-                     cudaStream_t s);
+                     cudaStream_t s, const KeyTable& kt = KeyTable{});
 
 // Gadget key switch core: digit decomposition + NTT of every digit + key
 // inner product + base add (launch_digit_ntt then launch_ks_inner).
@@ -140,7 +150,7 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
                       int base1_zero, int subst_power, int count, int L,
-                      cudaStream_t s);
+                      cudaStream_t s, const KeyTable& kt = KeyTable{});
 
 // ModReduceLsb (NTT form): Y [count][n] scratch; out [count][L-1][n].
 // sc.v[4i..4i+3] = (c1, Shoup(c1), c2, Shoup(c2)) for output limb i with
@@ -229,6 +239,6 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                      const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
-                     cudaStream_t s);
+                     cudaStream_t s, const KeyTable& kt = KeyTable{});
 
 }  // namespace shg

@@ -375,7 +375,7 @@ __global__ void __maxnreg__(72)
     k4_ks_rows(const uint64_t* buf, int k, int R, int chunk, const uint64_t* kb,
                const uint64_t* ka, uint64_t* out, const uint64_t* base,
                size_t base_ct_elems, CtMap map, int base1_zero, int subst_power,
-               int L, CtxDev c) {
+               int L, KeyTable kt, CtxDev c) {
   using S = Ntt4<LOG_N>;
   using C = typename S::RC;
   extern __shared__ uint64_t smem[];
@@ -384,6 +384,10 @@ __global__ void __maxnreg__(72)
   const int pl = blockIdx.x / tiles;
   const int l = pl % L;
   const size_t p = (size_t)(pl / L);
+  if (kt.kb) {
+    kb = kt.kb[p >> kt.shift];
+    ka = kt.ka[p >> kt.shift];
+  }
   const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
   const int r = sub / k, j = sub % k;
   const int row = tile * R + r;
@@ -622,7 +626,7 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                      const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
-                     cudaStream_t s) {
+                     cudaStream_t s, const KeyTable& kt) {
   const int R = ks4_rows_per_cta(k);
 #define F(LN)                                                                   \
   {                                                                             \
@@ -633,7 +637,7 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
     set_smem4(kern, smem);                                                      \
     kern<<<count * L * ((1 << S::A) / R), threads, smem, s>>>(                  \
         D, k, R, chunk, kb, ka, out, base, base_ct_elems, map, base1_zero,      \
-        subst_power, L, c);                                                     \
+        subst_power, L, kt, c);                                                 \
   }
   SHG_DISPATCH4(c.log_n, F)
 #undef F

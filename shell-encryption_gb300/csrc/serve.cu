@@ -39,18 +39,36 @@ struct Req {
   Clock::time_point t_submit, t_admit, t_launch, t_done;
 };
 
+// Requests batch together when they share context, operation and the shape
+// of their keys (limbs, gadget, power) -- not the keys themselves: a batch of
+// different clients' requests runs through the multi-key entry points.
 struct GroupKey {
   shg_context* ctx;
   int kind;
-  const shg_key* key;
-  const shg_key* const* keys;
+  int power, levels, num_items;
   const uint64_t* db;
-  int levels, num_items;
+  std::vector<int> log_bs;
   bool operator<(const GroupKey& o) const {
-    return std::tie(ctx, kind, key, keys, db, levels, num_items) <
-           std::tie(o.ctx, o.kind, o.key, o.keys, o.db, o.levels, o.num_items);
+    return std::tie(ctx, kind, power, levels, num_items, db, log_bs) <
+           std::tie(o.ctx, o.kind, o.power, o.levels, o.num_items, o.db, o.log_bs);
   }
 };
+
+GroupKey group_of(const shg_request& r) {
+  GroupKey g{r.ctx, r.kind, 0, 0, 0, nullptr, {}};
+  const shg_key* k = r.kind == SHG_REQ_EXPAND_ABSORB ? (r.levels ? r.keys[0] : nullptr) : r.key;
+  if (k) {
+    g.power = shg_key_power(k);
+    g.log_bs.resize(shg_key_num_limbs(k));
+    shg_key_log_bs(k, g.log_bs.data(), (int)g.log_bs.size());
+  }
+  if (r.kind == SHG_REQ_EXPAND_ABSORB) {
+    g.levels = r.levels;
+    g.num_items = r.num_items;
+    g.db = r.db;
+  }
+  return g;
+}
 
 struct Batch {
   int stream = 0;
@@ -159,12 +177,7 @@ bool shg_server::admit(Clock::time_point now) {
     bytes_in_flight += q.bytes;
     stats.peak_bytes_in_flight = std::max(stats.peak_bytes_in_flight, bytes_in_flight);
     q.t_admit = now;
-    const shg_request& r = q.r;
-    GroupKey gk{r.ctx, r.kind, r.key, r.kind == SHG_REQ_EXPAND_ABSORB ? r.keys : nullptr,
-                r.kind == SHG_REQ_EXPAND_ABSORB ? r.db : nullptr,
-                r.kind == SHG_REQ_EXPAND_ABSORB ? r.levels : 0,
-                r.kind == SHG_REQ_EXPAND_ABSORB ? r.num_items : 0};
-    ready[gk].push_back(pending.front());
+    ready[group_of(q.r)].push_back(pending.front());
     pending.pop_front();
     any = true;
   }
@@ -218,16 +231,35 @@ void shg_server::launch(const GroupKey& gk, std::deque<uint64_t>& q, int stream)
       e = cudaMemcpyAsync(db + i * in_e, rq[i]->in_b, in_e * 8, cudaMemcpyHostToDevice, s);
   }
   if (e == cudaSuccess) {
+    // One key for the whole batch when every request names the same one;
+    // otherwise per-request keys through the multi-key entry points.
+    bool same = true;
+    for (int i = 1; i < m && same; ++i)
+      same = gk.kind == SHG_REQ_EXPAND_ABSORB ? rq[i]->keys == r0->keys : rq[i]->key == r0->key;
+    std::vector<const shg_key*> keys;
+    if (!same) {
+      if (gk.kind == SHG_REQ_EXPAND_ABSORB) {
+        keys.reserve((size_t)m * r0->levels);
+        for (int i = 0; i < m; ++i)
+          keys.insert(keys.end(), rq[i]->keys, rq[i]->keys + r0->levels);
+      } else {
+        for (int i = 0; i < m; ++i) keys.push_back(rq[i]->key);
+      }
+    }
     switch (gk.kind) {
       case SHG_REQ_MUL_RELIN:
-        st = shg_bgv_mul_relin(gk.ctx, gk.key, dout, da, db, m, s);
+        st = same ? shg_bgv_mul_relin(gk.ctx, r0->key, dout, da, db, m, s)
+                  : shg_bgv_mul_relin_multikey(gk.ctx, keys.data(), dout, da, db, m, s);
         break;
       case SHG_REQ_ROTATE:
-        st = shg_bgv_rotate(gk.ctx, gk.key, dout, da, m, s);
+        st = same ? shg_bgv_rotate(gk.ctx, r0->key, dout, da, m, s)
+                  : shg_bgv_rotate_multikey(gk.ctx, keys.data(), dout, da, m, s);
         break;
       default:
-        st = shg_pir_expand_absorb(gk.ctx, r0->keys, r0->levels, r0->db, r0->num_items, dout,
-                                   da, m, s);
+        st = same ? shg_pir_expand_absorb(gk.ctx, r0->keys, r0->levels, r0->db, r0->num_items,
+                                          dout, da, m, s)
+                  : shg_pir_expand_absorb_multikey(gk.ctx, keys.data(), r0->levels, r0->db,
+                                                   r0->num_items, dout, da, m, s);
         break;
     }
   }

@@ -52,6 +52,7 @@ SIGNATURES = {
     "shg_key_destroy": (None, [_vp]),
     "shg_key_dimension": (ctypes.c_int, [_vp]),
     "shg_key_num_limbs": (ctypes.c_int, [_vp]),
+    "shg_key_log_bs": (ctypes.c_int, [_vp, _ip, ctypes.c_int]),
     "shg_key_power": (ctypes.c_int, [_vp]),
     "shg_key_context": (_vp, [_vp]),
     "shg_key_device_bytes": (_sz, [_vp]),
@@ -59,6 +60,12 @@ SIGNATURES = {
     "shg_relin_apply_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_galois_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_bgv_mul_relin_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp, _vp, _vp,
+                                                  ctypes.c_int, _vp]),
+    "shg_bgv_rotate_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int,
+                                               _vp]),
+    "shg_pir_expand_absorb_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp,
+                                                      ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_rotate": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_oblivious_expand": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp, _vp,

@@ -492,3 +492,78 @@ def test_pir_expand_absorb(sg, oracle, log_n, levels, log_b, items, count):
     with pytest.raises(sg.ShgError, match="Output length must be at most"):
         sg.check(sg.lib().shg_pir_expand_absorb(ctx.h, arr, levels, dd.ptr, (1 << levels) + 1,
                                                 out.ptr, dc.ptr, count, None))
+
+
+@pytest.mark.parametrize("log_n,qs,log_bs,ks_fused", [
+    (12, Q50[:3], [20] * 3, 1), (14, Q45, [20] * 6, 1), (14, Q45, [20] * 6, 0),
+    (13, Q50[:2], [50, 16], 1)])
+def test_multikey_batches_equal_per_key_calls(sg, oracle, log_n, qs, log_bs, ks_fused):
+    """Members with their own keys (one per client) in one batch: identical to
+    one call per key, for ct-mult+relin and rotation."""
+    import ctypes
+    lib = sg.lib()
+    n, L, count = 1 << log_n, len(qs), 5
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    ctx = sg.Context(log_n, qs)
+    sg.check(lib.shg_context_set_ks_fused(ctx.h, ks_fused))
+    if log_n < 14:
+        sg.check(lib.shg_context_set_four_step_min(ctx.h, log_n))  # four-step at small n too
+    mats = [(oracle.uniform_limbs(300 + i, qs, n, k), oracle.uniform_limbs(400 + i, qs, n, k))
+            for i in range(3)]
+    relin = [sg.Key(ctx, log_bs, 1, kb, ka) for kb, ka in mats]
+    galois = [sg.Key(ctx, log_bs, 5, kb, ka) for kb, ka in mats]
+    pick = [0, 2, 1, 2, 0]
+    a, b = _ct_pair(oracle, qs, n, count, 500)
+    da, db = _dev(sg, a), _dev(sg, b)
+    want = sg.DeviceBuffer(a.nbytes)
+    got = sg.DeviceBuffer(a.nbytes)
+    ct = 2 * L * n * 8
+    for i, kidx in enumerate(pick):
+        sg.check(lib.shg_bgv_mul_relin(ctx.h, relin[kidx].h, want.ptr + i * ct, da.ptr + i * ct,
+                                       db.ptr + i * ct, 1, None))
+    arr = (ctypes.c_void_p * count)(*[relin[kidx].h for kidx in pick])
+    _run(sg, lib.shg_bgv_mul_relin_multikey, ctx.h, arr, got.ptr, da.ptr, db.ptr, count, None)
+    assert np.array_equal(got.download(a.shape), want.download(a.shape))
+    # first member against the oracle as well
+    w0 = rns.relin(rns.tensor(a[0], b[0]), mats[pick[0]][0], mats[pick[0]][1], log_bs)
+    assert np.array_equal(got.download(a.shape)[0], w0)
+    for i, kidx in enumerate(pick):
+        sg.check(lib.shg_bgv_rotate(ctx.h, galois[kidx].h, want.ptr + i * ct, da.ptr + i * ct,
+                                    1, None))
+    arr = (ctypes.c_void_p * count)(*[galois[kidx].h for kidx in pick])
+    _run(sg, lib.shg_bgv_rotate_multikey, ctx.h, arr, got.ptr, da.ptr, count, None)
+    assert np.array_equal(got.download(a.shape), want.download(a.shape))
+    # keys of different powers cannot share a batch
+    bad = (ctypes.c_void_p * 2)(relin[0].h, galois[1].h)
+    with pytest.raises(sg.ShgError, match="share"):
+        sg.check(lib.shg_bgv_rotate_multikey(ctx.h, bad, got.ptr, da.ptr, 2, None))
+
+
+def test_pir_multikey_equals_per_query_calls(sg, oracle):
+    import ctypes
+    lib = sg.lib()
+    q, log_n, levels, log_b, items, count = Q60, 9, 5, 8, 20, 4
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    dim = p.gadget_size(log_b)
+    ctx = sg.Context(log_n, [q])
+    clients = []
+    for c in range(3):
+        keys = oracle.uniform_limbs(600 + c, [q], n, levels * 2 * dim).reshape(levels, 2, dim, n)
+        clients.append((keys, [sg.Key(ctx, [log_b], (n >> j) + 1, keys[j, 0], keys[j, 1])
+                               for j in range(levels)]))
+    pick = [1, 0, 2, 1]
+    cts = oracle.uniform_limbs(700, [q], n, 2 * count).reshape(count, 2, n)
+    db = oracle.uniform_limbs(701, [q], n, items).reshape(items, n)
+    dc, dd = _dev(sg, cts), _dev(sg, db)
+    flat = [clients[c][1][j].h for c in pick for j in range(levels)]
+    arr = (ctypes.c_void_p * len(flat))(*flat)
+    out = sg.DeviceBuffer(count * 2 * n * 8)
+    _run(sg, lib.shg_pir_expand_absorb_multikey, ctx.h, arr, levels, dd.ptr, items, out.ptr,
+         dc.ptr, count, None)
+    got = out.download((count, 2, n))
+    for i, c in enumerate(pick):
+        keys = clients[c][0]
+        want = p.absorb_sum(p.oblivious_expand(levels, log_b, keys, cts[i])[:items], db)
+        assert np.array_equal(got[i], want)
