@@ -61,9 +61,9 @@ int shg_context_reserve(shg_context* ctx, size_t bytes);
  * (0 = default). */
 int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
 /* Transforms of n >= 2^log_n use the two-kernel four-step NTT, log_n in
- * [12, 16] (14 = default; 12 or 13 also move n = 2^12 / 2^13 off the
- * one-CTA-per-limb kernels; 15 keeps n = 2^14 on them; n = 2^15 always uses
- * the four-step kernels). */
+ * [12, 16] (13 = default; 12 also moves n = 2^12 off the one-CTA-per-limb
+ * kernels; 14 or more keeps smaller n on them; n = 2^15 always uses the
+ * four-step kernels). */
 int shg_context_set_four_step_min(shg_context* ctx, int log_n);
 /* 1 (default): four-step key switches run the digit row phase and the key
  * inner product as one kernel; 0: separate row phase, digit NTTs written to

@@ -66,7 +66,7 @@ struct Group {
 };
 
 struct Tuning {
-  int chunk = 0, four_step_min = 14, ks_fused = 1;
+  int chunk = 0, four_step_min = 13, ks_fused = 1;
   double ms = 0;
 };
 using TuneKey = std::tuple<int, int, int, int, int>;  // log_n, L, dim, kind, bucket
