@@ -240,6 +240,26 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,
                    const uint64_t* ct, int count, shg_stream stream);
 
 /* ---------------------------------------------------------------------------
+ * Single-modulus symmetric RLWE, on a one-prime context (t = the context's
+ * plaintext modulus)
+ * ------------------------------------------------------------------------- */
+
+/* Encrypt (symmetric_encryption.h:1006-1021) with the randomness injected as
+ * in internal::Encrypt (symmetric_encryption.h:940-963): key s [n] (NTT
+ * form), a [count][n] (uniform, NTT form), e [count][n] (error samples,
+ * coefficient form), m [count][n] (plaintexts, NTT form), all Montgomery ->
+ * out [count][2][n] = (NTT(e) * t + m + a * s, -a).  Sampling stays with the
+ * caller. */
+int shg_symmetric_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* s,
+                          const uint64_t* a, const uint64_t* e, const uint64_t* m,
+                          int count, shg_stream stream);
+/* Decrypt (symmetric_encryption.h:1138-1152: ExtractErrorAndMessage then
+ * RemoveError): ct [count][len][n] (NTT form) -> out [count][n] plaintext
+ * integers in [0, t). */
+int shg_symmetric_decrypt(shg_context* ctx, uint64_t* out, const uint64_t* s,
+                          const uint64_t* ct, int len, int count, shg_stream stream);
+
+/* ---------------------------------------------------------------------------
  * Single-modulus oblivious expansion (PIR), on a one-prime context
  * ------------------------------------------------------------------------- */
 

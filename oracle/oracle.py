@@ -72,6 +72,8 @@ def lib():
             "so_oblivious_expand": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, U64P,
                                                    U64P, U64P]),
             "so_absorb_sum": (None, [vp, ctypes.c_int, U64P, U64P, U64P]),
+            "so_sym_encrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, U64P, U64P, U64P]),
+            "so_sym_decrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, ctypes.c_int, U64P]),
             "so_compute_normalizer": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int]),
         }
         for name, (res, args) in sig.items():
@@ -220,6 +222,21 @@ class Prime:
         st = lib().so_oblivious_expand(self._h, levels, log_b, _p(keys), _p(ct), _p(out))
         if st:
             raise ValueError("bad levels")
+        return out
+
+    def sym_encrypt(self, t, s, a, e, m):
+        """(c0, c1) = (NTT(e) * t + m + a * s, -a); s, a, m NTT form, e coefficients."""
+        arrs = [np.ascontiguousarray(x, dtype=np.uint64) for x in (s, a, e, m)]
+        out = np.empty((2, self.n), np.uint64)
+        lib().so_sym_encrypt(self._h, ctypes.c_uint64(int(t)), *[_p(x) for x in arrs], _p(out))
+        return out
+
+    def sym_decrypt(self, t, s, ct):
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        s = np.ascontiguousarray(s, dtype=np.uint64)
+        out = np.empty(self.n, np.uint64)
+        lib().so_sym_decrypt(self._h, ctypes.c_uint64(int(t)), _p(s), _p(ct), ct.shape[0],
+                             _p(out))
         return out
 
     def absorb_sum(self, cts, db):

@@ -759,6 +759,53 @@ void so_absorb_sum(const so_prime* p, int count, const uint64_t* cts,
   }
 }
 
+/* internal::Encrypt with the randomness injected (symmetric_encryption.h:
+ * 940-963) and c1 = -a (symmetric_encryption.h:1006-1021):
+ * c0 = NTT(e) * t + m + a * s, c1 = -a.  s, a, m in NTT form, e in
+ * coefficient form, all Montgomery; t = the plaintext modulus (an integer,
+ * imported like SymmetricRlweKey's t_mod).  out [2][n]. */
+void so_sym_encrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* a,
+                    const uint64_t* e, const uint64_t* m, uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  uint64_t* c0 = out;
+  memcpy(c0, e, n * sizeof(uint64_t));
+  so_ntt_fwd(p, c0);
+  const uint64_t t_mont = mont_import(p, t % p->q);
+  for (size_t i = 0; i < n; i++) c0[i] = mont_mul(p, c0[i], t_mont);
+  so_add(p, c0, m, c0, n);
+  so_fma(p, c0, a, s, n);
+  so_neg(p, a, out + n, n);
+}
+
+/* Decrypt (symmetric_encryption.h:1138-1152): ExtractErrorAndMessage
+ * (sum_i c_i * s^i in NTT form, inverse NTT; :966-1000) then RemoveError
+ * (ExportInt, values above floor(q/2) minus q mod t, then mod t; :1084-1110).
+ * ct [len][n] NTT form; out [n] integers in [0, t). */
+void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* ct,
+                    int len, uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  uint64_t* acc = (uint64_t*)calloc(n, sizeof(uint64_t));
+  uint64_t* pw = (uint64_t*)malloc(n * sizeof(uint64_t));
+  uint64_t* ci = (uint64_t*)malloc(n * sizeof(uint64_t));
+  memcpy(pw, s, n * sizeof(uint64_t));
+  for (int i = 0; i < len; i++) {
+    memcpy(ci, ct + (size_t)i * n, n * sizeof(uint64_t));
+    if (i > 1) so_mul(p, pw, s, pw, n);
+    if (i > 0) so_mul(p, ci, pw, ci, n);
+    so_add(p, acc, ci, acc, n);
+  }
+  so_ntt_inv(p, acc);
+  const uint64_t q = p->q, q_mod_t = q % t;
+  for (size_t i = 0; i < n; i++) {
+    uint64_t x = mont_export(p, acc[i]);
+    if (x > (q >> 1)) x -= q_mod_t;
+    out[i] = x % t;
+  }
+  free(acc);
+  free(pw);
+  free(ci);
+}
+
 /* ObliviousExpander::ComputeNormalizer (oblivious_expand.h:143-157). */
 uint64_t so_compute_normalizer(int k, int log_t) {
   int log_t_minus_r = log_t - (k % log_t);

@@ -128,6 +128,13 @@ int so_oblivious_expand(const so_prime* p, int levels, int log_b,
 /* out[2][n] = sum_i cts[i] * db[i] (FusedAbsorbAddInPlace chain). */
 void so_absorb_sum(const so_prime* p, int count, const uint64_t* cts,
                    const uint64_t* db, uint64_t* out);
+/* Symmetric RLWE encryption with injected randomness a (uniform, NTT form)
+ * and e (error, coefficient form): out [2][n] = (NTT(e)*t + m + a*s, -a). */
+void so_sym_encrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* a,
+                    const uint64_t* e, const uint64_t* m, uint64_t* out);
+/* Decrypt a ciphertext of `len` components [len][n]: out [n] in [0, t). */
+void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* ct,
+                    int len, uint64_t* out);
 /* ObliviousExpander::ComputeNormalizer */
 uint64_t so_compute_normalizer(int k, int log_t);
 

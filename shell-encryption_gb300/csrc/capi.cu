@@ -1208,6 +1208,53 @@ int shg_pir_expand_absorb_multikey(shg_context* ctx, const shg_key* const* keys,
                   (cudaStream_t)stream);
 }
 
+int shg_symmetric_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* s_ntt,
+                          const uint64_t* a, const uint64_t* e, const uint64_t* m, int count,
+                          shg_stream stream) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (ctx->L != 1)
+    return fail(SHG_INVALID_ARGUMENT, "symmetric encryption needs a one-prime context");
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  int st = check_ptrs({out, s_ntt, a, e, m});
+  if (st) return st;
+  const HostPrime& h = ctx->hp[0];
+  if (ctx->t == 0 || ctx->t >= h.q)
+    return fail(SHG_INVALID_ARGUMENT, "the plaintext modulus must lie in [1, q)");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t elems = (size_t)count * ctx->n;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(elems * sizeof(uint64_t)))) return st;
+  // c0 = e, in NTT form (Polynomial::ConvertToNtt of the error samples).
+  SHG_CUDA(cudaMemcpyAsync(ctx->ws, e, elems * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  shg::launch_ntt_fwd(ctx->dev(), ctx->ws, ctx->ws, count, 1, s);
+  shg::launch_sym_encrypt(ctx->dev(), out, ctx->ws, a, m, s_ntt, to_mont(ctx->t, h.q), count,
+                          s);
+  return launch_status("symmetric_encrypt");
+}
+
+int shg_symmetric_decrypt(shg_context* ctx, uint64_t* out, const uint64_t* s_ntt,
+                          const uint64_t* ct, int len, int count, shg_stream stream) {
+  if (!ctx) return fail(SHG_INVALID_ARGUMENT, "null context");
+  if (ctx->L != 1)
+    return fail(SHG_INVALID_ARGUMENT, "symmetric encryption needs a one-prime context");
+  if (ctx->t == 0) return fail(SHG_INVALID_ARGUMENT, "t is zero");
+  if (count < 0 || len < 1)
+    return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative and `len` positive.");
+  if (count == 0) return SHG_OK;
+  int st = check_ptrs({out, s_ntt, ct});
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t elems = (size_t)count * ctx->n;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(elems * sizeof(uint64_t)))) return st;
+  shg::launch_sym_dot(ctx->dev(), ctx->ws, ct, s_ntt, len, count, s);
+  // InverseNtt + ExportInt in one scaled inverse transform, then RemoveError.
+  shg::launch_ntt_inv(ctx->dev(), ctx->ws, ctx->ws, count, 1, 1, s);
+  shg::launch_remove_error(ctx->dev(), out, ctx->ws, ctx->hp[0].q, ctx->t, count, s);
+  return launch_status("symmetric_decrypt");
+}
+
 int shg_absorb_sum(shg_context* ctx, uint64_t* out, const uint64_t* cts,
                    const uint64_t* db, int num_items, int count,
                    shg_stream stream) {

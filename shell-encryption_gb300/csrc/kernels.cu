@@ -611,6 +611,59 @@ __global__ void k_monomials(uint64_t* mono, int levels, int log_n,
   }
 }
 
+// Symmetric RLWE encryption combine (symmetric_encryption.h:940-963,
+// 1006-1021) on limb 0: out [count][2][n] = (e_ntt * t + m + a * s, -a).
+__global__ void k_sym_encrypt(uint64_t* out, const uint64_t* e_ntt, const uint64_t* a,
+                              const uint64_t* m, const uint64_t* sk, uint64_t t_mont,
+                              size_t total /* count*n */, int log_n, CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const uint64_t q = c.primes[0].q, qinv = c.primes[0].inv_modulus;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e >> log_n, i = e & (n - 1);
+    uint64_t c0 = mont_mul(e_ntt[e], t_mont, q, qinv);
+    c0 = add_mod(c0, m[e], q);
+    c0 = add_mod(c0, mont_mul(a[e], sk[i], q, qinv), q);
+    out[p * 2 * n + i] = c0;
+    out[p * 2 * n + n + i] = neg_mod(a[e], q);
+  }
+}
+
+// ExtractErrorAndMessage's dot product (symmetric_encryption.h:966-1000) on
+// limb 0: acc [count][n] = sum_i ct[count][i] * s^i, NTT form.
+__global__ void k_sym_dot(uint64_t* acc, const uint64_t* ct, const uint64_t* sk, int len,
+                          size_t total /* count*n */, int log_n, CtxDev c) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const uint64_t q = c.primes[0].q, qinv = c.primes[0].inv_modulus;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e >> log_n, i = e & (n - 1);
+    const uint64_t* cp = ct + p * (size_t)len * n + i;
+    const uint64_t s = sk[i];
+    uint64_t sum = cp[0], pw = s;
+    for (int j = 1; j < len; ++j) {
+      sum = add_mod(sum, mont_mul(cp[(size_t)j * n], pw, q, qinv), q);
+      if (j + 1 < len) pw = mont_mul(pw, s, q, qinv);
+    }
+    acc[e] = sum;
+  }
+}
+
+// RemoveError (symmetric_encryption.h:1084-1110) on exported coefficients:
+// values above floor(q/2) stand for value - q; the message is that mod t.
+__global__ void k_remove_error(uint64_t* out, const uint64_t* x, size_t total, uint64_t q,
+                               uint64_t t, uint64_t q_mod_t) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    uint64_t v = x[e];
+    if (v > (q >> 1)) v -= q_mod_t;
+    out[e] = v % t;
+  }
+}
+
 // Seeded uniform residues: element e of [count][L][n] is splitmix64 output
 // e + 1 of state `seed`, reduced mod its limb's prime.
 __global__ void k_fill_uniform(uint64_t* out, uint64_t seed, size_t total,
@@ -961,6 +1014,32 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
   LaunchScope scope_("expand_combine", s);
   k_expand_combine<<<grid_for(total, 256), 256, 0, s>>>(base, ks, mono, map,
                                                         half, total, c.log_n, c);
+}
+
+void launch_sym_encrypt(const CtxDev& c, uint64_t* out, const uint64_t* e_ntt,
+                        const uint64_t* a, const uint64_t* m, const uint64_t* sk,
+                        uint64_t t_mont, int count, cudaStream_t s) {
+  const size_t total = (size_t)count * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("sym_encrypt", s);
+  k_sym_encrypt<<<grid_for(total, 256), 256, 0, s>>>(out, e_ntt, a, m, sk, t_mont, total,
+                                                     c.log_n, c);
+}
+
+void launch_sym_dot(const CtxDev& c, uint64_t* acc, const uint64_t* ct, const uint64_t* sk,
+                    int len, int count, cudaStream_t s) {
+  const size_t total = (size_t)count * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("sym_dot", s);
+  k_sym_dot<<<grid_for(total, 256), 256, 0, s>>>(acc, ct, sk, len, total, c.log_n, c);
+}
+
+void launch_remove_error(const CtxDev& c, uint64_t* out, const uint64_t* x, uint64_t q,
+                         uint64_t t, int count, cudaStream_t s) {
+  const size_t total = (size_t)count * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("remove_error", s);
+  k_remove_error<<<grid_for(total, 256), 256, 0, s>>>(out, x, total, q, t, q % t);
 }
 
 void launch_fill_uniform(const CtxDev& c, uint64_t* out, uint64_t seed, int count,

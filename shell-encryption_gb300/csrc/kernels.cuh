@@ -176,6 +176,17 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            const uint64_t* mono, CtMap map, int half,
                            int count, cudaStream_t s);
 
+// Symmetric RLWE on limb 0: encryption combine out [count][2][n] =
+// (e_ntt * t + m + a * s, -a); decryption dot product acc [count][n] =
+// sum_i ct[count][i] * s^i; RemoveError of exported coefficients.
+void launch_sym_encrypt(const CtxDev& c, uint64_t* out, const uint64_t* e_ntt,
+                        const uint64_t* a, const uint64_t* m, const uint64_t* sk,
+                        uint64_t t_mont, int count, cudaStream_t s);
+void launch_sym_dot(const CtxDev& c, uint64_t* acc, const uint64_t* ct, const uint64_t* sk,
+                    int len, int count, cudaStream_t s);
+void launch_remove_error(const CtxDev& c, uint64_t* out, const uint64_t* x, uint64_t q,
+                         uint64_t t, int count, cudaStream_t s);
+
 // Seeded uniform residues [count][L][n] (splitmix64, reduced per limb).
 void launch_fill_uniform(const CtxDev& c, uint64_t* out, uint64_t seed, int count,
                          int L, cudaStream_t s);

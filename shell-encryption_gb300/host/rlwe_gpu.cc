@@ -740,6 +740,46 @@ StatusOr<SymmetricRlweCiphertext> SymmetricRlweCiphertext::Substitute(
   return SymmetricRlweCiphertext(std::move(r), modulus_);
 }
 
+StatusOr<SymmetricRlweKey> SymmetricRlweKey::Create(Polynomial key,
+                                                    const PrimeModulus* modulus) {
+  if (!modulus) return InvalidArgumentError("`modulus` must not be null.");
+  if (modulus->Context()->NumMainPrimeModuli() != 1)
+    return InvalidArgumentError("symmetric encryption needs a one-prime context");
+  if (key.NumModuli() != 1 || key.LogN() != modulus->Context()->LogN() || !key.IsNttForm())
+    return InvalidArgumentError("the key must be one NTT-form polynomial of the ring");
+  return SymmetricRlweKey(std::move(key), modulus);
+}
+
+StatusOr<SymmetricRlweCiphertext> SymmetricRlweKey::Encrypt(const Polynomial& plaintext,
+                                                            const Polynomial& a,
+                                                            const Polynomial& e) const {
+  for (const Polynomial* q : {&plaintext, &a, &e})
+    if (q->NumModuli() != 1 || q->LogN() != key_.LogN())
+      return InvalidArgumentError("operands must be polynomials of the key's ring");
+  if (!plaintext.IsNttForm() || !a.IsNttForm() || e.IsNttForm())
+    return InvalidArgumentError(
+        "`plaintext` and `a` must be in NTT form, `e` in coefficient form");
+  DeviceArray out((size_t)2 << key_.LogN());
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_symmetric_encrypt(
+      modulus_->Context()->handle(), out.data(), key_.device_data(), a.device_data(),
+      e.device_data(), plaintext.device_data(), 1, g_stream)));
+  return SymmetricRlweCiphertext::FromDevice(std::move(out), 2, key_.LogN(), modulus_, 1, 0.0);
+}
+
+StatusOr<std::vector<uint64_t>> SymmetricRlweKey::Decrypt(
+    const SymmetricRlweCiphertext& ciphertext) const {
+  const RnsBgvCiphertext& ct = ciphertext.rns();
+  if (ct.LogN() != key_.LogN() || ct.NumModuli() != 1)
+    return InvalidArgumentError("ciphertext of another ring");
+  DeviceArray out((size_t)1 << key_.LogN());
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_symmetric_decrypt(
+      modulus_->Context()->handle(), out.data(), key_.device_data(), ct.device_data(),
+      ct.Len(), 1, g_stream)));
+  std::vector<uint64_t> m((size_t)1 << key_.LogN());
+  RLWE_GPU_RETURN_IF_ERROR(out.Download(m.data(), m.size()));
+  return m;
+}
+
 StatusOr<GaloisKey> GaloisKey::CreateFromKeyComponents(const std::vector<Polynomial>& key_0,
                                                        const std::vector<Polynomial>& key_1,
                                                        int substitution_power, int log_b,

@@ -410,6 +410,28 @@ class SymmetricRlweCiphertext {
   const PrimeModulus* modulus_;
 };
 
+// rlwe::SymmetricRlweKey over a one-prime context: the key polynomial s (NTT
+// form) and the context's plaintext modulus t (SymmetricRlweKey::Sample's
+// t = 2^log_t + 1 when the context was created with it).
+class SymmetricRlweKey {
+ public:
+  static StatusOr<SymmetricRlweKey> Create(Polynomial key, const PrimeModulus* modulus);
+  // rlwe::Encrypt with the randomness injected as in internal::Encrypt
+  // (symmetric_encryption.h:940-963, 1006-1021): `a` uniform (NTT form), `e`
+  // error samples (coefficient form), `plaintext` in NTT form.
+  StatusOr<SymmetricRlweCiphertext> Encrypt(const Polynomial& plaintext, const Polynomial& a,
+                                            const Polynomial& e) const;
+  // rlwe::Decrypt (symmetric_encryption.h:1138-1152): message coefficients
+  // in [0, t).
+  StatusOr<std::vector<uint64_t>> Decrypt(const SymmetricRlweCiphertext& ciphertext) const;
+  const Polynomial& Key() const { return key_; }
+
+ private:
+  SymmetricRlweKey(Polynomial key, const PrimeModulus* m) : key_(std::move(key)), modulus_(m) {}
+  Polynomial key_;
+  const PrimeModulus* modulus_;
+};
+
 // rlwe::GaloisKey: a single-modulus key-switching key for X -> X^power with
 // gadget base 2^log_b; key_0[i], key_1[i] are the rows of the key part
 // (relinearization_key.cc:99-141) in NTT form.

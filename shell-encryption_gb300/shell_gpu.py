@@ -72,6 +72,9 @@ SIGNATURES = {
                                             ctypes.c_int, _vp]),
     "shg_pir_expand_absorb": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp,
                                              ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_symmetric_encrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_symmetric_decrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                             _vp]),
     "shg_absorb_sum": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     # runtime plumbing (include/shell_gpu_runtime.h)
     "shg_device_count": (ctypes.c_int, [_ip]),

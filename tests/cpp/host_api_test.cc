@@ -364,9 +364,71 @@ void TestSingleModulus(int log_n, int levels, int log_b) {
   so_prime_destroy(p);
 }
 
+// The single-modulus flow (symmetric_encryption_test.cc): encrypt with
+// injected randomness, decrypt, ct + ct and ct * ct against the oracle.
+void TestSymmetric() {
+  const int log_n = 11, n = 1 << log_n;
+  const uint64_t q = 576460752303415297ull, t = 65537;
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, {q}, {}, t));
+  const PrimeModulus* m = ctx->MainPrimeModuli()[0];
+  so_prime* p = so_prime_create(q, log_n);
+  uint64_t st = 99;
+  auto small = [&](int var) {  // centred binomial samples, imported
+    std::vector<uint64_t> v(n);
+    for (int i = 0; i < n; ++i) {
+      int acc = 0;
+      for (int b = 0; b < 2 * var; ++b) acc += (SplitMix(st) & 1) ? 1 : 0;
+      const int64_t x = acc - var;
+      v[i] = x < 0 ? q - (uint64_t)(-x) : (uint64_t)x;
+    }
+    so_import(p, v.data(), v.data(), n);
+    return v;
+  };
+  std::vector<uint64_t> s = small(8);
+  so_ntt_fwd(p, s.data());
+  SymmetricRlweKey key = *SymmetricRlweKey::Create(*RnsPolynomial::Create({s}, true), m);
+  std::vector<std::vector<uint64_t>> msgs(2, std::vector<uint64_t>(n));
+  std::vector<SymmetricRlweCiphertext> cts;
+  std::vector<std::vector<uint64_t>> want_cts;
+  for (int c = 0; c < 2; ++c) {
+    for (int i = 0; i < n; ++i) msgs[c][i] = SplitMix(st) % t;
+    std::vector<uint64_t> mm = msgs[c];
+    so_import(p, mm.data(), mm.data(), n);
+    so_ntt_fwd(p, mm.data());
+    std::vector<uint64_t> a = Uniform(4000 + c, {q}, n, 1), e = small(8);
+    std::vector<uint64_t> w(2 * n);
+    so_sym_encrypt(p, t, s.data(), a.data(), e.data(), mm.data(), w.data());
+    want_cts.push_back(w);
+    auto ct = key.Encrypt(*RnsPolynomial::Create({mm}, true), *RnsPolynomial::Create({a}, true),
+                          *RnsPolynomial::Create({e}, false));
+    EXPECT(ct.ok() && FlatCt(ct->rns()) == w, "SymmetricRlweKey::Encrypt");
+    if (!ct.ok()) return;
+    cts.push_back(*ct);
+  }
+  std::vector<uint64_t> dec;
+  ASSERT_OK_AND_ASSIGN(dec, key.Decrypt(cts[0]));
+  EXPECT(dec == msgs[0], "Decrypt(Encrypt(m)) == m");
+  SymmetricRlweCiphertext sum = cts[0];
+  ASSERT_OK_AND_ASSIGN(sum, cts[0] + cts[1]);
+  ASSERT_OK_AND_ASSIGN(dec, key.Decrypt(sum));
+  bool ok = true;
+  for (int i = 0; i < n; ++i) ok &= dec[i] == (msgs[0][i] + msgs[1][i]) % t;
+  EXPECT(ok, "Decrypt(ct1 + ct2) == m1 + m2");
+  SymmetricRlweCiphertext prod = cts[0];
+  ASSERT_OK_AND_ASSIGN(prod, cts[0] * cts[1]);
+  ASSERT_OK_AND_ASSIGN(dec, key.Decrypt(prod));
+  std::vector<uint64_t> want(n);
+  auto fp = FlatCt(prod.rns());
+  so_sym_decrypt(p, t, s.data(), fp.data(), 3, want.data());
+  EXPECT(prod.Len() == 3 && dec == want, "Decrypt(ct1 * ct2) equals the oracle");
+  so_prime_destroy(p);
+}
+
 }  // namespace
 
 int main() {
+  TestSymmetric();
   TestContextErrors();
   TestPolynomial(4, {kQ45[0], kQ45[1]});
   TestPolynomial(11, kQ50);

@@ -567,3 +567,72 @@ def test_pir_multikey_equals_per_query_calls(sg, oracle):
         keys = clients[c][0]
         want = p.absorb_sum(p.oblivious_expand(levels, log_b, keys, cts[i])[:items], db)
         assert np.array_equal(got[i], want)
+
+
+def _cbd(rng, n, variance=8):
+    """Centred binomial samples of the given variance (sample_error.h:43-100's
+    distribution; drawn here with numpy, the device path never samples)."""
+    k = 2 * variance
+    bits = rng.integers(0, 2, size=(n, 2 * k))
+    return bits[:, :k].sum(1) - bits[:, k:].sum(1)
+
+
+def test_symmetric_rlwe_flow(sg, oracle):
+    """The single-modulus flow: encrypt 64 messages, NTT round trip, ct + ct,
+    ct * ct, decrypt -- bit-exact with the oracle and decrypting to m1 + m2 and
+    the negacyclic product m1 * m2 mod t."""
+    lib = sg.lib()
+    q, log_n, t, count = Q59, 12, 65537, 64
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    rng = np.random.default_rng(2024)
+
+    def mont(v):
+        return p.import_(np.array([int(x) % q for x in v], dtype=np.uint64))
+
+    s = p.ntt_fwd(mont(_cbd(rng, n)))
+    msgs = rng.integers(0, t, size=(count, n))
+    m = np.stack([p.ntt_fwd(mont(msgs[i])) for i in range(count)])
+    a = oracle.uniform_limbs(31, [q], n, count).reshape(count, n)
+    e = np.stack([mont(_cbd(rng, n)) for _ in range(count)])
+    want = np.stack([p.sym_encrypt(t, s, a[i], e[i], m[i]) for i in range(count)])
+    ctx = sg.Context(log_n, [q], t)
+    ds, da, de, dm = (_dev(sg, x) for x in (s, a, e, m))
+    ct = sg.DeviceBuffer(want.nbytes)
+    _run(sg, lib.shg_symmetric_encrypt, ctx.h, ct.ptr, ds.ptr, da.ptr, de.ptr, dm.ptr, count,
+         None)
+    assert np.array_equal(ct.download(want.shape), want)
+    # NTT round trip of every component
+    _run(sg, lib.shg_ntt_inverse, ctx.h, ct.ptr, 2 * count, 1, None)
+    _run(sg, lib.shg_ntt_forward, ctx.h, ct.ptr, 2 * count, 1, None)
+    assert np.array_equal(ct.download(want.shape), want)
+    half = count // 2
+    cts = ct.download(want.shape)
+    lo, hi = _dev(sg, cts[:half]), _dev(sg, cts[half:])
+    # ct + ct
+    summ = sg.DeviceBuffer(half * 2 * n * 8)
+    _run(sg, lib.shg_poly_add, ctx.h, summ.ptr, lo.ptr, hi.ptr, 2 * half, 1, None)
+    # ct * ct (3 components)
+    prod = sg.DeviceBuffer(half * 3 * n * 8)
+    _run(sg, lib.shg_ct_tensor, ctx.h, prod.ptr, lo.ptr, hi.ptr, half, 1, None)
+    # decrypt everything
+    dec = sg.DeviceBuffer(count * n * 8)
+    _run(sg, lib.shg_symmetric_decrypt, ctx.h, dec.ptr, ds.ptr, ct.ptr, 2, count, None)
+    got = dec.download((count, n))
+    assert np.array_equal(got, np.stack([p.sym_decrypt(t, s, want[i]) for i in range(count)]))
+    assert np.array_equal(got.astype(np.int64), msgs)
+    _run(sg, lib.shg_symmetric_decrypt, ctx.h, dec.ptr, ds.ptr, summ.ptr, 2, half, None)
+    got = dec.download((half, n)).astype(np.int64)
+    assert np.array_equal(got, (msgs[:half] + msgs[half:]) % t)
+    _run(sg, lib.shg_symmetric_decrypt, ctx.h, dec.ptr, ds.ptr, prod.ptr, 3, half, None)
+    got = dec.download((half, n))
+    prods = prod.download((half, 3, n))
+    for i in (0, 1, half - 1):
+        assert np.array_equal(got[i], p.sym_decrypt(t, s, prods[i]))
+        full = np.convolve(msgs[i], msgs[half + i])  # length 2n - 1
+        neg = full[:n].copy()
+        neg[: n - 1] -= full[n:]
+        assert np.array_equal(got[i].astype(np.int64), neg % t)
+    with pytest.raises(sg.ShgError, match="one-prime"):
+        ctx2 = sg.Context(log_n, Q50[:2], t)
+        sg.check(lib.shg_symmetric_decrypt(ctx2.h, dec.ptr, ds.ptr, ct.ptr, 2, 1, None))

@@ -219,3 +219,28 @@ def test_oblivious_expand_selects_index(oracle):
         dec = [((int(x) - q) if int(x) > q // 2 else int(x)) % t for x in v]
         assert dec[0] == (1 if i == idx else 0)
         assert all(d == 0 for d in dec[1:])
+
+
+def test_symmetric_encrypt_decrypt_round_trip(oracle):
+    """decrypt(encrypt(m)) == m and decrypt(ct1 + ct2) == m1 + m2 mod t
+    (symmetric_encryption_test.cc's round-trip and additive properties)."""
+    q, log_n, t = 576460752303415297, 10, 65537
+    n = 1 << log_n
+    p = oracle.Prime(q, log_n)
+    rng = np.random.default_rng(5)
+
+    def cbd():
+        b = rng.integers(0, 2, size=(n, 32))
+        return b[:, :16].sum(1) - b[:, 16:].sum(1)
+
+    def mont(v):
+        return p.import_(np.array([int(x) % q for x in v], dtype=np.uint64))
+
+    s = p.ntt_fwd(mont(cbd()))
+    m1, m2 = rng.integers(0, t, n), rng.integers(0, t, n)
+    c1 = p.sym_encrypt(t, s, oracle.uniform_limbs(1, [q], n, 1).reshape(n), mont(cbd()),
+                       p.ntt_fwd(mont(m1)))
+    c2 = p.sym_encrypt(t, s, oracle.uniform_limbs(2, [q], n, 1).reshape(n), mont(cbd()),
+                       p.ntt_fwd(mont(m2)))
+    assert np.array_equal(p.sym_decrypt(t, s, c1).astype(np.int64), m1)
+    assert np.array_equal(p.sym_decrypt(t, s, p.add(c1, c2)).astype(np.int64), (m1 + m2) % t)
