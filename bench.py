@@ -1093,6 +1093,43 @@ def main():
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
                "ms_per_step": e2e_ms / args.steps}
 
+    # End to end in the wire format: host ciphertexts serialized as the
+    # reference serializes them (log q-bit packed limbs), packed bytes over the
+    # host link, (de)serialization on the device.
+    e2e_wire = None
+    if not args.no_e2e:
+        pb = lib.shg_poly_serialized_bytes(ctx.h, L)
+        wct = 2 * pb
+        hw_a, hw_b, hw_out = host(B * wct), host(B * wct), host(B * wct)
+        dw = sg.DeviceBuffer(B * wct)
+        for dsrc, hdst in ((d_a, hw_a), (d_b, hw_b)):
+            sg.check(lib.shg_poly_serialize(ctx.h, dw.ptr, dsrc.ptr, 2 * B, L, s))
+            sg.check(lib.shg_memcpy_d2h(hdst, dw.ptr, B * wct, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        dw.free()
+
+        def step_wire():
+            sg.check(lib.shg_bgv_mul_relin_host_serialized(ctx.h, key.h, hw_out, hw_a, hw_b, B,
+                                                           s))
+        for _ in range(2):
+            step_wire()
+        sg.check(lib.shg_stream_synchronize(s))
+        w0, w1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(w0, s))
+        for _ in range(args.steps):
+            step_wire()
+        sg.check(lib.shg_event_record(w1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        barrier(dist)
+        wire_ms = max_over_ranks(dist, elapsed(w0, w1))
+        e2e_wire = {"value": ops_all / (wire_ms / 1e3), "unit": UNIT,
+                    "h2d_bytes_per_step": 2 * B * wct, "d2h_bytes_per_step": B * wct,
+                    "ms_per_step": wire_ms / args.steps,
+                    "format": "SHELL serialization (MontgomeryInt::SerializeVector per limb)"}
+        for hp in (hw_a, hw_b, hw_out):
+            lib.shg_host_free(hp)
+
     # Plain drop-in path: one ct_tensor + one relin_apply call per ciphertext.
     P = min(args.plain_ops, B)
     d_ct3 = sg.DeviceBuffer(P * 3 * L * n * 8)
@@ -1198,7 +1235,7 @@ def main():
                   "path": "shg_ct_tensor + shg_relin_apply per ciphertext"},
         "batched_over_plain": value / world / plain_rate,
         "bit_exact_batched_vs_plain": bit_exact,
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": e2e, "e2e_wire": e2e_wire, "roofline": roofline, "cpu_baseline": cpu,
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clk,
     }

@@ -131,6 +131,21 @@ int shg_gadget_decompose(shg_context* ctx, int num_limbs, const int* log_bs,
                          uint64_t* out, const uint64_t* in, int count,
                          shg_stream stream);
 
+/* Wire format: RnsPolynomial::Serialize / Deserialize (rns/rns_polynomial.h:
+ * 99-140) limb by limb, each limb MontgomeryInt::SerializeVector /
+ * DeserializeVector (montgomery.cc:142-215): the n Montgomery residues as a
+ * little-endian bit stream of log q_l bits each (value i at stream bits
+ * [i*b, i*b + b), bit j in byte j/8 at position j%8), ceil(n*b/8) bytes.
+ * A serialized polynomial is its limbs' streams back to back
+ * (shg_poly_serialized_bytes bytes); batches are polynomials back to back.
+ * Device buffers; for n >= 64 the serialized buffer must be 8-byte aligned.
+ * Deserialization, like the reference's, does not range-check values. */
+size_t shg_poly_serialized_bytes(const shg_context* ctx, int num_limbs);
+int shg_poly_serialize(shg_context* ctx, uint8_t* out, const uint64_t* polys,
+                       int count, int num_limbs, shg_stream stream);
+int shg_poly_deserialize(shg_context* ctx, uint64_t* polys, const uint8_t* in,
+                         int count, int num_limbs, shg_stream stream);
+
 /* ---------------------------------------------------------------------------
  * Ciphertexts
  * ------------------------------------------------------------------------- */
@@ -233,6 +248,14 @@ int shg_pir_expand_absorb_multikey(shg_context* ctx, const shg_key* const* keys,
 int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* relin_key,
                            uint64_t* out, const uint64_t* a, const uint64_t* b,
                            int count, shg_stream stream);
+/* shg_bgv_mul_relin_host on serialized ciphertexts (the wire format above:
+ * each ciphertext is its two polynomials' streams, 2 *
+ * shg_poly_serialized_bytes(ctx, L) bytes, ciphertexts back to back in host
+ * memory): the packed bytes cross the host link and are deserialized and
+ * re-serialized on the device.  n >= 64. */
+int shg_bgv_mul_relin_host_serialized(shg_context* ctx, const shg_key* relin_key,
+                                      uint8_t* out, const uint8_t* a, const uint8_t* b,
+                                      int count, shg_stream stream);
 
 /* RnsBgvCiphertext::Substitute(power) then RnsGaloisKey::ApplyTo
  * (rns/rns_bgv_ciphertext.h:161-174): ct [count][2][L][n] -> out. */

@@ -72,6 +72,10 @@ def lib():
             "so_oblivious_expand": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, U64P,
                                                    U64P, U64P]),
             "so_absorb_sum": (None, [vp, ctypes.c_int, U64P, U64P, U64P]),
+            "so_serialize_vector": (ctypes.c_size_t, [vp, U64P, ctypes.c_size_t,
+                                                      ctypes.POINTER(ctypes.c_uint8)]),
+            "so_deserialize_vector": (None, [vp, ctypes.POINTER(ctypes.c_uint8),
+                                             ctypes.c_size_t, U64P]),
             "so_sym_encrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, U64P, U64P, U64P]),
             "so_sym_decrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, ctypes.c_int, U64P]),
             "so_compute_normalizer": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int]),
@@ -222,6 +226,20 @@ class Prime:
         st = lib().so_oblivious_expand(self._h, levels, log_b, _p(keys), _p(ct), _p(out))
         if st:
             raise ValueError("bad levels")
+        return out
+
+    def serialize(self, v):
+        v = np.ascontiguousarray(v, dtype=np.uint64).reshape(-1)
+        out = np.zeros((v.size * self.info()["log_q"] + 7) // 8, np.uint8)
+        nb = lib().so_serialize_vector(self._h, _p(v), v.size,
+                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        return out[:nb]
+
+    def deserialize(self, data, count):
+        data = np.ascontiguousarray(data, dtype=np.uint8)
+        out = np.empty(count, np.uint64)
+        lib().so_deserialize_vector(self._h, data.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                    count, _p(out))
         return out
 
     def sym_encrypt(self, t, s, a, e, m):

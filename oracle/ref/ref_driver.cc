@@ -328,6 +328,35 @@ int ref_oblivious_expand(uint64_t q, int log_n, int log_t, int levels, int log_b
   return 0;
 }
 
+// MontgomeryInt::SerializeVector of `count` Montgomery residues mod q into
+// `out` (capacity `cap` bytes); *len receives the byte count.
+int ref_serialize_vector(uint64_t q, const uint64_t* data, int count, uint8_t* out,
+                         size_t cap, size_t* len) {
+  auto params = M::Params::Create(q);
+  if (!params.ok()) return fail(params.status());
+  auto s = M::SerializeVector(to_vec(data, count), params->get());
+  if (!s.ok()) return fail(s.status());
+  if (s->size() > cap) {
+    g_err = "output too small";
+    return 3;
+  }
+  std::memcpy(out, s->data(), s->size());
+  *len = s->size();
+  return 0;
+}
+
+// MontgomeryInt::DeserializeVector of `count` values.
+int ref_deserialize_vector(uint64_t q, const uint8_t* in, size_t len, int count,
+                           uint64_t* out) {
+  auto params = M::Params::Create(q);
+  if (!params.ok()) return fail(params.status());
+  auto v = M::DeserializeVector(
+      count, std::string(reinterpret_cast<const char*>(in), len), params->get());
+  if (!v.ok()) return fail(v.status());
+  from_vec(*v, out);
+  return 0;
+}
+
 // ObliviousExpander::ComputeNormalizer.
 uint64_t ref_compute_normalizer(int k, int log_t) {
   return rlwe::ObliviousExpander<M>::ComputeNormalizer(k, log_t);

@@ -40,6 +40,11 @@ def lib():
         L.ref_oblivious_expand.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, _U64P, _U64P,
                                            ctypes.c_int, _U64P]
+        L.ref_serialize_vector.argtypes = [ctypes.c_uint64, _U64P, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_size_t)]
+        L.ref_deserialize_vector.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint8),
+                                             ctypes.c_size_t, ctypes.c_int, _U64P]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -130,3 +135,23 @@ def oblivious_expand(q, log_n, log_t, levels, log_b, keys, cts):
 
 def compute_normalizer(k, log_t):
     return int(lib().ref_compute_normalizer(k, log_t))
+
+
+def serialize_vector(q, values):
+    """MontgomeryInt<uint64>::SerializeVector of the reference."""
+    v = np.ascontiguousarray(values, dtype=np.uint64).reshape(-1)
+    out = np.zeros(v.size * 8 + 16, np.uint8)
+    nb = ctypes.c_size_t()
+    _check(lib().ref_serialize_vector(q, _p(v), v.size,
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                      out.size, ctypes.byref(nb)))
+    return out[:nb.value].copy()
+
+
+def deserialize_vector(q, data, count):
+    """MontgomeryInt<uint64>::DeserializeVector of the reference."""
+    data = np.ascontiguousarray(data, dtype=np.uint8)
+    out = np.empty(count, np.uint64)
+    _check(lib().ref_deserialize_vector(q, data.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                        data.size, count, _p(out)))
+    return out

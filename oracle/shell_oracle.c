@@ -806,6 +806,40 @@ void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint
   free(ci);
 }
 
+/* MontgomeryInt::SerializeVector (montgomery.cc:142-166) through
+ * TranscribeBits (transcription.h:43-118): the log_q-bit Montgomery
+ * representations as one little-endian bit stream -- value i fills stream
+ * bits [i*b, i*b + b) from its least significant bit, stream bit j is bit
+ * j % 8 of byte j / 8.  Returns ceil(count * b / 8), the bytes written. */
+size_t so_serialize_vector(const so_prime* p, const uint64_t* in, size_t count,
+                           uint8_t* out) {
+  const int b = p->log_q;
+  const size_t bytes = (count * (size_t)b + 7) / 8;
+  memset(out, 0, bytes);
+  for (size_t i = 0; i < count; i++)
+    for (int k = 0; k < b; k++) {
+      const size_t pos = i * (size_t)b + (size_t)k;
+      out[pos >> 3] |= (uint8_t)(((in[i] >> k) & 1u) << (pos & 7));
+    }
+  return bytes;
+}
+
+/* MontgomeryInt::DeserializeVector (montgomery.cc:186-215): the inverse bit
+ * stream; values are taken as Montgomery representations unchecked, as the
+ * reference does. */
+void so_deserialize_vector(const so_prime* p, const uint8_t* in, size_t count,
+                           uint64_t* out) {
+  const int b = p->log_q;
+  for (size_t i = 0; i < count; i++) {
+    uint64_t v = 0;
+    for (int k = 0; k < b; k++) {
+      const size_t pos = i * (size_t)b + (size_t)k;
+      v |= (uint64_t)((in[pos >> 3] >> (pos & 7)) & 1u) << k;
+    }
+    out[i] = v;
+  }
+}
+
 /* ObliviousExpander::ComputeNormalizer (oblivious_expand.h:143-157). */
 uint64_t so_compute_normalizer(int k, int log_t) {
   int log_t_minus_r = log_t - (k % log_t);

@@ -135,6 +135,12 @@ void so_sym_encrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint
 /* Decrypt a ciphertext of `len` components [len][n]: out [n] in [0, t). */
 void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* ct,
                     int len, uint64_t* out);
+/* MontgomeryInt::SerializeVector / DeserializeVector bit streams of `count`
+ * values of one prime; serialize returns the byte count. */
+size_t so_serialize_vector(const so_prime* p, const uint64_t* in, size_t count,
+                           uint8_t* out);
+void so_deserialize_vector(const so_prime* p, const uint8_t* in, size_t count,
+                           uint64_t* out);
 /* ObliviousExpander::ComputeNormalizer */
 uint64_t so_compute_normalizer(int k, int log_t);
 

@@ -244,6 +244,18 @@ int check_limbs(const shg_context* ctx, int count, int num_limbs) {
   return SHG_OK;
 }
 
+// Serialized layout of a polynomial of num_limbs limbs (the wire format of
+// shg_poly_serialize).
+shg::SerLayout ser_layout(const shg_context* ctx, int num_limbs) {
+  shg::SerLayout lay{};
+  lay.offset[0] = 0;
+  for (int l = 0; l < num_limbs; ++l) {
+    lay.bits[l] = ctx->hp[l].log_q;
+    lay.offset[l + 1] = lay.offset[l] + ((size_t)ctx->n * lay.bits[l] + 7) / 8;
+  }
+  return lay;
+}
+
 int launch_status(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -872,21 +884,39 @@ int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
   return keyswitch(ctx, key, out, KsArgs{ct, 2, 1, 0, 1}, count, (cudaStream_t)s);
 }
 
-int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
-                           const uint64_t* a, const uint64_t* b, int count,
-                           shg_stream stream) {
+}  // extern "C"
+
+namespace {
+// Host-buffer ct-mult+relin pipeline.  wire: a, b, out hold serialized
+// ciphertexts (shg_poly_serialize layout, two polynomials each), which cross
+// the host link packed and are (de)serialized on the device.
+int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const void* a_v,
+                        const void* b_v, int count, shg_stream stream, bool wire) {
   int st = check_key(ctx, key);
   if (st) return st;
+  if (key->power != 1)
+    return fail(SHG_INVALID_ARGUMENT,
+                "Relinearization key can only apply to a ciphertext of power 1.");
   if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
   if (count == 0) return SHG_OK;
-  if (!out || !a || !b) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  if (!out_v || !a_v || !b_v) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
   const size_t ct_elems = 2 * (size_t)key->L * ctx->n;
   const size_t ct_bytes = ct_elems * sizeof(uint64_t);
+  const shg::SerLayout lay = ser_layout(ctx, key->L);
+  // Bytes of one ciphertext on the host side (packed when wire), rounded to
+  // 16 so every staged piece stays aligned.
+  const size_t host_ct = wire ? 2 * (size_t)lay.offset[key->L] : ct_bytes;
+  const size_t host_ct_pad = (host_ct + 15) / 16 * 16;
+  const uint8_t* a = static_cast<const uint8_t*>(a_v);
+  const uint8_t* b = static_cast<const uint8_t*>(b_v);
+  uint8_t* out = static_cast<uint8_t*>(out_v);
   // Pieces of host_piece ciphertexts through host_slots staging slots of
-  // (a, b, out); a and b come in on two copy streams.
+  // (a, b, out) plus, when wire, their packed forms; a and b come in on two
+  // copy streams.
   const int P = std::min(count, ctx->host_piece);
   const int S = ctx->host_slots;
-  const size_t slot = 3 * (size_t)P * ct_bytes;
+  const size_t packed = wire ? 3 * (size_t)P * host_ct_pad : 0;
+  const size_t slot = 3 * (size_t)P * ct_bytes + packed;
   std::lock_guard<std::mutex> io_lock(ctx->io_mu);
   if (ctx->io_bytes < S * slot) {
     SHG_CUDA(cudaDeviceSynchronize());
@@ -929,26 +959,46 @@ int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
     uint64_t* da = ctx->io + (size_t)(i % S) * (slot / sizeof(uint64_t));
     uint64_t* db = da + (size_t)P * ct_elems;
     uint64_t* dout = db + (size_t)P * ct_elems;
+    uint8_t* pa = reinterpret_cast<uint8_t*>(dout + (size_t)P * ct_elems);
+    uint8_t* pb = pa + (size_t)P * host_ct_pad;
+    uint8_t* pout = pb + (size_t)P * host_ct_pad;
     // Slot reuse: piece i-S must have been copied back (its compute also
     // finished reading a, b before that).
     if (i >= S) {
       SHG_CUDA(cudaStreamWaitEvent(s_in, stored[i - S], 0));
       SHG_CUDA(cudaStreamWaitEvent(s_in2, stored[i - S], 0));
     }
-    SHG_CUDA(cudaMemcpyAsync(da, a + (size_t)c0 * ct_elems, cc * ct_bytes,
-                             cudaMemcpyHostToDevice, s_in));
-    SHG_CUDA(cudaMemcpyAsync(db, b + (size_t)c0 * ct_elems, cc * ct_bytes,
-                             cudaMemcpyHostToDevice, s_in2));
+    if (wire) {
+      // Packed ciphertexts are host_ct bytes each, back to back.
+      SHG_CUDA(cudaMemcpyAsync(pa, a + (size_t)c0 * host_ct, cc * host_ct,
+                               cudaMemcpyHostToDevice, s_in));
+      SHG_CUDA(cudaMemcpyAsync(pb, b + (size_t)c0 * host_ct, cc * host_ct,
+                               cudaMemcpyHostToDevice, s_in2));
+    } else {
+      SHG_CUDA(cudaMemcpyAsync(da, a + (size_t)c0 * ct_bytes, cc * ct_bytes,
+                               cudaMemcpyHostToDevice, s_in));
+      SHG_CUDA(cudaMemcpyAsync(db, b + (size_t)c0 * ct_bytes, cc * ct_bytes,
+                               cudaMemcpyHostToDevice, s_in2));
+    }
     SHG_CUDA(cudaEventRecord(loaded[i], s_in));
     SHG_CUDA(cudaEventRecord(loaded2[i], s_in2));
     SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded[i], 0));
     SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded2[i], 0));
+    if (wire) {
+      shg::launch_deserialize(ctx->dev(), da, pa, lay, 2 * cc, key->L, s_comp);
+      shg::launch_deserialize(ctx->dev(), db, pb, lay, 2 * cc, key->L, s_comp);
+    }
     rc = shg_bgv_mul_relin(ctx, key, dout, da, db, cc, (shg_stream)s_comp);
     if (rc) break;
+    if (wire) shg::launch_serialize(ctx->dev(), pout, dout, lay, 2 * cc, key->L, s_comp);
     SHG_CUDA(cudaEventRecord(computed[i], s_comp));
     SHG_CUDA(cudaStreamWaitEvent(s_out, computed[i], 0));
-    SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * ct_elems, dout, cc * ct_bytes,
-                             cudaMemcpyDeviceToHost, s_out));
+    if (wire)
+      SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * host_ct, pout, cc * host_ct,
+                               cudaMemcpyDeviceToHost, s_out));
+    else
+      SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * ct_bytes, dout, cc * ct_bytes,
+                               cudaMemcpyDeviceToHost, s_out));
     SHG_CUDA(cudaEventRecord(stored[i], s_out));
   }
   if (rc == SHG_OK) {
@@ -956,6 +1006,23 @@ int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
   }
   for (cudaEvent_t e : evs) cudaEventDestroy(e);
   return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int shg_bgv_mul_relin_host(shg_context* ctx, const shg_key* key, uint64_t* out,
+                           const uint64_t* a, const uint64_t* b, int count,
+                           shg_stream stream) {
+  return mul_relin_host_impl(ctx, key, out, a, b, count, stream, false);
+}
+
+int shg_bgv_mul_relin_host_serialized(shg_context* ctx, const shg_key* key, uint8_t* out,
+                                      const uint8_t* a, const uint8_t* b, int count,
+                                      shg_stream stream) {
+  if (ctx && ctx->n < 64)
+    return fail(SHG_INVALID_ARGUMENT, "the serialized pipeline needs n >= 64");
+  return mul_relin_host_impl(ctx, key, out, a, b, count, stream, true);
 }
 
 int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,
@@ -1206,6 +1273,39 @@ int shg_pir_expand_absorb_multikey(shg_context* ctx, const shg_key* const* keys,
                                    const uint64_t* ct, int count, shg_stream stream) {
   return pir_impl(ctx, keys, true, levels, db, num_items, out, ct, count,
                   (cudaStream_t)stream);
+}
+
+size_t shg_poly_serialized_bytes(const shg_context* ctx, int num_limbs) {
+  if (!ctx || num_limbs <= 0 || num_limbs > ctx->L) return 0;
+  return (size_t)ser_layout(ctx, num_limbs).offset[num_limbs];
+}
+
+int shg_poly_serialize(shg_context* ctx, uint8_t* out, const uint64_t* polys, int count,
+                       int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if (!out) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  if ((st = check_ptrs({polys}))) return st;
+  if (ctx->n >= 64 && ((uintptr_t)out & 7))
+    return fail(SHG_INVALID_ARGUMENT, "serialized buffers must be 8-byte aligned");
+  shg::launch_serialize(ctx->dev(), out, polys, ser_layout(ctx, num_limbs), count, num_limbs,
+                        (cudaStream_t)s);
+  return launch_status("serialize");
+}
+
+int shg_poly_deserialize(shg_context* ctx, uint64_t* polys, const uint8_t* in, int count,
+                         int num_limbs, shg_stream s) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if (!in) return fail(SHG_INVALID_ARGUMENT, "null buffer pointer");
+  if ((st = check_ptrs({polys}))) return st;
+  if (ctx->n >= 64 && ((uintptr_t)in & 7))
+    return fail(SHG_INVALID_ARGUMENT, "serialized buffers must be 8-byte aligned");
+  shg::launch_deserialize(ctx->dev(), polys, in, ser_layout(ctx, num_limbs), count, num_limbs,
+                          (cudaStream_t)s);
+  return launch_status("deserialize");
 }
 
 int shg_symmetric_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* s_ntt,

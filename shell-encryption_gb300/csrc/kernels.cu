@@ -611,6 +611,83 @@ __global__ void k_monomials(uint64_t* mono, int levels, int log_n,
   }
 }
 
+// MontgomeryInt::DeserializeVector (montgomery.cc:186-215) of every limb:
+// value i of a limb stream is stream bits [i*b, i*b + b) (TranscribeBits,
+// transcription.h:43-118, least significant bit first).  WORDS: every limb
+// stream starts on an 8-byte boundary (n * b a multiple of 64), so a value is
+// read from at most two aligned 64-bit words; otherwise bytes are gathered.
+template <bool WORDS>
+__global__ void k_deserialize(uint64_t* polys, const uint8_t* in, SerLayout lay,
+                              size_t total /* count*L*n */, int log_n, int L) {
+  const size_t n = (size_t)1 << log_n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t pl = e >> log_n, i = e & (n - 1);
+    const size_t p = pl / L;
+    const int l = (int)(pl % L);
+    const int b = lay.bits[l];
+    const uint8_t* stream = in + p * lay.offset[L] + lay.offset[l];
+    const size_t bit = i * (size_t)b;
+    const uint64_t mask = b == 64 ? ~0ull : ((1ull << b) - 1);
+    uint64_t v;
+    if (WORDS) {
+      const uint64_t* w = reinterpret_cast<const uint64_t*>(stream);
+      const size_t w0 = bit >> 6;
+      const int o = (int)(bit & 63);
+      v = w[w0] >> o;
+      if (o + b > 64) v |= w[w0 + 1] << (64 - o);
+    } else {
+      const size_t byte0 = bit >> 3;
+      const int o = (int)(bit & 7);
+      const int nbytes = (o + b + 7) >> 3;
+      unsigned __int128 acc = 0;
+      for (int k = 0; k < nbytes; ++k)
+        acc |= (unsigned __int128)stream[byte0 + k] << (8 * k);
+      v = (uint64_t)(acc >> o);
+    }
+    polys[e] = v & mask;
+  }
+}
+
+// MontgomeryInt::SerializeVector (montgomery.cc:142-166) of every limb: one
+// thread per output unit (a 64-bit word, or a byte without WORDS) ORs in the
+// parts of the values that overlap it.
+template <bool WORDS>
+__global__ void k_serialize(uint8_t* out, const uint64_t* polys, SerLayout lay,
+                            size_t units_per_poly, size_t total /* count*units */,
+                            int log_n, int L) {
+  const size_t n = (size_t)1 << log_n;
+  const int U = WORDS ? 64 : 8;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += stride) {
+    const size_t p = e / units_per_poly, u = e % units_per_poly;
+    // limb of this unit: offsets are multiples of the unit
+    int l = 0;
+    while (l + 1 < L && (size_t)lay.offset[l + 1] * 8 / U <= u) ++l;
+    const int b = lay.bits[l];
+    const size_t bit0 = (u - (size_t)lay.offset[l] * 8 / U) * U;  // stream bit of the unit
+    const uint64_t* vals = polys + (p * L + l) * n;
+    const size_t stream_bits = n * (size_t)b;
+    uint64_t acc = 0;
+    for (size_t i = bit0 / b; i < n && i * (size_t)b < bit0 + U && i * (size_t)b < stream_bits;
+         ++i) {
+      const long long sh = (long long)(i * (size_t)b) - (long long)bit0;  // value bit 0 in the unit
+      const uint64_t v = vals[i] & (b == 64 ? ~0ull : ((1ull << b) - 1));
+      if (sh >= 0)
+        acc |= sh < 64 ? v << sh : 0;
+      else
+        acc |= v >> (-sh);
+    }
+    if (WORDS) {
+      reinterpret_cast<uint64_t*>(out)[e] = acc;
+    } else {
+      out[e] = (uint8_t)acc;
+    }
+  }
+}
+
 // Symmetric RLWE encryption combine (symmetric_encryption.h:940-963,
 // 1006-1021) on limb 0: out [count][2][n] = (e_ntt * t + m + a * s, -a).
 __global__ void k_sym_encrypt(uint64_t* out, const uint64_t* e_ntt, const uint64_t* a,
@@ -1014,6 +1091,32 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
   LaunchScope scope_("expand_combine", s);
   k_expand_combine<<<grid_for(total, 256), 256, 0, s>>>(base, ks, mono, map,
                                                         half, total, c.log_n, c);
+}
+
+void launch_deserialize(const CtxDev& c, uint64_t* polys, const uint8_t* in,
+                        const SerLayout& lay, int count, int L, cudaStream_t s) {
+  const size_t total = (size_t)count * L * c.n;
+  if (total == 0) return;
+  LaunchScope scope_("deserialize", s);
+  if (lay.offset[L] % 8 == 0 && c.n >= 64)
+    k_deserialize<true><<<grid_for(total, 256), 256, 0, s>>>(polys, in, lay, total, c.log_n, L);
+  else
+    k_deserialize<false><<<grid_for(total, 256), 256, 0, s>>>(polys, in, lay, total, c.log_n, L);
+}
+
+void launch_serialize(const CtxDev& c, uint8_t* out, const uint64_t* polys,
+                      const SerLayout& lay, int count, int L, cudaStream_t s) {
+  if (count <= 0) return;
+  LaunchScope scope_("serialize", s);
+  if (lay.offset[L] % 8 == 0 && c.n >= 64) {
+    const size_t units = lay.offset[L] / 8, total = units * count;
+    k_serialize<true><<<grid_for(total, 256), 256, 0, s>>>(out, polys, lay, units, total,
+                                                           c.log_n, L);
+  } else {
+    const size_t units = lay.offset[L], total = units * count;
+    k_serialize<false><<<grid_for(total, 256), 256, 0, s>>>(out, polys, lay, units, total,
+                                                            c.log_n, L);
+  }
 }
 
 void launch_sym_encrypt(const CtxDev& c, uint64_t* out, const uint64_t* e_ntt,

@@ -176,6 +176,19 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            const uint64_t* mono, CtMap map, int half,
                            int count, cudaStream_t s);
 
+// Serialized polynomial layout (MontgomeryInt::SerializeVector per limb):
+// limb l is an n * bits[l] bit little-endian stream of the Montgomery
+// residues, starting at byte offset[l] of the polynomial; a polynomial takes
+// offset[L] bytes.
+struct SerLayout {
+  int bits[kMaxLimbs];
+  unsigned long long offset[kMaxLimbs + 1];
+};
+void launch_deserialize(const CtxDev& c, uint64_t* polys, const uint8_t* in,
+                        const SerLayout& lay, int count, int L, cudaStream_t s);
+void launch_serialize(const CtxDev& c, uint8_t* out, const uint64_t* polys,
+                      const SerLayout& lay, int count, int L, cudaStream_t s);
+
 // Symmetric RLWE on limb 0: encryption combine out [count][2][n] =
 // (e_ntt * t + m + a * s, -a); decryption dot product acc [count][n] =
 // sum_i ct[count][i] * s^i; RemoveError of exported coefficients.

@@ -46,6 +46,9 @@ SIGNATURES = {
                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]),
     "shg_gadget_decompose": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _vp, _vp, ctypes.c_int,
                                             _vp]),
+    "shg_poly_serialized_bytes": (_sz, [_vp, ctypes.c_int]),
+    "shg_poly_serialize": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_poly_deserialize": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "shg_ct_tensor": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "shg_key_create": (ctypes.c_int, [_vp, ctypes.c_int, _ip, ctypes.c_int, _u64p, _u64p,
                                       ctypes.POINTER(_vp)]),
@@ -66,6 +69,8 @@ SIGNATURES = {
                                                _vp]),
     "shg_pir_expand_absorb_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp,
                                                       ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_bgv_mul_relin_host_serialized": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int,
+                                                         _vp]),
     "shg_bgv_mul_relin_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_rotate": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_oblivious_expand": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp, _vp,

@@ -91,6 +91,13 @@ def main():
     g["expand_cts"] = cts
     g["expand_out"] = R.oblivious_expand(q, log_n, 16, levels, log_b, keys, cts)
     g["normalizer_10_16"] = np.array([R.compute_normalizer(10, 16)], np.uint64)
+    # MontgomeryInt::SerializeVector bit streams (montgomery.cc:142-215),
+    # including a 17- and a 31-bit modulus (streams that cross bytes oddly).
+    for q, count in [(Q45[0], 1000), (Q50[3], 777), (Q59, 64), (Q60, 33), (65537, 101),
+                     (2147483629, 57)]:
+        v = O.splitmix64(8000 + count, count) % np.uint64(q)
+        g[f"ser_{q}_values"] = v
+        g[f"ser_{q}_bytes"] = R.serialize_vector(q, v)
     np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **g)
 
     # Full-size workloads: digests of the reference's outputs on seeded inputs.

@@ -306,3 +306,18 @@ def test_gpu_ntt_q59_digest(sg, oracle):
     buf.upload(x)
     _run(sg, sg.lib().shg_ntt_inverse, ctx.h, buf.ptr, 64, 1, None)
     assert digest(buf.download((64, 1 << 12))) == d["inv_sha256"]
+
+
+SER_TAGS = sorted({k[len("ser_"):-len("_values")] for k in SMALL.files
+                   if k.startswith("ser_") and k.endswith("_values")})
+
+
+@pytest.mark.parametrize("q", SER_TAGS)
+def test_oracle_serialization_golden(oracle, q):
+    """MontgomeryInt::SerializeVector / DeserializeVector streams of the
+    reference (17- to 60-bit moduli)."""
+    v = SMALL[f"ser_{q}_values"]
+    want = SMALL[f"ser_{q}_bytes"]
+    p = oracle.Prime(int(q), 1)
+    assert np.array_equal(p.serialize(v), want)
+    assert np.array_equal(p.deserialize(want, v.size), v)

@@ -636,3 +636,58 @@ def test_symmetric_rlwe_flow(sg, oracle):
     with pytest.raises(sg.ShgError, match="one-prime"):
         ctx2 = sg.Context(log_n, Q50[:2], t)
         sg.check(lib.shg_symmetric_decrypt(ctx2.h, dec.ptr, ds.ptr, ct.ptr, 2, 1, None))
+
+
+@pytest.mark.parametrize("log_n,qs", [(3, Q45[:2]), (6, [65537]), (10, Q50[:3]),
+                                      (14, Q45), (12, [Q59, Q60])])
+def test_serialize_deserialize(sg, oracle, log_n, qs):
+    """The wire format (MontgomeryInt::SerializeVector per limb): device
+    streams equal the oracle's (pinned to the reference by the golden
+    streams); deserializing gives the values back."""
+    lib = sg.lib()
+    n, L, count = 1 << log_n, len(qs), 3
+    x = oracle.uniform_limbs(910 + log_n, qs, n, count)
+    want = np.concatenate([oracle.Prime(q, log_n).serialize(x[c, l])
+                           for c in range(count) for l, q in enumerate(qs)])
+    ctx = sg.Context(log_n, qs)
+    per_poly = lib.shg_poly_serialized_bytes(ctx.h, L)
+    assert per_poly * count == want.size
+    d = _dev(sg, x)
+    buf = sg.DeviceBuffer(want.size + 16)
+    _run(sg, lib.shg_poly_serialize, ctx.h, buf.ptr, d.ptr, count, L, None)
+    got = np.empty(want.size, np.uint8)
+    sg.check(lib.shg_memcpy_d2h(got.ctypes.data, buf.ptr, got.nbytes, None))
+    sg.synchronize()
+    assert np.array_equal(got, want)
+    back = sg.DeviceBuffer(x.nbytes)
+    sg.check(lib.shg_memcpy_h2d(buf.ptr, want.ctypes.data, want.nbytes, None))
+    _run(sg, lib.shg_poly_deserialize, ctx.h, back.ptr, buf.ptr, count, L, None)
+    assert np.array_equal(back.download(x.shape), x)
+
+
+@pytest.mark.parametrize("piece,slots", [(2, 2), (64, 4)])
+def test_mul_relin_host_serialized(sg, oracle, piece, slots):
+    """Host ciphertexts in the wire format in, wire format out: equals the
+    oracle's ct-mult+relin serialized like the reference would."""
+    lib = sg.lib()
+    log_n, qs, log_bs, count = 12, Q50[:3], [20] * 3, 5
+    n, L = 1 << log_n, len(qs)
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    kb, ka = oracle.uniform_limbs(21, qs, n, k), oracle.uniform_limbs(22, qs, n, k)
+    a, b = _ct_pair(oracle, qs, n, count, 23)
+    primes = [oracle.Prime(q, log_n) for q in qs]
+
+    def ser(x):
+        return np.concatenate([primes[l].serialize(x[c, comp, l]) for c in range(x.shape[0])
+                               for comp in range(2) for l in range(L)])
+
+    want = np.stack([rns.relin(rns.tensor(a[i], b[i]), kb, ka, log_bs) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    sg.check(lib.shg_context_set_host_pipeline(ctx.h, piece, slots))
+    key = sg.Key(ctx, log_bs, 1, kb, ka)
+    sa, sb = ser(a), ser(b)
+    out = np.zeros_like(sa)
+    _run(sg, lib.shg_bgv_mul_relin_host_serialized, ctx.h, key.h, out.ctypes.data,
+         sa.ctypes.data, sb.ctypes.data, count, None)
+    assert np.array_equal(out, ser(want))
