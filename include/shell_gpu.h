@@ -214,6 +214,22 @@ int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key, uint64_t* out,
 int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
                      const uint64_t* ct, int count, shg_stream stream);
 
+/* RnsGaloisKey::PrecomputeRandomPad (rns/rns_galois_key.h:170-175,
+ * .cc:289-306): pad_digits [count][k][L][n] = the gadget digits of each
+ * ciphertext's "a" part (c1) in NTT form -> out [count][L][n] =
+ * sum_j pad_j * key_a_j, the key-switched "a" part. */
+int shg_galois_precompute_pad(shg_context* ctx, const shg_key* galois_key,
+                              uint64_t* out, const uint64_t* pad_digits, int count,
+                              shg_stream stream);
+/* RnsGaloisKey::ApplyToWithRandomPad (rns/rns_galois_key.h:177-192,
+ * .cc:308-346): ct [count][2][L][n] at the key's power, its c1 digits
+ * pad_digits and the precomputed pad_new [count][L][n] -> out
+ * [count][2][L][n] = (c0 + sum_j pad_j * key_b_j, pad_new). */
+int shg_galois_apply_with_pad(shg_context* ctx, const shg_key* galois_key,
+                              uint64_t* out, const uint64_t* ct,
+                              const uint64_t* pad_digits, const uint64_t* pad_new,
+                              int count, shg_stream stream);
+
 /* Batched fused form of RnsBgvCiphertext::operator* followed by
  * RnsRelinKey::ApplyTo (rns/rns_bgv_ciphertext.h:134-139 +
  * rns/rns_relinearization_key.cc:184-232): a, b [count][2][L][n] ->

@@ -76,6 +76,8 @@ def lib():
                                                       ctypes.POINTER(ctypes.c_uint8)]),
             "so_deserialize_vector": (None, [vp, ctypes.POINTER(ctypes.c_uint8),
                                              ctypes.c_size_t, U64P]),
+            "so_rns_galois_pad": (None, [vp, ctypes.c_int, ctypes.c_int, U64P, U64P, U64P, U64P,
+                                         U64P]),
             "so_sym_encrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, U64P, U64P, U64P]),
             "so_sym_decrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, ctypes.c_int, U64P]),
             "so_compute_normalizer": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int]),
@@ -359,6 +361,17 @@ class Rns:
         out = np.empty((2, L, self.n), np.uint64)
         lib().so_rns_galois(self._h, L, p, _p(ct), _p(np.ascontiguousarray(key_b)),
                             _p(np.ascontiguousarray(key_a)), _p(out))
+        return out
+
+    def galois_pad(self, ct, pad, key_b, key_a):
+        """RnsGaloisKey::PrecomputeRandomPad + ApplyToWithRandomPad."""
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        pad = np.ascontiguousarray(pad, dtype=np.uint64)
+        L = ct.shape[1]
+        out = np.empty_like(ct)
+        lib().so_rns_galois_pad(self._h, L, pad.shape[0], _p(ct), _p(pad),
+                                _p(np.ascontiguousarray(key_b, dtype=np.uint64)),
+                                _p(np.ascontiguousarray(key_a, dtype=np.uint64)), _p(out))
         return out
 
     def modreduce_lsb(self, poly, t, is_ntt=True):

@@ -328,6 +328,54 @@ int ref_oblivious_expand(uint64_t q, int log_n, int log_t, int levels, int log_b
   return 0;
 }
 
+// RnsGaloisKey::PrecomputeRandomPad then ApplyToWithRandomPad on `count`
+// ciphertexts at the key's power with their c1 digits given: out
+// [count][2][L][n] = the key-switched ciphertexts.
+int ref_galois_random_pad(int log_n, const uint64_t* qs, int L, const int* log_bs,
+                          int power, const uint64_t* key_b, const uint64_t* key_a,
+                          const uint64_t* ct, const uint64_t* pad_digits, int count,
+                          uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto q_hats = ctx->MainPrimeModulusComplements(L - 1).value();
+  auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(L - 1).value();
+  auto gadget = rlwe::RnsGadget<M>::Create(
+      log_n, std::vector<size_t>(log_bs, log_bs + L), q_hats, q_hat_invs, moduli);
+  if (!gadget.ok()) return fail(gadget.status());
+  const int k = gadget->Dimension();
+  std::vector<rlwe::RnsPolynomial<M>> kas, kbs;
+  for (int j = 0; j < k; ++j) {
+    kbs.push_back(make_poly(key_b + (size_t)j * P, L, n, true));
+    kas.push_back(make_poly(key_a + (size_t)j * P, L, n, true));
+  }
+  auto key = rlwe::RnsGaloisKey<M>::CreateFromKeyComponents(
+      std::move(kas), std::move(kbs), power, &*gadget, moduli, "",
+      rlwe::PRNG_TYPE_HKDF);
+  if (!key.ok()) return fail(key.status());
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, {}, 16, 3.19);
+  if (!ep.ok()) return fail(ep.status());
+  for (int c = 0; c < count; ++c) {
+    std::vector<rlwe::RnsPolynomial<M>> comps;
+    for (int i = 0; i < 2; ++i)
+      comps.push_back(make_poly(ct + ((size_t)c * 2 + i) * P, L, n, true));
+    rlwe::RnsBgvCiphertext<M> x(std::move(comps), moduli, power, 1.0, &*ep);
+    std::vector<rlwe::RnsPolynomial<M>> digits;
+    for (int j = 0; j < k; ++j)
+      digits.push_back(make_poly(pad_digits + ((size_t)c * k + j) * P, L, n, true));
+    auto pad = key->PrecomputeRandomPad(digits);
+    if (!pad.ok()) return fail(pad.status());
+    auto r = key->ApplyToWithRandomPad(x, digits, *pad);
+    if (!r.ok()) return fail(r.status());
+    for (int i = 0; i < 2; ++i)
+      store_poly(r->Component(i).value(), out + ((size_t)c * 2 + i) * P);
+  }
+  return 0;
+}
+
 // MontgomeryInt::SerializeVector of `count` Montgomery residues mod q into
 // `out` (capacity `cap` bytes); *len receives the byte count.
 int ref_serialize_vector(uint64_t q, const uint64_t* data, int count, uint8_t* out,

@@ -45,6 +45,8 @@ def lib():
                                            ctypes.POINTER(ctypes.c_size_t)]
         L.ref_deserialize_vector.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint8),
                                              ctypes.c_size_t, ctypes.c_int, _U64P]
+        L.ref_galois_random_pad.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _IP, ctypes.c_int,
+                                            _U64P, _U64P, _U64P, _U64P, ctypes.c_int, _U64P]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -154,4 +156,21 @@ def deserialize_vector(q, data, count):
     out = np.empty(count, np.uint64)
     _check(lib().ref_deserialize_vector(q, data.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
                                         data.size, count, _p(out)))
+    return out
+
+
+def galois_random_pad(log_n, qs, log_bs, power, key_b, key_a, cts, pad_digits):
+    """RnsGaloisKey::PrecomputeRandomPad + ApplyToWithRandomPad of the reference."""
+    q = _qs(qs)
+    L, n = len(q), 1 << log_n
+    cts = np.ascontiguousarray(cts, dtype=np.uint64)
+    count = cts.shape[0]
+    lb = np.ascontiguousarray(log_bs, dtype=np.int32)
+    out = np.empty((count, 2, L, n), np.uint64)
+    _check(lib().ref_galois_random_pad(log_n, _p(q), L, lb.ctypes.data_as(_IP), power,
+                                       _p(np.ascontiguousarray(key_b, dtype=np.uint64)),
+                                       _p(np.ascontiguousarray(key_a, dtype=np.uint64)),
+                                       _p(cts), _p(np.ascontiguousarray(pad_digits,
+                                                                         dtype=np.uint64)),
+                                       count, _p(out)))
     return out

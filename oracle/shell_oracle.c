@@ -806,6 +806,25 @@ void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint
   free(ci);
 }
 
+/* RnsGaloisKey::PrecomputeRandomPad (rns/rns_galois_key.cc:289-306) and
+ * ApplyToRlweCiphertextWithRandomPad (:308-346): with the gadget digits of
+ * c1 given in NTT form (pad [k][L][n]), out [2][L][n] =
+ * (c0 + sum_j pad_j * key_b_j, sum_j pad_j * key_a_j). */
+void so_rns_galois_pad(const so_rns* r, int L, int k, const uint64_t* ct,
+                       const uint64_t* pad, const uint64_t* key_b, const uint64_t* key_a,
+                       uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n, P = (size_t)L * n;
+  memcpy(out, ct, P * sizeof(uint64_t));
+  memset(out + P, 0, P * sizeof(uint64_t));
+  for (int j = 0; j < k; j++)
+    for (int l = 0; l < L; l++) {
+      const so_prime* p = r->primes[l];
+      const size_t o = (size_t)j * P + (size_t)l * n;
+      so_fma(p, out + (size_t)l * n, pad + o, key_b + o, n);
+      so_fma(p, out + P + (size_t)l * n, pad + o, key_a + o, n);
+    }
+}
+
 /* MontgomeryInt::SerializeVector (montgomery.cc:142-166) through
  * TranscribeBits (transcription.h:43-118): the log_q-bit Montgomery
  * representations as one little-endian bit stream -- value i fills stream

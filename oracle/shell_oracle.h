@@ -110,6 +110,12 @@ void so_rns_mul_relin_batch(const so_rns* r, int L, const int* log_bs,
                             const uint64_t* key_b, const uint64_t* key_a,
                             uint64_t* out, int count, int threads);
 
+/* RnsGaloisKey with a precomputed random pad: ct [2][L][n] at the key's
+ * power, pad [k][L][n] = the NTT-form gadget digits of c1; out [2][L][n]. */
+void so_rns_galois_pad(const so_rns* r, int L, int k, const uint64_t* ct,
+                       const uint64_t* pad, const uint64_t* key_b, const uint64_t* key_a,
+                       uint64_t* out);
+
 /* ---- single-modulus key switching / oblivious expansion ------------------- */
 int so_gadget_size(const so_prime* p, int log_b);
 /* ApplyPartTo: (out0, out1) = sum_i NTT(digit_i(c)) * (k0[i], k1[i]).

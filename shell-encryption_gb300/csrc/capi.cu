@@ -1037,6 +1037,32 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,
                    (cudaStream_t)s);
 }
 
+int shg_galois_precompute_pad(shg_context* ctx, const shg_key* key, uint64_t* out,
+                              const uint64_t* pad_digits, int count, shg_stream s) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, pad_digits}))) return st;
+  shg::launch_pad_inner(ctx->dev(), out, pad_digits, key->ka, key->k, key->chunk, nullptr,
+                        nullptr, 0, count, key->L, (cudaStream_t)s);
+  return launch_status("galois_precompute_pad");
+}
+
+int shg_galois_apply_with_pad(shg_context* ctx, const shg_key* key, uint64_t* out,
+                              const uint64_t* ct, const uint64_t* pad_digits,
+                              const uint64_t* pad_new, int count, shg_stream s) {
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct, pad_digits, pad_new}))) return st;
+  if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
+  shg::launch_pad_inner(ctx->dev(), out, pad_digits, key->kb, key->k, key->chunk, ct, pad_new,
+                        1, count, key->L, (cudaStream_t)s);
+  return launch_status("galois_apply_with_pad");
+}
+
 int shg_bgv_rotate_multikey(shg_context* ctx, const shg_key* const* keys, uint64_t* out,
                             const uint64_t* ct, int count, shg_stream s) {
   if (count < 0) return fail(SHG_INVALID_ARGUMENT, "`count` must be non-negative.");

@@ -509,6 +509,46 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
   out[p * 2 * Ln + Ln + r] = add_mod(b1, s1, q);
 }
 
+// RnsGaloisKey with a precomputed random pad (rns/rns_galois_key.cc:289-346):
+// the digits pad [count][k][L][n] are Montgomery NTT polynomials, so the
+// products with the stored keys (premultiplied by 2^64) need one REDC per
+// chunk and one more for the Montgomery scaling: the lazy 128-bit sum of
+// LazyRnsPolynomial and its export give the same canonical value.
+// mode 0 (PrecomputeRandomPad): out [count][L][n] = sum_j pad_j * key_a_j.
+// mode 1 (ApplyToRlweCiphertextWithRandomPad): out [count][2][L][n] =
+// (c0 + sum_j pad_j * key_b_j, pad_new).
+__global__ void k_pad_inner(uint64_t* out, const uint64_t* pad, const uint64_t* key,
+                            int k, int chunk, const uint64_t* ct, const uint64_t* pad_new,
+                            int mode, int log_n, int L, CtxDev c) {
+  const int Ln = L << log_n;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= Ln) return;
+  const size_t p = blockIdx.y;
+  const int l = r >> log_n;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, qinv = P->inv_modulus;
+  const uint64_t* dp = pad + p * (size_t)k * Ln + r;
+  const uint64_t* kp = key + r;
+  uint64_t s = 0;
+  for (int j0 = 0; j0 < k; j0 += chunk) {
+    const int j1 = min(k, j0 + chunk);
+    uint64_t lo = 0, hi = 0;
+    for (int j = j0; j < j1; ++j) {
+      mac128(lo, hi, *dp, __ldg(kp));
+      dp += Ln;
+      kp += Ln;
+    }
+    s = add_mod(s, redc128(lo, hi, q, qinv), q);
+  }
+  s = redc128(s, 0, q, qinv);
+  if (mode == 0) {
+    out[p * Ln + r] = s;
+  } else {
+    out[p * 2 * Ln + r] = add_mod(ct[p * 2 * Ln + r], s, q);
+    out[p * 2 * Ln + Ln + r] = pad_new[p * Ln + r];
+  }
+}
+
 // RnsGadget::Decompose (rns/rns_gadget.cc:108-153) of coefficient-form
 // polys: digit d of limb i's exported residue (BaseDecompose, gadget.h:
 // 50-79), imported to limb i as is and to every other limb l through
@@ -1071,6 +1111,23 @@ void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
   LaunchScope scope_("modreduce_coeff", s);
   k_modreduce_coeff<<<grid_for(total, 256), 256, 0, s>>>(
       out, in, k_plain, k_shoup, sc, total, c.log_n, L, c);
+}
+
+void launch_pad_inner(const CtxDev& c, uint64_t* out, const uint64_t* pad,
+                      const uint64_t* key, int k, int chunk, const uint64_t* ct,
+                      const uint64_t* pad_new, int mode, int count, int L, cudaStream_t s) {
+  if (count <= 0) return;
+  LaunchScope scope_("pad_inner", s);
+  const int Ln = L << c.log_n;
+  for (int p0 = 0; p0 < count; p0 += 65535) {
+    const int cc = std::min(count - p0, 65535);
+    const dim3 grid((Ln + 255) / 256, cc);
+    const size_t o_out = (size_t)p0 * (mode == 0 ? 1 : 2) * Ln;
+    k_pad_inner<<<grid, 256, 0, s>>>(out + o_out, pad + (size_t)p0 * k * Ln, key, k, chunk,
+                                     ct ? ct + (size_t)p0 * 2 * Ln : nullptr,
+                                     pad_new ? pad_new + (size_t)p0 * Ln : nullptr, mode,
+                                     c.log_n, L, c);
+  }
 }
 
 void launch_decompose(const CtxDev& c, uint64_t* out, const uint64_t* in,

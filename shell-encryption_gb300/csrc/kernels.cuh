@@ -164,6 +164,13 @@ void launch_modreduce_coeff(const CtxDev& c, uint64_t* out, const uint64_t* in,
                             const ScalarPack& sc, int count, int L,
                             cudaStream_t s);
 
+// Galois key with a precomputed random pad: mode 0 out [count][L][n] =
+// sum_j pad_j * key_j (key = the stored key_a); mode 1 out [count][2][L][n] =
+// (c0 + sum_j pad_j * key_j, pad_new) (key = the stored key_b).
+void launch_pad_inner(const CtxDev& c, uint64_t* out, const uint64_t* pad,
+                      const uint64_t* key, int k, int chunk, const uint64_t* ct,
+                      const uint64_t* pad_new, int mode, int count, int L, cudaStream_t s);
+
 // RnsGadget::Decompose: in [count][L][n] coefficient form -> out
 // [count][k][L][n] coefficient form (k = sum_i GadgetSize(log q_i, log_b_i)).
 void launch_decompose(const CtxDev& c, uint64_t* out, const uint64_t* in,

@@ -693,6 +693,54 @@ StatusOr<RnsBgvCiphertext> RnsGaloisKey::ApplyTo(const RnsBgvCiphertext& ct) con
   return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
 }
 
+StatusOr<DeviceArray> RnsGaloisKey::PackDigits(
+    const std::vector<RnsPolynomial>& digits) const {
+  if (static_cast<int>(digits.size()) != Dimension())
+    return InvalidArgumentError("`ciphertext_pad_digits` has incorrect size");
+  const int L = static_cast<int>(moduli_.size());
+  const size_t poly = (size_t)L << moduli_[0]->Context()->LogN();
+  DeviceArray all(poly * digits.size());
+  for (size_t j = 0; j < digits.size(); ++j) {
+    if (digits[j].NumModuli() != L || !digits[j].IsNttForm())
+      return InvalidArgumentError("`ciphertext_pad_digits` must be in NTT form");
+    RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_memcpy_d2d(all.data() + j * poly,
+                                                     digits[j].device_data(),
+                                                     poly * sizeof(uint64_t), g_stream)));
+  }
+  return all;
+}
+
+StatusOr<RnsPolynomial> RnsGaloisKey::PrecomputeRandomPad(
+    const std::vector<RnsPolynomial>& ciphertext_pad_digits) const {
+  DeviceArray pad;
+  RLWE_GPU_ASSIGN_OR_RETURN(pad, PackDigits(ciphertext_pad_digits));
+  const int L = static_cast<int>(moduli_.size());
+  const int log_n = moduli_[0]->Context()->LogN();
+  DeviceArray out((size_t)L << log_n);
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_galois_precompute_pad(
+      ContextOf(moduli_), key_.get(), out.data(), pad.data(), 1, g_stream)));
+  return RnsPolynomial::FromDevice(std::move(out), log_n, L, true);
+}
+
+StatusOr<RnsBgvCiphertext> RnsGaloisKey::ApplyToWithRandomPad(
+    const RnsBgvCiphertext& ct, const std::vector<RnsPolynomial>& ciphertext_pad_digits,
+    const RnsPolynomial& ciphertext_pad_new) const {
+  // rns/rns_galois_key.cc:313-330
+  if (ct.PowerOfS() != power_)
+    return InvalidArgumentError("`ciphertext` does not have a matching substitution power.");
+  if (ct.NumModuli() != static_cast<int>(moduli_.size()))
+    return InvalidArgumentError("`ciphertext` does not have a matching RNS moduli set.");
+  if (ct.Degree() > 1)
+    return InvalidArgumentError("Galois key can only apply to a ciphertext of degree 1.");
+  DeviceArray pad;
+  RLWE_GPU_ASSIGN_OR_RETURN(pad, PackDigits(ciphertext_pad_digits));
+  DeviceArray out(2 * ct.component_elems());
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_galois_apply_with_pad(
+      ContextOf(moduli_), key_.get(), out.data(), ct.device_data(), pad.data(),
+      ciphertext_pad_new.device_data(), 1, g_stream)));
+  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
+}
+
 // ---------------------------------------------------------------------------
 // Single modulus
 // ---------------------------------------------------------------------------

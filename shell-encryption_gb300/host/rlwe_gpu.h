@@ -364,11 +364,23 @@ class RnsGaloisKey {
   // ApplyTo on a ciphertext whose power of s equals the key's
   // (rns/rns_galois_key.h:146-156, .cc:238-287).
   StatusOr<RnsBgvCiphertext> ApplyTo(const RnsBgvCiphertext& ciphertext) const;
+  // PrecomputeRandomPad(ciphertext_pad_digits) (rns/rns_galois_key.cc:
+  // 289-306): the key-switched "a" part from the NTT-form gadget digits of a
+  // ciphertext's c1.
+  StatusOr<RnsPolynomial> PrecomputeRandomPad(
+      const std::vector<RnsPolynomial>& ciphertext_pad_digits) const;
+  // ApplyToWithRandomPad(ciphertext, pad digits, pad_new)
+  // (rns/rns_galois_key.h:177-192).
+  StatusOr<RnsBgvCiphertext> ApplyToWithRandomPad(
+      const RnsBgvCiphertext& ciphertext,
+      const std::vector<RnsPolynomial>& ciphertext_pad_digits,
+      const RnsPolynomial& ciphertext_pad_new) const;
   int SubstitutionPower() const { return power_; }
   int Dimension() const;
   shg_key* handle() const { return key_.get(); }
 
  private:
+  StatusOr<DeviceArray> PackDigits(const std::vector<RnsPolynomial>& digits) const;
   std::shared_ptr<shg_key> key_;
   Moduli moduli_;
   int power_ = 1;

@@ -63,6 +63,8 @@ SIGNATURES = {
     "shg_relin_apply_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_galois_apply": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_galois_precompute_pad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_galois_apply_with_pad": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_bgv_mul_relin_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp, _vp, _vp,
                                                   ctypes.c_int, _vp]),
     "shg_bgv_rotate_multikey": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp, _vp, ctypes.c_int,

@@ -288,6 +288,31 @@ void TestGadgetAndKeys(int log_n, const std::vector<uint64_t>& qs, std::vector<i
   so_rns_galois(orc, L, log_bs.data(), sc.data(), kb.data(), ka.data(), wr.data());
   EXPECT(rot.PowerOfS() == 1 && FlatCt(rot) == wr, "RnsGaloisKey::ApplyTo");
 
+  // Random-pad path (rns_galois_key.cc:289-346): pad digits = NTT-form
+  // gadget digits of the substituted ciphertext's c1.
+  {
+    RnsPolynomial c1;
+    ASSERT_OK_AND_ASSIGN(c1, sub.Component(1));
+    EXPECT_OK(c1.ConvertToCoeffForm(moduli));
+    std::vector<RnsPolynomial> pad_digits;
+    ASSERT_OK_AND_ASSIGN(pad_digits, gadget.Decompose(c1, moduli));
+    for (auto& d : pad_digits) EXPECT_OK(d.ConvertToNttForm(moduli));
+    RnsPolynomial pad_new;
+    ASSERT_OK_AND_ASSIGN(pad_new, galois.PrecomputeRandomPad(pad_digits));
+    RnsBgvCiphertext padded = sub;
+    ASSERT_OK_AND_ASSIGN(padded, galois.ApplyToWithRandomPad(sub, pad_digits, pad_new));
+    std::vector<uint64_t> flat_pad;
+    for (auto& d : pad_digits) {
+      auto f = Flat(d.Coeffs());
+      flat_pad.insert(flat_pad.end(), f.begin(), f.end());
+    }
+    std::vector<uint64_t> wp((size_t)2 * L * n);
+    so_rns_galois_pad(orc, L, k, sc.data(), flat_pad.data(), kb.data(), ka.data(), wp.data());
+    EXPECT(FlatCt(padded) == wp, "ApplyToWithRandomPad equals the oracle");
+    // with the pad being c1's own digits, the result is the plain key switch
+    EXPECT(FlatCt(padded) == wr, "random-pad key switch equals ApplyTo");
+  }
+
   // ModReduce drops the top prime of every component.
   if (L > 1) {
     std::vector<uint64_t> ql_inv;

@@ -81,6 +81,20 @@ def main():
         power = 5
         g[rtag + "_power"] = np.array([power], np.int32)
         g[rtag + "_out"] = R.bgv_rotate(log_n, qs, log_bs, power, kb, ka, a)
+    # RnsGaloisKey::PrecomputeRandomPad + ApplyToWithRandomPad.
+    for log_n, qs, log_bs in [(6, Q45[:2], [20, 20]), (9, Q50[:3], [50, 16, 20])]:
+        tag = f"galoispad_{log_n}_{len(qs)}"
+        n, L = 1 << log_n, len(qs)
+        k = O.Rns(log_n, qs).gadget_dim(log_bs)
+        kb = O.uniform_limbs(6000 + log_n, qs, n, k)
+        ka = O.uniform_limbs(6100 + log_n, qs, n, k)
+        ct = O.uniform_limbs(6200 + log_n, qs, n, 4).reshape(2, 2, L, n)
+        pad = O.uniform_limbs(6300 + log_n, qs, n, 2 * k).reshape(2, k, L, n)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_log_bs"] = np.array(log_bs, np.int32)
+        for nm, v in (("kb", kb), ("ka", ka), ("ct", ct), ("pad", pad)):
+            g[f"{tag}_{nm}"] = v
+        g[tag + "_out"] = R.galois_random_pad(log_n, qs, log_bs, 5, kb, ka, ct, pad)
     # Oblivious expansion (n = 128, 60-bit q, base 2^10, 3 levels).
     q, log_n, levels, log_b = Q60, 7, 3, 10
     n = 1 << log_n

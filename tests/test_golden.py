@@ -321,3 +321,42 @@ def test_oracle_serialization_golden(oracle, q):
     p = oracle.Prime(int(q), 1)
     assert np.array_equal(p.serialize(v), want)
     assert np.array_equal(p.deserialize(want, v.size), v)
+
+
+PAD_TAGS = sorted({k[:-len("_out")] for k in SMALL.files
+                   if k.startswith("galoispad_") and k.endswith("_out")})
+
+
+@pytest.mark.parametrize("tag", PAD_TAGS)
+def test_oracle_galois_random_pad_golden(oracle, tag):
+    """RnsGaloisKey::PrecomputeRandomPad + ApplyToWithRandomPad of the reference."""
+    _, log_n, _ = tag.split("_")
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    rns = oracle.Rns(int(log_n), qs)
+    ct, pad = SMALL[tag + "_ct"], SMALL[tag + "_pad"]
+    got = np.stack([rns.galois_pad(ct[i], pad[i], SMALL[tag + "_kb"], SMALL[tag + "_ka"])
+                    for i in range(ct.shape[0])])
+    assert np.array_equal(got, SMALL[tag + "_out"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", PAD_TAGS)
+def test_gpu_galois_random_pad_golden(sg, tag):
+    """Device PrecomputeRandomPad + ApplyToWithRandomPad against the reference."""
+    _, log_n, _ = tag.split("_")
+    log_n = int(log_n)
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    lib = sg.lib()
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, [int(b) for b in SMALL[tag + "_log_bs"]], 5, SMALL[tag + "_kb"],
+                 SMALL[tag + "_ka"])
+    ct, pad, want = SMALL[tag + "_ct"], SMALL[tag + "_pad"], SMALL[tag + "_out"]
+    count, L, n = ct.shape[0], ct.shape[2], ct.shape[3]
+    dct, dpad = sg.DeviceBuffer.from_array(ct), sg.DeviceBuffer.from_array(pad)
+    dnew = sg.DeviceBuffer(count * L * n * 8)
+    sg.check(lib.shg_galois_precompute_pad(ctx.h, key.h, dnew.ptr, dpad.ptr, count, None))
+    out = sg.DeviceBuffer(want.nbytes)
+    sg.check(lib.shg_galois_apply_with_pad(ctx.h, key.h, out.ptr, dct.ptr, dpad.ptr, dnew.ptr,
+                                           count, None))
+    sg.synchronize()
+    assert np.array_equal(out.download(want.shape), want)
