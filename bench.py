@@ -1158,10 +1158,13 @@ def main():
     bit_exact = bool(np.array_equal(out_graph, out_plain))
 
     # Dominant kernel timing (live CUDA events on the launch stream) for the
-    # roofline: one more batched step with per-launch events.
+    # roofline: one more batched step with per-launch events, its chunks on
+    # one stream so the kernels' event intervals do not overlap.
+    sg.check(lib.shg_context_set_ks_lanes(ctx.h, 1))
     sg.check(lib.shg_profile_start())
     step_device()
     sg.check(lib.shg_profile_stop())
+    sg.check(lib.shg_context_set_ks_lanes(ctx.h, 2))
     prof = {}
     for name in SCOPES:
         ms, cnt = ctypes.c_double(), ctypes.c_uint64()

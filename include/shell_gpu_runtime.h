@@ -69,6 +69,10 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n);
  * inner product as one kernel; 0: separate row phase, digit NTTs written to
  * scratch, then the inner product.  Results are identical. */
 int shg_context_set_ks_fused(shg_context* ctx, int on);
+/* Streams the chunks of a batched ct-mult+relin alternate over (2 = default:
+ * the caller's stream and a second one, so one chunk fills the other's tail;
+ * 1 = the caller's stream only, e.g. to time kernels one at a time). */
+int shg_context_set_ks_lanes(shg_context* ctx, int lanes);
 /* shg_bgv_mul_relin_host pipeline shape: ciphertexts per piece (default 128)
  * and device staging slots in flight (default 4, at most 8). */
 int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots);

@@ -176,6 +176,7 @@ struct shg_context {
   int ntt4_min = 13;  // four-step transforms from this log_n up (measured faster
                       // for every operation from n = 2^13; mixed at 2^12)
   int ks_fused = 1;   // fused digit row phase + key inner product
+  int ks_lanes = 2;      // streams the batched key-switch chunks alternate over
   int host_piece = 128;  // host pipeline: ciphertexts per piece
   int host_slots = 4;    // host pipeline: device staging slots in flight
   std::mutex mu;
@@ -183,6 +184,10 @@ struct shg_context {
   uint64_t* io = nullptr;
   size_t io_bytes = 0;
   cudaStream_t io_streams[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Second stream of the batched key switch (chunks alternate between the
+  // caller's stream and this one) with its fork / join events.
+  cudaStream_t ks_side = nullptr;
+  cudaEvent_t ks_fork = nullptr, ks_join = nullptr;
   std::mutex io_mu;
 
   CtxDev dev() const {
@@ -373,6 +378,9 @@ void shg_context_destroy(shg_context* ctx) {
   cudaFree(ctx->io);
   for (cudaStream_t s : ctx->io_streams)
     if (s) cudaStreamDestroy(s);
+  if (ctx->ks_side) cudaStreamDestroy(ctx->ks_side);
+  if (ctx->ks_fork) cudaEventDestroy(ctx->ks_fork);
+  if (ctx->ks_join) cudaEventDestroy(ctx->ks_join);
   delete ctx;
 }
 
@@ -834,25 +842,48 @@ int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* k
   C = std::max(1, std::min(C, count));
   const size_t tab_bytes = keys ? 2 * (size_t)count * sizeof(void*) : 0;
   std::lock_guard<std::mutex> lock(ctx->mu);
-  if ((st = ctx->ensure_ws(x_bytes + d_per_ct * C + tab_bytes))) return st;
+  // Chunks alternate between the caller's stream and a second one, each with
+  // its own digit scratch, so one chunk's kernels fill the other's tail.  The
+  // second stream is created outside any stream capture (the first call).
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  SHG_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (!ctx->ks_side && cap == cudaStreamCaptureStatusNone) {
+    SHG_CUDA(cudaStreamCreateWithFlags(&ctx->ks_side, cudaStreamNonBlocking));
+    SHG_CUDA(cudaEventCreateWithFlags(&ctx->ks_fork, cudaEventDisableTiming));
+    SHG_CUDA(cudaEventCreateWithFlags(&ctx->ks_join, cudaEventDisableTiming));
+  }
+  const int nchunks = (count + C - 1) / C;
+  const int lanes = (ctx->ks_side && nchunks > 1 && ctx->ks_lanes > 1) ? 2 : 1;
+  if ((st = ctx->ensure_ws(x_bytes + lanes * d_per_ct * C + tab_bytes))) return st;
   uint64_t* X = ctx->ws;
-  uint64_t* D = X + (size_t)count * Ln;
+  uint64_t* D0 = X + (size_t)count * Ln;
+  uint64_t* D1 = D0 + (size_t)C * k * Ln;
   shg::KeyTable kt;
   if (keys &&
       (st = upload_key_table(keys, count, 1, 0,
-                             reinterpret_cast<const uint64_t**>(D + (size_t)C * k * Ln),
+                             reinterpret_cast<const uint64_t**>(D0 + (size_t)lanes * C * k * Ln),
                              &kt, s)))
     return st;
   const CtxDev dv = ctx->dev();
   shg::launch_tensor_intt(dv, out, X, a, b, count, L, s);
-  for (int c0 = 0; c0 < count; c0 += C) {
-    const int cc = std::min(C, count - c0);
+  if (lanes == 2) {
+    SHG_CUDA(cudaEventRecord(ctx->ks_fork, s));
+    SHG_CUDA(cudaStreamWaitEvent(ctx->ks_side, ctx->ks_fork, 0));
+  }
+  for (int i = 0; i < nchunks; ++i) {
+    const int c0 = i * C, cc = std::min(C, count - c0);
+    const bool side = lanes == 2 && (i & 1);
     uint64_t* o = out + (size_t)c0 * 2 * Ln;
     shg::KeyTable kc;
     if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0};
-    shg::launch_keyswitch(dv, D, X + (size_t)c0 * Ln, key->d_digits, k,
+    shg::launch_keyswitch(dv, side ? D1 : D0, X + (size_t)c0 * Ln, key->d_digits, k,
                           key->need_lift, key->chunk, key->kb, key->ka, o, o,
-                          2 * Ln, CtMap::identity(), 0, 0, cc, L, s, kc);
+                          2 * Ln, CtMap::identity(), 0, 0, cc, L, side ? ctx->ks_side : s,
+                          kc);
+  }
+  if (lanes == 2) {
+    SHG_CUDA(cudaEventRecord(ctx->ks_join, ctx->ks_side));
+    SHG_CUDA(cudaStreamWaitEvent(s, ctx->ks_join, 0));
   }
   return launch_status("bgv_mul_relin");
 }
@@ -1585,6 +1616,12 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
   if (!ctx || log_n < 12 || log_n > 16)
     return fail(SHG_INVALID_ARGUMENT, "four-step threshold must lie in [12, 16]");
   ctx->ntt4_min = log_n;
+  return SHG_OK;
+}
+int shg_context_set_ks_lanes(shg_context* ctx, int lanes) {
+  if (!ctx || lanes < 1 || lanes > 2)
+    return fail(SHG_INVALID_ARGUMENT, "key-switch lanes must be 1 or 2");
+  ctx->ks_lanes = lanes;
   return SHG_OK;
 }
 int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots) {
