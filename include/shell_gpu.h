@@ -279,6 +279,31 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,
                    const uint64_t* ct, int count, shg_stream stream);
 
 /* ---------------------------------------------------------------------------
+ * Encryption randomness from SHELL's ChaCha PRNG, sampled on the device.
+ * Ciphertext c uses the stream of SingleThreadChaChaPrng::Create(seed)
+ * (prng/single_thread_chacha_prng.h:35-80, prng/chacha_prng_util.cc:30-98)
+ * with seed = seeds[32c .. 32c+31] (device bytes), so results equal the
+ * reference's for the same seeds.
+ * ------------------------------------------------------------------------- */
+
+/* RnsPolynomial::SampleUniform (rns/rns_polynomial.h:74-77, 638-667) then
+ * SampleError (rns/error_distribution.h:40-60) from one stream per seed:
+ * a, e [count][num_limbs][n], both NTT form.  1 <= variance <= 256. */
+int shg_sample_uniform_error(shg_context* ctx, uint64_t* a, uint64_t* e,
+                             const uint8_t* seeds, int num_limbs, int count, int variance,
+                             shg_stream stream);
+
+/* RnsRlweSecretKey::EncryptPolynomialBgv (rns/rns_secret_key.h:70-74,
+ * 188-231) for `count` plaintexts, the PRNG of ciphertext c seeded with
+ * seeds[c]: key s [num_limbs][n], plaintexts m [count][num_limbs][n] (NTT
+ * form) -> out [count][2][num_limbs][n] = (e * t + m + a * s, -a) with a, e
+ * as shg_sample_uniform_error draws them and t the context's plaintext
+ * modulus.  1 <= variance <= 256. */
+int shg_bgv_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* key,
+                    const uint64_t* plaintexts, const uint8_t* seeds, int num_limbs,
+                    int count, int variance, shg_stream stream);
+
+/* ---------------------------------------------------------------------------
  * Single-modulus symmetric RLWE, on a one-prime context (t = the context's
  * plaintext modulus)
  * ------------------------------------------------------------------------- */

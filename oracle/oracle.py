@@ -78,6 +78,14 @@ def lib():
                                              ctypes.c_size_t, U64P]),
             "so_rns_galois_pad": (None, [vp, ctypes.c_int, ctypes.c_int, U64P, U64P, U64P, U64P,
                                          U64P]),
+            "so_chacha20_block": (None, [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_char_p,
+                                         ctypes.POINTER(ctypes.c_uint8)]),
+            "so_prng_bytes": (None, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_size_t,
+                                     ctypes.POINTER(ctypes.c_uint8)]),
+            "so_rns_sample_uniform_error": (None, [vp, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_char_p, U64P, U64P]),
+            "so_rns_encrypt_bgv": (None, [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, U64P,
+                                          U64P, ctypes.c_char_p, U64P]),
             "so_sym_encrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, U64P, U64P, U64P]),
             "so_sym_decrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, ctypes.c_int, U64P]),
             "so_compute_normalizer": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int]),
@@ -374,6 +382,23 @@ class Rns:
                                 _p(np.ascontiguousarray(key_a, dtype=np.uint64)), _p(out))
         return out
 
+    def sample_uniform_error(self, L, variance, seed):
+        """SampleUniform then SampleError from the ChaCha PRNG of `seed`."""
+        a = np.empty((L, self.n), np.uint64)
+        e = np.empty((L, self.n), np.uint64)
+        lib().so_rns_sample_uniform_error(self._h, L, variance, bytes(seed), _p(a), _p(e))
+        return a, e
+
+    def encrypt_bgv(self, t, variance, key, m, seed):
+        """RnsRlweSecretKey::EncryptPolynomialBgv with the PRNG of `seed`."""
+        key = np.ascontiguousarray(key, dtype=np.uint64)
+        m = np.ascontiguousarray(m, dtype=np.uint64)
+        L = m.shape[0]
+        out = np.empty((2, L, self.n), np.uint64)
+        lib().so_rns_encrypt_bgv(self._h, L, ctypes.c_uint64(int(t)), variance, _p(key), _p(m),
+                                 bytes(seed), _p(out))
+        return out
+
     def modreduce_lsb(self, poly, t, is_ntt=True):
         poly = np.ascontiguousarray(poly, dtype=np.uint64)
         L = poly.shape[0]
@@ -424,3 +449,18 @@ def uniform_limbs(seed, qs, n, count=1):
     raw = splitmix64(seed, count * L * n).reshape(count, L, n)
     q = np.array([int(x) for x in qs], dtype=np.uint64).reshape(1, L, 1)
     return raw % q
+
+
+def prng_bytes(seed, start, count):
+    """Bytes [start, start + count) of SHELL's ChaChaPrng stream of a 32-byte seed."""
+    out = np.empty(count, np.uint8)
+    lib().so_prng_bytes(bytes(seed), start, count, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return out
+
+
+def chacha20_block(key, counter, nonce):
+    """One RFC 7539 ChaCha20 keystream block."""
+    out = np.empty(64, np.uint8)
+    lib().so_chacha20_block(bytes(key), counter, bytes(nonce),
+                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return out.tobytes()

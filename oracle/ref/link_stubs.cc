@@ -1,6 +1,8 @@
-// Test infrastructure: link-time stand-ins for the reference's PRNG seed
-// generators.  They are referenced only by key-generation paths, which the
-// driver never calls (keys are passed in as data), so they report an error.
+// Test infrastructure: link-time stand-ins for the reference's HKDF PRNG seed
+// generator and PRNG (referenced only by key-generation paths the driver never
+// calls), which report an error.  The ChaCha PRNG is the reference's own code
+// (prng/single_thread_chacha_prng.cc, prng/chacha_prng_util.cc) over the
+// ChaCha20 stand-in of openssl_standin.cc.
 #include <string>
 
 #include "absl/status/status.h"
@@ -9,9 +11,6 @@
 namespace rlwe {
 namespace internal {
 absl::StatusOr<std::string> HkdfPrngGenerateKey() {
-  return absl::UnimplementedError("PRNG seeding is not built into the oracle");
-}
-absl::StatusOr<std::string> ChaChaPrngGenerateKey() {
   return absl::UnimplementedError("PRNG seeding is not built into the oracle");
 }
 }  // namespace internal
@@ -30,10 +29,6 @@ absl::StatusOr<std::string> ChaChaPrngGenerateKey() {
 namespace rlwe {
 
 absl::StatusOr<std::unique_ptr<SingleThreadHkdfPrng>> SingleThreadHkdfPrng::Create(
-    absl::string_view) {
-  return absl::UnimplementedError("PRNG seeding is not built into the oracle");
-}
-absl::StatusOr<std::unique_ptr<SingleThreadChaChaPrng>> SingleThreadChaChaPrng::Create(
     absl::string_view) {
   return absl::UnimplementedError("PRNG seeding is not built into the oracle");
 }

@@ -56,6 +56,9 @@
 #include "shell_encryption/rns/rns_galois_key.h"
 #include "shell_encryption/rns/rns_polynomial.h"
 #include "shell_encryption/rns/rns_relinearization_key.h"
+#include "shell_encryption/rns/rns_secret_key.h"
+#include "shell_encryption/rns/error_distribution.h"
+#include "shell_encryption/prng/single_thread_chacha_prng.h"
 #include "shell_encryption/symmetric_encryption.h"
 #undef private
 #undef protected
@@ -372,6 +375,74 @@ int ref_galois_random_pad(int log_n, const uint64_t* qs, int L, const int* log_b
     if (!r.ok()) return fail(r.status());
     for (int i = 0; i < 2; ++i)
       store_poly(r->Component(i).value(), out + ((size_t)c * 2 + i) * P);
+  }
+  return 0;
+}
+
+// The first `count` bytes (Rand8) of SingleThreadChaChaPrng::Create(seed).
+int ref_prng_bytes(const uint8_t* seed, int count, uint8_t* out) {
+  auto prng = rlwe::SingleThreadChaChaPrng::Create(
+      std::string(reinterpret_cast<const char*>(seed), 32));
+  if (!prng.ok()) return fail(prng.status());
+  for (int i = 0; i < count; ++i) {
+    auto b = (*prng)->Rand8();
+    if (!b.ok()) return fail(b.status());
+    out[i] = *b;
+  }
+  return 0;
+}
+
+// RnsPolynomial::SampleUniform then SampleError (rns/error_distribution.h)
+// from one ChaCha PRNG of `seed`, as EncryptPolynomialBgv draws them;
+// a_out, e_out [L][n] NTT form.
+int ref_sample_uniform_error(int log_n, const uint64_t* qs, int L, int variance,
+                             const uint8_t* seed, uint64_t* a_out, uint64_t* e_out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  auto moduli = ctx->MainPrimeModuli();
+  auto prng = rlwe::SingleThreadChaChaPrng::Create(
+      std::string(reinterpret_cast<const char*>(seed), 32));
+  if (!prng.ok()) return fail(prng.status());
+  auto a = rlwe::RnsPolynomial<M>::SampleUniform(log_n, prng->get(), moduli);
+  if (!a.ok()) return fail(a.status());
+  auto e = rlwe::SampleError<M>(log_n, variance, moduli, prng->get());
+  if (!e.ok()) return fail(e.status());
+  store_poly(*a, a_out);
+  store_poly(*e, e_out);
+  return 0;
+}
+
+struct PlainModulus {
+  uint64_t t;
+  uint64_t PlaintextModulus() const { return t; }
+};
+
+// RnsRlweSecretKey::EncryptPolynomialBgv (rns/rns_secret_key.h:188-231) of
+// `count` NTT-form plaintexts, ciphertext c drawing its randomness from the
+// ChaCha PRNG of seeds + 32 c: out [count][2][L][n].
+int ref_encrypt_bgv(int log_n, const uint64_t* qs, int L, uint64_t t, int variance,
+                    const uint64_t* key, const uint64_t* plaintexts, const uint8_t* seeds,
+                    int count, uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, t, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  rlwe::RnsRlweSecretKey<M> sk(make_poly(key, L, n, true), moduli, variance);
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, {}, 16, 3.19);
+  if (!ep.ok()) return fail(ep.status());
+  PlainModulus enc{t};
+  for (int c = 0; c < count; ++c) {
+    auto prng = rlwe::SingleThreadChaChaPrng::Create(
+        std::string(reinterpret_cast<const char*>(seeds + 32 * c), 32));
+    if (!prng.ok()) return fail(prng.status());
+    auto ct = sk.EncryptPolynomialBgv(make_poly(plaintexts + (size_t)c * P, L, n, true), &enc,
+                                      &*ep, prng->get());
+    if (!ct.ok()) return fail(ct.status());
+    for (int i = 0; i < 2; ++i)
+      store_poly(ct->Component(i).value(), out + ((size_t)c * 2 + i) * P);
   }
   return 0;
 }

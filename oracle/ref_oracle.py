@@ -47,6 +47,12 @@ def lib():
                                              ctypes.c_size_t, ctypes.c_int, _U64P]
         L.ref_galois_random_pad.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _IP, ctypes.c_int,
                                             _U64P, _U64P, _U64P, _U64P, ctypes.c_int, _U64P]
+        L.ref_prng_bytes.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]
+        L.ref_sample_uniform_error.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_char_p, _U64P, _U64P]
+        L.ref_encrypt_bgv.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.c_int, _U64P, _U64P, ctypes.c_char_p, ctypes.c_int,
+                                      _U64P]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -173,4 +179,35 @@ def galois_random_pad(log_n, qs, log_bs, power, key_b, key_a, cts, pad_digits):
                                        _p(cts), _p(np.ascontiguousarray(pad_digits,
                                                                          dtype=np.uint64)),
                                        count, _p(out)))
+    return out
+
+
+def prng_bytes(seed, count):
+    """The first `count` Rand8 outputs of SingleThreadChaChaPrng::Create(seed)."""
+    out = np.empty(count, np.uint8)
+    _check(lib().ref_prng_bytes(bytes(seed), count,
+                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+    return out
+
+
+def sample_uniform_error(log_n, qs, variance, seed):
+    """RnsPolynomial::SampleUniform then SampleError from one ChaCha PRNG."""
+    q = _qs(qs)
+    L, n = len(q), 1 << log_n
+    a = np.empty((L, n), np.uint64)
+    e = np.empty((L, n), np.uint64)
+    _check(lib().ref_sample_uniform_error(log_n, _p(q), L, variance, bytes(seed), _p(a), _p(e)))
+    return a, e
+
+
+def encrypt_bgv(log_n, qs, t, variance, key, plaintexts, seeds):
+    """RnsRlweSecretKey::EncryptPolynomialBgv, ciphertext c from seeds[c]."""
+    q = _qs(qs)
+    L, n = len(q), 1 << log_n
+    plaintexts = np.ascontiguousarray(plaintexts, dtype=np.uint64)
+    count = plaintexts.shape[0]
+    out = np.empty((count, 2, L, n), np.uint64)
+    _check(lib().ref_encrypt_bgv(log_n, _p(q), L, t, variance,
+                                 _p(np.ascontiguousarray(key, dtype=np.uint64)), _p(plaintexts),
+                                 b"".join(bytes(s) for s in seeds), count, _p(out)))
     return out

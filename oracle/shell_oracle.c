@@ -5,6 +5,7 @@
  * check and the benchmark's CPU-baseline leg use it.
  */
 #include "shell_oracle.h"
+#include "chacha20.h"
 
 #include <pthread.h>
 #include <stdlib.h>
@@ -823,6 +824,128 @@ void so_rns_galois_pad(const so_rns* r, int L, int k, const uint64_t* ct,
       so_fma(p, out + (size_t)l * n, pad + o, key_b + o, n);
       so_fma(p, out + P + (size_t)l * n, pad + o, key_a + o, n);
     }
+}
+
+/* ---- ChaCha PRNG, samplers and BGV encryption -------------------------- */
+
+/* One ChaCha20 keystream block (RFC 7539 section 2.3.2). */
+void so_chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                       uint8_t out[64]) {
+  shg_chacha20_block(key, counter, nonce, out);
+}
+
+void so_prng_bytes(const uint8_t seed[32], uint64_t start, size_t len, uint8_t* out) {
+  shg_chacha_prng_bytes(seed, start, len, out);
+}
+
+static uint64_t prng_rand64(const uint8_t seed[32], uint64_t* pos) {
+  uint8_t b[8];
+  shg_chacha_prng_bytes(seed, *pos, 8, b);
+  *pos += 8;
+  uint64_t v = 0;
+  for (int i = 0; i < 8; i++) v |= (uint64_t)b[i] << (8 * i);
+  return v;
+}
+
+static uint8_t prng_rand8(const uint8_t seed[32], uint64_t* pos) {
+  uint8_t b;
+  shg_chacha_prng_bytes(seed, *pos, 1, &b);
+  *pos += 1;
+  return b;
+}
+
+static int popcount64(uint64_t x) {
+  int c = 0;
+  while (x) {
+    x &= x - 1;
+    c++;
+  }
+  return c;
+}
+
+/* RnsPolynomial::SampleUniform (rns/rns_polynomial.h:638-667): limb by limb,
+ * each coefficient the first 8-byte candidate (Rand64, masked to log q bits)
+ * below q (MontgomeryInt::ImportRandom, montgomery.h:261-272, 629-655); the
+ * value is taken as the Montgomery representation.  Then SampleError
+ * (rns/error_distribution.h:40-60): centred binomial coefficients of
+ * variance `variance` mod q_0 (SampleFromErrorDistribution,
+ * sample_error.h:43-100), lifted balanced to every limb and put in NTT form.
+ * Both from the PRNG stream of `seed` starting at *pos. */
+static void sample_uniform_error(const so_rns* r, int L, int variance, const uint8_t seed[32],
+                                 uint64_t* pos, uint64_t* a, uint64_t* e) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int l = 0; l < L; l++) {
+    const so_prime* p = r->primes[l];
+    const uint64_t mask = p->log_q >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << p->log_q) - 1);
+    for (size_t j = 0; j < n; j++) {
+      uint64_t v;
+      do {
+        v = prng_rand64(seed, pos) & mask;
+      } while (v >= p->q);
+      a[(size_t)l * n + j] = v;
+    }
+  }
+  const so_prime* p0 = r->primes[0];
+  for (size_t j = 0; j < n; j++) {
+    uint64_t c = p0->q;
+    int k = 2 * variance;
+    while (k > 0) {
+      if (k >= 64) {
+        c += popcount64(prng_rand64(seed, pos));
+        c -= popcount64(prng_rand64(seed, pos));
+        k -= 64;
+      } else if (k >= 8) {
+        c += popcount64(prng_rand8(seed, pos));
+        c -= popcount64(prng_rand8(seed, pos));
+        k -= 8;
+      } else {
+        const uint8_t m = (uint8_t)((1u << k) - 1);
+        c += popcount64(prng_rand8(seed, pos) & m);
+        c -= popcount64(prng_rand8(seed, pos) & m);
+        break;
+      }
+    }
+    if (c >= p0->q) c -= p0->q;
+    /* ConvertModulusBalanced (modulus_conversion.h:30-157) of c (mod q0) */
+    for (int l = 0; l < L; l++) {
+      const so_prime* p = r->primes[l];
+      uint64_t v;
+      if (c > (p0->q >> 1))
+        v = p->q - ((p0->q - c) % p->q);
+      else
+        v = c % p->q;
+      if (v == p->q) v = 0;
+      e[(size_t)l * n + j] = mont_import(p, v);
+    }
+  }
+  for (int l = 0; l < L; l++) so_ntt_fwd(r->primes[l], e + (size_t)l * n);
+}
+
+void so_rns_sample_uniform_error(const so_rns* r, int L, int variance, const uint8_t seed[32],
+                                 uint64_t* a, uint64_t* e) {
+  uint64_t pos = 0;
+  sample_uniform_error(r, L, variance, seed, &pos, a, e);
+}
+
+/* RnsRlweSecretKey::EncryptPolynomialBgv (rns/rns_secret_key.h:188-231):
+ * a, e drawn from the PRNG of `seed`, c0 = e * t + m + a * s, c1 = -a.
+ * key, m [L][n] NTT form; out [2][L][n]. */
+void so_rns_encrypt_bgv(const so_rns* r, int L, uint64_t t, int variance, const uint64_t* key,
+                        const uint64_t* m, const uint8_t seed[32], uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n, P = (size_t)L * n;
+  uint64_t* a = (uint64_t*)malloc(P * sizeof(uint64_t));
+  uint64_t pos = 0;
+  sample_uniform_error(r, L, variance, seed, &pos, a, out);
+  for (int l = 0; l < L; l++) {
+    const so_prime* p = r->primes[l];
+    const uint64_t tm = mont_import(p, t % p->q);
+    uint64_t* c0 = out + (size_t)l * n;
+    for (size_t j = 0; j < n; j++) c0[j] = mont_mul(p, c0[j], tm);
+    so_add(p, c0, m + (size_t)l * n, c0, n);
+    so_fma(p, c0, a + (size_t)l * n, key + (size_t)l * n, n);
+    so_neg(p, a + (size_t)l * n, out + P + (size_t)l * n, n);
+  }
+  free(a);
 }
 
 /* MontgomeryInt::SerializeVector (montgomery.cc:142-166) through

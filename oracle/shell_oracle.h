@@ -110,6 +110,17 @@ void so_rns_mul_relin_batch(const so_rns* r, int L, const int* log_bs,
                             const uint64_t* key_b, const uint64_t* key_a,
                             uint64_t* out, int count, int threads);
 
+/* ChaChaPrng stream bytes [start, start + len) of a 32-byte seed. */
+void so_chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                       uint8_t out[64]);
+void so_prng_bytes(const uint8_t seed[32], uint64_t start, size_t len, uint8_t* out);
+/* SampleUniform then SampleError from the PRNG of seed: a, e [L][n] NTT. */
+void so_rns_sample_uniform_error(const so_rns* r, int L, int variance, const uint8_t seed[32],
+                                 uint64_t* a, uint64_t* e);
+/* EncryptPolynomialBgv: key, m [L][n] NTT; out [2][L][n]. */
+void so_rns_encrypt_bgv(const so_rns* r, int L, uint64_t t, int variance, const uint64_t* key,
+                        const uint64_t* m, const uint8_t seed[32], uint64_t* out);
+
 /* RnsGaloisKey with a precomputed random pad: ct [2][L][n] at the key's
  * power, pad [k][L][n] = the NTT-form gadget digits of c1; out [2][L][n]. */
 void so_rns_galois_pad(const so_rns* r, int L, int k, const uint64_t* ct,

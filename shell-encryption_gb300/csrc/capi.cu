@@ -1649,6 +1649,82 @@ int shg_poly_fill_uniform(shg_context* ctx, uint64_t* polys, int count, int num_
   shg::launch_fill_uniform(ctx->dev(), polys, seed, count, num_limbs, (cudaStream_t)s);
   return launch_status("fill_uniform");
 }
+// SampleError's variance bounds (rns/error_distribution.h:44-49,
+// sample_error.h:47-50, kMaxVariance = 256 in constants.h).
+static int check_variance(int variance) {
+  if (variance <= 0) return fail(SHG_INVALID_ARGUMENT, "`variance` must be positive.");
+  if (variance > 256)
+    return fail(SHG_INVALID_ARGUMENT, "The variance, " + std::to_string(variance) +
+                                          ", must be at most 256.");
+  return SHG_OK;
+}
+
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int shg_sample_uniform_error(shg_context* ctx, uint64_t* a, uint64_t* e,
+                             const uint8_t* seeds, int num_limbs, int count, int variance,
+                             shg_stream stream) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if ((st = check_variance(variance))) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({a, e, seeds}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = num_limbs;
+  const size_t Ln = (size_t)L * ctx->n;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(round256((size_t)count * ctx->n * sizeof(int32_t))))) return st;
+  int32_t* err = reinterpret_cast<int32_t*>(ctx->ws);
+  const shg::CtxDev dev = ctx->dev();
+  shg::launch_sample_uniform_error(dev, a, Ln, 0, err, seeds, L, variance, count, s);
+  shg::launch_error_lift(dev, e, err, count, L, s);
+  shg::launch_ntt_fwd(dev, e, e, count * L, L, s);
+  return launch_status("sample_uniform_error");
+}
+
+int shg_bgv_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* key,
+                    const uint64_t* plaintexts, const uint8_t* seeds, int num_limbs,
+                    int count, int variance, shg_stream stream) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if ((st = check_variance(variance))) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, key, plaintexts, seeds}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = num_limbs;
+  const size_t n = ctx->n, Ln = (size_t)L * n;
+  shg::ScalarPack tm{};
+  for (int l = 0; l < L; ++l) tm.v[l] = to_mont(ctx->t % ctx->hp[l].q, ctx->hp[l].q);
+  const bool four = ctx->log_n >= 12 && (ctx->log_n >= ctx->ntt4_min || ctx->log_n > 14);
+  // Transform chunks of about 32 MiB, so the transform scratch stays in L2.
+  const size_t per_ct = Ln * sizeof(uint64_t);
+  const int C = (int)std::max<size_t>(
+      1, std::min<size_t>((size_t)count, std::max<size_t>(16, ((size_t)32 << 20) / per_ct)));
+  const size_t err_bytes = round256((size_t)count * n * sizeof(int32_t));
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(err_bytes + (size_t)C * per_ct))) return st;
+  int32_t* err = reinterpret_cast<int32_t*>(ctx->ws);
+  uint64_t* buf = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(ctx->ws) + err_bytes);
+  const shg::CtxDev dev = ctx->dev();
+  // c1 = -a straight from the sampler; the error waits in err.
+  shg::launch_sample_uniform_error(dev, out + Ln, 2 * Ln, 1, err, seeds, L, variance, count,
+                                   s);
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    uint64_t* o = out + (size_t)c0 * 2 * Ln;
+    const uint64_t* m = plaintexts + (size_t)c0 * Ln;
+    const int32_t* e = err + (size_t)c0 * n;
+    if (four) {
+      shg::launch4_bgv_encrypt(dev, o, e, m, key, tm, buf, cc, L, s);
+    } else {
+      shg::launch_error_lift(dev, buf, e, cc, L, s);
+      shg::launch_ntt_fwd(dev, buf, buf, cc * L, L, s);
+      shg::launch_bgv_enc_combine(dev, o, buf, m, key, tm, cc, L, s);
+    }
+  }
+  return launch_status("bgv_encrypt");
+}
+
 int shg_context_set_ks_fused(shg_context* ctx, int on) {
   if (!ctx || (on != 0 && on != 1))
     return fail(SHG_INVALID_ARGUMENT, "fused key switch switch must be 0 or 1");

@@ -15,28 +15,6 @@ std::vector<ProfEntry> g_prof_pending;
 
 namespace {
 
-// Counts every launch; with profiling on, brackets it with CUDA events on the
-// launch stream (these also work inside stream capture).
-struct LaunchScope {
-  const char* name;
-  cudaStream_t s;
-  cudaEvent_t a = nullptr, b = nullptr;
-  LaunchScope(const char* n, cudaStream_t st) : name(n), s(st) {
-    g_launch_count++;
-    if (g_prof_on.load()) {
-      cudaEventCreate(&a);
-      cudaEventCreate(&b);
-      cudaEventRecord(a, s);
-    }
-  }
-  ~LaunchScope() {
-    if (a) {
-      cudaEventRecord(b, s);
-      std::lock_guard<std::mutex> lock(g_prof_mu);
-      g_prof_pending.push_back(ProfEntry{name, a, b});
-    }
-  }
-};
 
 template <int LOG_N>
 struct Cfg {
@@ -850,6 +828,8 @@ __global__ void k_absorb_sum(uint64_t* out, const uint64_t* cts,
   }
 }
 
+}  // namespace
+
 int grid_for(size_t work, int threads) {
   size_t blocks = (work + threads - 1) / threads;
   const size_t cap = 152 * 16;
@@ -857,6 +837,8 @@ int grid_for(size_t work, int threads) {
   if (blocks < 1) blocks = 1;
   return (int)blocks;
 }
+
+namespace {
 
 // Runtime log_n -> template dispatch for CTA-resident transforms.
 #define SHG_DISPATCH_LOGN(log_n, F)                                  \

@@ -82,6 +82,32 @@ extern std::atomic<bool> g_prof_on;
 extern std::mutex g_prof_mu;
 extern std::vector<ProfEntry> g_prof_pending;
 
+// Counts every launch; with profiling on, brackets it with CUDA events on the
+// launch stream (these also work inside stream capture).
+struct LaunchScope {
+  const char* name;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LaunchScope(const char* n, cudaStream_t st) : name(n), s(st) {
+    g_launch_count++;
+    if (g_prof_on.load()) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~LaunchScope() {
+    if (a) {
+      cudaEventRecord(b, s);
+      std::lock_guard<std::mutex> lock(g_prof_mu);
+      g_prof_pending.push_back(ProfEntry{name, a, b});
+    }
+  }
+};
+
+// Blocks for a grid-stride loop over `work` items (at most 16 per SM).
+int grid_for(size_t work, int threads);
+
 // `num` limb transforms; limb index of transform g is g % L.
 void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                     int L, cudaStream_t s);
@@ -220,6 +246,23 @@ void launch_scatter(uint64_t* const* dsts, const uint64_t* src, size_t elems, in
 // returns `code`.
 int set_error(int code, const std::string& msg);
 
+// BGV encryption randomness from the ChaCha PRNG of seeds [count][32]
+// (RnsPolynomial::SampleUniform then SampleError): ciphertext p's uniform
+// polynomial (negated when `negate`) goes to a_dst + p * a_stride as [L][n],
+// its signed error coefficients to err [count][n].
+void launch_sample_uniform_error(const CtxDev& c, uint64_t* a_dst, size_t a_stride,
+                                 int negate, int32_t* err, const uint8_t* seeds, int L,
+                                 int variance, int count, cudaStream_t s);
+// Stream bytes one error coefficient of this variance takes.
+int sample_error_bytes(int variance);
+// out [count][L][n] <- err [count][n] lifted to every limb (Montgomery).
+void launch_error_lift(const CtxDev& c, uint64_t* out, const int32_t* err, int count, int L,
+                       cudaStream_t s);
+// out [count][2][L][n]: c0 <- e_ntt * t + m + (-c1) * key (c1 holds -a).
+void launch_bgv_enc_combine(const CtxDev& c, uint64_t* out, const uint64_t* e_ntt,
+                            const uint64_t* m, const uint64_t* key, const ScalarPack& tm,
+                            int count, int L, cudaStream_t s);
+
 // mono [levels][n] <- -x^{n - 2^j} in coefficient form (minus_one = the
 // Montgomery form of -1).
 void launch_monomials(const CtxDev& c, uint64_t* mono, int levels,
@@ -255,6 +298,12 @@ void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
 void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
                             const uint64_t* in, const ScalarPack& sc, int count,
                             int L, cudaStream_t s);
+
+// Fused four-step encryption tail: NTT of the lifted error err [count][n]
+// with the combine of launch_bgv_enc_combine as its sink; buf [count][L][n].
+void launch4_bgv_encrypt(const CtxDev& c, uint64_t* out, const int32_t* err,
+                         const uint64_t* m, const uint64_t* key, const ScalarPack& tm,
+                         uint64_t* buf, int count, int L, cudaStream_t s);
 
 // Fused four-step key switch: launch4_digit_cols runs the digit extraction and
 // column phase of every digit transform into D [count][k][L][n];

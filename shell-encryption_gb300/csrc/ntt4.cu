@@ -102,6 +102,28 @@ struct FwdSrcModLift {
   }
 };
 
+// Encryption error (SampleError, rns/error_distribution.h:40-60): the signed
+// centred-binomial coefficient of ciphertext g / L, lifted balanced to limb
+// i and put in Montgomery form.
+template <int LOG_N>
+struct FwdSrcError {
+  const int32_t* err;
+  int L;
+  struct H {
+    const int32_t* base;
+    uint64_t q, r, rp;
+    __device__ __forceinline__ uint64_t operator()(int i) const {
+      const int e = base[i];
+      const uint64_t u = shoup((uint64_t)(e < 0 ? -e : e), r, rp, q);
+      return (e < 0 && u) ? q - u : u;
+    }
+  };
+  __device__ H bind(int g, int i, const CtxDev& c) const {
+    return H{err + ((size_t)(g / L) << LOG_N), c.primes[i].q, c.primes[i].r_mod_q,
+             c.primes[i].r_mod_q_shoup};
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Forward phase-2 sinks: 16 canonical values at idx0..idx0+15 of transform g.
 // ---------------------------------------------------------------------------
@@ -154,6 +176,51 @@ struct FwdDstModCombine {
     h.c1p = sc.v[4 * i + 1];
     h.c2 = sc.v[4 * i + 2];
     h.c2p = sc.v[4 * i + 3];
+    return h;
+  }
+};
+
+// EncryptPolynomialBgv combine (rns/rns_secret_key.h:216-226): with x the
+// NTT of the error, c0 = x * t + m + a * s where c1 already holds -a;
+// out [count][2][L][n], m [count][L][n], key [L][n], tm.v[i] = t (Montgomery).
+template <int LOG_N>
+struct FwdDstBgvEnc {
+  uint64_t* out;
+  const uint64_t* m;
+  const uint64_t* key;
+  int L;
+  ScalarPack tm;
+  struct H {
+    uint64_t* o;
+    const uint64_t* mm;
+    const uint64_t* s;
+    uint64_t q, qinv, t;
+    int c1_off;
+    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
+#pragma unroll
+      for (int k = 0; k < 16; k += 2) {
+        const ulonglong2 mv = *reinterpret_cast<const ulonglong2*>(mm + i0 + k);
+        const ulonglong2 sv = *reinterpret_cast<const ulonglong2*>(s + i0 + k);
+        const ulonglong2 c1 = *reinterpret_cast<const ulonglong2*>(o + c1_off + i0 + k);
+        ulonglong2 r;
+        r.x = add_mod(add_mod(mont_mul(x[k], t, q, qinv), mv.x, q),
+                      mont_mul(q - c1.x, sv.x, q, qinv), q);
+        r.y = add_mod(add_mod(mont_mul(x[k + 1], t, q, qinv), mv.y, q),
+                      mont_mul(q - c1.y, sv.y, q, qinv), q);
+        *reinterpret_cast<ulonglong2*>(o + i0 + k) = r;
+      }
+    }
+  };
+  __device__ H bind(int g, int i, const CtxDev& c) const {
+    const int p = g / L;
+    H h;
+    h.o = out + (((size_t)p * 2 * L + i) << LOG_N);
+    h.mm = m + ((size_t)g << LOG_N);
+    h.s = key + ((size_t)i << LOG_N);
+    h.q = c.primes[i].q;
+    h.qinv = c.primes[i].inv_modulus;
+    h.t = tm.v[i];
+    h.c1_off = L << LOG_N;
     return h;
   }
 };
@@ -649,6 +716,19 @@ void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
 #define F(LN)                                                                  \
   fwd4<LN>(c, FwdSrcModLift<LN>{Y, L - 1}, FwdDstModCombine<LN>{out, in, L, sc}, \
            PrimeMap{0, 1, L - 1}, out, count * (L - 1), s)
+  SHG_DISPATCH4(c.log_n, F)
+#undef F
+}
+
+void launch4_bgv_encrypt(const CtxDev& c, uint64_t* out, const int32_t* err,
+                         const uint64_t* m, const uint64_t* key, const ScalarPack& tm,
+                         uint64_t* buf, int count, int L, cudaStream_t s) {
+  if (count <= 0) return;
+  LaunchScope scope_("bgv_encrypt_ntt", s);
+  g_launch_count++;  // second phase kernel
+#define F(LN)                                                                       \
+  fwd4<LN>(c, FwdSrcError<LN>{err, L}, FwdDstBgvEnc<LN>{out, m, key, L, tm},         \
+           PrimeMap{0, 1, L}, buf, count * L, s)
   SHG_DISPATCH4(c.log_n, F)
 #undef F
 }

@@ -79,6 +79,10 @@ SIGNATURES = {
                                             ctypes.c_int, _vp]),
     "shg_pir_expand_absorb": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp,
                                              ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_sample_uniform_error": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, _vp]),
+    "shg_bgv_encrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _vp]),
     "shg_symmetric_encrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),
     "shg_symmetric_decrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                              _vp]),

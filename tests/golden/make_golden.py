@@ -112,6 +112,37 @@ def main():
         v = O.splitmix64(8000 + count, count) % np.uint64(q)
         g[f"ser_{q}_values"] = v
         g[f"ser_{q}_bytes"] = R.serialize_vector(q, v)
+    # SingleThreadChaChaPrng's stream (prng/chacha_prng_util.cc:30-98) across
+    # two salt boundaries, and SampleUniform + SampleError drawn from it
+    # (rns/rns_polynomial.h:638-667, rns/error_distribution.h:40-60); 65537
+    # rejects about half of its 17-bit candidates.
+    seed = bytes(range(40, 72))
+    g["prng_seed"] = np.frombuffer(seed, np.uint8).copy()
+    g["prng_bytes"] = R.prng_bytes(seed, 2 * 8160 + 100)
+    for log_n, qs, var in [(6, [Q45[0], 65537], 1), (7, Q50[:2], 8), (5, [Q60], 256),
+                           (6, Q45[:3], 33), (8, [65537], 3)]:
+        tag = f"sample_{log_n}_{len(qs)}_{var}"
+        sd = bytes((i * 7 + log_n + var) % 256 for i in range(32))
+        a, e = R.sample_uniform_error(log_n, qs, var, sd)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_variance"] = np.array([var], np.int32)
+        g[tag + "_seed"] = np.frombuffer(sd, np.uint8).copy()
+        g[tag + "_a"] = a
+        g[tag + "_e"] = e
+    # RnsRlweSecretKey::EncryptPolynomialBgv (rns/rns_secret_key.h:188-231).
+    for log_n, qs, t, var, count in [(6, Q45[:2], 65537, 8, 3), (10, [Q59], 2, 4, 2),
+                                     (7, [Q45[0], 65537], 3, 1, 2)]:
+        tag = f"encrypt_{log_n}_{len(qs)}"
+        n, L = 1 << log_n, len(qs)
+        key = O.uniform_limbs(9000 + log_n, qs, n).reshape(L, n)
+        m = O.uniform_limbs(9100 + log_n, qs, n, count).reshape(count, L, n)
+        seeds = [bytes((i * 13 + c * 5 + log_n) % 256 for i in range(32)) for c in range(count)]
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_params"] = np.array([t, var], np.uint64)
+        g[tag + "_key"] = key
+        g[tag + "_m"] = m
+        g[tag + "_seeds"] = np.frombuffer(b"".join(seeds), np.uint8).reshape(count, 32).copy()
+        g[tag + "_out"] = R.encrypt_bgv(log_n, qs, t, var, key, m, seeds)
     np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **g)
 
     # Full-size workloads: digests of the reference's outputs on seeded inputs.
@@ -146,6 +177,15 @@ def main():
     x = O.uniform_limbs(7020, [Q59], 1 << 12, 64).reshape(64, -1)
     d["ntt_q59_n12_x64"] = {"seed": 7020, "fwd_sha256": digest(R.ntt(Q59, 12, x)),
                             "inv_sha256": digest(R.ntt(Q59, 12, x, inverse=True))}
+    log_n, qs, n = 14, Q45, 1 << 14
+    key = O.uniform_limbs(7030, qs, n).reshape(6, n)
+    m = O.uniform_limbs(7031, qs, n, 4).reshape(4, 6, n)
+    seeds = [bytes([c + 1] * 32) for c in range(4)]
+    d["encrypt_n14_L6"] = {"log_n": 14, "qs": qs, "t": 65537, "variance": 8, "count": 4,
+                           "seeds": {"key": 7030, "m": 7031},
+                           "prng_seeds": "ciphertext c: 32 bytes of value c + 1",
+                           "out_sha256": digest(R.encrypt_bgv(log_n, qs, 65537, 8, key, m,
+                                                              seeds))}
     with open(os.path.join(HERE, "digests.json"), "w") as fh:
         json.dump(d, fh, indent=1)
     print("wrote", os.path.join(HERE, "reference_small.npz"), "and digests.json")

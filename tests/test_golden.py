@@ -360,3 +360,115 @@ def test_gpu_galois_random_pad_golden(sg, tag):
                                            count, None))
     sg.synchronize()
     assert np.array_equal(out.download(want.shape), want)
+
+
+# --------------------------------------------------------------------------
+# ChaCha PRNG, SampleUniform / SampleError and EncryptPolynomialBgv
+# --------------------------------------------------------------------------
+
+SAMPLE_TAGS = sorted({k[:-len("_a")] for k in SMALL.files
+                      if k.startswith("sample_") and k.endswith("_a")})
+ENC_TAGS = sorted({k[:-len("_out")] for k in SMALL.files
+                   if k.startswith("encrypt_") and k.endswith("_out")})
+
+
+def _seed_words(seeds):
+    """32-byte seeds as the uint64 words a device buffer holds (byte order kept)."""
+    return np.frombuffer(np.ascontiguousarray(seeds, dtype=np.uint8).tobytes(), np.uint64)
+
+
+def test_oracle_prng_golden(oracle):
+    """SingleThreadChaChaPrng's byte stream across two salt boundaries."""
+    seed = SMALL["prng_seed"].tobytes()
+    want = SMALL["prng_bytes"]
+    assert np.array_equal(oracle.prng_bytes(seed, 0, want.size), want)
+    assert np.array_equal(oracle.prng_bytes(seed, 8150, 30), want[8150:8180])
+
+
+@pytest.mark.parametrize("tag", SAMPLE_TAGS)
+def test_oracle_sample_uniform_error_golden(oracle, tag):
+    """RnsPolynomial::SampleUniform then SampleError of the reference."""
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    a, e = oracle.Rns(log_n, qs).sample_uniform_error(
+        len(qs), int(SMALL[tag + "_variance"][0]), SMALL[tag + "_seed"].tobytes())
+    assert np.array_equal(a, SMALL[tag + "_a"])
+    assert np.array_equal(e, SMALL[tag + "_e"])
+
+
+@pytest.mark.parametrize("tag", ENC_TAGS)
+def test_oracle_encrypt_bgv_golden(oracle, tag):
+    """RnsRlweSecretKey::EncryptPolynomialBgv of the reference."""
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    t, var = (int(x) for x in SMALL[tag + "_params"])
+    rns = oracle.Rns(log_n, qs)
+    m, seeds = SMALL[tag + "_m"], SMALL[tag + "_seeds"]
+    got = np.stack([rns.encrypt_bgv(t, var, SMALL[tag + "_key"], m[i], seeds[i].tobytes())
+                    for i in range(m.shape[0])])
+    assert np.array_equal(got, SMALL[tag + "_out"])
+
+
+def _encrypt_digest_inputs(oracle):
+    d = DIGESTS["encrypt_n14_L6"]
+    n, qs = 1 << d["log_n"], d["qs"]
+    key = oracle.uniform_limbs(d["seeds"]["key"], qs, n).reshape(6, n)
+    m = oracle.uniform_limbs(d["seeds"]["m"], qs, n, d["count"]).reshape(d["count"], 6, n)
+    seeds = np.array([[c + 1] * 32 for c in range(d["count"])], np.uint8)
+    return d, key, m, seeds
+
+
+def test_oracle_encrypt_full_size_digest(oracle):
+    d, key, m, seeds = _encrypt_digest_inputs(oracle)
+    rns = oracle.Rns(d["log_n"], d["qs"])
+    got = np.stack([rns.encrypt_bgv(d["t"], d["variance"], key, m[i], seeds[i].tobytes())
+                    for i in range(d["count"])])
+    assert digest(got) == d["out_sha256"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", SAMPLE_TAGS)
+def test_gpu_sample_uniform_error_golden(sg, tag):
+    """Device SampleUniform + SampleError against the reference."""
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    want_a, want_e = SMALL[tag + "_a"], SMALL[tag + "_e"]
+    ctx = sg.Context(log_n, qs)
+    da, de = sg.DeviceBuffer(want_a.nbytes), sg.DeviceBuffer(want_e.nbytes)
+    ds = sg.DeviceBuffer.from_array(_seed_words(SMALL[tag + "_seed"]))
+    _run(sg, sg.lib().shg_sample_uniform_error, ctx.h, da.ptr, de.ptr, ds.ptr, len(qs), 1,
+         int(SMALL[tag + "_variance"][0]), None)
+    assert np.array_equal(da.download(want_a.shape), want_a)
+    assert np.array_equal(de.download(want_e.shape), want_e)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", ENC_TAGS)
+def test_gpu_encrypt_bgv_golden(sg, tag):
+    """Device EncryptPolynomialBgv against the reference."""
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    t, var = (int(x) for x in SMALL[tag + "_params"])
+    want, m = SMALL[tag + "_out"], SMALL[tag + "_m"]
+    ctx = sg.Context(log_n, qs, t)
+    dk, dm = sg.DeviceBuffer.from_array(SMALL[tag + "_key"]), sg.DeviceBuffer.from_array(m)
+    ds = sg.DeviceBuffer.from_array(_seed_words(SMALL[tag + "_seeds"]))
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, len(qs),
+         m.shape[0], var, None)
+    assert np.array_equal(out.download(want.shape), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("four_step_min", [13, 15])
+def test_gpu_encrypt_full_size_digest(sg, oracle, four_step_min):
+    """n = 2^14, six 45-bit primes: fused four-step tail and the plain one."""
+    d, key, m, seeds = _encrypt_digest_inputs(oracle)
+    ctx = sg.Context(d["log_n"], d["qs"], d["t"])
+    sg.check(sg.lib().shg_context_set_four_step_min(ctx.h, four_step_min))
+    dk, dm = sg.DeviceBuffer.from_array(key), sg.DeviceBuffer.from_array(m)
+    ds = sg.DeviceBuffer.from_array(_seed_words(seeds))
+    out = sg.DeviceBuffer(2 * m.nbytes)
+    _run(sg, sg.lib().shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, 6, d["count"],
+         d["variance"], None)
+    assert digest(out.download((d["count"], 2, 6, 1 << 14))) == d["out_sha256"]

@@ -691,3 +691,118 @@ def test_mul_relin_host_serialized(sg, oracle, piece, slots):
     _run(sg, lib.shg_bgv_mul_relin_host_serialized, ctx.h, key.h, out.ctypes.data,
          sa.ctypes.data, sb.ctypes.data, count, None)
     assert np.array_equal(out, ser(want))
+
+
+# --------------------------------------------------------------------------
+# On-device sampling (ChaCha PRNG) and EncryptPolynomialBgv
+# --------------------------------------------------------------------------
+
+def _seeds(count, salt):
+    return np.array([[(i * 31 + c * 17 + salt) % 256 for i in range(32)]
+                     for c in range(count)], np.uint8)
+
+
+def _seed_buf(sg, seeds):
+    return sg.DeviceBuffer.from_array(np.frombuffer(seeds.tobytes(), np.uint64))
+
+
+@pytest.mark.parametrize("log_n,qs,variance,count", [
+    (5, [Q45[0]], 1, 3),
+    (10, [Q45[0], 65537], 8, 4),        # 65537: about half the candidates rejected
+    (12, Q50[:3], 3, 2),
+    (13, Q45[:2], 256, 2),
+    (14, Q45, 8, 2),
+    (15, [Q50[0]], 33, 1),
+])
+def test_sample_uniform_error(sg, oracle, log_n, qs, variance, count):
+    """RnsPolynomial::SampleUniform + SampleError from SingleThreadChaChaPrng,
+    one stream per seed, bit-exact with the oracle."""
+    lib = sg.lib()
+    L, n = len(qs), 1 << log_n
+    seeds = _seeds(count, log_n)
+    rns = oracle.Rns(log_n, qs)
+    want = [rns.sample_uniform_error(L, variance, seeds[c].tobytes()) for c in range(count)]
+    ctx = sg.Context(log_n, qs)
+    da, de = sg.DeviceBuffer(count * L * n * 8), sg.DeviceBuffer(count * L * n * 8)
+    ds = _seed_buf(sg, seeds)
+    _run(sg, lib.shg_sample_uniform_error, ctx.h, da.ptr, de.ptr, ds.ptr, L, count, variance,
+         None)
+    a, e = da.download((count, L, n)), de.download((count, L, n))
+    for c in range(count):
+        assert np.array_equal(a[c], want[c][0]), c
+        assert np.array_equal(e[c], want[c][1]), c
+
+
+@pytest.mark.parametrize("log_n,qs,count,four_step_min", [
+    (6, Q45[:2], 5, 13),
+    (11, [Q59], 3, 13),
+    (12, Q50[:3], 4, 12),    # four-step tail at 2^12
+    (12, Q50[:3], 4, 13),
+    (13, Q45[:4], 3, 13),
+    (14, Q45, 45, 13),       # two transform chunks
+    (14, Q45, 3, 15),        # CTA-resident transforms
+    (15, Q50[:2], 2, 13),
+])
+def test_bgv_encrypt(sg, oracle, log_n, qs, count, four_step_min):
+    """RnsRlweSecretKey::EncryptPolynomialBgv with on-device sampling,
+    bit-exact with the oracle for every ciphertext."""
+    lib = sg.lib()
+    L, n, t, variance = len(qs), 1 << log_n, 65537, 8
+    key = oracle.uniform_limbs(400 + log_n, qs, n).reshape(L, n)
+    m = oracle.uniform_limbs(500 + log_n, qs, n, count).reshape(count, L, n)
+    seeds = _seeds(count, 3 * log_n)
+    rns = oracle.Rns(log_n, qs)
+    ctx = sg.Context(log_n, qs, t)
+    sg.check(lib.shg_context_set_four_step_min(ctx.h, four_step_min))
+    dk, dm, ds = _dev(sg, key), _dev(sg, m), _seed_buf(sg, seeds)
+    out = sg.DeviceBuffer(count * 2 * L * n * 8)
+    _run(sg, lib.shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, L, count, variance,
+         None)
+    got = out.download((count, 2, L, n))
+    for c in sorted({0, count // 2, count - 1}):
+        want = rns.encrypt_bgv(t, variance, key, m[c], seeds[c].tobytes())
+        assert np.array_equal(got[c], want), c
+
+
+def test_bgv_encrypt_decrypts(sg, oracle):
+    """c0 + c1 * s = e * t + m: the error part is small and divisible by t
+    (the secret-key encryption identity of rns_secret_key_test.cc)."""
+    lib = sg.lib()
+    log_n, qs, t, variance, count = 12, Q50[:2], 65537, 8, 3
+    L, n = len(qs), 1 << log_n
+    rns = oracle.Rns(log_n, qs)
+    p0 = oracle.Prime(qs[0], log_n)
+    key = oracle.uniform_limbs(77, qs, n).reshape(L, n)
+    m = oracle.uniform_limbs(78, qs, n, count).reshape(count, L, n)
+    ctx = sg.Context(log_n, qs, t)
+    seeds = _seeds(count, 1)
+    dk, dm, ds = _dev(sg, key), _dev(sg, m), _seed_buf(sg, seeds)
+    out = sg.DeviceBuffer(count * 2 * L * n * 8)
+    _run(sg, lib.shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, L, count, variance,
+         None)
+    got = out.download((count, 2, L, n))
+    for c in range(count):
+        # limb 0: c0 + c1 * s - m = e * t, with |e| <= 2 * variance
+        x = p0.add(got[c, 0, 0], p0.mul(got[c, 1, 0], key[0]))
+        x = p0.sub(x, m[c, 0])
+        v = p0.export(p0.ntt_inv(x)).astype(object)
+        q = qs[0]
+        s = [int(y) - q if int(y) > q // 2 else int(y) for y in v]
+        assert all(y % t == 0 and abs(y // t) <= 2 * variance for y in s)
+
+
+def test_sampling_validation(sg):
+    lib = sg.lib()
+    ctx = sg.Context(10, Q45[:2], 65537)
+    buf = sg.DeviceBuffer(2 * 2 * 1024 * 8)
+    seeds = sg.DeviceBuffer(64)
+    for var, msg in [(0, "must be positive"), (257, "must be at most 256")]:
+        with pytest.raises(sg.ShgError, match=msg):
+            sg.check(lib.shg_sample_uniform_error(ctx.h, buf.ptr, buf.ptr, seeds.ptr, 2, 1, var,
+                                                  None))
+        with pytest.raises(sg.ShgError, match=msg):
+            sg.check(lib.shg_bgv_encrypt(ctx.h, buf.ptr, buf.ptr, buf.ptr, seeds.ptr, 2, 1, var,
+                                         None))
+    with pytest.raises(sg.ShgError, match="RNS moduli"):
+        sg.check(lib.shg_bgv_encrypt(ctx.h, buf.ptr, buf.ptr, buf.ptr, seeds.ptr, 3, 1, 8, None))
+    sg.check(lib.shg_bgv_encrypt(ctx.h, buf.ptr, buf.ptr, buf.ptr, seeds.ptr, 2, 0, 8, None))

@@ -244,3 +244,56 @@ def test_symmetric_encrypt_decrypt_round_trip(oracle):
                        p.ntt_fwd(mont(m2)))
     assert np.array_equal(p.sym_decrypt(t, s, c1).astype(np.int64), m1)
     assert np.array_equal(p.sym_decrypt(t, s, p.add(c1, c2)).astype(np.int64), (m1 + m2) % t)
+
+
+def test_chacha20_block_rfc7539(oracle):
+    """RFC 7539 section 2.3.2's test vector for the block function."""
+    key = bytes(range(32))
+    nonce = bytes.fromhex("000000090000004a00000000")
+    want = bytes.fromhex("10f1e7e4d13b5915500fdd1fa32071c4c7d1f4c733c068030422aa9ac3d46c4e"
+                         "d2826446079faa0914c2d705d98b02a2b5129cd1de164eb9cbd083e8a2503c4e")
+    assert oracle.chacha20_block(key, 1, nonce) == want
+
+
+def test_chacha_prng_stream_matches_cryptography(oracle):
+    """The PRNG stream (prng/chacha_prng_util.cc:30-98): salt s gives 8160
+    bytes of ChaCha20 keystream under nonce "salt" || LE64(s), counter 0 --
+    checked against an independent ChaCha20 (Python `cryptography`)."""
+    ciphers = pytest.importorskip("cryptography.hazmat.primitives.ciphers")
+    seed = bytes(range(100, 132))
+    got = oracle.prng_bytes(seed, 0, 3 * 8160 + 77).tobytes()
+    want = b""
+    for salt in range(4):
+        nonce = (0).to_bytes(4, "little") + b"salt" + salt.to_bytes(8, "little")
+        enc = ciphers.Cipher(ciphers.algorithms.ChaCha20(seed, nonce), mode=None).encryptor()
+        want += enc.update(bytes(8160))
+    assert got == want[: len(got)]
+    # an unaligned window
+    assert oracle.prng_bytes(seed, 8155, 20).tobytes() == want[8155:8175]
+
+
+@pytest.mark.parametrize("variance", [1, 3, 4, 8, 33, 256])
+def test_sample_error_distribution(oracle, variance):
+    """SampleError's centred binomial: |e| <= 2 * variance, mean ~0 and
+    variance ~`variance` (sample_error.h:43-100)."""
+    q, log_n = Q45[0], 12
+    n = 1 << log_n
+    r = oracle.Rns(log_n, [q])
+    p = oracle.Prime(q, log_n)
+    _, e = r.sample_uniform_error(1, variance, bytes([variance % 256] * 32))
+    v = p.export(p.ntt_inv(e[0])).astype(object)
+    s = np.array([int(x) - q if int(x) > q // 2 else int(x) for x in v], dtype=np.int64)
+    assert np.abs(s).max() <= 2 * variance
+    assert abs(s.mean()) < 6 * np.sqrt(variance / n)
+    assert abs(s.var() / variance - 1) < 0.15
+
+
+def test_sample_uniform_in_range(oracle):
+    """SampleUniform: every value below its prime, 65537 (half the 17-bit
+    candidates rejected) included."""
+    qs = [Q45[0], 65537]
+    r = oracle.Rns(10, qs)
+    a, _ = r.sample_uniform_error(2, 8, bytes(32))
+    for l, q in enumerate(qs):
+        assert int(a[l].max()) < q
+        assert len(np.unique(a[l])) > (1 << 10) * 0.9 if q > 1 << 20 else True
