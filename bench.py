@@ -914,6 +914,257 @@ def run_serve(args, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Encryption: RnsRlweSecretKey::EncryptPolynomialBgv with the randomness drawn
+# on the device from SHELL's ChaCha PRNG (one 32-byte seed per ciphertext),
+# n = 2^14, the six 45-bit primes, variance 8, 1024 ciphertexts per step.
+# ---------------------------------------------------------------------------
+
+ENC_METRIC = "BGV encryptions/sec (EncryptPolynomialBgv, ChaCha sampling on the device, " \
+             "bit-exact)"
+ENC_UNIT = "encryptions/s"
+ENC_VARIANCE = 8
+ENC_SCOPES = ("sample_uniform_error", "bgv_encrypt_ntt", "error_lift", "ntt_fwd",
+              "bgv_enc_combine")
+
+
+def enc_config(count):
+    return {"workload": "bgv-encrypt n=2^14 6x45-bit primes t=65537 variance 8",
+            "log_n": LOG_N, "log_q": 45, "limbs": len(QS), "variance": ENC_VARIANCE,
+            "ciphertexts": count, "l2": "plaintexts and ciphertexts per step (2.4 GB) exceed L2",
+            "parallelism": "replicas"}
+
+
+def enc_scope_model(name, n, L, cts):
+    """(algorithmic DRAM bytes, ChaCha keystream bytes) of one step of a scope."""
+    poly = L * n * 8
+    if name == "sample_uniform_error":
+        # c1 out plus the int32 error coefficients; keystream: the uniform
+        # words plus 4 bytes per error coefficient at variance 8
+        return (poly + n * 4) * cts, (L * n * 8 + n * 4) * cts
+    if name == "bgv_encrypt_ntt":
+        # error in, plaintext and c1 in, c0 out (the transform scratch stays in L2)
+        return (n * 4 + 3 * poly) * cts, 0
+    if name == "error_lift":
+        return (n * 4 + poly) * cts, 0
+    if name == "ntt_fwd":
+        return 2 * poly * cts, 0
+    if name == "bgv_enc_combine":
+        return 4 * poly * cts, 0
+    raise KeyError(name)
+
+
+def cpu_encrypt(seconds, threads, seed=7):
+    """The reference's CPU encryption (oracle restatement of
+    EncryptPolynomialBgv with the ChaCha PRNG), one ciphertext per host thread
+    per round, for about `seconds`."""
+    import concurrent.futures
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    n = 1 << LOG_N
+    L = len(QS)
+    rns = O.Rns(LOG_N, QS)
+    key = splitmix_limbs(seed, 1, QS, n).reshape(L, n)
+    m = splitmix_limbs(seed + 1, threads, QS, n).reshape(threads, L, n)
+
+    def one(i):
+        return rns.encrypt_bgv(T_PLAIN, ENC_VARIANCE, key, m[i], bytes([i % 256] * 32))
+
+    ops = 0
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        while True:
+            list(ex.map(one, range(threads)))
+            ops += threads
+            dt = time.perf_counter() - t0
+            if dt >= seconds:
+                break
+    return ops / dt, ops, dt
+
+
+def run_encrypt_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    per_step, ops_total = [], 0
+    for i in range(args.warmup + args.steps):
+        _, ops, dt = cpu_encrypt(2.0, threads, seed=100 + i)
+        if i >= args.warmup:
+            per_step.append(dt)
+            ops_total += ops
+    total = sum(per_step)
+    value = ops_total / total
+    print(json.dumps({
+        "metric": ENC_METRIC, "value": value, "unit": ENC_UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": enc_config(threads),
+        "cpu_baseline": {"value": value, "unit": ENC_UNIT, "cores": threads, "kind": "port",
+                         "sample": "each step: about 2 s of whole encryptions, one per host "
+                                   "thread per round"},
+        "e2e": {"value": value, "unit": ENC_UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_encrypt(args, world, rank, local, dist):
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    n = 1 << LOG_N
+    L = len(QS)
+    B = args.batch
+    ctx = sg.Context(LOG_N, QS, T_PLAIN)
+    if args.four_step_min:
+        sg.check(lib.shg_context_set_four_step_min(ctx.h, args.four_step_min))
+    if args.chunk:
+        sg.check(lib.shg_context_set_chunk(ctx.h, args.chunk))
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+    key = splitmix_limbs(4000 + rank, 1, QS, n).reshape(L, n)
+    d_key = sg.DeviceBuffer.from_array(key)
+    m_bytes, ct_bytes, seed_bytes = B * L * n * 8, B * 2 * L * n * 8, B * 32
+
+    def host(nbytes):
+        p = ctypes.c_void_p()
+        sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+        return p.value
+
+    h_m, h_out, h_seeds = host(m_bytes), host(ct_bytes), host(seed_bytes)
+    np.ctypeslib.as_array((ctypes.c_uint64 * (B * L * n)).from_address(h_m))[:] = \
+        splitmix_limbs(4100 + rank, B, QS, n).reshape(-1)
+    np.ctypeslib.as_array((ctypes.c_uint8 * seed_bytes).from_address(h_seeds))[:] = \
+        np.frombuffer(splitmix_limbs(4200 + rank, B * 4, [1 << 62], 1).tobytes(), np.uint8)
+    d_m, d_out, d_seeds = (sg.DeviceBuffer(m_bytes), sg.DeviceBuffer(ct_bytes),
+                           sg.DeviceBuffer(seed_bytes))
+    sg.check(lib.shg_memcpy_h2d(d_m.ptr, h_m, m_bytes, s))
+    sg.check(lib.shg_memcpy_h2d(d_seeds.ptr, h_seeds, seed_bytes, s))
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def step_device():
+        sg.check(lib.shg_bgv_encrypt(ctx.h, d_out.ptr, d_key.ptr, d_m.ptr, d_seeds.ptr, L, B,
+                                     ENC_VARIANCE, s))
+
+    step_device()
+    sg.check(lib.shg_stream_synchronize(s))
+    n0 = lib.shg_launch_count()
+    sg.check(lib.shg_graph_capture_begin(s))
+    step_device()
+    g = ctypes.c_void_p()
+    sg.check(lib.shg_graph_capture_end(s, ctypes.byref(g)))
+    graph = g.value
+    launches_per_step = lib.shg_launch_count() - n0
+    for _ in range(args.warmup):
+        sg.check(lib.shg_graph_launch(graph, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    evs = [ev() for _ in range(args.steps + 1)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    sg.check(lib.shg_event_record(evs[0], s))
+    for i in range(args.steps):
+        sg.check(lib.shg_graph_launch(graph, s))
+        sg.check(lib.shg_event_record(evs[i + 1], s))
+    sg.check(lib.shg_stream_synchronize(s))
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = [elapsed(evs[i], evs[i + 1]) for i in range(args.steps)]
+    total_ms = max_over_ranks(dist, elapsed(evs[0], evs[-1]))
+    ops_all = sum_over_ranks(dist, float(B * args.steps))
+    value = ops_all / (total_ms / 1e3)
+
+    # End to end: plaintexts and seeds in from pinned host memory, ciphertexts
+    # back, per step.
+    e2e = None
+    if not args.no_e2e:
+        def step_e2e():
+            sg.check(lib.shg_memcpy_h2d(d_m.ptr, h_m, m_bytes, s))
+            sg.check(lib.shg_memcpy_h2d(d_seeds.ptr, h_seeds, seed_bytes, s))
+            step_device()
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, ct_bytes, s))
+        step_e2e()
+        sg.check(lib.shg_stream_synchronize(s))
+        e0, e1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(e0, s))
+        for _ in range(args.steps):
+            step_e2e()
+        sg.check(lib.shg_event_record(e1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": ENC_UNIT,
+               "h2d_bytes_per_step": m_bytes + seed_bytes, "d2h_bytes_per_step": ct_bytes,
+               "ms_per_step": e2e_ms / args.steps}
+
+    sg.check(lib.shg_profile_start())
+    step_device()
+    sg.check(lib.shg_profile_stop())
+    prof = {}
+    for name in ENC_SCOPES:
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        if cnt.value:
+            prof[name] = (ms.value, cnt.value)
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    step_total = sum(v[0] for v in prof.values())
+    kernels = {}
+    for name, (ms, cnt) in prof.items():
+        nbytes, ks = enc_scope_model(name, n, L, B)
+        kernels[name] = {"share_of_step": ms / step_total, "launches": cnt,
+                         "avg_launch_ms": ms / cnt,
+                         "algorithmic_bytes_per_launch": nbytes / cnt,
+                         "achieved_gbs": nbytes / (ms / 1e3) / 1e9,
+                         "keystream_gbs": (ks / (ms / 1e3) / 1e9) if ks else None}
+    top = max(prof, key=lambda nm: prof[nm][0])
+    tk = kernels[top]
+    roofline = {
+        "kernel": top, "bound": "hbm", "achieved": tk["achieved_gbs"], "peak": peak,
+        "unit": "GB/s", "frac": tk["achieved_gbs"] / peak, "peak_source": peak_src,
+        "traffic": None, "algorithmic_bytes_per_launch": tk["algorithmic_bytes_per_launch"],
+        "avg_launch_ms": tk["avg_launch_ms"], "kernels": kernels,
+        "step_bytes_min": 3 * L * n * 8 * B,
+        "step_frac_of_hbm": 3 * L * n * 8 * B / (total_ms / args.steps / 1e3) / 1e9 / peak,
+    }
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, ops, dt = cpu_encrypt(10.0, threads)
+        cpu = {"value": rate, "unit": ENC_UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ops} encryptions in {dt:.1f} s, one per host thread per round"}
+    lat = sorted(step_ms)
+    line = {
+        "metric": ENC_METRIC, "value": value, "unit": ENC_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded uniform key, plaintexts and PRNG seeds)",
+        "config": enc_config(B),
+        "latency_ms": {"step_p50": lat[len(lat) // 2], "step_p99": lat[-1]},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "gpu_launches": int(launches_per_step * args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sg.check(lib.shg_graph_destroy(graph))
+    for hp in (h_m, h_out, h_seeds):
+        lib.shg_host_free(hp)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -937,10 +1188,11 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
-                    choices=["ct-mult-relin", "pir", "uneven", "serve"],
+                    choices=["ct-mult-relin", "pir", "uneven", "serve", "encrypt"],
                     help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
                          "pir: oblivious expansion + database absorb (n=2^12, one prime); "
-                         "uneven: 4096 mixed instances through the batch executor")
+                         "uneven: 4096 mixed instances through the batch executor; "
+                         "encrypt: EncryptPolynomialBgv with on-device ChaCha sampling")
     ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -965,6 +1217,12 @@ def main():
                                                  "workloads"}), flush=True)
         else:
             run_uneven(args, world, rank, local, dist)
+        return
+    if args.workload == "encrypt":
+        if args.impl == "reference":
+            run_encrypt_reference(args, world, rank)
+        else:
+            run_encrypt(args, world, rank, local, dist)
         return
     if args.workload == "pir":
         if args.impl == "reference":

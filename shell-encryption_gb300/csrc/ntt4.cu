@@ -12,6 +12,11 @@ void set_smem4(K kernel, int smem) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
+// Pulls the 128-byte line at p into L2 ahead of its use.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 template <bool LAZY, int E>
 __device__ __forceinline__ void finish_fwd(uint64_t (&x)[E], uint64_t q,
                                            uint64_t two_q, uint64_t bar) {
@@ -125,7 +130,7 @@ struct FwdSrcError {
 };
 
 // ---------------------------------------------------------------------------
-// Forward phase-2 sinks: 16 canonical values at idx0..idx0+15 of transform g.
+// Forward phase-2 sinks: the canonical values at i, i + 1 of transform g.
 // ---------------------------------------------------------------------------
 
 template <int LOG_N>
@@ -133,13 +138,12 @@ struct FwdDstPlain {
   uint64_t* p;
   struct H {
     uint64_t* base;
-    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
-#pragma unroll
-      for (int k = 0; k < 16; k += 2)
-        *reinterpret_cast<ulonglong2*>(base + i0 + k) = make_ulonglong2(x[k], x[k + 1]);
+    __device__ __forceinline__ void pair(int i, uint64_t x0, uint64_t x1) const {
+      *reinterpret_cast<ulonglong2*>(base + i) = make_ulonglong2(x0, x1);
     }
   };
   __device__ H bind(int g, int, const CtxDev&) const { return H{p + ((size_t)g << LOG_N)}; }
+  __device__ void prefetch(int, int, int) const {}
 };
 
 // ModReduceLsb combine: out_i = in_i * c1 + delta_i * c2
@@ -154,15 +158,12 @@ struct FwdDstModCombine {
     uint64_t* o;
     const uint64_t* a;
     uint64_t q, c1, c1p, c2, c2p;
-    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
-#pragma unroll
-      for (int k = 0; k < 16; k += 2) {
-        const ulonglong2 av = *reinterpret_cast<const ulonglong2*>(a + i0 + k);
-        ulonglong2 r;
-        r.x = reduce_2q_full(shoup(av.x, c1, c1p, q) + shoup(x[k], c2, c2p, q), q);
-        r.y = reduce_2q_full(shoup(av.y, c1, c1p, q) + shoup(x[k + 1], c2, c2p, q), q);
-        *reinterpret_cast<ulonglong2*>(o + i0 + k) = r;
-      }
+    __device__ __forceinline__ void pair(int i, uint64_t x0, uint64_t x1) const {
+      const ulonglong2 av = *reinterpret_cast<const ulonglong2*>(a + i);
+      ulonglong2 r;
+      r.x = reduce_2q_full(shoup(av.x, c1, c1p, q) + shoup(x0, c2, c2p, q), q);
+      r.y = reduce_2q_full(shoup(av.y, c1, c1p, q) + shoup(x1, c2, c2p, q), q);
+      *reinterpret_cast<ulonglong2*>(o + i) = r;
     }
   };
   __device__ H bind(int g, int i, const CtxDev& c) const {
@@ -177,6 +178,10 @@ struct FwdDstModCombine {
     h.c2 = sc.v[4 * i + 2];
     h.c2p = sc.v[4 * i + 3];
     return h;
+  }
+  // The 16 values of limb i of `in` that the sink reads at i0.
+  __device__ void prefetch(int g, int i, int i0) const {
+    prefetch_l2(in + ((((size_t)(g / (L - 1)) * L + i) << LOG_N) + i0));
   }
 };
 
@@ -196,19 +201,16 @@ struct FwdDstBgvEnc {
     const uint64_t* s;
     uint64_t q, qinv, t;
     int c1_off;
-    __device__ __forceinline__ void operator()(int i0, const uint64_t (&x)[16]) const {
-#pragma unroll
-      for (int k = 0; k < 16; k += 2) {
-        const ulonglong2 mv = *reinterpret_cast<const ulonglong2*>(mm + i0 + k);
-        const ulonglong2 sv = *reinterpret_cast<const ulonglong2*>(s + i0 + k);
-        const ulonglong2 c1 = *reinterpret_cast<const ulonglong2*>(o + c1_off + i0 + k);
-        ulonglong2 r;
-        r.x = add_mod(add_mod(mont_mul(x[k], t, q, qinv), mv.x, q),
-                      mont_mul(q - c1.x, sv.x, q, qinv), q);
-        r.y = add_mod(add_mod(mont_mul(x[k + 1], t, q, qinv), mv.y, q),
-                      mont_mul(q - c1.y, sv.y, q, qinv), q);
-        *reinterpret_cast<ulonglong2*>(o + i0 + k) = r;
-      }
+    __device__ __forceinline__ void pair(int i, uint64_t x0, uint64_t x1) const {
+      const ulonglong2 mv = *reinterpret_cast<const ulonglong2*>(mm + i);
+      const ulonglong2 sv = *reinterpret_cast<const ulonglong2*>(s + i);
+      const ulonglong2 c1 = *reinterpret_cast<const ulonglong2*>(o + c1_off + i);
+      ulonglong2 r;
+      r.x = add_mod(add_mod(mont_mul(x0, t, q, qinv), mv.x, q),
+                    mont_mul(q - c1.x, sv.x, q, qinv), q);
+      r.y = add_mod(add_mod(mont_mul(x1, t, q, qinv), mv.y, q),
+                    mont_mul(q - c1.y, sv.y, q, qinv), q);
+      *reinterpret_cast<ulonglong2*>(o + i) = r;
     }
   };
   __device__ H bind(int g, int i, const CtxDev& c) const {
@@ -222,6 +224,12 @@ struct FwdDstBgvEnc {
     h.t = tm.v[i];
     h.c1_off = L << LOG_N;
     return h;
+  }
+  // Plaintext and c1 lines the sink reads at i0, fetched while the row
+  // transform runs.
+  __device__ void prefetch(int g, int i, int i0) const {
+    prefetch_l2(m + ((size_t)g << LOG_N) + i0);
+    prefetch_l2(out + ((((size_t)(g / L) * 2 + 1) * L + i) << LOG_N) + i0);
   }
 };
 
@@ -413,6 +421,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
   const PrimeDev* P = c.primes + l;
   const uint64_t q = P->q, two_q = P->two_q;
   const uint64_t* src = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
+  if (active) dst.prefetch(g, l, (row << S::B) | C::fwd_out_idx(tid, 0));
   uint64_t x[C::E];
 #pragma unroll
   for (int k = 0; k < C::E; ++k) x[k] = src[C::fwd_in_idx(tid, k)];
@@ -420,7 +429,30 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
                               c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
                               two_q);
   finish_fwd<LAZY>(x, q, two_q, P->barrett);
-  if (active) dst.bind(g, l, c)((row << S::B) | C::fwd_out_idx(tid, 0), x);
+  // Thread tid holds elements 16 tid .. 16 tid + 15 of its sub-row.  They
+  // go through shared memory (pair slots XOR-swizzled by tid, so neither
+  // side has bank conflicts) and each warp then hands whole sub-rows to the
+  // sink, 32 consecutive pairs per access.
+  static_assert(C::T == 8 && (1 << S::B) == 128 && C::fwd_clo(C::P - 1) == 0,
+                "row epilogue assumes 8 threads x 16 consecutive values per row");
+  __syncthreads();
+  ulonglong2* t2 = reinterpret_cast<ulonglong2*>(smem);
+#pragma unroll
+  for (int p = 0; p < 8; ++p)
+    t2[sub * 64 + tid * 8 + ((p ^ tid) & 7)] = make_ulonglong2(x[2 * p], x[2 * p + 1]);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int s2 = warp; s2 < S::ROWS; s2 += S::ROW_THREADS / 32) {
+    const int m2 = grp * S::ROWS + s2;
+    if (m2 >= per_class) break;
+    const auto h = dst.bind(l + pm.L * m2, l, c);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int pp = half * 32 + lane, tq = pp >> 3;
+      const ulonglong2 v = t2[s2 * 64 + tq * 8 + ((pp ^ tq) & 7)];
+      h.pair((row << S::B) + 2 * pp, v.x, v.y);
+    }
+  }
 }
 
 // Forward row phase of all k gadget digits of (ciphertext p, limb l), fused

@@ -3,6 +3,8 @@
 // every numeric operation is a libshellgpu.so call.
 #include "rlwe_gpu.h"
 
+#include <cstring>
+
 #include <utility>
 
 namespace rlwe_gpu {
@@ -796,6 +798,72 @@ StatusOr<SymmetricRlweKey> SymmetricRlweKey::Create(Polynomial key,
   if (key.NumModuli() != 1 || key.LogN() != modulus->Context()->LogN() || !key.IsNttForm())
     return InvalidArgumentError("the key must be one NTT-form polynomial of the ring");
   return SymmetricRlweKey(std::move(key), modulus);
+}
+
+StatusOr<RnsRlweSecretKey> RnsRlweSecretKey::CreateFromKey(RnsPolynomial key, Moduli moduli,
+                                                           int variance) {
+  if (moduli.empty()) return InvalidArgumentError("`moduli` must not be empty.");
+  if (key.NumModuli() != (int)moduli.size())
+    return InvalidArgumentError("`key` must have one limb per modulus.");
+  if (!key.IsNttForm()) return InvalidArgumentError("`key` must be in NTT form.");
+  if (variance <= 0) return InvalidArgumentError("`variance` must be positive.");
+  if (variance > 256)
+    return InvalidArgumentError("The variance, " + std::to_string(variance) +
+                                ", must be at most 256.");
+  return RnsRlweSecretKey(std::move(key), std::move(moduli), variance);
+}
+
+StatusOr<std::vector<RnsBgvCiphertext>> RnsRlweSecretKey::EncryptPolynomialBgv(
+    const std::vector<RnsPolynomial>& plaintexts, const std::vector<std::string>& prng_seeds,
+    double error_bound) const {
+  if (plaintexts.size() != prng_seeds.size())
+    return InvalidArgumentError("one PRNG seed per plaintext is needed");
+  const int L = key_.NumModuli(), log_n = key_.LogN();
+  const size_t limb_elems = (size_t)L << log_n, count = plaintexts.size();
+  for (const RnsPolynomial& pt : plaintexts) {
+    if (!pt.IsNttForm()) return InvalidArgumentError("`plaintext` must be in NTT form.");
+    if (pt.NumModuli() != L || pt.LogN() != log_n)
+      return InvalidArgumentError("`plaintext` must have the key's ring and moduli");
+  }
+  std::vector<uint64_t> seed_words(count * 4);
+  for (size_t i = 0; i < count; ++i) {
+    if (prng_seeds[i].size() != 32)
+      return InvalidArgumentError(
+          "Cannot create Prng with key of the wrong size. Real key length of " +
+          std::to_string(prng_seeds[i].size()) + " instead of expected key length of 32.");
+    std::memcpy(&seed_words[i * 4], prng_seeds[i].data(), 32);
+  }
+  std::vector<RnsBgvCiphertext> out;
+  if (count == 0) return out;
+  DeviceArray seeds(count * 4), pts(count * limb_elems), cts(count * 2 * limb_elems);
+  RLWE_GPU_RETURN_IF_ERROR(seeds.Upload(seed_words.data(), seed_words.size()));
+  shg_context* h = moduli_[0]->Context()->handle();
+  for (size_t i = 0; i < count; ++i)
+    RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_memcpy_d2d(pts.data() + i * limb_elems,
+                                                      plaintexts[i].device_data(),
+                                                      limb_elems * 8, g_stream)));
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(
+      shg_bgv_encrypt(h, cts.data(), key_.device_data(), pts.data(),
+                      reinterpret_cast<const uint8_t*>(seeds.data()), L, (int)count, variance_,
+                      g_stream)));
+  out.reserve(count);
+  for (size_t i = 0; i < count; ++i) {
+    DeviceArray one(2 * limb_elems);
+    RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_memcpy_d2d(one.data(), cts.data() + i * 2 * limb_elems,
+                                                      2 * limb_elems * 8, g_stream)));
+    out.push_back(RnsBgvCiphertext::FromDevice(std::move(one), 2, log_n, moduli_, 1,
+                                               error_bound));
+  }
+  return out;
+}
+
+StatusOr<RnsBgvCiphertext> RnsRlweSecretKey::EncryptPolynomialBgv(
+    const RnsPolynomial& plaintext, const std::string& prng_seed, double error_bound) const {
+  RLWE_GPU_ASSIGN_OR_RETURN(std::vector<RnsBgvCiphertext> cts,
+                            EncryptPolynomialBgv(std::vector<RnsPolynomial>{plaintext},
+                                                 std::vector<std::string>{prng_seed},
+                                                 error_bound));
+  return std::move(cts[0]);
 }
 
 StatusOr<SymmetricRlweCiphertext> SymmetricRlweKey::Encrypt(const Polynomial& plaintext,

@@ -422,6 +422,37 @@ class SymmetricRlweCiphertext {
   const PrimeModulus* modulus_;
 };
 
+// rlwe::RnsRlweSecretKey (rns/rns_secret_key.h): the secret key s in NTT form
+// over `moduli` and the error variance.  Key sampling stays with the caller;
+// encryption draws its randomness on the device from SHELL's ChaCha PRNG.
+class RnsRlweSecretKey {
+ public:
+  // `key` in NTT form with one limb per modulus; 1 <= variance <= 256.
+  static StatusOr<RnsRlweSecretKey> CreateFromKey(RnsPolynomial key, Moduli moduli,
+                                                  int variance);
+  // EncryptPolynomialBgv(plaintext, encoder, error_params, prng)
+  // (rns/rns_secret_key.h:188-231) with prng = SingleThreadChaChaPrng::Create
+  // (prng_seed) (32 bytes) and t the context's plaintext modulus; the result
+  // carries `error_bound` (error_params->B_secretkey_encryption()).
+  StatusOr<RnsBgvCiphertext> EncryptPolynomialBgv(const RnsPolynomial& plaintext,
+                                                  const std::string& prng_seed,
+                                                  double error_bound = 0) const;
+  // The same for a batch: plaintext i with prng_seeds[i], one launch set.
+  StatusOr<std::vector<RnsBgvCiphertext>> EncryptPolynomialBgv(
+      const std::vector<RnsPolynomial>& plaintexts, const std::vector<std::string>& prng_seeds,
+      double error_bound = 0) const;
+  const RnsPolynomial& Key() const { return key_; }
+  const Moduli& moduli() const { return moduli_; }
+  int Variance() const { return variance_; }
+
+ private:
+  RnsRlweSecretKey(RnsPolynomial key, Moduli moduli, int variance)
+      : key_(std::move(key)), moduli_(std::move(moduli)), variance_(variance) {}
+  RnsPolynomial key_;
+  Moduli moduli_;
+  int variance_;
+};
+
 // rlwe::SymmetricRlweKey over a one-prime context: the key polynomial s (NTT
 // form) and the context's plaintext modulus t (SymmetricRlweKey::Sample's
 // t = 2^log_t + 1 when the context was created with it).

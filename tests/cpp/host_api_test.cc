@@ -450,10 +450,61 @@ void TestSymmetric() {
   so_prime_destroy(p);
 }
 
+// RnsRlweSecretKey::EncryptPolynomialBgv with the ChaCha PRNG on the device
+// against the oracle's restatement (rns/rns_secret_key_test.cc's encryption
+// cases), plus the reference's messages on bad seeds and plaintexts.
+void TestRnsSecretKey(int log_n, const std::vector<uint64_t>& qs) {
+  const int n = 1 << log_n, L = (int)qs.size();
+  const uint64_t t = 65537;
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, qs, {}, t));
+  const Moduli moduli = ctx->MainPrimeModuli();
+  std::vector<uint64_t> s = Uniform(31, qs, n, 1);
+  RnsRlweSecretKey key = *RnsRlweSecretKey::CreateFromKey(
+      *RnsPolynomial::Create(Limbs(s.data(), L, n), true), moduli, 8);
+  so_rns* r = so_rns_create(log_n, qs.data(), L);
+  std::vector<RnsPolynomial> pts;
+  std::vector<std::string> seeds;
+  std::vector<std::vector<uint64_t>> want;
+  for (int c = 0; c < 3; ++c) {
+    std::vector<uint64_t> m = Uniform(500 + c, qs, n, 1);
+    pts.push_back(*RnsPolynomial::Create(Limbs(m.data(), L, n), true));
+    std::string seed(32, '\0');
+    for (int i = 0; i < 32; ++i) seed[i] = (char)(i * 11 + c);
+    seeds.push_back(seed);
+    std::vector<uint64_t> w((size_t)2 * L * n);
+    so_rns_encrypt_bgv(r, L, t, 8, s.data(), m.data(),
+                       reinterpret_cast<const uint8_t*>(seed.data()), w.data());
+    want.push_back(w);
+  }
+  RnsBgvCiphertext one = *key.EncryptPolynomialBgv(pts[1], seeds[1]);
+  EXPECT(FlatCt(one) == want[1] && one.PowerOfS() == 1 && one.Len() == 2,
+         "EncryptPolynomialBgv equals the oracle");
+  std::vector<RnsBgvCiphertext> batch;
+  ASSERT_OK_AND_ASSIGN(batch, key.EncryptPolynomialBgv(pts, seeds));
+  bool ok = batch.size() == 3;
+  for (int c = 0; ok && c < 3; ++c) ok &= FlatCt(batch[c]) == want[c];
+  EXPECT(ok, "batched EncryptPolynomialBgv equals the oracle");
+  EXPECT_ERROR(key.EncryptPolynomialBgv(pts[0], std::string(16, 'x')).status(),
+               "Cannot create Prng with key of the wrong size. Real key length of 16 instead "
+               "of expected key length of 32.");
+  RnsPolynomial coeff = pts[0];
+  EXPECT_OK(coeff.ConvertToCoeffForm(moduli));
+  EXPECT_ERROR(key.EncryptPolynomialBgv(coeff, seeds[0]).status(),
+               "`plaintext` must be in NTT form.");
+  EXPECT_ERROR(RnsRlweSecretKey::CreateFromKey(pts[0], moduli, 0).status(),
+               "`variance` must be positive.");
+  EXPECT_ERROR(RnsRlweSecretKey::CreateFromKey(pts[0], moduli, 257).status(),
+               "The variance, 257, must be at most 256.");
+  so_rns_destroy(r);
+}
+
 }  // namespace
 
 int main() {
   TestSymmetric();
+  TestRnsSecretKey(10, {kQ45[0], kQ45[1]});
+  TestRnsSecretKey(14, kQ45);
   TestContextErrors();
   TestPolynomial(4, {kQ45[0], kQ45[1]});
   TestPolynomial(11, kQ50);

@@ -733,17 +733,17 @@ def test_sample_uniform_error(sg, oracle, log_n, qs, variance, count):
         assert np.array_equal(e[c], want[c][1]), c
 
 
-@pytest.mark.parametrize("log_n,qs,count,four_step_min", [
-    (6, Q45[:2], 5, 13),
-    (11, [Q59], 3, 13),
-    (12, Q50[:3], 4, 12),    # four-step tail at 2^12
-    (12, Q50[:3], 4, 13),
-    (13, Q45[:4], 3, 13),
-    (14, Q45, 45, 13),       # two transform chunks
-    (14, Q45, 3, 15),        # CTA-resident transforms
-    (15, Q50[:2], 2, 13),
+@pytest.mark.parametrize("log_n,qs,count,four_step_min,chunk", [
+    (6, Q45[:2], 5, 13, 0),
+    (11, [Q59], 3, 13, 0),
+    (12, Q50[:3], 4, 12, 0),    # four-step tail at 2^12
+    (12, Q50[:3], 4, 13, 0),
+    (13, Q45[:4], 3, 13, 0),
+    (14, Q45, 45, 13, 16),      # three transform chunks
+    (14, Q45, 20, 15, 8),       # CTA-resident transforms, three chunks
+    (15, Q50[:2], 2, 13, 0),
 ])
-def test_bgv_encrypt(sg, oracle, log_n, qs, count, four_step_min):
+def test_bgv_encrypt(sg, oracle, log_n, qs, count, four_step_min, chunk):
     """RnsRlweSecretKey::EncryptPolynomialBgv with on-device sampling,
     bit-exact with the oracle for every ciphertext."""
     lib = sg.lib()
@@ -754,12 +754,13 @@ def test_bgv_encrypt(sg, oracle, log_n, qs, count, four_step_min):
     rns = oracle.Rns(log_n, qs)
     ctx = sg.Context(log_n, qs, t)
     sg.check(lib.shg_context_set_four_step_min(ctx.h, four_step_min))
+    sg.check(lib.shg_context_set_chunk(ctx.h, chunk))
     dk, dm, ds = _dev(sg, key), _dev(sg, m), _seed_buf(sg, seeds)
     out = sg.DeviceBuffer(count * 2 * L * n * 8)
     _run(sg, lib.shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, L, count, variance,
          None)
     got = out.download((count, 2, L, n))
-    for c in sorted({0, count // 2, count - 1}):
+    for c in sorted({0, 1, count // 2, count - 2, count - 1}):
         want = rns.encrypt_bgv(t, variance, key, m[c], seeds[c].tobytes())
         assert np.array_equal(got[c], want), c
 
