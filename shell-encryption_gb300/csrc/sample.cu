@@ -27,10 +27,8 @@
 namespace shg {
 namespace {
 
-constexpr int kSampThreads = 512;
 constexpr int kSaltWords = 1020;   // 8160 bytes of keystream per salt
 constexpr int kSaltBytes = 8160;
-constexpr int kStageWords = kSampThreads * 8;
 
 __device__ __forceinline__ uint32_t rotl32(uint32_t v, int c) {
   return __funnelshift_l(v, v, c);
@@ -85,8 +83,11 @@ __host__ __device__ __forceinline__ int error_bytes(int k) {
   return 16 * (k / 64) + 2 * ((k % 64) / 8) + ((k % 8) ? 2 : 0);
 }
 
-// Exclusive block-wide prefix sum of v; *total gets the sum.
+// Exclusive block-wide prefix sum of v over THREADS threads; *total gets
+// the sum.
+template <int THREADS>
 __device__ __forceinline__ int block_scan(int v, int* warp_sums, int* total) {
+  constexpr int W = THREADS / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int x = v;
 #pragma unroll
@@ -97,28 +98,35 @@ __device__ __forceinline__ int block_scan(int v, int* warp_sums, int* total) {
   if (lane == 31) warp_sums[wid] = x;
   __syncthreads();
   if (wid == 0) {
-    int w = lane < kSampThreads / 32 ? warp_sums[lane] : 0;
+    int w = lane < W ? warp_sums[lane] : 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < W; o <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += y;
     }
-    if (lane < kSampThreads / 32) warp_sums[lane] = w;
+    if (lane < W) warp_sums[lane] = w;
   }
   __syncthreads();
   const int before = wid ? warp_sums[wid - 1] : 0;
-  *total = warp_sums[kSampThreads / 32 - 1];
+  *total = warp_sums[W - 1];
   return before + x - v;
 }
 
-// One CTA per ciphertext p.  a (uniform, Montgomery values; negated when
-// `negate`, i.e. written as c1 = -a) goes to a_dst + p * a_stride as
-// [L][n]; the signed error coefficients to err [p][n].
-__global__ void __launch_bounds__(kSampThreads)
+// Staging slot of accepted word r: the low four bits XORed with the next
+// four, so eight words per thread at consecutive ranks (the usual case) and
+// the in-order copy-out both run without shared-memory bank conflicts.
+__device__ __forceinline__ int stage_slot(int r) { return r ^ ((r >> 4) & 15); }
+
+// One CTA of THREADS threads per ciphertext p.  a (uniform, Montgomery
+// values; negated when `negate`, i.e. written as c1 = -a) goes to
+// a_dst + p * a_stride as [L][n]; the signed error coefficients to err [p][n].
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS)
     k_sample_uniform_error(uint64_t* a_dst, size_t a_stride, int negate, int32_t* err,
                            const uint8_t* seeds, int L, int variance, int log_n, CtxDev c) {
+  constexpr int kStageWords = THREADS * 8;
   __shared__ uint64_t stage[kStageWords];  // accepted words / error keystream bytes
-  __shared__ int warp_sums[kSampThreads / 32];
+  __shared__ int warp_sums[THREADS / 32];
   __shared__ unsigned long long s_stop;
   const int p = blockIdx.x, tid = threadIdx.x;
   const int n = 1 << log_n;
@@ -141,48 +149,42 @@ __global__ void __launch_bounds__(kSampThreads)
       // Blocks this pass: what `need` words take without rejections, plus
       // one for a start inside a block and one for a short block; a pass
       // that falls short is followed by another.
-      const int nb = min(kSampThreads, need / 8 + 2);
+      const int nb = min(THREADS, need / 8 + 2);
       const uint64_t g0 = block_of_word(pos);
+      const uint64_t g = g0 + tid;
+      const uint64_t w0 = word0(g);
       uint64_t v[8];
       unsigned ok = 0;
-      int cnt = 0;
-      uint64_t w0 = 0;
       if (tid < nb) {
-        const uint64_t g = g0 + tid;
         uint32_t x[16];
         chacha_block(key, (uint32_t)(g & 127), g >> 7, x);
-        w0 = word0(g);
+        // words before `pos` (only in block g0) and past a short block's end
+        // are not candidates
+        const int first = tid == 0 ? (int)(pos - w0) : 0;
         const int nw = (g & 127) == 127 ? 4 : 8;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
           v[k] = ((uint64_t)x[2 * k + 1] << 32 | x[2 * k]) & mask;
-          if (k < nw && w0 + k >= pos && v[k] < q) {
-            ok |= 1u << k;
-            ++cnt;
-          }
+          if (k >= first && k < nw && v[k] < q) ok |= 1u << k;
         }
       }
       int total;
-      int r = block_scan(cnt, warp_sums, &total);
+      int r = block_scan<THREADS>(__popc(ok), warp_sums, &total);
       const int take = min(total, need);
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         if (ok >> k & 1u) {
-          if (r < need) stage[r] = v[k];
+          if (r < need) stage[stage_slot(r)] = v[k];
           if (r == need - 1) s_stop = w0 + k + 1;
           ++r;
         }
       }
       __syncthreads();
-      for (int i = tid; i < take; i += kSampThreads) {
-        const uint64_t a = stage[i];
+      for (int i = tid; i < take; i += THREADS) {
+        const uint64_t a = stage[stage_slot(i)];
         dst[accepted + i] = negate ? q - a : a;
       }
-      if (total >= need) {
-        pos = s_stop;
-      } else {
-        pos = word0(g0 + nb);
-      }
+      pos = total >= need ? s_stop : word0(g0 + nb);
       accepted += take;
       __syncthreads();  // stage and s_stop are rewritten by the next pass
     }
@@ -199,19 +201,25 @@ __global__ void __launch_bounds__(kSampThreads)
     const int J = min(per_pass, n - j0);
     const uint64_t r0 = e0 + (uint64_t)j0 * B, r1 = r0 + (uint64_t)J * B;
     const uint64_t gb0 = block_of_byte(r0), gb1 = block_of_byte(r1 - 1);
-    for (uint64_t g = gb0 + tid; g <= gb1; g += kSampThreads) {
+    for (uint64_t g = gb0 + tid; g <= gb1; g += THREADS) {
       uint32_t x[16];
       chacha_block(key, (uint32_t)(g & 127), g >> 7, x);
       const uint64_t b0 = (g >> 7) * kSaltBytes + (g & 127) * 64;
       const int len = (g & 127) == 127 ? 32 : 64;
       const uint64_t lo = max(b0, r0), hi = min(b0 + len, r1);
-      for (uint64_t b = lo; b < hi; ++b) {
-        const uint32_t w = x[(b - b0) >> 2];
-        bytes[b - r0] = (uint8_t)(w >> (8 * ((b - b0) & 3)));
+      if (((lo | hi) & 3) == 0 && ((b0 - r0) & 3) == 0) {
+        // whole 32-bit words (block starts are 32-byte aligned)
+        uint32_t* words = reinterpret_cast<uint32_t*>(bytes);
+        for (uint64_t b = lo; b < hi; b += 4) words[(b - r0) >> 2] = x[(b - b0) >> 2];
+      } else {
+        for (uint64_t b = lo; b < hi; ++b) {
+          const uint32_t w = x[(b - b0) >> 2];
+          bytes[b - r0] = (uint8_t)(w >> (8 * ((b - b0) & 3)));
+        }
       }
     }
     __syncthreads();
-    for (int j = tid; j < J; j += kSampThreads) {
+    for (int j = tid; j < J; j += THREADS) {
       const uint8_t* cb = bytes + (size_t)j * B;
       int val = 0, kk = k2;
       while (kk > 0) {
@@ -294,8 +302,11 @@ void launch_sample_uniform_error(const CtxDev& c, uint64_t* a_dst, size_t a_stri
                                  int variance, int count, cudaStream_t s) {
   if (count <= 0) return;
   LaunchScope scope_("sample_uniform_error", s);
-  k_sample_uniform_error<<<count, kSampThreads, 0, s>>>(a_dst, a_stride, negate, err, seeds,
-                                                        L, variance, c.log_n, c);
+  // 256-thread CTAs: four per SM (64 registers each), so 1024 ciphertexts
+  // take 1.7 waves of 608 slots rather than 3.4 waves of 304.
+  constexpr int T = 256;
+  k_sample_uniform_error<T><<<count, T, 0, s>>>(a_dst, a_stride, negate, err, seeds, L,
+                                                variance, c.log_n, c);
 }
 
 void launch_error_lift(const CtxDev& c, uint64_t* out, const int32_t* err, int count, int L,
