@@ -57,6 +57,14 @@ const char* shg_last_error(void);
  * reference's smallest-t search and uploads twiddle and CRT tables. */
 int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
                        uint64_t plaintext_modulus, shg_context** out);
+/* RnsContext::Create(log_n, qs, ps, t) with auxiliary primes ps (the BFV
+ * basis extension, rns/rns_context.cc:22-76): main limbs are q_0..q_{L-1};
+ * the auxiliary primes get their own NTT tables and the CRT constants of
+ * GenerateCrtConstantsForAuxModulus (:317-377).  Every prime is validated
+ * as in shg_context_create, and all must be distinct. */
+int shg_context_create_with_aux(int log_n, const uint64_t* qs, int num_qs, const uint64_t* ps,
+                                int num_ps, uint64_t plaintext_modulus, shg_context** out);
+int shg_context_num_aux_moduli(const shg_context* ctx);
 void shg_context_destroy(shg_context* ctx);
 int shg_context_log_n(const shg_context* ctx);
 int shg_context_num_moduli(const shg_context* ctx);
@@ -277,6 +285,63 @@ int shg_bgv_mul_relin_host_serialized(shg_context* ctx, const shg_key* relin_key
  * (rns/rns_bgv_ciphertext.h:161-174): ct [count][2][L][n] -> out. */
 int shg_bgv_rotate(shg_context* ctx, const shg_key* galois_key, uint64_t* out,
                    const uint64_t* ct, int count, shg_stream stream);
+
+/* ---------------------------------------------------------------------------
+ * RNS basis conversion and BFV, on a context with auxiliary primes.
+ * `num_limbs` main limbs q_0..q_{num_limbs-1} (the ciphertext's level + 1)
+ * and all K auxiliary primes p_0..p_{K-1}; main polys [count][num_limbs][n],
+ * auxiliary polys [count][K][n].  The reference evaluates round(sum_i v_i /
+ * q_i) in double precision inside SwitchRnsBasis; the kernels reproduce that
+ * value exactly.
+ * ------------------------------------------------------------------------- */
+
+/* RnsPolynomial::SwitchRnsBasis (rns/rns_polynomial.cc:419-525), coefficient
+ * form in and out: direction 0 main -> aux with the tables of
+ * MainPrimeModulusCrtFactors / MainPrimeModulusComplementResidues /
+ * MainLeveledModulusAuxResidues(level), direction 1 aux -> main with
+ * AuxPrimeModulusCrtFactors / AuxPrimeModulusComplementResidues /
+ * AuxModulusResidues (rns/rns_context.h:142-200). */
+int shg_poly_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                              int direction, int num_limbs, int count, shg_stream stream);
+/* ScaleAndSwitchRnsBasis main -> aux (rns/rns_polynomial.cc:527-640):
+ * round(P/Q a) mod P, coefficient form. */
+int shg_poly_scale_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                                    int num_limbs, int count, shg_stream stream);
+/* ApproxSwitchRnsBasis (rns/rns_polynomial.cc:653-724): input in NTT form when
+ * is_ntt, output coefficient form; balanced: ConvertModulusBalanced. */
+int shg_poly_approx_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                                     int direction, int num_limbs, int is_ntt, int balanced,
+                                     int count, shg_stream stream);
+/* RnsPolynomial::ModReduceMsb (rns/rns_polynomial.cc:349-417): in
+ * [count][num_limbs][n] -> out [count][num_limbs-1][n] = round(a / q_l),
+ * ql_inv as for shg_poly_modreduce_lsb.  Works on any context. */
+int shg_poly_modreduce_msb(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                           const uint64_t* ql_inv, int is_ntt, int count, int num_limbs,
+                           shg_stream stream);
+/* ScaleAndReduceRnsBasisInPlace (rns/rns_polynomial.h:458-490): (main mod Q,
+ * aux mod P) -> out = (t main - SwitchRnsBasis(t aux)) / P mod Q, in main's
+ * form. */
+int shg_poly_scale_reduce_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* main,
+                                    const uint64_t* aux, uint64_t t, int is_ntt_main,
+                                    int is_ntt_aux, int num_limbs, int count,
+                                    shg_stream stream);
+/* ApproxModReduceLsb (lsb = 1, rns/rns_polynomial.cc:726-791) or
+ * ApproxModReduceMsb (lsb = 0, :793-852) of (main mod Q, aux mod P): out
+ * [count][num_limbs][n] in NTT form. */
+int shg_poly_approx_modreduce(shg_context* ctx, uint64_t* out, const uint64_t* main,
+                              const uint64_t* aux, int lsb, uint64_t t, int is_ntt_main,
+                              int is_ntt_aux, int num_limbs, int count, shg_stream stream);
+/* RnsBfvCiphertext::operator* (Mul, rns/rns_bfv_ciphertext.cc:100-205) for
+ * `count` pairs: a, b [count][2][num_limbs][n] (NTT form) -> out
+ * [count][3][num_limbs][n]; t = the context's plaintext modulus. */
+int shg_bfv_mul(shg_context* ctx, uint64_t* out, const uint64_t* a, const uint64_t* b,
+                int count, int num_limbs, shg_stream stream);
+/* RnsBfvCiphertext::AbsorbInPlace (rns/rns_bfv_ciphertext.cc:33-98):
+ * ct [count][len][num_limbs][n] times the NTT-form plaintext [num_limbs][n]
+ * -> out (same shape). */
+int shg_bfv_absorb(shg_context* ctx, uint64_t* out, const uint64_t* ct,
+                   const uint64_t* plaintext, int len, int count, int num_limbs,
+                   shg_stream stream);
 
 /* ---------------------------------------------------------------------------
  * Encryption randomness from SHELL's ChaCha PRNG, sampled on the device.

@@ -78,6 +78,26 @@ def lib():
                                              ctypes.c_size_t, U64P]),
             "so_rns_galois_pad": (None, [vp, ctypes.c_int, ctypes.c_int, U64P, U64P, U64P, U64P,
                                          U64P]),
+            "so_rns_switch_basis": (None, [vp, INTP, ctypes.c_int, INTP, ctypes.c_int, U64P,
+                                           U64P]),
+            "so_rns_scale_switch_basis": (None, [vp, INTP, ctypes.c_int, INTP, ctypes.c_int,
+                                                 U64P, U64P]),
+            "so_rns_approx_switch_basis": (None, [vp, INTP, ctypes.c_int, INTP, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_int, U64P, U64P]),
+            "so_rns_modreduce_msb": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, U64P,
+                                                    U64P]),
+            "so_rns_scale_reduce": (None, [vp, ctypes.c_int, INTP, ctypes.c_int, ctypes.c_uint64,
+                                           ctypes.c_int, U64P, ctypes.c_int, U64P, U64P]),
+            "so_rns_approx_modreduce_lsb": (None, [vp, ctypes.c_int, INTP, ctypes.c_int,
+                                                   ctypes.c_uint64, ctypes.c_int, U64P,
+                                                   ctypes.c_int, U64P, U64P]),
+            "so_rns_approx_modreduce_msb": (None, [vp, ctypes.c_int, INTP, ctypes.c_int,
+                                                   ctypes.c_int, U64P, ctypes.c_int, U64P,
+                                                   U64P]),
+            "so_bfv_mul": (None, [vp, ctypes.c_int, INTP, ctypes.c_int, ctypes.c_uint64, U64P,
+                                  U64P, U64P]),
+            "so_bfv_absorb": (None, [vp, ctypes.c_int, INTP, ctypes.c_int, ctypes.c_uint64,
+                                     ctypes.c_int, U64P, U64P, U64P]),
             "so_chacha20_block": (None, [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_char_p,
                                          ctypes.POINTER(ctypes.c_uint8)]),
             "so_prng_bytes": (None, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_size_t,
@@ -397,6 +417,77 @@ class Rns:
         out = np.empty((2, L, self.n), np.uint64)
         lib().so_rns_encrypt_bgv(self._h, L, ctypes.c_uint64(int(t)), variance, _p(key), _p(m),
                                  bytes(seed), _p(out))
+        return out
+
+    # ---- basis conversion and BFV: the context's primes are the main primes
+    # followed by the auxiliary ones; src / dst / aux are prime indices. ----
+
+    def switch_basis(self, src, dst, poly, scale=False):
+        """SwitchRnsBasis (scale=False) or ScaleAndSwitchRnsBasis (scale=True)
+        of a coefficient-form polynomial [len(src)][n] -> [len(dst)][n]."""
+        s, sp = _ip(src)
+        d, dp = _ip(dst)
+        poly = np.ascontiguousarray(poly, dtype=np.uint64)
+        out = np.empty((len(d), self.n), np.uint64)
+        fn = lib().so_rns_scale_switch_basis if scale else lib().so_rns_switch_basis
+        fn(self._h, sp, len(s), dp, len(d), _p(poly), _p(out))
+        return out
+
+    def approx_switch_basis(self, src, dst, poly, is_ntt, balanced):
+        s, sp = _ip(src)
+        d, dp = _ip(dst)
+        poly = np.ascontiguousarray(poly, dtype=np.uint64)
+        out = np.empty((len(d), self.n), np.uint64)
+        lib().so_rns_approx_switch_basis(self._h, sp, len(s), dp, len(d), int(is_ntt),
+                                         int(balanced), _p(poly), _p(out))
+        return out
+
+    def modreduce_msb(self, poly, is_ntt=True):
+        poly = np.ascontiguousarray(poly, dtype=np.uint64)
+        L = poly.shape[0]
+        out = np.empty((L - 1, self.n), np.uint64)
+        if lib().so_rns_modreduce_msb(self._h, L, int(is_ntt), _p(poly), _p(out)):
+            raise ValueError("ModReduceMsb needs two or more limbs")
+        return out
+
+    def scale_reduce(self, aux, t, main, aux_poly, main_ntt=True, aux_ntt=True, mode=0):
+        """mode 0 ScaleAndReduceRnsBasisInPlace, 1 ApproxModReduceLsb,
+        2 ApproxModReduceMsb; main [nm][n] over primes 0..nm-1."""
+        a, ap = _ip(aux)
+        main = np.ascontiguousarray(main, dtype=np.uint64)
+        aux_poly = np.ascontiguousarray(aux_poly, dtype=np.uint64)
+        nm = main.shape[0]
+        out = np.empty_like(main)
+        if mode == 0:
+            lib().so_rns_scale_reduce(self._h, nm, ap, len(a), ctypes.c_uint64(t),
+                                      int(main_ntt), _p(main), int(aux_ntt), _p(aux_poly),
+                                      _p(out))
+        elif mode == 1:
+            lib().so_rns_approx_modreduce_lsb(self._h, nm, ap, len(a), ctypes.c_uint64(t),
+                                              int(main_ntt), _p(main), int(aux_ntt),
+                                              _p(aux_poly), _p(out))
+        else:
+            lib().so_rns_approx_modreduce_msb(self._h, nm, ap, len(a), int(main_ntt), _p(main),
+                                              int(aux_ntt), _p(aux_poly), _p(out))
+        return out
+
+    def bfv_mul(self, nm, aux, t, a, b):
+        """RnsBfvCiphertext::Mul: a, b [2][nm][n] -> [3][nm][n]."""
+        x, xp = _ip(aux)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        out = np.empty((3, nm, self.n), np.uint64)
+        lib().so_bfv_mul(self._h, nm, xp, len(x), ctypes.c_uint64(t), _p(a), _p(b), _p(out))
+        return out
+
+    def bfv_absorb(self, nm, aux, t, ct, pt):
+        """RnsBfvCiphertext::AbsorbInPlace: ct [len][nm][n], pt [nm][n]."""
+        x, xp = _ip(aux)
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        pt = np.ascontiguousarray(pt, dtype=np.uint64)
+        out = np.empty_like(ct)
+        lib().so_bfv_absorb(self._h, nm, xp, len(x), ctypes.c_uint64(t), ct.shape[0], _p(ct),
+                            _p(pt), _p(out))
         return out
 
     def modreduce_lsb(self, poly, t, is_ntt=True):

@@ -49,6 +49,7 @@
 #include "shell_encryption/oblivious_expand.h"
 #include "shell_encryption/polynomial.h"
 #include "shell_encryption/relinearization_key.h"
+#include "shell_encryption/rns/rns_bfv_ciphertext.h"
 #include "shell_encryption/rns/rns_bgv_ciphertext.h"
 #include "shell_encryption/rns/rns_context.h"
 #include "shell_encryption/rns/rns_error_params.h"
@@ -106,6 +107,18 @@ using Ctx = rlwe::RnsContext<M>;
 std::unique_ptr<Ctx> make_ctx(int log_n, const uint64_t* qs, int L, uint64_t t,
                               int* st) {
   auto ctx = Ctx::Create(log_n, std::vector<uint64_t>(qs, qs + L), {}, t);
+  if (!ctx.ok()) {
+    *st = fail(ctx.status());
+    return nullptr;
+  }
+  *st = 0;
+  return std::make_unique<Ctx>(std::move(*ctx));
+}
+
+std::unique_ptr<Ctx> make_ctx_aux(int log_n, const uint64_t* qs, int L, const uint64_t* ps,
+                                  int K, uint64_t t, int* st) {
+  auto ctx = Ctx::Create(log_n, std::vector<uint64_t>(qs, qs + L),
+                         std::vector<uint64_t>(ps, ps + K), t);
   if (!ctx.ok()) {
     *st = fail(ctx.status());
     return nullptr;
@@ -473,6 +486,137 @@ int ref_deserialize_vector(uint64_t q, const uint8_t* in, size_t len, int count,
       count, std::string(reinterpret_cast<const char*>(in), len), params->get());
   if (!v.ok()) return fail(v.status());
   from_vec(*v, out);
+  return 0;
+}
+
+// RNS basis conversions of one polynomial with the context's own tables
+// (rns/rns_context.h:142-240): mode 0 SwitchRnsBasis main (q_0..q_level) ->
+// aux; 1 SwitchRnsBasis aux -> main (every main prime); 2
+// ScaleAndSwitchRnsBasis main (level) -> aux; 3 ApproxSwitchRnsBasis aux ->
+// main (q_0..q_level); 4 ApproxSwitchRnsBasis main (level) -> aux.
+int ref_switch_basis(int log_n, const uint64_t* qs, int L, const uint64_t* ps, int K,
+                     int level, int mode, int is_ntt, int balanced, const uint64_t* in,
+                     uint64_t* out) {
+  int st;
+  auto ctx = make_ctx_aux(log_n, qs, L, ps, K, 65537, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  auto main = ctx->MainPrimeModuli();
+  main.resize(mode == 1 ? L : level + 1);
+  auto aux = ctx->AuxPrimeModuli();
+  const bool from_main = mode == 0 || mode == 2 || mode == 4;
+  auto a = make_poly(in, from_main ? (int)main.size() : K, n, is_ntt != 0);
+  absl::StatusOr<rlwe::RnsPolynomial<M>> r = absl::InternalError("mode");
+  if (mode == 0) {
+    auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(level).value();
+    auto q_hat_mod_ps = ctx->MainPrimeModulusComplementResidues(level).value();
+    auto q_mod_ps = ctx->MainLeveledModulusAuxResidues(level).value();
+    r = a.SwitchRnsBasis(main, aux, q_hat_invs, q_hat_mod_ps, q_mod_ps.RnsRep());
+  } else if (mode == 1) {
+    r = a.SwitchRnsBasis(aux, main, ctx->AuxPrimeModulusCrtFactors(),
+                         ctx->AuxPrimeModulusComplementResidues(), ctx->AuxModulusResidues());
+  } else if (mode == 2) {
+    auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(level).value();
+    r = a.ScaleAndSwitchRnsBasis(main, aux, q_hat_invs,
+                                 ctx->MainPrimeModulusInverseAuxResidues(),
+                                 ctx->AuxModulusResidues());
+  } else if (mode == 3) {
+    r = a.ApproxSwitchRnsBasis(aux, main, ctx->AuxPrimeModulusCrtFactors(),
+                               ctx->AuxPrimeModulusComplementResidues(), balanced != 0);
+  } else if (mode == 4) {
+    auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(level).value();
+    auto q_hat_mod_ps = ctx->MainPrimeModulusComplementResidues(level).value();
+    r = a.ApproxSwitchRnsBasis(main, aux, q_hat_invs, q_hat_mod_ps, balanced != 0);
+  }
+  if (!r.ok()) return fail(r.status());
+  store_poly(*r, out);
+  return 0;
+}
+
+// RnsPolynomial::ModReduceMsb with MainPrimeModulusInverseResidues()[L-1].
+int ref_modreduce_msb(int log_n, const uint64_t* qs, int L, int is_ntt, const uint64_t* in,
+                      uint64_t* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  auto moduli = ctx->MainPrimeModuli();
+  auto a = make_poly(in, L, 1 << log_n, is_ntt != 0);
+  auto ql_inv = ctx->MainPrimeModulusInverseResidues()[L - 1].Prefix(L - 1);
+  auto s2 = a.ModReduceMsb(ql_inv, moduli);
+  if (!s2.ok()) return fail(s2);
+  store_poly(a, out);
+  return 0;
+}
+
+// ScaleAndReduceRnsBasisInPlace (mode 0), ApproxModReduceLsb (1) and
+// ApproxModReduceMsb (2) of (main mod Q, aux mod P) with the context's tables.
+int ref_scale_reduce(int log_n, const uint64_t* qs, int L, const uint64_t* ps, int K,
+                     uint64_t t, int mode, int is_ntt_main, const uint64_t* main_in,
+                     int is_ntt_aux, const uint64_t* aux_in, uint64_t* out) {
+  int st;
+  auto ctx = make_ctx_aux(log_n, qs, L, ps, K, t, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  auto main = ctx->MainPrimeModuli();
+  auto aux = ctx->AuxPrimeModuli();
+  auto a = make_poly(main_in, L, n, is_ntt_main != 0);
+  auto b = make_poly(aux_in, K, n, is_ntt_aux != 0);
+  absl::Status s2;
+  if (mode == 0) {
+    s2 = a.ScaleAndReduceRnsBasisInPlace(
+        std::move(b), t, main, aux, ctx->AuxPrimeModulusCrtFactors(),
+        ctx->AuxPrimeModulusComplementResidues(), ctx->AuxModulusResidues(),
+        ctx->AuxModulusInverseResidues());
+  } else if (mode == 1) {
+    s2 = a.ApproxModReduceLsb(std::move(b), main, aux, ctx->AuxModulusInverseResidues(),
+                              ctx->AuxPrimeModulusCrtFactors(),
+                              ctx->AuxPrimeModulusComplementResidues(),
+                              ctx->PlaintextModulusInverseAuxResidues(),
+                              ctx->AuxModulusPlaintextResidue(), t);
+  } else {
+    s2 = a.ApproxModReduceMsb(std::move(b), main, aux, ctx->AuxModulusInverseResidues(),
+                              ctx->AuxPrimeModulusCrtFactors(),
+                              ctx->AuxPrimeModulusComplementResidues());
+  }
+  if (!s2.ok()) return fail(s2);
+  store_poly(a, out);
+  return 0;
+}
+
+// RnsBfvCiphertext::operator* (Mul) of `count` pairs a, b [count][2][L][n]
+// -> out [count][3][L][n]; op 1: AbsorbInPlace of a [count][len][L][n]
+// with the plaintext b [L][n] -> out [count][len][L][n].
+int ref_bfv(int log_n, const uint64_t* qs, int L, const uint64_t* ps, int K, uint64_t t,
+            int op, int len, const uint64_t* a, const uint64_t* b, int count,
+            uint64_t* out) {
+  int st;
+  auto ctx = make_ctx_aux(log_n, qs, L, ps, K, t, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, ctx->AuxPrimeModuli(), 16, 3.19);
+  if (!ep.ok()) return fail(ep.status());
+  for (int c = 0; c < count; ++c) {
+    std::vector<rlwe::RnsPolynomial<M>> ca;
+    const int la = op == 0 ? 2 : len;
+    for (int i = 0; i < la; ++i) ca.push_back(make_poly(a + ((size_t)c * la + i) * P, L, n, true));
+    rlwe::RnsBfvCiphertext<M> x(std::move(ca), moduli, 1, 1.0, &*ep, ctx.get());
+    if (op == 0) {
+      std::vector<rlwe::RnsPolynomial<M>> cb;
+      for (int i = 0; i < 2; ++i) cb.push_back(make_poly(b + ((size_t)c * 2 + i) * P, L, n, true));
+      rlwe::RnsBfvCiphertext<M> y(std::move(cb), moduli, 1, 1.0, &*ep, ctx.get());
+      auto xy = x * y;
+      if (!xy.ok()) return fail(xy.status());
+      for (int i = 0; i < 3; ++i)
+        store_poly(xy->Component(i).value(), out + ((size_t)c * 3 + i) * P);
+    } else {
+      auto s2 = x.AbsorbInPlace(make_poly(b, L, n, true));
+      if (!s2.ok()) return fail(s2);
+      for (int i = 0; i < la; ++i)
+        store_poly(x.Component(i).value(), out + ((size_t)c * la + i) * P);
+    }
+  }
   return 0;
 }
 

@@ -53,6 +53,17 @@ def lib():
         L.ref_encrypt_bgv.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_int, _U64P, _U64P, ctypes.c_char_p, ctypes.c_int,
                                       _U64P]
+        L.ref_switch_basis.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _U64P, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       _U64P, _U64P]
+        L.ref_modreduce_msb.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, ctypes.c_int, _U64P,
+                                        _U64P]
+        L.ref_scale_reduce.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _U64P, ctypes.c_int,
+                                       ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _U64P,
+                                       ctypes.c_int, _U64P, _U64P]
+        L.ref_bfv.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _U64P, ctypes.c_int,
+                              ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _U64P, _U64P,
+                              ctypes.c_int, _U64P]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -210,4 +221,61 @@ def encrypt_bgv(log_n, qs, t, variance, key, plaintexts, seeds):
     _check(lib().ref_encrypt_bgv(log_n, _p(q), L, t, variance,
                                  _p(np.ascontiguousarray(key, dtype=np.uint64)), _p(plaintexts),
                                  b"".join(bytes(s) for s in seeds), count, _p(out)))
+    return out
+
+
+def switch_basis(log_n, qs, ps, level, mode, poly, is_ntt=False, balanced=False):
+    """Basis conversions with the context's tables: mode 0 SwitchRnsBasis
+    main -> aux, 1 aux -> main, 2 ScaleAndSwitchRnsBasis main -> aux,
+    3 ApproxSwitchRnsBasis aux -> main, 4 ApproxSwitchRnsBasis main -> aux."""
+    q, p = _qs(qs), _qs(ps)
+    n = 1 << log_n
+    n_out = len(ps) if mode in (0, 2, 4) else (len(qs) if mode == 1 else level + 1)
+    poly = np.ascontiguousarray(poly, dtype=np.uint64)
+    out = np.empty((n_out, n), np.uint64)
+    _check(lib().ref_switch_basis(log_n, _p(q), len(q), _p(p), len(p), level, mode,
+                                  int(is_ntt), int(balanced), _p(poly), _p(out)))
+    return out
+
+
+def modreduce_msb(log_n, qs, poly, is_ntt=True):
+    q = _qs(qs)
+    poly = np.ascontiguousarray(poly, dtype=np.uint64)
+    out = np.empty_like(poly)
+    _check(lib().ref_modreduce_msb(log_n, _p(q), len(q), int(is_ntt), _p(poly), _p(out)))
+    return out[:-1]
+
+
+def scale_reduce(log_n, qs, ps, t, mode, main, aux, main_ntt=True, aux_ntt=True):
+    """mode 0 ScaleAndReduceRnsBasisInPlace, 1 ApproxModReduceLsb,
+    2 ApproxModReduceMsb."""
+    q, p = _qs(qs), _qs(ps)
+    main = np.ascontiguousarray(main, dtype=np.uint64)
+    aux = np.ascontiguousarray(aux, dtype=np.uint64)
+    out = np.empty_like(main)
+    _check(lib().ref_scale_reduce(log_n, _p(q), len(q), _p(p), len(p), t, mode,
+                                  int(main_ntt), _p(main), int(aux_ntt), _p(aux), _p(out)))
+    return out
+
+
+def bfv_mul(log_n, qs, ps, t, a, b):
+    """RnsBfvCiphertext::operator* of pairs a, b [count][2][L][n]."""
+    q, p = _qs(qs), _qs(ps)
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    count = a.shape[0]
+    out = np.empty((count, 3) + a.shape[2:], np.uint64)
+    _check(lib().ref_bfv(log_n, _p(q), len(q), _p(p), len(p), t, 0, 2, _p(a), _p(b), count,
+                         _p(out)))
+    return out
+
+
+def bfv_absorb(log_n, qs, ps, t, cts, pt):
+    """RnsBfvCiphertext::AbsorbInPlace of cts [count][len][L][n] by pt [L][n]."""
+    q, p = _qs(qs), _qs(ps)
+    cts = np.ascontiguousarray(cts, dtype=np.uint64)
+    pt = np.ascontiguousarray(pt, dtype=np.uint64)
+    out = np.empty_like(cts)
+    _check(lib().ref_bfv(log_n, _p(q), len(q), _p(p), len(p), t, 1, cts.shape[1], _p(cts),
+                         _p(pt), cts.shape[0], _p(out)))
     return out

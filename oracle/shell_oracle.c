@@ -7,6 +7,7 @@
 #include "shell_oracle.h"
 #include "chacha20.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -989,4 +990,335 @@ uint64_t so_compute_normalizer(int k, int log_t) {
   if (pp % 2 == 0)
     return (((uint64_t)1 << log_t) + 1) - ((uint64_t)1 << log_t_minus_r);
   return (uint64_t)1 << log_t_minus_r;
+}
+
+/* ---------------------------------------------------------------------------
+ * RNS basis conversion and BFV (rns/rns_polynomial.cc:349-852,
+ * rns/rns_polynomial.h:458-490, rns/rns_bfv_ciphertext.cc:33-205).  The
+ * so_rns holds the main primes first and the auxiliary primes after them;
+ * index lists name primes of that context.
+ * ------------------------------------------------------------------------- */
+
+/* prod_{k != skip} primes[idx[k]] mod p (Montgomery rep). */
+static uint64_t prod_mod(const so_rns* r, const int* idx, int cnt, int skip,
+                         const so_prime* p) {
+  uint64_t acc = p->r_mod_q;
+  for (int k = 0; k < cnt; k++)
+    if (k != skip) acc = mont_mul(p, acc, mont_import(p, r->primes[idx[k]]->q));
+  return acc;
+}
+
+static uint64_t mont_inverse(const so_prime* p, uint64_t x) {
+  return mont_pow(p, x, p->q - 2);
+}
+
+/* SwitchRnsBasis (rns/rns_polynomial.cc:419-525) when scale == 0, and
+ * ScaleAndSwitchRnsBasis (:527-640) when scale == 1, for Q = prod src and
+ * P = prod dst:
+ *   s_i = a_i * [P mod q_i if scale] * (Q/q_i)^-1 mod q_i,
+ *   u = round(sum_i (double)s_i / (double)q_i), summed in order i = 0..,
+ *   out_j = sum_i s_i * (Q/q_i mod p_j) - u * (Q mod p_j)         (scale 0)
+ *   out_j = sum_i s_i * (-q_i^-1 mod p_j) + u                      (scale 1).
+ * in [ns][n] and out [nd][n] coefficient form. */
+static void switch_basis(const so_rns* r, const int* src, int ns, const int* dst, int nd,
+                         int scale, const uint64_t* in, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  uint64_t* s = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)ns * n);
+  double* us = (double*)calloc(n, sizeof(double));
+  for (int i = 0; i < ns; i++) {
+    const so_prime* qi = r->primes[src[i]];
+    const uint64_t qhat_inv = mont_inverse(qi, prod_mod(r, src, ns, i, qi));
+    const uint64_t pmod = scale ? prod_mod(r, dst, nd, -1, qi) : 0;
+    const double qd = (double)qi->q;
+    for (size_t k = 0; k < n; k++) {
+      uint64_t x = in[(size_t)i * n + k];
+      if (scale) x = mont_mul(qi, x, pmod);
+      x = mont_mul(qi, x, qhat_inv);
+      s[(size_t)i * n + k] = x;
+      us[k] += (double)mont_export(qi, x) / qd;
+    }
+  }
+  for (int j = 0; j < nd; j++) {
+    const so_prime* pj = r->primes[dst[j]];
+    uint64_t* o = out + (size_t)j * n;
+    for (size_t k = 0; k < n; k++) o[k] = 0;
+    for (int i = 0; i < ns; i++) {
+      const so_prime* qi = r->primes[src[i]];
+      uint64_t w;
+      if (scale)
+        w = mont_neg(pj, mont_inverse(pj, mont_import(pj, qi->q)));
+      else
+        w = prod_mod(r, src, ns, i, pj);
+      for (size_t k = 0; k < n; k++) {
+        const uint64_t v = mont_import(pj, mont_export(qi, s[(size_t)i * n + k]));
+        o[k] = mont_add(pj, o[k], mont_mul(pj, v, w));
+      }
+    }
+    const uint64_t qmod = prod_mod(r, src, ns, -1, pj);
+    for (size_t k = 0; k < n; k++) {
+      const uint64_t u = (uint64_t)round(us[k]);
+      const uint64_t um = mont_import(pj, u);
+      o[k] = scale ? mont_add(pj, o[k], um) : mont_sub(pj, o[k], mont_mul(pj, um, qmod));
+    }
+  }
+  free(s);
+  free(us);
+}
+
+void so_rns_switch_basis(const so_rns* r, const int* src, int ns, const int* dst, int nd,
+                         const uint64_t* in, uint64_t* out) {
+  switch_basis(r, src, ns, dst, nd, 0, in, out);
+}
+
+void so_rns_scale_switch_basis(const so_rns* r, const int* src, int ns, const int* dst,
+                               int nd, const uint64_t* in, uint64_t* out) {
+  switch_basis(r, src, ns, dst, nd, 1, in, out);
+}
+
+/* ApproxSwitchRnsBasis (rns/rns_polynomial.cc:653-724): a_i * (Q/q_i)^-1 mod
+ * q_i (then iNTT when is_ntt), converted to every p_j (balanced or not),
+ * times Q/q_i mod p_j, summed.  Output coefficient form. */
+void so_rns_approx_switch_basis(const so_rns* r, const int* src, int ns, const int* dst,
+                                int nd, int is_ntt, int balanced, const uint64_t* in,
+                                uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  memset(out, 0, sizeof(uint64_t) * (size_t)nd * n);
+  for (int i = 0; i < ns; i++) {
+    const so_prime* qi = r->primes[src[i]];
+    const uint64_t qhat_inv = mont_inverse(qi, prod_mod(r, src, ns, i, qi));
+    for (size_t k = 0; k < n; k++) a[k] = mont_mul(qi, in[(size_t)i * n + k], qhat_inv);
+    if (is_ntt) so_ntt_inv(qi, a);
+    for (int j = 0; j < nd; j++) {
+      const so_prime* pj = r->primes[dst[j]];
+      const uint64_t w = prod_mod(r, src, ns, i, pj);
+      uint64_t* o = out + (size_t)j * n;
+      for (size_t k = 0; k < n; k++) {
+        const uint64_t x = mont_export(qi, a[k]);
+        const uint64_t v = balanced ? convert_balanced(qi, pj, x)
+                                    : (qi->q == pj->q ? a[k] : mont_import(pj, x));
+        o[k] = mont_add(pj, o[k], mont_mul(pj, v, w));
+      }
+    }
+  }
+  free(a);
+}
+
+/* ModReduceMsb (rns/rns_polynomial.cc:349-417): round(a / q_{L-1}) mod
+ * q_0..q_{L-2}: the last limb (iNTT when is_ntt), lifted balanced to every
+ * other limb (NTT when is_ntt), subtracted, times q_{L-1}^-1.  in [L][n] ->
+ * out [L-1][n].  3 when L <= 1. */
+int so_rns_modreduce_msb(const so_rns* r, int L, int is_ntt, const uint64_t* in,
+                         uint64_t* out) {
+  if (L <= 1) return 3;
+  const size_t n = (size_t)1 << r->log_n;
+  const so_prime* ql = r->primes[L - 1];
+  uint64_t* last = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  uint64_t* d = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  memcpy(last, in + (size_t)(L - 1) * n, sizeof(uint64_t) * n);
+  if (is_ntt) so_ntt_inv(ql, last);
+  for (int i = 0; i < L - 1; i++) {
+    const so_prime* qi = r->primes[i];
+    for (size_t k = 0; k < n; k++) d[k] = convert_balanced(ql, qi, mont_export(ql, last[k]));
+    if (is_ntt) so_ntt_fwd(qi, d);
+    const uint64_t ql_inv = r->q_invs[(size_t)(L - 1) * r->L + i];
+    for (size_t k = 0; k < n; k++)
+      out[(size_t)i * n + k] = mont_mul(qi, mont_sub(qi, in[(size_t)i * n + k], d[k]), ql_inv);
+  }
+  free(last);
+  free(d);
+  return 0;
+}
+
+static void seq_idx(int* idx, int first, int cnt) {
+  for (int k = 0; k < cnt; k++) idx[k] = first + k;
+}
+
+/* RnsPolynomial::MulInPlace(Int scalar) (rns/rns_polynomial.h:243-259). */
+static void mul_int(const so_rns* r, const int* idx, int cnt, uint64_t* poly, uint64_t c) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int i = 0; i < cnt; i++) {
+    const so_prime* p = r->primes[idx[i]];
+    const uint64_t cm = mont_import(p, c);
+    for (size_t k = 0; k < n; k++) poly[(size_t)i * n + k] = mont_mul(p, poly[(size_t)i * n + k], cm);
+  }
+}
+
+static void ntt_idx(const so_rns* r, const int* idx, int cnt, uint64_t* poly, int inverse) {
+  const size_t n = (size_t)1 << r->log_n;
+  for (int i = 0; i < cnt; i++) {
+    if (inverse)
+      so_ntt_inv(r->primes[idx[i]], poly + (size_t)i * n);
+    else
+      so_ntt_fwd(r->primes[idx[i]], poly + (size_t)i * n);
+  }
+}
+
+/* ScaleAndReduceRnsBasisInPlace (rns/rns_polynomial.h:458-490): main
+ * [nm][n] over q_0..q_{nm-1} and aux [na][n] over aux[]:
+ * out = (t * main - SwitchRnsBasis(t * aux, aux -> main)) * P^-1 mod Q, in
+ * main's form.  Note the reference's SwitchRnsBasis takes P mod q_i for
+ * every main prime of the context, so it needs nm == the context's count. */
+void so_rns_scale_reduce(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                         int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                         const uint64_t* aux_in, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  int* mi = (int*)calloc(nm, sizeof(int));
+  seq_idx(mi, 0, nm);
+  uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)na * n);
+  uint64_t* delta = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)nm * n);
+  memcpy(out, main_in, sizeof(uint64_t) * (size_t)nm * n);
+  memcpy(a, aux_in, sizeof(uint64_t) * (size_t)na * n);
+  mul_int(r, mi, nm, out, t);
+  mul_int(r, aux, na, a, t);
+  if (is_ntt_aux) ntt_idx(r, aux, na, a, 1);
+  switch_basis(r, aux, na, mi, nm, 0, a, delta);
+  if (is_ntt_main) ntt_idx(r, mi, nm, delta, 0);
+  for (int i = 0; i < nm; i++) {
+    const so_prime* qi = r->primes[i];
+    const uint64_t pinv = mont_inverse(qi, prod_mod(r, aux, na, -1, qi));
+    for (size_t k = 0; k < n; k++) {
+      uint64_t* o = out + (size_t)i * n + k;
+      *o = mont_mul(qi, mont_sub(qi, *o, delta[(size_t)i * n + k]), pinv);
+    }
+  }
+  free(mi);
+  free(a);
+  free(delta);
+}
+
+/* ApproxModReduceLsb (rns/rns_polynomial.cc:726-791) when lsb, else
+ * ApproxModReduceMsb (:793-852): out [nm][n] NTT form. */
+static void approx_modreduce(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                             int lsb, int is_ntt_main, const uint64_t* main_in,
+                             int is_ntt_aux, const uint64_t* aux_in, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n;
+  int* mi = (int*)calloc(nm, sizeof(int));
+  seq_idx(mi, 0, nm);
+  uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)na * n);
+  uint64_t* delta = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)nm * n);
+  memcpy(a, aux_in, sizeof(uint64_t) * (size_t)na * n);
+  uint64_t p_mod_t = 0;
+  if (lsb) {
+    /* P mod t over the integers (rns/rns_context.cc GeneratePlaintextModulusConstants) */
+    u128 pm = 1 % t;
+    for (int j = 0; j < na; j++) pm = (pm * (r->primes[aux[j]]->q % t)) % t;
+    p_mod_t = (uint64_t)pm;
+    for (int j = 0; j < na; j++) {
+      const so_prime* pj = r->primes[aux[j]];
+      const uint64_t rr = mont_import(pj, p_mod_t);
+      const uint64_t tinv = mont_neg(pj, mont_inverse(pj, mont_import(pj, t)));
+      uint64_t* row = a + (size_t)j * n;
+      for (size_t k = 0; k < n; k++) row[k] = mont_mul(pj, mont_mul(pj, row[k], rr), tinv);
+    }
+  }
+  so_rns_approx_switch_basis(r, aux, na, mi, nm, is_ntt_aux, lsb, a, delta);
+  ntt_idx(r, mi, nm, delta, 0);
+  if (lsb) mul_int(r, mi, nm, delta, t);
+  memcpy(out, main_in, sizeof(uint64_t) * (size_t)nm * n);
+  if (!is_ntt_main) ntt_idx(r, mi, nm, out, 0);
+  if (lsb) mul_int(r, mi, nm, out, p_mod_t);
+  for (int i = 0; i < nm; i++) {
+    const so_prime* qi = r->primes[i];
+    const uint64_t pinv = mont_inverse(qi, prod_mod(r, aux, na, -1, qi));
+    for (size_t k = 0; k < n; k++) {
+      uint64_t* o = out + (size_t)i * n + k;
+      const uint64_t dv = delta[(size_t)i * n + k];
+      *o = mont_mul(qi, lsb ? mont_add(qi, *o, dv) : mont_sub(qi, *o, dv), pinv);
+    }
+  }
+  free(mi);
+  free(a);
+  free(delta);
+}
+
+void so_rns_approx_modreduce_lsb(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                                 int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                                 const uint64_t* aux_in, uint64_t* out) {
+  approx_modreduce(r, nm, aux, na, t, 1, is_ntt_main, main_in, is_ntt_aux, aux_in, out);
+}
+
+void so_rns_approx_modreduce_msb(const so_rns* r, int nm, const int* aux, int na,
+                                 int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                                 const uint64_t* aux_in, uint64_t* out) {
+  approx_modreduce(r, nm, aux, na, 0, 0, is_ntt_main, main_in, is_ntt_aux, aux_in, out);
+}
+
+/* RnsBfvCiphertext::Mul (rns/rns_bfv_ciphertext.cc:100-205), after Kim et
+ * al.: b_j -> coefficient form -> SwitchRnsBasis to P -> NTT; a_i ->
+ * coefficient form -> ScaleAndSwitchRnsBasis to P (round(P/Q a_i)) ->
+ * SwitchRnsBasis back to Q -> NTT both; the tensor product mod Q and mod P;
+ * each component ScaleAndReduceRnsBasisInPlace'd by t.  a, b [2][nm][n]
+ * NTT form over q_0..q_{nm-1} -> out [3][nm][n]. */
+void so_bfv_mul(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                const uint64_t* a, const uint64_t* b, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n, Pm = (size_t)nm * n, Pa = (size_t)na * n;
+  int* mi = (int*)calloc(nm, sizeof(int));
+  seq_idx(mi, 0, nm);
+  uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * Pm);
+  uint64_t* b_aux = (uint64_t*)malloc(sizeof(uint64_t) * 2 * Pa);
+  uint64_t* a_aux = (uint64_t*)malloc(sizeof(uint64_t) * 2 * Pa);
+  uint64_t* a_main = (uint64_t*)malloc(sizeof(uint64_t) * 2 * Pm);
+  uint64_t* t_main = (uint64_t*)calloc(3 * Pm, sizeof(uint64_t));
+  uint64_t* t_aux = (uint64_t*)calloc(3 * Pa, sizeof(uint64_t));
+  for (int j = 0; j < 2; j++) {
+    memcpy(tmp, b + j * Pm, sizeof(uint64_t) * Pm);
+    ntt_idx(r, mi, nm, tmp, 1);
+    switch_basis(r, mi, nm, aux, na, 0, tmp, b_aux + j * Pa);
+    ntt_idx(r, aux, na, b_aux + j * Pa, 0);
+  }
+  for (int i = 0; i < 2; i++) {
+    memcpy(tmp, a + i * Pm, sizeof(uint64_t) * Pm);
+    ntt_idx(r, mi, nm, tmp, 1);
+    switch_basis(r, mi, nm, aux, na, 1, tmp, a_aux + i * Pa);
+    switch_basis(r, aux, na, mi, nm, 0, a_aux + i * Pa, a_main + i * Pm);
+    ntt_idx(r, mi, nm, a_main + i * Pm, 0);
+    ntt_idx(r, aux, na, a_aux + i * Pa, 0);
+  }
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) {
+      for (int l = 0; l < nm; l++)
+        so_fma(r->primes[l], t_main + (i + j) * Pm + l * n, a_main + i * Pm + l * n,
+               b + j * Pm + l * n, n);
+      for (int l = 0; l < na; l++)
+        so_fma(r->primes[aux[l]], t_aux + (i + j) * Pa + l * n, a_aux + i * Pa + l * n,
+               b_aux + j * Pa + l * n, n);
+    }
+  for (int k = 0; k < 3; k++)
+    so_rns_scale_reduce(r, nm, aux, na, t, 1, t_main + k * Pm, 1, t_aux + k * Pa,
+                        out + k * Pm);
+  free(mi); free(tmp); free(b_aux); free(a_aux); free(a_main); free(t_main); free(t_aux);
+}
+
+/* RnsBfvCiphertext::AbsorbInPlace (rns/rns_bfv_ciphertext.cc:33-98): the
+ * plaintext (NTT form) is switched to P as for the second factor of Mul;
+ * each component is scaled to P, switched back, multiplied by the plaintext
+ * mod Q and mod P and scale-reduced by t.  ct [len][nm][n] -> out. */
+void so_bfv_absorb(const so_rns* r, int nm, const int* aux, int na, uint64_t t, int len,
+                   const uint64_t* ct, const uint64_t* pt, uint64_t* out) {
+  const size_t n = (size_t)1 << r->log_n, Pm = (size_t)nm * n, Pa = (size_t)na * n;
+  int* mi = (int*)calloc(nm, sizeof(int));
+  seq_idx(mi, 0, nm);
+  uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * Pm);
+  uint64_t* pt_aux = (uint64_t*)malloc(sizeof(uint64_t) * Pa);
+  uint64_t* c_aux = (uint64_t*)malloc(sizeof(uint64_t) * Pa);
+  uint64_t* c_main = (uint64_t*)malloc(sizeof(uint64_t) * Pm);
+  memcpy(tmp, pt, sizeof(uint64_t) * Pm);
+  ntt_idx(r, mi, nm, tmp, 1);
+  switch_basis(r, mi, nm, aux, na, 0, tmp, pt_aux);
+  ntt_idx(r, aux, na, pt_aux, 0);
+  for (int c = 0; c < len; c++) {
+    memcpy(tmp, ct + c * Pm, sizeof(uint64_t) * Pm);
+    ntt_idx(r, mi, nm, tmp, 1);
+    switch_basis(r, mi, nm, aux, na, 1, tmp, c_aux);
+    switch_basis(r, aux, na, mi, nm, 0, c_aux, c_main);
+    ntt_idx(r, mi, nm, c_main, 0);
+    for (int l = 0; l < nm; l++)
+      so_mul(r->primes[l], c_main + l * n, pt + l * n, c_main + l * n, n);
+    ntt_idx(r, aux, na, c_aux, 0);
+    for (int l = 0; l < na; l++)
+      so_mul(r->primes[aux[l]], c_aux + l * n, pt_aux + l * n, c_aux + l * n, n);
+    so_rns_scale_reduce(r, nm, aux, na, t, 1, c_main, 1, c_aux, out + c * Pm);
+  }
+  free(mi); free(tmp); free(pt_aux); free(c_aux); free(c_main);
 }

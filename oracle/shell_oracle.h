@@ -161,6 +161,39 @@ void so_deserialize_vector(const so_prime* p, const uint8_t* in, size_t count,
 /* ObliviousExpander::ComputeNormalizer */
 uint64_t so_compute_normalizer(int k, int log_t);
 
+/* ---- RNS basis conversion and BFV: the so_rns holds the main primes first
+ * and the auxiliary primes after them; index lists name its primes. -------- */
+/* SwitchRnsBasis: in [ns][n] over src[] (coefficient form) -> out [nd][n]. */
+void so_rns_switch_basis(const so_rns* r, const int* src, int ns, const int* dst, int nd,
+                         const uint64_t* in, uint64_t* out);
+/* ScaleAndSwitchRnsBasis: round(P/Q * a) mod P, Q = prod src, P = prod dst. */
+void so_rns_scale_switch_basis(const so_rns* r, const int* src, int ns, const int* dst,
+                               int nd, const uint64_t* in, uint64_t* out);
+/* ApproxSwitchRnsBasis; is_ntt: input in NTT form; output coefficient form. */
+void so_rns_approx_switch_basis(const so_rns* r, const int* src, int ns, const int* dst,
+                                int nd, int is_ntt, int balanced, const uint64_t* in,
+                                uint64_t* out);
+/* ModReduceMsb: in [L][n] over q_0..q_{L-1} -> out [L-1][n]; 3 if L <= 1. */
+int so_rns_modreduce_msb(const so_rns* r, int L, int is_ntt, const uint64_t* in,
+                         uint64_t* out);
+/* ScaleAndReduceRnsBasisInPlace: main [nm][n] over q_0.., aux [na][n] over aux[]. */
+void so_rns_scale_reduce(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                         int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                         const uint64_t* aux_in, uint64_t* out);
+/* ApproxModReduceLsb / ApproxModReduceMsb: out [nm][n] NTT form. */
+void so_rns_approx_modreduce_lsb(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                                 int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                                 const uint64_t* aux_in, uint64_t* out);
+void so_rns_approx_modreduce_msb(const so_rns* r, int nm, const int* aux, int na,
+                                 int is_ntt_main, const uint64_t* main_in, int is_ntt_aux,
+                                 const uint64_t* aux_in, uint64_t* out);
+/* RnsBfvCiphertext::Mul: a, b [2][nm][n] NTT form -> out [3][nm][n]. */
+void so_bfv_mul(const so_rns* r, int nm, const int* aux, int na, uint64_t t,
+                const uint64_t* a, const uint64_t* b, uint64_t* out);
+/* RnsBfvCiphertext::AbsorbInPlace: ct [len][nm][n], pt [nm][n] NTT -> out. */
+void so_bfv_absorb(const so_rns* r, int nm, const int* aux, int na, uint64_t t, int len,
+                   const uint64_t* ct, const uint64_t* pt, uint64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -161,6 +161,9 @@ int set_error(int code, const std::string& msg) { return fail(code, msg); }
 
 struct shg_context {
   int log_n = 0, n = 0, L = 0;
+  int K = 0;  // auxiliary primes (BFV basis extension), after the L main ones
+  // Basis-conversion tables (BasisConv) by slot, see conv_slot(); K > 0 only.
+  shg::BasisConv* d_conv = nullptr;
   uint64_t t = 0;
   int device = 0;
   std::vector<HostPrime> hp;
@@ -193,6 +196,12 @@ struct shg_context {
   CtxDev dev() const {
     return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min,
                   ks_fused};
+  }
+  // The auxiliary primes as a context of their own (NTTs and pointwise ops
+  // over aux limbs); there is no cross-prime table in this view.
+  CtxDev aux_dev() const {
+    return CtxDev{log_n, n, K, d_primes + L, d_tw_fwd + (size_t)L * n,
+                  d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -277,6 +286,109 @@ int chunk_for(shg_context* ctx, size_t per_ct_bytes, int count) {
   return std::max(c, 1);
 }
 
+// ---- RNS basis conversion tables (BFV) --------------------------------------
+//
+// Slots of ctx->d_conv for a main prefix q_0..q_l (l = level) and all K
+// auxiliary primes p_0..p_{K-1}:
+//   l           SwitchRnsBasis main -> aux (MainPrimeModulusCrtFactors(l),
+//               MainPrimeModulusComplementResidues(l), MainLeveledModulusAuxResidues(l))
+//   L + l       ScaleAndSwitchRnsBasis main -> aux (times P mod q_i,
+//               -q_i^-1 mod p_j, MainPrimeModulusInverseAuxResidues)
+//   2L + 2l + b ApproxSwitchRnsBasis main -> aux, b = balanced
+//   4L + l      SwitchRnsBasis aux -> main q_0..q_l (AuxPrimeModulusCrtFactors,
+//               AuxPrimeModulusComplementResidues, AuxModulusResidues)
+//   5L + 2l + b ApproxSwitchRnsBasis aux -> main q_0..q_l
+//   7L + l      slot 4L + l with the source first multiplied by the context's t
+//               (ScaleAndReduceRnsBasisInPlace's t * polynomial_aux)
+// (rns/rns_context.cc:169-317 define the tables; every value here is the
+// same residue computed directly.)
+enum ConvKind { CONV_SWITCH_UP = 0, CONV_SCALE_UP = 1, CONV_APPROX_UP = 2, CONV_SWITCH_DOWN = 4,
+                CONV_APPROX_DOWN = 5, CONV_SWITCH_DOWN_T = 7 };
+
+int conv_slot(const shg_context* ctx, int kind, int level, int balanced = 0) {
+  const int L = ctx->L;
+  switch (kind) {
+    case CONV_SWITCH_UP: return level;
+    case CONV_SCALE_UP: return L + level;
+    case CONV_APPROX_UP: return 2 * L + 2 * level + balanced;
+    case CONV_SWITCH_DOWN: return 4 * L + level;
+    case CONV_APPROX_DOWN: return 5 * L + 2 * level + balanced;
+    default: return 7 * L + level;
+  }
+}
+
+// prod_{k in [k0, k1), k != skip} hp[k].q mod q (plain).
+uint64_t prod_mod(const shg_context* ctx, int k0, int k1, int skip, uint64_t q) {
+  uint64_t acc = 1 % q;
+  for (int k = k0; k < k1; ++k)
+    if (k != skip) acc = mulmod(acc, ctx->hp[k].q % q, q);
+  return acc;
+}
+
+uint64_t invmod(uint64_t x, uint64_t q) { return powmod(x, q - 2, q); }
+
+// Table for sources [s0, s0 + ns) -> destinations [d0, d0 + nd) of the
+// context's prime array.  mode 0 switch, 1 scale and switch, 2 approximate;
+// `pre` is a plain factor applied to every source value first.
+shg::BasisConv make_conv(const shg_context* ctx, int s0, int ns, int d0, int nd, int mode,
+                         int balanced, uint64_t pre) {
+  shg::BasisConv bc;
+  memset(&bc, 0, sizeof(bc));
+  bc.ns = ns;
+  bc.nd = nd;
+  bc.src0 = s0;
+  bc.dst0 = d0;
+  bc.mode = mode;
+  bc.balanced = balanced;
+  for (int i = 0; i < ns; ++i) {
+    const uint64_t q = ctx->hp[s0 + i].q;
+    uint64_t m = invmod(prod_mod(ctx, s0, s0 + ns, s0 + i, q), q);  // (Q/q_i)^-1
+    if (mode == 1) m = mulmod(m, prod_mod(ctx, d0, d0 + nd, -1, q), q);  // * P
+    m = mulmod(m, pre % q, q);
+    bc.smul[i] = to_mont(m, q);
+    const u128 two64 = (u128)1 << 64;
+    bc.rinv[i] = (uint64_t)(two64 / q);
+    bc.rho[i] = (uint64_t)((((u128)(uint64_t)(two64 % q)) << 64) / q);
+    bc.qd[i] = (double)q;
+  }
+  for (int j = 0; j < nd; ++j) {
+    const uint64_t p = ctx->hp[d0 + j].q;
+    for (int i = 0; i < ns; ++i) {
+      const uint64_t qi = ctx->hp[s0 + i].q;
+      uint64_t w;
+      if (mode == 1)
+        w = (p - invmod(qi % p, p)) % p;  // -q_i^-1 mod p_j
+      else
+        w = prod_mod(ctx, s0, s0 + ns, s0 + i, p);  // (Q/q_i) mod p_j
+      const uint64_t wm = to_mont(w, p);
+      bc.w[i * nd + j] = wm;
+      bc.ws[i * nd + j] = shoup_of(wm, p);
+      bc.wq[i * nd + j] = mulmod(qi % p, wm, p);
+    }
+    const uint64_t z = mode == 1 ? 1 % p : prod_mod(ctx, s0, s0 + ns, -1, p);
+    bc.z[j] = to_mont(z, p);
+    bc.zs[j] = shoup_of(bc.z[j], p);
+  }
+  return bc;
+}
+
+std::vector<shg::BasisConv> make_conv_tables(const shg_context* ctx) {
+  const int L = ctx->L, K = ctx->K;
+  std::vector<shg::BasisConv> t((size_t)8 * L);
+  for (int l = 0; l < L; ++l) {
+    const int m = l + 1;
+    t[conv_slot(ctx, CONV_SWITCH_UP, l)] = make_conv(ctx, 0, m, L, K, 0, 0, 1);
+    t[conv_slot(ctx, CONV_SCALE_UP, l)] = make_conv(ctx, 0, m, L, K, 1, 0, 1);
+    for (int b = 0; b < 2; ++b) {
+      t[conv_slot(ctx, CONV_APPROX_UP, l, b)] = make_conv(ctx, 0, m, L, K, 2, b, 1);
+      t[conv_slot(ctx, CONV_APPROX_DOWN, l, b)] = make_conv(ctx, L, K, 0, m, 2, b, 1);
+    }
+    t[conv_slot(ctx, CONV_SWITCH_DOWN, l)] = make_conv(ctx, L, K, 0, m, 0, 0, 1);
+    t[conv_slot(ctx, CONV_SWITCH_DOWN_T, l)] = make_conv(ctx, L, K, 0, m, 0, 0, ctx->t);
+  }
+  return t;
+}
+
 }  // namespace
 
 extern "C" {
@@ -285,6 +397,11 @@ const char* shg_last_error(void) { return t_last_error.c_str(); }
 
 int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
                        uint64_t plaintext_modulus, shg_context** out) {
+  return shg_context_create_with_aux(log_n, qs, num_qs, nullptr, 0, plaintext_modulus, out);
+}
+
+int shg_context_create_with_aux(int log_n, const uint64_t* qs, int num_qs, const uint64_t* ps,
+                                int num_ps, uint64_t plaintext_modulus, shg_context** out) {
   if (out == nullptr) return fail(SHG_INVALID_ARGUMENT, "null output handle");
   *out = nullptr;
   if (plaintext_modulus == 0)
@@ -297,24 +414,35 @@ int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
     return fail(SHG_INVALID_ARGUMENT,
                 "`qs` must hold between 1 and " + std::to_string(shg::kMaxLimbs) +
                     " prime moduli");
+  if (num_ps < 0 || num_ps > shg::kMaxLimbs || (num_ps > 0 && ps == nullptr))
+    return fail(SHG_INVALID_ARGUMENT, "`ps` must hold at most " +
+                                          std::to_string(shg::kMaxLimbs) + " prime moduli");
+  std::vector<uint64_t> all(qs, qs + num_qs);
+  if (num_ps > 0) all.insert(all.end(), ps, ps + num_ps);
+  for (size_t i = 0; i < all.size(); ++i)
+    for (size_t j = 0; j < i; ++j)
+      if (all[i] == all[j])
+        return fail(SHG_INVALID_ARGUMENT, "the prime moduli must be distinct");
   shg_context* ctx = new shg_context();
   ctx->log_n = log_n;
   ctx->n = 1 << log_n;
   ctx->L = num_qs;
+  ctx->K = num_ps;
   ctx->t = plaintext_modulus;
   cudaGetDevice(&ctx->device);
-  ctx->hp.resize(num_qs);
-  for (int i = 0; i < num_qs; ++i) {
-    int st = make_prime(qs[i], log_n, &ctx->hp[i]);
+  const int NP = num_qs + num_ps;  // main primes, then auxiliary ones
+  ctx->hp.resize(NP);
+  for (int i = 0; i < NP; ++i) {
+    int st = make_prime(all[i], log_n, &ctx->hp[i]);
     if (st != SHG_OK) {
       delete ctx;
       return st;
     }
   }
   const int n = ctx->n, L = num_qs;
-  std::vector<PrimeDev> pd(L);
-  std::vector<Tw> twf((size_t)L * n), twi((size_t)L * n);
-  for (int i = 0; i < L; ++i) {
+  std::vector<PrimeDev> pd(NP);
+  std::vector<Tw> twf((size_t)NP * n), twi((size_t)NP * n);
+  for (int i = 0; i < NP; ++i) {
     const HostPrime& h = ctx->hp[i];
     PrimeDev& d = pd[i];
     memset(&d, 0, sizeof(d));
@@ -338,25 +466,32 @@ int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
     }
   }
   ctx->small_q = 1;
-  for (int i = 0; i < L; ++i)
-    if ((qs[i] >> 58) != 0) ctx->small_q = 0;
+  for (int i = 0; i < NP; ++i)
+    if ((all[i] >> 58) != 0) ctx->small_q = 0;
   ctx->qmod.resize((size_t)L * L);
   for (int i = 0; i < L; ++i)
     for (int j = 0; j < L; ++j) ctx->qmod[(size_t)i * L + j] = qs[i] % qs[j];
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_primes, sizeof(PrimeDev) * L);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_fwd, sizeof(Tw) * L * n);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_inv, sizeof(Tw) * L * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_primes, sizeof(PrimeDev) * NP);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_fwd, sizeof(Tw) * NP * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tw_inv, sizeof(Tw) * NP * n);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_qmod, sizeof(uint64_t) * L * L);
   if (e == cudaSuccess)
-    e = cudaMemcpy(ctx->d_primes, pd.data(), sizeof(PrimeDev) * L,
+    e = cudaMemcpy(ctx->d_primes, pd.data(), sizeof(PrimeDev) * NP,
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = cudaMemcpy(ctx->d_tw_fwd, twf.data(), sizeof(Tw) * L * n,
+    e = cudaMemcpy(ctx->d_tw_fwd, twf.data(), sizeof(Tw) * NP * n,
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = cudaMemcpy(ctx->d_tw_inv, twi.data(), sizeof(Tw) * L * n,
+    e = cudaMemcpy(ctx->d_tw_inv, twi.data(), sizeof(Tw) * NP * n,
                    cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && num_ps > 0) {
+    std::vector<shg::BasisConv> tables = make_conv_tables(ctx);
+    e = cudaMalloc(&ctx->d_conv, sizeof(shg::BasisConv) * tables.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(ctx->d_conv, tables.data(), sizeof(shg::BasisConv) * tables.size(),
+                     cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess)
     e = cudaMemcpy(ctx->d_qmod, ctx->qmod.data(), sizeof(uint64_t) * L * L,
                    cudaMemcpyHostToDevice);
@@ -370,6 +505,7 @@ int shg_context_create(int log_n, const uint64_t* qs, int num_qs,
 
 void shg_context_destroy(shg_context* ctx) {
   if (!ctx) return;
+  cudaFree(ctx->d_conv);
   cudaFree(ctx->d_primes);
   cudaFree(ctx->d_tw_fwd);
   cudaFree(ctx->d_tw_inv);
@@ -558,19 +694,30 @@ int shg_gadget_decompose(shg_context* ctx, int num_limbs, const int* log_bs,
   return launch_status("gadget decompose");
 }
 
-int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
-                           uint64_t t, const uint64_t* ql_inv, int is_ntt,
-                           int count, int num_limbs, shg_stream s) {
+}  // extern "C"
+
+namespace {
+
+// ModReduceLsb (msb = 0, rns/rns_polynomial.cc:262-344) and ModReduceMsb
+// (msb = 1, :349-417) share one pipeline: the top limb times k (iNTT and
+// ExportInt folded in), lifted balanced to every other limb (NTT), then
+// out_i = in_i * c1 + delta_i * c2 with (k, c1, c2) = ((q_l - r) / t,
+// r * ql_inv, t * ql_inv) for Lsb (r = q_l mod t) and (1, ql_inv, -ql_inv)
+// for Msb.
+int modreduce_impl(shg_context* ctx, uint64_t* out, const uint64_t* in, uint64_t t,
+                   const uint64_t* ql_inv, int is_ntt, int count, int num_limbs, shg_stream s,
+                   int msb) {
   int st = check_limbs(ctx, count, num_limbs);
   if (st) return st;
   if (num_limbs <= 1)
     return fail(SHG_INVALID_ARGUMENT,
-                "ModReduceLsb cannot apply with only one prime modulus.");
+                msb ? "ModReduceMsb cannot apply with only one prime modulus."
+                    : "ModReduceLsb cannot apply with only one prime modulus.");
   if (!ql_inv)
     return fail(SHG_INVALID_ARGUMENT,
                 "`ql_inv` must be defined with respect to " +
                     std::to_string(num_limbs - 1) + " moduli.");
-  if (t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
+  if (!msb && t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
   if (count == 0) return SHG_OK;
   if ((st = check_ptrs({out, in}))) return st;
   {
@@ -582,16 +729,18 @@ int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
   }
   const int Lr = num_limbs - 1;
   const HostPrime& hl = ctx->hp[Lr];
-  const uint64_t r = hl.q % t;
-  const uint64_t k = (hl.q - r) / t;
+  const uint64_t r = msb ? 1 : hl.q % t;
+  const uint64_t k = msb ? 1 : (hl.q - r) / t;
   ScalarPack sc{};
   for (int i = 0; i < Lr; ++i) {
     const HostPrime& h = ctx->hp[i];
     const uint64_t qlinv_plain = from_mont(ql_inv[i], h.q, h.inv_r);
-    // out = (in * r + delta * t) * ql^{-1}; in and out are Montgomery, delta
-    // is produced in plain form, hence c2 carries an extra 2^64.
+    // out = (in * r + delta * t) * ql^{-1} (Lsb) or (in - delta) * ql^{-1}
+    // (Msb); in and out are Montgomery, delta is produced in plain form,
+    // hence c2 carries an extra 2^64.
     const uint64_t c1 = mulmod(r % h.q, qlinv_plain, h.q);
-    const uint64_t c2 = mulmod(mulmod(t % h.q, h.r_mod_q, h.q), qlinv_plain, h.q);
+    const uint64_t tm = msb ? (h.q - 1) : t % h.q;
+    const uint64_t c2 = mulmod(mulmod(tm, h.r_mod_q, h.q), qlinv_plain, h.q);
     sc.v[4 * i] = c1;
     sc.v[4 * i + 1] = shoup_of(c1, h.q);
     sc.v[4 * i + 2] = c2;
@@ -611,7 +760,23 @@ int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
     shg::launch_modreduce_coeff(ctx->dev(), out, in, kp, shoup_of(kp, hl.q), sc,
                                 count, num_limbs, (cudaStream_t)s);
   }
-  return launch_status("modreduce_lsb");
+  return launch_status(msb ? "modreduce_msb" : "modreduce_lsb");
+}
+
+}  // namespace
+
+extern "C" {
+
+int shg_poly_modreduce_lsb(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                           uint64_t t, const uint64_t* ql_inv, int is_ntt,
+                           int count, int num_limbs, shg_stream s) {
+  return modreduce_impl(ctx, out, in, t, ql_inv, is_ntt, count, num_limbs, s, 0);
+}
+
+int shg_poly_modreduce_msb(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                           const uint64_t* ql_inv, int is_ntt, int count, int num_limbs,
+                           shg_stream s) {
+  return modreduce_impl(ctx, out, in, 0, ql_inv, is_ntt, count, num_limbs, s, 1);
 }
 
 int shg_ct_tensor(shg_context* ctx, uint64_t* out, const uint64_t* a,
@@ -1727,6 +1892,340 @@ int shg_bgv_encrypt(shg_context* ctx, uint64_t* out, const uint64_t* key,
     }
   }
   return launch_status("bgv_encrypt");
+}
+
+// ---------------------------------------------------------------------------
+// RNS basis conversion and BFV (auxiliary primes)
+// ---------------------------------------------------------------------------
+
+int shg_context_num_aux_moduli(const shg_context* ctx) { return ctx ? ctx->K : 0; }
+
+static int check_aux(shg_context* ctx, int count, int num_limbs) {
+  int st = check_limbs(ctx, count, num_limbs);
+  if (st) return st;
+  if (ctx->K == 0)
+    return fail(SHG_INVALID_ARGUMENT, "the context has no auxiliary prime moduli");
+  return SHG_OK;
+}
+
+static const shg::BasisConv* conv(const shg_context* ctx, int kind, int level, int balanced = 0) {
+  return ctx->d_conv + conv_slot(ctx, kind, level, balanced);
+}
+
+int shg_poly_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                              int direction, int num_limbs, int count, shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (direction != 0 && direction != 1)
+    return fail(SHG_INVALID_ARGUMENT, "`direction` must be 0 (main to aux) or 1 (aux to main)");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  const size_t n = ctx->n, m = (size_t)num_limbs * n, a = (size_t)ctx->K * n;
+  const int l = num_limbs - 1;
+  if (direction == 0)
+    shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SWITCH_UP, l), num_limbs, ctx->K, in,
+                             m, out, a, count, ctx->log_n, (cudaStream_t)stream);
+  else
+    shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SWITCH_DOWN, l), ctx->K, num_limbs,
+                             in, a, out, m, count, ctx->log_n, (cudaStream_t)stream);
+  return launch_status("switch_rns_basis");
+}
+
+int shg_poly_scale_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                                    int num_limbs, int count, shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  const size_t n = ctx->n;
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SCALE_UP, num_limbs - 1), num_limbs,
+                           ctx->K, in, (size_t)num_limbs * n, out, (size_t)ctx->K * n, count,
+                           ctx->log_n, (cudaStream_t)stream);
+  return launch_status("scale_switch_rns_basis");
+}
+
+int shg_poly_approx_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
+                                     int direction, int num_limbs, int is_ntt, int balanced,
+                                     int count, shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (direction != 0 && direction != 1)
+    return fail(SHG_INVALID_ARGUMENT, "`direction` must be 0 (main to aux) or 1 (aux to main)");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, in}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t n = ctx->n, m = (size_t)num_limbs * n, a = (size_t)ctx->K * n;
+  const int l = num_limbs - 1, ns = direction == 0 ? num_limbs : ctx->K;
+  const size_t in_elems = direction == 0 ? m : a;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  const uint64_t* src = in;
+  if (is_ntt) {
+    // ApproxSwitchRnsBasis's inverse NTT after the (Q/q_i)^-1 factor; the
+    // two commute, so the inputs are transformed first.
+    if ((st = ctx->ensure_ws((size_t)count * in_elems * sizeof(uint64_t)))) return st;
+    const shg::CtxDev view = direction == 0 ? ctx->dev() : ctx->aux_dev();
+    shg::launch_ntt_inv(view, in, ctx->ws, count * ns, ns, 0, s);
+    src = ctx->ws;
+  }
+  if (direction == 0)
+    shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_APPROX_UP, l, balanced != 0),
+                             num_limbs, ctx->K, src, m, out, a, count, ctx->log_n, s);
+  else
+    shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_APPROX_DOWN, l, balanced != 0),
+                             ctx->K, num_limbs, src, a, out, m, count, ctx->log_n, s);
+  return launch_status("approx_switch_rns_basis");
+}
+
+// P^-1 mod q_i (plain), P = the product of the auxiliary primes.
+static uint64_t p_inv_mod(const shg_context* ctx, int i) {
+  const uint64_t q = ctx->hp[i].q;
+  return invmod(prod_mod(ctx, ctx->L, ctx->L + ctx->K, -1, q), q);
+}
+
+// out_i = main_i * c_i - delta_i * d_i (sign 1) or + (sign 0), c, d plain.
+static void combine(shg_context* ctx, uint64_t* out, const uint64_t* main_ntt,
+                    const uint64_t* delta, const uint64_t* c, const uint64_t* d, int sign,
+                    int count, int Lm, cudaStream_t s) {
+  shg::ScalarPack cd{};
+  for (int i = 0; i < Lm; ++i) {
+    const uint64_t q = ctx->hp[i].q;
+    cd.v[2 * i] = to_mont(c[i], q);
+    cd.v[2 * i + 1] = to_mont(d[i], q);
+  }
+  shg::launch_lin2(ctx->dev(), out, main_ntt, delta, cd, sign, count, Lm, s);
+}
+
+// aux [count][K][n] times a plain factor per aux prime into dst.
+static void scale_aux(shg_context* ctx, uint64_t* dst, const uint64_t* aux,
+                      const std::vector<uint64_t>& f, int count, cudaStream_t s) {
+  shg::ScalarPack sc{};
+  for (int j = 0; j < ctx->K; ++j) {
+    const uint64_t p = ctx->hp[ctx->L + j].q;
+    sc.v[2 * j] = f[j] % p;
+    sc.v[2 * j + 1] = shoup_of(sc.v[2 * j], p);
+  }
+  shg::launch_pointwise(ctx->aux_dev(), shg::PW_MUL_SHOUP, dst, aux, nullptr, sc, count,
+                        ctx->K, s);
+}
+
+int shg_poly_scale_reduce_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* main,
+                                    const uint64_t* aux, uint64_t t, int is_ntt_main,
+                                    int is_ntt_aux, int num_limbs, int count,
+                                    shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, main, aux}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Lm = num_limbs, K = ctx->K, l = Lm - 1;
+  const size_t n = ctx->n, a_elems = (size_t)count * K * n, m_elems = (size_t)count * Lm * n;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws((a_elems + m_elems) * sizeof(uint64_t)))) return st;
+  uint64_t* aux_c = ctx->ws;
+  uint64_t* delta = ctx->ws + a_elems;
+  const shg::CtxDev aux_view = ctx->aux_dev();
+  const shg::BasisConv* bc;
+  if (t == ctx->t) {  // t folded into the conversion's source factor
+    if (is_ntt_aux) shg::launch_ntt_inv(aux_view, aux, aux_c, count * K, K, 0, s);
+    bc = conv(ctx, CONV_SWITCH_DOWN_T, l);
+  } else {
+    scale_aux(ctx, aux_c, aux, std::vector<uint64_t>(K, t), count, s);
+    if (is_ntt_aux) shg::launch_ntt_inv(aux_view, aux_c, aux_c, count * K, K, 0, s);
+    bc = conv(ctx, CONV_SWITCH_DOWN, l);
+  }
+  shg::launch_switch_basis(ctx->d_primes, bc, K, Lm,
+                           (is_ntt_aux || t != ctx->t) ? aux_c : aux, (size_t)K * n, delta,
+                           (size_t)Lm * n, count, ctx->log_n, s);
+  if (is_ntt_main) shg::launch_ntt_fwd(ctx->dev(), delta, delta, count * Lm, Lm, s);
+  std::vector<uint64_t> c(Lm), d(Lm);
+  for (int i = 0; i < Lm; ++i) {
+    d[i] = p_inv_mod(ctx, i);
+    c[i] = mulmod(t % ctx->hp[i].q, d[i], ctx->hp[i].q);
+  }
+  combine(ctx, out, main, delta, c.data(), d.data(), 1, count, Lm, s);
+  return launch_status("scale_reduce_rns_basis");
+}
+
+int shg_poly_approx_modreduce(shg_context* ctx, uint64_t* out, const uint64_t* main,
+                              const uint64_t* aux, int lsb, uint64_t t, int is_ntt_main,
+                              int is_ntt_aux, int num_limbs, int count, shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (lsb && t == 0) return fail(SHG_INVALID_ARGUMENT, "`t` must be positive.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, main, aux}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Lm = num_limbs, K = ctx->K, l = Lm - 1;
+  const size_t n = ctx->n, a_elems = (size_t)count * K * n, m_elems = (size_t)count * Lm * n;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws((a_elems + 2 * m_elems) * sizeof(uint64_t)))) return st;
+  uint64_t* aux_c = ctx->ws;
+  uint64_t* delta = ctx->ws + a_elems;
+  uint64_t* main_c = delta + m_elems;
+  const shg::CtxDev aux_view = ctx->aux_dev();
+  uint64_t p_mod_t = 0;
+  const uint64_t* src = aux;
+  if (lsb) {
+    // P mod t over the integers; aux times p_mod_t * (-t^-1) mod p_j
+    // (ApproxModReduceLsb, rns/rns_polynomial.cc:769-779)
+    u128 pm = 1 % t;
+    for (int j = 0; j < K; ++j) pm = pm * (ctx->hp[ctx->L + j].q % t) % t;
+    p_mod_t = (uint64_t)pm;
+    std::vector<uint64_t> f(K);
+    for (int j = 0; j < K; ++j) {
+      const uint64_t p = ctx->hp[ctx->L + j].q;
+      f[j] = mulmod(p_mod_t % p, (p - invmod(t % p, p)) % p, p);
+    }
+    scale_aux(ctx, aux_c, aux, f, count, s);
+    src = aux_c;
+  }
+  if (is_ntt_aux) {
+    shg::launch_ntt_inv(aux_view, src, aux_c, count * K, K, 0, s);
+    src = aux_c;
+  }
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_APPROX_DOWN, l, lsb ? 1 : 0), K, Lm,
+                           src, (size_t)K * n, delta, (size_t)Lm * n, count, ctx->log_n, s);
+  shg::launch_ntt_fwd(ctx->dev(), delta, delta, count * Lm, Lm, s);
+  const uint64_t* m = main;
+  if (!is_ntt_main) {
+    shg::launch_ntt_fwd(ctx->dev(), main, main_c, count * Lm, Lm, s);
+    m = main_c;
+  }
+  std::vector<uint64_t> c(Lm), d(Lm);
+  for (int i = 0; i < Lm; ++i) {
+    const uint64_t q = ctx->hp[i].q, pinv = p_inv_mod(ctx, i);
+    c[i] = lsb ? mulmod(p_mod_t % q, pinv, q) : pinv;
+    d[i] = lsb ? mulmod(t % q, pinv, q) : pinv;
+  }
+  combine(ctx, out, m, delta, c.data(), d.data(), lsb ? 0 : 1, count, Lm, s);
+  return launch_status("approx_modreduce");
+}
+
+// Ciphertext components x [count][Lm][n] (NTT form) -> the ScaleAndSwitch /
+// Switch round trip of RnsBfvCiphertext::Mul (rns/rns_bfv_ciphertext.cc:161-179):
+// x_aux = ScaleAndSwitchRnsBasis(x) = round(P/Q x) mod P and x_main =
+// SwitchRnsBasis(x_aux) = the same integer mod Q, both returned in NTT form.
+// X: [count][Lm][n] scratch.
+static void bfv_scale_up(shg_context* ctx, const uint64_t* x, uint64_t* X, uint64_t* x_aux,
+                         uint64_t* x_main, int count, int Lm, cudaStream_t s) {
+  const size_t n = ctx->n;
+  const int K = ctx->K, l = Lm - 1;
+  shg::launch_ntt_inv(ctx->dev(), x, X, count * Lm, Lm, 0, s);
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SCALE_UP, l), Lm, K, X,
+                           (size_t)Lm * n, x_aux, (size_t)K * n, count, ctx->log_n, s);
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SWITCH_DOWN, l), K, Lm, x_aux,
+                           (size_t)K * n, x_main, (size_t)Lm * n, count, ctx->log_n, s);
+  shg::launch_ntt_fwd(ctx->dev(), x_main, x_main, count * Lm, Lm, s);
+  shg::launch_ntt_fwd(ctx->aux_dev(), x_aux, x_aux, count * K, K, s);
+}
+
+// NTT-form x [count][Lm][n] -> its SwitchRnsBasis to the auxiliary primes in
+// NTT form [count][K][n]; X: [count][Lm][n] scratch.
+static void bfv_switch_up(shg_context* ctx, const uint64_t* x, uint64_t* X, uint64_t* x_aux,
+                          int count, int Lm, cudaStream_t s) {
+  const size_t n = ctx->n;
+  const int K = ctx->K;
+  shg::launch_ntt_inv(ctx->dev(), x, X, count * Lm, Lm, 0, s);
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SWITCH_UP, Lm - 1), Lm, K, X,
+                           (size_t)Lm * n, x_aux, (size_t)K * n, count, ctx->log_n, s);
+  shg::launch_ntt_fwd(ctx->aux_dev(), x_aux, x_aux, count * K, K, s);
+}
+
+// ScaleAndReduceRnsBasisInPlace with the context's t of (t_main, t_aux) [count]
+// (NTT form both) into out; t_aux is consumed, D [count][Lm][n] scratch.
+static void bfv_scale_reduce(shg_context* ctx, uint64_t* out, const uint64_t* t_main,
+                             uint64_t* t_aux, uint64_t* D, int count, int Lm, cudaStream_t s) {
+  const size_t n = ctx->n;
+  const int K = ctx->K;
+  shg::launch_ntt_inv(ctx->aux_dev(), t_aux, t_aux, count * K, K, 0, s);
+  shg::launch_switch_basis(ctx->d_primes, conv(ctx, CONV_SWITCH_DOWN_T, Lm - 1), K, Lm, t_aux,
+                           (size_t)K * n, D, (size_t)Lm * n, count, ctx->log_n, s);
+  shg::launch_ntt_fwd(ctx->dev(), D, D, count * Lm, Lm, s);
+  std::vector<uint64_t> c(Lm), d(Lm);
+  for (int i = 0; i < Lm; ++i) {
+    d[i] = p_inv_mod(ctx, i);
+    c[i] = mulmod(ctx->t % ctx->hp[i].q, d[i], ctx->hp[i].q);
+  }
+  combine(ctx, out, t_main, D, c.data(), d.data(), 1, count, Lm, s);
+}
+
+int shg_bfv_mul(shg_context* ctx, uint64_t* out, const uint64_t* a, const uint64_t* b,
+                int count, int num_limbs, shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, a, b}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Lm = num_limbs, K = ctx->K;
+  const size_t n = ctx->n, pm = (size_t)Lm * n, pa = (size_t)K * n;
+  // per ciphertext: X [4][Lm] (a, b coefficient forms; later the deltas),
+  // b_aux [2][K], a_aux [2][K], a_main [2][Lm], t_main [3][Lm], t_aux [3][K]
+  const size_t per_ct = (9 * pm + 7 * pa) * sizeof(uint64_t);
+  const size_t want = ctx->chunk_cts > 0 ? (size_t)ctx->chunk_cts
+                                         : std::max<size_t>(1, ((size_t)1 << 30) / per_ct);
+  const int C = (int)std::min<size_t>((size_t)count, want);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws((size_t)C * per_ct))) return st;
+  uint64_t* X = ctx->ws;
+  uint64_t* b_aux = X + (size_t)C * 4 * pm;
+  uint64_t* a_aux = b_aux + (size_t)C * 2 * pa;
+  uint64_t* a_main = a_aux + (size_t)C * 2 * pa;
+  uint64_t* t_main = a_main + (size_t)C * 2 * pm;
+  uint64_t* t_aux = t_main + (size_t)C * 3 * pm;
+  for (int c0 = 0; c0 < count; c0 += C) {
+    const int cc = std::min(C, count - c0);
+    const uint64_t* ac = a + (size_t)c0 * 2 * pm;
+    const uint64_t* bc = b + (size_t)c0 * 2 * pm;
+    // Q/t * b_j (mod P): b -> coefficient form -> SwitchRnsBasis -> NTT
+    bfv_switch_up(ctx, bc, X, b_aux, cc * 2, Lm, s);
+    // P/t * a_i (mod P) and (mod Q)
+    bfv_scale_up(ctx, ac, X, a_aux, a_main, cc * 2, Lm, s);
+    // the tensor product mod Q and mod P
+    shg::launch_tensor(ctx->dev(), t_main, a_main, bc, cc, Lm, s);
+    shg::launch_tensor(ctx->aux_dev(), t_aux, a_aux, b_aux, cc, K, s);
+    // Q/t * tensor (mod Q)
+    bfv_scale_reduce(ctx, out + (size_t)c0 * 3 * pm, t_main, t_aux, X, cc * 3, Lm, s);
+  }
+  return launch_status("bfv_mul");
+}
+
+int shg_bfv_absorb(shg_context* ctx, uint64_t* out, const uint64_t* ct,
+                   const uint64_t* plaintext, int len, int count, int num_limbs,
+                   shg_stream stream) {
+  int st = check_aux(ctx, count, num_limbs);
+  if (st) return st;
+  if (len < 1) return fail(SHG_INVALID_ARGUMENT, "`len` must be positive.");
+  if (count == 0) return SHG_OK;
+  if ((st = check_ptrs({out, ct, plaintext}))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Lm = num_limbs, K = ctx->K;
+  const size_t n = ctx->n, pm = (size_t)Lm * n, pa = (size_t)K * n;
+  const int members = count * len;
+  // pt_aux [K]; per component: X [Lm], c_aux [K], c_main [Lm]
+  const size_t per = (2 * pm + pa) * sizeof(uint64_t);
+  const size_t want = ctx->chunk_cts > 0 ? (size_t)ctx->chunk_cts * len
+                                         : std::max<size_t>(1, ((size_t)1 << 30) / per);
+  const int C = (int)std::min<size_t>((size_t)members, want);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if ((st = ctx->ensure_ws(pa * sizeof(uint64_t) + (size_t)C * per))) return st;
+  uint64_t* pt_aux = ctx->ws;
+  uint64_t* X = pt_aux + pa;
+  uint64_t* c_aux = X + (size_t)C * pm;
+  uint64_t* c_main = c_aux + (size_t)C * pa;
+  // Q/t * plaintext (mod P) (rns/rns_bfv_ciphertext.cc:48-56)
+  bfv_switch_up(ctx, plaintext, X, pt_aux, 1, Lm, s);
+  for (int m0 = 0; m0 < members; m0 += C) {
+    const int mc = std::min(C, members - m0);
+    bfv_scale_up(ctx, ct + (size_t)m0 * pm, X, c_aux, c_main, mc, Lm, s);
+    shg::ScalarPack none{};
+    shg::launch_pointwise(ctx->dev(), shg::PW_MUL_BCAST, c_main, c_main, plaintext, none, mc,
+                          Lm, s);
+    shg::launch_pointwise(ctx->aux_dev(), shg::PW_MUL_BCAST, c_aux, c_aux, pt_aux, none, mc, K,
+                          s);
+    bfv_scale_reduce(ctx, out + (size_t)m0 * pm, c_main, c_aux, X, mc, Lm, s);
+  }
+  return launch_status("bfv_absorb");
 }
 
 int shg_context_set_ks_fused(shg_context* ctx, int on) {

@@ -388,6 +388,13 @@ __global__ void k_pointwise(PwOp op, uint64_t* out, const uint64_t* a,
         r.y = add_mod(acc.y, mont_mul(va.y, vb.y, q, P->inv_modulus), q);
         break;
       }
+      case PW_MUL_BCAST: {
+        const ulonglong2 vb =
+            *reinterpret_cast<const ulonglong2*>(b + (e % ((size_t)L << log_n)));
+        r.x = mont_mul(va.x, vb.x, q, P->inv_modulus);
+        r.y = mont_mul(va.y, vb.y, q, P->inv_modulus);
+        break;
+      }
       case PW_MUL_MONT: {
         const uint64_t s = sc.v[l];
         r.x = mont_mul(va.x, s, q, P->inv_modulus);

@@ -123,6 +123,7 @@ enum PwOp {
   PW_FMA,         // out += REDC(a, b)
   PW_MUL_MONT,    // REDC(a, scalar_l)      v[l] = Montgomery scalar
   PW_MUL_SHOUP,   // a * w_l mod q          v[2l], v[2l+1] = w, Shoup(w)
+  PW_MUL_BCAST,   // REDC(a, b) with one b [L][n] for every member of a
 };
 void launch_pointwise(const CtxDev& c, PwOp op, uint64_t* out, const uint64_t* a,
                       const uint64_t* b, const ScalarPack& sc, int count, int L,
@@ -208,6 +209,41 @@ void launch_decompose(const CtxDev& c, uint64_t* out, const uint64_t* in,
 void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
                            const uint64_t* mono, CtMap map, int half,
                            int count, cudaStream_t s);
+
+// One RNS basis conversion between two prime sets of a context
+// (RnsPolynomial::SwitchRnsBasis, ScaleAndSwitchRnsBasis, ApproxSwitchRnsBasis,
+// rns/rns_polynomial.cc:419-724), kept in device memory.  Source limb i's
+// value is s_i = x_i * smul_i (Montgomery), v_i = ExportInt(s_i); destination
+// j gets sum_i v_i * w[i][j] mod p_j (w a Montgomery rep, so that product is
+// ImportInt(v_i) * w), then
+//   mode 0: minus u * (Q mod p_j),  mode 1: plus u,  mode 2: nothing,
+// with u = round(sum_i v_i / q_i) as the reference computes it in double
+// precision.  balanced (mode 2): v_i > q_i / 2 stands for v_i - q_i, whose
+// product is corrected by wq[i][j] = q_i * w[i][j] mod p_j.
+struct BasisConv {
+  int ns, nd;          // source / destination prime counts
+  int src0, dst0;      // first prime index of each set in the context
+  int mode, balanced;
+  uint64_t smul[kMaxLimbs];     // Montgomery multiplier of source limb i
+  uint64_t rinv[kMaxLimbs];     // floor(2^64 / q_i)
+  uint64_t rho[kMaxLimbs];      // floor(frac(2^64 / q_i) * 2^64)
+  double qd[kMaxLimbs];         // (double) q_i
+  uint64_t z[kMaxLimbs], zs[kMaxLimbs];  // per destination: u's multiplier, Shoup
+  // [i * nd + j], ns * nd entries used
+  uint64_t w[kMaxLimbs * kMaxLimbs], ws[kMaxLimbs * kMaxLimbs], wq[kMaxLimbs * kMaxLimbs];
+};
+
+// out [count][nd][n] (member p at out + p * out_stride) <- the conversion of
+// in [count][ns][n] (coefficient form, member p at in + p * in_stride);
+// `primes` = the context's full prime array.
+void launch_switch_basis(const PrimeDev* primes, const BasisConv* bc, int ns, int nd,
+                         const uint64_t* in, size_t in_stride, uint64_t* out,
+                         size_t out_stride, int count, int log_n, cudaStream_t s);
+
+// out_i = (a_i * c[i] - b_i * d[i]) mod q_i over [count][L][n] with c, d
+// Montgomery scalars per limb (ScaleAndReduce / ModReduceMsb combines).
+void launch_lin2(const CtxDev& c, uint64_t* out, const uint64_t* a, const uint64_t* b,
+                 const ScalarPack& cd, int sign, int count, int L, cudaStream_t s);
 
 // Serialized polynomial layout (MontgomeryInt::SerializeVector per limb):
 // limb l is an n * bits[l] bit little-endian stream of the Montgomery

@@ -79,6 +79,28 @@ SIGNATURES = {
                                             ctypes.c_int, _vp]),
     "shg_pir_expand_absorb": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int, _vp,
                                              ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]),
+    "shg_context_create_with_aux": (ctypes.c_int, [ctypes.c_int, _u64p, ctypes.c_int, _u64p,
+                                                   ctypes.c_int, ctypes.c_uint64,
+                                                   ctypes.POINTER(_vp)]),
+    "shg_context_num_aux_moduli": (ctypes.c_int, [_vp]),
+    "shg_poly_switch_rns_basis": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, _vp]),
+    "shg_poly_scale_switch_rns_basis": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int,
+                                                       ctypes.c_int, _vp]),
+    "shg_poly_approx_switch_rns_basis": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int,
+                                                        ctypes.c_int, ctypes.c_int,
+                                                        ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_poly_modreduce_msb": (ctypes.c_int, [_vp, _vp, _vp, _u64p, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_poly_scale_reduce_rns_basis": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_uint64,
+                                                       ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                       ctypes.c_int, _vp]),
+    "shg_poly_approx_modreduce": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int,
+                                                 ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_bfv_mul": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "shg_bfv_absorb": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, _vp]),
     "shg_sample_uniform_error": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, _vp]),
     "shg_bgv_encrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
@@ -263,15 +285,23 @@ class DeviceBuffer:
 class Context:
     """RnsContext on the GPU (shg_context_create)."""
 
-    def __init__(self, log_n, qs, t=65537):
+    def __init__(self, log_n, qs, t=65537, ps=()):
         self.log_n = log_n
         self.n = 1 << log_n
         self.qs = [int(q) for q in qs]
+        self.ps = [int(p) for p in ps]
         arr = np.array(self.qs, dtype=np.uint64)
         h = _vp()
-        check(lib().shg_context_create(log_n, _u64(arr), len(self.qs), int(t), ctypes.byref(h)))
+        if self.ps:
+            parr = np.array(self.ps, dtype=np.uint64)
+            check(lib().shg_context_create_with_aux(log_n, _u64(arr), len(self.qs), _u64(parr),
+                                                    len(self.ps), int(t), ctypes.byref(h)))
+        else:
+            check(lib().shg_context_create(log_n, _u64(arr), len(self.qs), int(t),
+                                           ctypes.byref(h)))
         self.h = h.value
         self.L = len(self.qs)
+        self.K = len(self.ps)
 
     def close(self):
         if getattr(self, "h", None):

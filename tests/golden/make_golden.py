@@ -143,6 +143,38 @@ def main():
         g[tag + "_m"] = m
         g[tag + "_seeds"] = np.frombuffer(b"".join(seeds), np.uint8).reshape(count, 32).copy()
         g[tag + "_out"] = R.encrypt_bgv(log_n, qs, t, var, key, m, seeds)
+    # RNS basis conversion and BFV (rns/rns_polynomial.cc:349-852,
+    # rns/rns_bfv_ciphertext.cc) on the reference's own BFV test parameters
+    # (rns/testing/parameters.h GetBfvParametersForFiniteFieldEncoding).
+    for tag, log_n, qs, ps, t in [("bfv_a", 11, [549755523073], [549755731969, 4169729], 40961),
+                                  ("bfv_b", 11, [8589905921, 8589852673, 8589844481],
+                                   [1073692673, 1073668097], 40961)]:
+        n, L, K = 1 << log_n, len(qs), len(ps)
+        x = O.uniform_limbs(9500 + L, qs, n).reshape(L, n)
+        y = O.uniform_limbs(9600 + L, ps, n).reshape(K, n)
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_ps"] = np.array(ps, np.uint64)
+        g[tag + "_params"] = np.array([log_n, t], np.uint64)
+        g[tag + "_x"] = x
+        g[tag + "_y"] = y
+        lv = L - 1
+        g[tag + "_switch_up"] = R.switch_basis(log_n, qs, ps, lv, 0, x)
+        g[tag + "_switch_down"] = R.switch_basis(log_n, qs, ps, lv, 1, y)
+        g[tag + "_scale_up"] = R.switch_basis(log_n, qs, ps, lv, 2, x)
+        g[tag + "_approx_down_ntt_bal"] = R.switch_basis(log_n, qs, ps, lv, 3, y, True, True)
+        g[tag + "_approx_up"] = R.switch_basis(log_n, qs, ps, lv, 4, x, False, False)
+        if L > 1:
+            g[tag + "_modreduce_msb_ntt"] = R.modreduce_msb(log_n, qs, x, True)
+            g[tag + "_modreduce_msb_coeff"] = R.modreduce_msb(log_n, qs, x, False)
+        g[tag + "_scale_reduce"] = R.scale_reduce(log_n, qs, ps, t, 0, x, y, True, True)
+        g[tag + "_approx_lsb"] = R.scale_reduce(log_n, qs, ps, t, 1, x, y, False, True)
+        g[tag + "_approx_msb"] = R.scale_reduce(log_n, qs, ps, t, 2, x, y, True, False)
+        a = O.uniform_limbs(9700 + L, qs, n, 4).reshape(2, 2, L, n)
+        b = O.uniform_limbs(9800 + L, qs, n, 4).reshape(2, 2, L, n)
+        g[tag + "_a"] = a
+        g[tag + "_b"] = b
+        g[tag + "_mul"] = R.bfv_mul(log_n, qs, ps, t, a, b)
+        g[tag + "_absorb"] = R.bfv_absorb(log_n, qs, ps, t, a, x)
     np.savez_compressed(os.path.join(HERE, "reference_small.npz"), **g)
 
     # Full-size workloads: digests of the reference's outputs on seeded inputs.
@@ -186,6 +218,13 @@ def main():
                            "prng_seeds": "ciphertext c: 32 bytes of value c + 1",
                            "out_sha256": digest(R.encrypt_bgv(log_n, qs, 65537, 8, key, m,
                                                               seeds))}
+    P45 = [35184368320513, 35184368025601, 35184367828993, 35184367337473, 35184366911489,
+           35184366551041, 35184366223361]
+    a = O.uniform_limbs(7040, qs, n, 4).reshape(2, 2, 6, n)
+    b = O.uniform_limbs(7041, qs, n, 4).reshape(2, 2, 6, n)
+    d["bfv_mul_n14_L6_K7"] = {"log_n": 14, "qs": qs, "ps": P45, "t": 65537, "count": 2,
+                              "seeds": {"a": 7040, "b": 7041},
+                              "out_sha256": digest(R.bfv_mul(14, qs, P45, 65537, a, b))}
     with open(os.path.join(HERE, "digests.json"), "w") as fh:
         json.dump(d, fh, indent=1)
     print("wrote", os.path.join(HERE, "reference_small.npz"), "and digests.json")

@@ -472,3 +472,133 @@ def test_gpu_encrypt_full_size_digest(sg, oracle, four_step_min):
     _run(sg, sg.lib().shg_bgv_encrypt, ctx.h, out.ptr, dk.ptr, dm.ptr, ds.ptr, 6, d["count"],
          d["variance"], None)
     assert digest(out.download((d["count"], 2, 6, 1 << 14))) == d["out_sha256"]
+
+
+# --------------------------------------------------------------------------
+# RNS basis conversion and BFV (reference's BFV test parameters)
+# --------------------------------------------------------------------------
+
+BFV_TAGS = sorted({k[:-len("_mul")] for k in SMALL.files
+                   if k.startswith("bfv_") and k.endswith("_mul")})
+
+
+def _bfv_case(tag):
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    ps = [int(p) for p in SMALL[tag + "_ps"]]
+    log_n, t = (int(v) for v in SMALL[tag + "_params"])
+    return log_n, qs, ps, t
+
+
+@pytest.mark.parametrize("tag", BFV_TAGS)
+def test_oracle_bfv_golden(oracle, tag):
+    """SwitchRnsBasis, ScaleAndSwitchRnsBasis, ApproxSwitchRnsBasis,
+    ModReduceMsb, ScaleAndReduceRnsBasisInPlace, ApproxModReduceLsb/Msb,
+    RnsBfvCiphertext::Mul and AbsorbInPlace of the reference."""
+    log_n, qs, ps, t = _bfv_case(tag)
+    L, K = len(qs), len(ps)
+    rns = oracle.Rns(log_n, qs + ps)
+    main, aux = list(range(L)), list(range(L, L + K))
+    x, y = SMALL[tag + "_x"], SMALL[tag + "_y"]
+    assert np.array_equal(rns.switch_basis(main, aux, x), SMALL[tag + "_switch_up"])
+    assert np.array_equal(rns.switch_basis(aux, main, y), SMALL[tag + "_switch_down"])
+    assert np.array_equal(rns.switch_basis(main, aux, x, scale=True), SMALL[tag + "_scale_up"])
+    assert np.array_equal(rns.approx_switch_basis(aux, main, y, True, True),
+                          SMALL[tag + "_approx_down_ntt_bal"])
+    assert np.array_equal(rns.approx_switch_basis(main, aux, x, False, False),
+                          SMALL[tag + "_approx_up"])
+    if L > 1:
+        assert np.array_equal(rns.modreduce_msb(x, True), SMALL[tag + "_modreduce_msb_ntt"])
+        assert np.array_equal(rns.modreduce_msb(x, False), SMALL[tag + "_modreduce_msb_coeff"])
+    assert np.array_equal(rns.scale_reduce(aux, t, x, y, True, True, 0),
+                          SMALL[tag + "_scale_reduce"])
+    assert np.array_equal(rns.scale_reduce(aux, t, x, y, False, True, 1),
+                          SMALL[tag + "_approx_lsb"])
+    assert np.array_equal(rns.scale_reduce(aux, 0, x, y, True, False, 2),
+                          SMALL[tag + "_approx_msb"])
+    a, b = SMALL[tag + "_a"], SMALL[tag + "_b"]
+    assert np.array_equal(np.stack([rns.bfv_mul(L, aux, t, a[c], b[c]) for c in range(2)]),
+                          SMALL[tag + "_mul"])
+    assert np.array_equal(np.stack([rns.bfv_absorb(L, aux, t, a[c], x) for c in range(2)]),
+                          SMALL[tag + "_absorb"])
+
+
+def _bfv_digest_inputs(oracle):
+    d = DIGESTS["bfv_mul_n14_L6_K7"]
+    n = 1 << d["log_n"]
+    a = oracle.uniform_limbs(d["seeds"]["a"], d["qs"], n, 4).reshape(2, 2, 6, n)
+    b = oracle.uniform_limbs(d["seeds"]["b"], d["qs"], n, 4).reshape(2, 2, 6, n)
+    return d, a, b
+
+
+def test_oracle_bfv_full_size_digest(oracle):
+    d, a, b = _bfv_digest_inputs(oracle)
+    rns = oracle.Rns(d["log_n"], d["qs"] + d["ps"])
+    aux = list(range(6, 13))
+    got = np.stack([rns.bfv_mul(6, aux, d["t"], a[c], b[c]) for c in range(2)])
+    assert digest(got) == d["out_sha256"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", BFV_TAGS)
+def test_gpu_bfv_golden(sg, tag):
+    """The device basis conversions and BFV operations against the reference."""
+    log_n, qs, ps, t = _bfv_case(tag)
+    L, K, n = len(qs), len(ps), 1 << log_n
+    lib = sg.lib()
+    ctx = sg.Context(log_n, qs, t, ps=ps)
+    x, y = SMALL[tag + "_x"], SMALL[tag + "_y"]
+    dx, dy = sg.DeviceBuffer.from_array(x), sg.DeviceBuffer.from_array(y)
+    big = sg.DeviceBuffer(4 * 3 * max(L, K) * n * 8)
+
+    def get(shape):
+        return big.download(shape)
+
+    _run(sg, lib.shg_poly_switch_rns_basis, ctx.h, big.ptr, dx.ptr, 0, L, 1, None)
+    assert np.array_equal(get((K, n)), SMALL[tag + "_switch_up"])
+    _run(sg, lib.shg_poly_switch_rns_basis, ctx.h, big.ptr, dy.ptr, 1, L, 1, None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_switch_down"])
+    _run(sg, lib.shg_poly_scale_switch_rns_basis, ctx.h, big.ptr, dx.ptr, L, 1, None)
+    assert np.array_equal(get((K, n)), SMALL[tag + "_scale_up"])
+    _run(sg, lib.shg_poly_approx_switch_rns_basis, ctx.h, big.ptr, dy.ptr, 1, L, 1, 1, 1, None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_approx_down_ntt_bal"])
+    _run(sg, lib.shg_poly_approx_switch_rns_basis, ctx.h, big.ptr, dx.ptr, 0, L, 0, 0, 1, None)
+    assert np.array_equal(get((K, n)), SMALL[tag + "_approx_up"])
+    if L > 1:
+        ql = np.zeros(L - 1, np.uint64)
+        sg.check(lib.shg_context_ql_inv(ctx.h, L - 1,
+                                        ql.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        qp = ql.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        for is_ntt, key in ((1, "_modreduce_msb_ntt"), (0, "_modreduce_msb_coeff")):
+            _run(sg, lib.shg_poly_modreduce_msb, ctx.h, big.ptr, dx.ptr, qp, is_ntt, 1, L, None)
+            assert np.array_equal(get((L - 1, n)), SMALL[tag + key])
+    _run(sg, lib.shg_poly_scale_reduce_rns_basis, ctx.h, big.ptr, dx.ptr, dy.ptr, t, 1, 1, L,
+         1, None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_scale_reduce"])
+    # the same with a t other than the context's (the unfolded route)
+    ctx2 = sg.Context(log_n, qs, t + 2, ps=ps)
+    _run(sg, lib.shg_poly_scale_reduce_rns_basis, ctx2.h, big.ptr, dx.ptr, dy.ptr, t, 1, 1, L,
+         1, None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_scale_reduce"])
+    _run(sg, lib.shg_poly_approx_modreduce, ctx.h, big.ptr, dx.ptr, dy.ptr, 1, t, 0, 1, L, 1,
+         None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_approx_lsb"])
+    _run(sg, lib.shg_poly_approx_modreduce, ctx.h, big.ptr, dx.ptr, dy.ptr, 0, 0, 1, 0, L, 1,
+         None)
+    assert np.array_equal(get((L, n)), SMALL[tag + "_approx_msb"])
+    a, b = SMALL[tag + "_a"], SMALL[tag + "_b"]
+    da, db = sg.DeviceBuffer.from_array(a), sg.DeviceBuffer.from_array(b)
+    _run(sg, lib.shg_bfv_mul, ctx.h, big.ptr, da.ptr, db.ptr, 2, L, None)
+    assert np.array_equal(get((2, 3, L, n)), SMALL[tag + "_mul"])
+    _run(sg, lib.shg_bfv_absorb, ctx.h, big.ptr, da.ptr, dx.ptr, 2, 2, L, None)
+    assert np.array_equal(get((2, 2, L, n)), SMALL[tag + "_absorb"])
+
+
+@pytest.mark.gpu
+def test_gpu_bfv_full_size_digest(sg, oracle):
+    """BFV ct x ct at n = 2^14, six 45-bit main and seven 45-bit aux primes."""
+    d, a, b = _bfv_digest_inputs(oracle)
+    ctx = sg.Context(d["log_n"], d["qs"], d["t"], ps=d["ps"])
+    da, db = sg.DeviceBuffer.from_array(a), sg.DeviceBuffer.from_array(b)
+    out = sg.DeviceBuffer(2 * 3 * 6 * (1 << 14) * 8)
+    _run(sg, sg.lib().shg_bfv_mul, ctx.h, out.ptr, da.ptr, db.ptr, 2, 6, None)
+    assert digest(out.download((2, 3, 6, 1 << 14))) == d["out_sha256"]

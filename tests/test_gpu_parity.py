@@ -807,3 +807,129 @@ def test_sampling_validation(sg):
     with pytest.raises(sg.ShgError, match="RNS moduli"):
         sg.check(lib.shg_bgv_encrypt(ctx.h, buf.ptr, buf.ptr, buf.ptr, seeds.ptr, 3, 1, 8, None))
     sg.check(lib.shg_bgv_encrypt(ctx.h, buf.ptr, buf.ptr, buf.ptr, seeds.ptr, 2, 0, 8, None))
+
+
+# --------------------------------------------------------------------------
+# RNS basis conversion and BFV (auxiliary primes)
+# --------------------------------------------------------------------------
+
+P45 = [35184368320513, 35184368025601, 35184367828993, 35184367337473, 35184366911489,
+       35184366551041, 35184366223361]
+P50 = [1125899884625921, 1125899884167169, 1125899884036097]
+
+
+@pytest.mark.parametrize("log_n,qs,ps,level", [
+    (10, Q45, P45, 5),
+    (12, Q45, P45, 2),          # a lower level: main prefix q_0..q_2
+    (13, Q50[:3], P50[:2], 2),
+    (14, Q45, P45, 5),
+])
+def test_switch_rns_basis(sg, oracle, log_n, qs, ps, level):
+    """SwitchRnsBasis both ways, ScaleAndSwitchRnsBasis and ApproxSwitchRnsBasis
+    (both forms, balanced and not) on 3 polynomials, bit-exact."""
+    lib = sg.lib()
+    n, K, m = 1 << log_n, len(ps), level + 1
+    rns = oracle.Rns(log_n, qs + ps)
+    main, aux = list(range(m)), list(range(len(qs), len(qs) + K))
+    x = oracle.uniform_limbs(600 + log_n, qs[:m], n, 3).reshape(3, m, n)
+    y = oracle.uniform_limbs(700 + log_n, ps, n, 3).reshape(3, K, n)
+    ctx = sg.Context(log_n, qs, 65537, ps=ps)
+    dx, dy = _dev(sg, x), _dev(sg, y)
+    out = sg.DeviceBuffer(3 * max(m, K) * n * 8)
+    _run(sg, lib.shg_poly_switch_rns_basis, ctx.h, out.ptr, dx.ptr, 0, m, 3, None)
+    assert np.array_equal(out.download((3, K, n)),
+                          np.stack([rns.switch_basis(main, aux, x[c]) for c in range(3)]))
+    _run(sg, lib.shg_poly_switch_rns_basis, ctx.h, out.ptr, dy.ptr, 1, m, 3, None)
+    assert np.array_equal(out.download((3, m, n)),
+                          np.stack([rns.switch_basis(aux, main, y[c]) for c in range(3)]))
+    _run(sg, lib.shg_poly_scale_switch_rns_basis, ctx.h, out.ptr, dx.ptr, m, 3, None)
+    assert np.array_equal(out.download((3, K, n)),
+                          np.stack([rns.switch_basis(main, aux, x[c], scale=True)
+                                    for c in range(3)]))
+    for is_ntt in (0, 1):
+        for bal in (0, 1):
+            _run(sg, lib.shg_poly_approx_switch_rns_basis, ctx.h, out.ptr, dy.ptr, 1, m, is_ntt,
+                 bal, 3, None)
+            assert np.array_equal(out.download((3, m, n)),
+                                  np.stack([rns.approx_switch_basis(aux, main, y[c], is_ntt, bal)
+                                            for c in range(3)]))
+            _run(sg, lib.shg_poly_approx_switch_rns_basis, ctx.h, out.ptr, dx.ptr, 0, m, is_ntt,
+                 bal, 3, None)
+            assert np.array_equal(out.download((3, K, n)),
+                                  np.stack([rns.approx_switch_basis(main, aux, x[c], is_ntt, bal)
+                                            for c in range(3)]))
+
+
+def test_switch_rns_basis_rounding_ties(sg, oracle):
+    """Coefficients whose sum_i v_i / q_i sits within 2^-32 of a half integer
+    take the exact double-precision route; built by hand from the CRT."""
+    lib = sg.lib()
+    log_n, qs, ps = 10, Q45[:3], P45[:2]
+    n = 1 << log_n
+    rns = oracle.Rns(log_n, qs + ps)
+    p0 = [oracle.Prime(q, log_n) for q in qs]
+    # v_0 / q_0 + v_1 / q_1 + v_2 / q_2 ~ 1.5 with v_0 = (q_0 - 1) / 2 etc.
+    rng = np.random.default_rng(3)
+    x = np.zeros((3, n), dtype=object)
+    for k in range(n):
+        v = [(qs[0] - 1) // 2 + int(rng.integers(-2, 3)), qs[1] // 2, qs[2] // 2 + int(rng.integers(0, 2))]
+        for i in range(3):
+            x[i, k] = v[i]
+    # x holds the scaled values s_i; undo the (Q/q_i)^-1 factor so the kernel's s_i are them
+    xin = np.empty((3, n), np.uint64)
+    for i, q in enumerate(qs):
+        qhat = 1
+        for j, qj in enumerate(qs):
+            if j != i:
+                qhat = qhat * qj % q
+        vals = np.array([int(v) * qhat % q for v in x[i]], np.uint64)
+        xin[i] = p0[i].import_(vals)
+    want = rns.switch_basis([0, 1, 2], [3, 4], xin)
+    ctx = sg.Context(log_n, qs, 65537, ps=ps)
+    d, out = _dev(sg, xin), sg.DeviceBuffer(2 * n * 8)
+    _run(sg, lib.shg_poly_switch_rns_basis, ctx.h, out.ptr, d.ptr, 0, 3, 1, None)
+    assert np.array_equal(out.download((2, n)), want)
+
+
+@pytest.mark.parametrize("log_n,qs,ps,count,chunk", [
+    (11, [8589905921, 8589852673, 8589844481], [1073692673, 1073668097], 3, 0),
+    (13, Q45[:4], P45[:5], 2, 0),
+    (14, Q45, P45, 5, 2),       # three chunks
+])
+def test_bfv_mul_and_absorb(sg, oracle, log_n, qs, ps, count, chunk):
+    """RnsBfvCiphertext::operator* and AbsorbInPlace, bit-exact per ciphertext."""
+    lib = sg.lib()
+    n, L, K, t = 1 << log_n, len(qs), len(ps), 65537
+    rns = oracle.Rns(log_n, qs + ps)
+    aux = list(range(L, L + K))
+    a = oracle.uniform_limbs(800 + log_n, qs, n, 2 * count).reshape(count, 2, L, n)
+    b = oracle.uniform_limbs(900 + log_n, qs, n, 2 * count).reshape(count, 2, L, n)
+    pt = oracle.uniform_limbs(950 + log_n, qs, n).reshape(L, n)
+    ctx = sg.Context(log_n, qs, t, ps=ps)
+    sg.check(lib.shg_context_set_chunk(ctx.h, chunk))
+    da, db, dp = _dev(sg, a), _dev(sg, b), _dev(sg, pt)
+    out = sg.DeviceBuffer(count * 3 * L * n * 8)
+    _run(sg, lib.shg_bfv_mul, ctx.h, out.ptr, da.ptr, db.ptr, count, L, None)
+    got = out.download((count, 3, L, n))
+    for c in sorted({0, count // 2, count - 1}):
+        assert np.array_equal(got[c], rns.bfv_mul(L, aux, t, a[c], b[c])), c
+    _run(sg, lib.shg_bfv_absorb, ctx.h, out.ptr, da.ptr, dp.ptr, 2, count, L, None)
+    got = out.download((count, 2, L, n))
+    for c in sorted({0, count - 1}):
+        assert np.array_equal(got[c], rns.bfv_absorb(L, aux, t, a[c], pt)), c
+
+
+def test_bfv_validation(sg):
+    lib = sg.lib()
+    ctx = sg.Context(10, Q45[:2], 65537)
+    buf = sg.DeviceBuffer(4 * 2 * 1024 * 8)
+    with pytest.raises(sg.ShgError, match="no auxiliary prime moduli"):
+        sg.check(lib.shg_bfv_mul(ctx.h, buf.ptr, buf.ptr, buf.ptr, 1, 2, None))
+    with pytest.raises(sg.ShgError, match="distinct"):
+        sg.Context(10, Q45[:2], 65537, ps=[Q45[1]])
+    ctx = sg.Context(10, Q45[:2], 65537, ps=P45[:1])
+    assert lib.shg_context_num_aux_moduli(ctx.h) == 1
+    with pytest.raises(sg.ShgError, match="direction"):
+        sg.check(lib.shg_poly_switch_rns_basis(ctx.h, buf.ptr, buf.ptr, 2, 2, 1, None))
+    with pytest.raises(sg.ShgError, match="RNS moduli"):
+        sg.check(lib.shg_bfv_mul(ctx.h, buf.ptr, buf.ptr, buf.ptr, 1, 3, None))
