@@ -1165,6 +1165,242 @@ def run_encrypt(args, world, rank, local, dist):
         lib.shg_host_free(hp)
 
 
+# ---------------------------------------------------------------------------
+# BFV: RnsBfvCiphertext::operator* (Kim et al. tensor with basis extension),
+# n = 2^14, six 45-bit main and seven 45-bit auxiliary primes, 1024 pairs.
+# ---------------------------------------------------------------------------
+
+BFV_METRIC = "RNS BFV ct*ct/sec (RnsBfvCiphertext::Mul, bit-exact)"
+BFV_UNIT = "bfv-mul/s"
+P45_AUX = [35184368320513, 35184368025601, 35184367828993, 35184367337473, 35184366911489,
+           35184366551041, 35184366223361]
+BFV_SCOPES = ("ntt_inv", "ntt_fwd", "switch_basis", "tensor", "lin2")
+
+
+def bfv_config(count):
+    return {"workload": "bfv-mul n=2^14 6x45-bit main + 7x45-bit aux primes t=65537",
+            "log_n": LOG_N, "log_q": 45, "limbs": len(QS), "aux_limbs": len(P45_AUX),
+            "pairs": count, "l2": "inputs and outputs per step (8 GB) exceed L2",
+            "parallelism": "replicas"}
+
+
+def bfv_scope_model(name, n, Lm, K, pairs):
+    """Algorithmic DRAM bytes of one step of a scope (limb = n * 8 bytes)."""
+    limb = n * 8
+    per = {"ntt_inv": 2 * (4 * Lm + 3 * K), "ntt_fwd": 2 * (2 * K + 2 * Lm + 2 * K + 3 * Lm),
+           "switch_basis": 9 * (Lm + K), "tensor": 7 * Lm + 7 * K, "lin2": 9 * Lm}[name]
+    return per * limb * pairs
+
+
+def cpu_bfv(seconds, threads, seed=7):
+    """The reference's CPU RnsBfvCiphertext::Mul (oracle restatement), one pair
+    per host thread per round, for about `seconds`."""
+    import concurrent.futures
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    n = 1 << LOG_N
+    L, K = len(QS), len(P45_AUX)
+    rns = O.Rns(LOG_N, QS + P45_AUX)
+    aux = list(range(L, L + K))
+    a = splitmix_limbs(seed, 2 * threads, QS, n).reshape(threads, 2, L, n)
+    b = splitmix_limbs(seed + 1, 2 * threads, QS, n).reshape(threads, 2, L, n)
+
+    def one(i):
+        return rns.bfv_mul(L, aux, T_PLAIN, a[i], b[i])
+
+    ops = 0
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        while True:
+            list(ex.map(one, range(threads)))
+            ops += threads
+            dt = time.perf_counter() - t0
+            if dt >= seconds:
+                break
+    return ops / dt, ops, dt
+
+
+def run_bfv_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    per_step, ops_total = [], 0
+    for i in range(args.warmup + args.steps):
+        _, ops, dt = cpu_bfv(2.0, threads, seed=100 + i)
+        if i >= args.warmup:
+            per_step.append(dt)
+            ops_total += ops
+    total = sum(per_step)
+    value = ops_total / total
+    print(json.dumps({
+        "metric": BFV_METRIC, "value": value, "unit": BFV_UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": bfv_config(threads),
+        "cpu_baseline": {"value": value, "unit": BFV_UNIT, "cores": threads, "kind": "port",
+                         "sample": "each step: about 2 s of whole BFV products, one per host "
+                                   "thread per round"},
+        "e2e": {"value": value, "unit": BFV_UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_bfv(args, world, rank, local, dist):
+    import shell_gpu as sg
+    lib = sg.lib()
+    sg.check(lib.shg_set_device(local))
+    n = 1 << LOG_N
+    L, K = len(QS), len(P45_AUX)
+    B = args.batch
+    ctx = sg.Context(LOG_N, QS, T_PLAIN, ps=P45_AUX)
+    if args.four_step_min:
+        sg.check(lib.shg_context_set_four_step_min(ctx.h, args.four_step_min))
+    if args.chunk:
+        sg.check(lib.shg_context_set_chunk(ctx.h, args.chunk))
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+    in_bytes, out_bytes = B * 2 * L * n * 8, B * 3 * L * n * 8
+
+    def host(nbytes):
+        p = ctypes.c_void_p()
+        sg.check(lib.shg_host_alloc(nbytes, ctypes.byref(p)))
+        return p.value
+
+    h_a, h_b, h_out = host(in_bytes), host(in_bytes), host(out_bytes)
+    for hp, seed in ((h_a, 5100 + rank), (h_b, 5200 + rank)):
+        np.ctypeslib.as_array((ctypes.c_uint64 * (B * 2 * L * n)).from_address(hp))[:] = \
+            splitmix_limbs(seed, 2 * B, QS, n).reshape(-1)
+    d_a, d_b, d_out = (sg.DeviceBuffer(in_bytes), sg.DeviceBuffer(in_bytes),
+                       sg.DeviceBuffer(out_bytes))
+    sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, in_bytes, s))
+    sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, in_bytes, s))
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def step_device():
+        sg.check(lib.shg_bfv_mul(ctx.h, d_out.ptr, d_a.ptr, d_b.ptr, B, L, s))
+
+    step_device()
+    sg.check(lib.shg_stream_synchronize(s))
+    n0 = lib.shg_launch_count()
+    sg.check(lib.shg_graph_capture_begin(s))
+    step_device()
+    g = ctypes.c_void_p()
+    sg.check(lib.shg_graph_capture_end(s, ctypes.byref(g)))
+    graph = g.value
+    launches_per_step = lib.shg_launch_count() - n0
+    for _ in range(args.warmup):
+        sg.check(lib.shg_graph_launch(graph, s))
+    sg.check(lib.shg_stream_synchronize(s))
+    evs = [ev() for _ in range(args.steps + 1)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(dist)
+    sg.check(lib.shg_event_record(evs[0], s))
+    for i in range(args.steps):
+        sg.check(lib.shg_graph_launch(graph, s))
+        sg.check(lib.shg_event_record(evs[i + 1], s))
+    sg.check(lib.shg_stream_synchronize(s))
+    barrier(dist)
+    clk = clocks.stop()
+    step_ms = [elapsed(evs[i], evs[i + 1]) for i in range(args.steps)]
+    total_ms = max_over_ranks(dist, elapsed(evs[0], evs[-1]))
+    ops_all = sum_over_ranks(dist, float(B * args.steps))
+    value = ops_all / (total_ms / 1e3)
+
+    e2e = None
+    if not args.no_e2e:
+        def step_e2e():
+            sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, in_bytes, s))
+            sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, in_bytes, s))
+            step_device()
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, out_bytes, s))
+        step_e2e()
+        sg.check(lib.shg_stream_synchronize(s))
+        e0, e1 = ev(), ev()
+        barrier(dist)
+        sg.check(lib.shg_event_record(e0, s))
+        for _ in range(args.steps):
+            step_e2e()
+        sg.check(lib.shg_event_record(e1, s))
+        sg.check(lib.shg_stream_synchronize(s))
+        e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": BFV_UNIT,
+               "h2d_bytes_per_step": 2 * in_bytes, "d2h_bytes_per_step": out_bytes,
+               "ms_per_step": e2e_ms / args.steps}
+
+    sg.check(lib.shg_profile_start())
+    step_device()
+    sg.check(lib.shg_profile_stop())
+    prof = {}
+    for name in BFV_SCOPES:
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        sg.check(lib.shg_profile_query(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        if cnt.value:
+            prof[name] = (ms.value, cnt.value)
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    bfly_peak = ctypes.c_double()
+    sg.check(lib.shg_measure_butterfly_rate(ctypes.byref(bfly_peak)))
+    step_total = sum(v[0] for v in prof.values())
+    kernels = {}
+    limb_bfly = n // 2 * LOG_N
+    bfly_limbs = {"ntt_inv": 4 * L + 3 * K, "ntt_fwd": 4 * K + 5 * L}
+    for name, (ms, cnt) in prof.items():
+        nbytes = bfv_scope_model(name, n, L, K, B)
+        kernels[name] = {"share_of_step": ms / step_total, "launches": cnt,
+                         "avg_launch_ms": ms / cnt,
+                         "algorithmic_bytes_per_launch": nbytes / cnt,
+                         "achieved_gbs": nbytes / (ms / 1e3) / 1e9}
+        if name in bfly_limbs:
+            kernels[name]["int_frac"] = (bfly_limbs[name] * limb_bfly * B / (ms / 1e3)
+                                         / bfly_peak.value)
+    top = max(prof, key=lambda nm: prof[nm][0])
+    tk = kernels[top]
+    roofline = {
+        "kernel": top, "bound": "hbm", "achieved": tk["achieved_gbs"], "peak": peak,
+        "unit": "GB/s", "frac": tk["achieved_gbs"] / peak, "peak_source": peak_src,
+        "traffic": None, "algorithmic_bytes_per_launch": tk["algorithmic_bytes_per_launch"],
+        "avg_launch_ms": tk["avg_launch_ms"], "kernels": kernels,
+        "butterfly_peak_per_s": bfly_peak.value,
+    }
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, ops, dt = cpu_bfv(10.0, threads)
+        cpu = {"value": rate, "unit": BFV_UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ops} BFV products in {dt:.1f} s, one per host thread per round"}
+    lat = sorted(step_ms)
+    line = {
+        "metric": BFV_METRIC, "value": value, "unit": BFV_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded uniform ciphertexts)", "config": bfv_config(B),
+        "latency_ms": {"step_p50": lat[len(lat) // 2], "step_p99": lat[-1]},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "gpu_launches": int(launches_per_step * args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sg.check(lib.shg_graph_destroy(graph))
+    for hp in (h_a, h_b, h_out):
+        lib.shg_host_free(hp)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1188,11 +1424,12 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
-                    choices=["ct-mult-relin", "pir", "uneven", "serve", "encrypt"],
+                    choices=["ct-mult-relin", "pir", "uneven", "serve", "encrypt", "bfv-mul"],
                     help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
                          "pir: oblivious expansion + database absorb (n=2^12, one prime); "
                          "uneven: 4096 mixed instances through the batch executor; "
-                         "encrypt: EncryptPolynomialBgv with on-device ChaCha sampling")
+                         "encrypt: EncryptPolynomialBgv with on-device ChaCha sampling; "
+                         "bfv-mul: RnsBfvCiphertext ct x ct with basis extension")
     ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -1217,6 +1454,12 @@ def main():
                                                  "workloads"}), flush=True)
         else:
             run_uneven(args, world, rank, local, dist)
+        return
+    if args.workload == "bfv-mul":
+        if args.impl == "reference":
+            run_bfv_reference(args, world, rank)
+        else:
+            run_bfv(args, world, rank, local, dist)
         return
     if args.workload == "encrypt":
         if args.impl == "reference":

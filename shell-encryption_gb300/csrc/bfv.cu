@@ -50,7 +50,9 @@ __global__ void __launch_bounds__(kConvThreads)
                    const uint64_t* __restrict__ in, size_t in_stride,
                    uint64_t* __restrict__ out, size_t out_stride, size_t total, int log_n) {
   const BasisConv& bc = *bcp;
-  const int ns = bc.ns, nd = bc.nd, mode = bc.mode, balanced = bc.balanced;
+  const int ns = bc.ns, nd = bc.nd, mode = bc.mode, balanced = bc.balanced, chunk = bc.chunk;
+  const PrimeDev* src = primes + bc.src0;
+  const PrimeDev* dst = primes + bc.dst0;
   const size_t n = (size_t)1 << log_n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
@@ -60,31 +62,45 @@ __global__ void __launch_bounds__(kConvThreads)
 #pragma unroll
     for (int i = 0; i < MAXS; ++i) {
       v[i] = 0;
-      if (i < ns) {
-        const PrimeDev& P = primes[bc.src0 + i];
-        const uint64_t s = mont_mul(x[(size_t)i << log_n], bc.smul[i], P.q, P.inv_modulus);
-        v[i] = mont_mul(s, 1, P.q, P.inv_modulus);  // ExportInt
-      }
+      // ExportInt(x_i * S_i) in one REDC
+      if (i < ns) v[i] = mont_mul(x[(size_t)i << log_n], bc.smul[i], src[i].q, src[i].inv_modulus);
     }
     const uint64_t u = mode == 2 ? 0 : round_sum<MAXS>(v, bc, ns);
     uint64_t* o = out + p * out_stride + k;
-    for (int j = 0; j < nd; ++j) {
-      const uint64_t q = primes[bc.dst0 + j].q;
-      uint64_t acc = 0;
+    if (!balanced) {
+      for (int j = 0; j < nd; ++j) {
+        const uint64_t q = dst[j].q, qinv = dst[j].inv_modulus;
+        const uint64_t* w2 = bc.w2 + j;
+        uint64_t lo = 0, hi = 0, acc = 0;
+        int left = chunk;
 #pragma unroll
-      for (int i = 0; i < MAXS; ++i) {
-        if (i < ns) {
-          uint64_t t = shoup(v[i], bc.w[i * nd + j], bc.ws[i * nd + j], q);
-          if (balanced && v[i] > primes[bc.src0 + i].half_q)
-            t = sub_mod(t, bc.wq[i * nd + j], q);
-          acc = add_mod(acc, t, q);
+        for (int i = 0; i < MAXS; ++i) {
+          if (i < ns) {
+            mac128(lo, hi, v[i], w2[i * nd]);
+            if (--left == 0 && i + 1 < ns) {
+              acc = add_mod(acc, redc128(lo, hi, q, qinv), q);
+              lo = hi = 0;
+              left = chunk;
+            }
+          }
         }
+        if (mode != 2) mac128(lo, hi, u, bc.z2[j]);
+        o[(size_t)j << log_n] = add_mod(acc, redc128(lo, hi, q, qinv), q);
       }
-      if (mode != 2) {
-        const uint64_t c = shoup(u, bc.z[j], bc.zs[j], q);
-        acc = mode == 0 ? sub_mod(acc, c, q) : add_mod(acc, c, q);
+    } else {
+      for (int j = 0; j < nd; ++j) {
+        const uint64_t q = dst[j].q;
+        uint64_t acc = 0;
+#pragma unroll
+        for (int i = 0; i < MAXS; ++i) {
+          if (i < ns) {
+            uint64_t t = shoup(v[i], bc.w[i * nd + j], bc.ws[i * nd + j], q);
+            if (v[i] > src[i].half_q) t = sub_mod(t, bc.wq[i * nd + j], q);
+            acc = add_mod(acc, t, q);
+          }
+        }
+        o[(size_t)j << log_n] = acc;
       }
-      o[(size_t)j << log_n] = acc;
     }
   }
 }

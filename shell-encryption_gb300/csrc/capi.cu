@@ -340,12 +340,21 @@ shg::BasisConv make_conv(const shg_context* ctx, int s0, int ns, int d0, int nd,
   bc.dst0 = d0;
   bc.mode = mode;
   bc.balanced = balanced;
+  // REDC of a 128-bit sum needs it below p * 2^64: sum_i v_i + u < 2^64 per chunk
+  u128 bound = 64;
+  bc.chunk = 0;
+  for (int i = 0; i < ns; ++i) {
+    bound += ctx->hp[s0 + i].q;
+    if (bound >= ((u128)1 << 64)) break;
+    ++bc.chunk;
+  }
+  if (bc.chunk < 1) bc.chunk = 1;
   for (int i = 0; i < ns; ++i) {
     const uint64_t q = ctx->hp[s0 + i].q;
     uint64_t m = invmod(prod_mod(ctx, s0, s0 + ns, s0 + i, q), q);  // (Q/q_i)^-1
     if (mode == 1) m = mulmod(m, prod_mod(ctx, d0, d0 + nd, -1, q), q);  // * P
     m = mulmod(m, pre % q, q);
-    bc.smul[i] = to_mont(m, q);
+    bc.smul[i] = m;
     const u128 two64 = (u128)1 << 64;
     bc.rinv[i] = (uint64_t)(two64 / q);
     bc.rho[i] = (uint64_t)((((u128)(uint64_t)(two64 % q)) << 64) / q);
@@ -364,10 +373,11 @@ shg::BasisConv make_conv(const shg_context* ctx, int s0, int ns, int d0, int nd,
       bc.w[i * nd + j] = wm;
       bc.ws[i * nd + j] = shoup_of(wm, p);
       bc.wq[i * nd + j] = mulmod(qi % p, wm, p);
+      bc.w2[i * nd + j] = to_mont(wm, p);
     }
-    const uint64_t z = mode == 1 ? 1 % p : prod_mod(ctx, s0, s0 + ns, -1, p);
-    bc.z[j] = to_mont(z, p);
-    bc.zs[j] = shoup_of(bc.z[j], p);
+    // mode 0: -u * (Q mod p_j); mode 1: + u (as a Montgomery rep)
+    const uint64_t z = mode == 1 ? 1 % p : (p - prod_mod(ctx, s0, s0 + ns, -1, p)) % p;
+    bc.z2[j] = to_mont(to_mont(z, p), p);
   }
   return bc;
 }

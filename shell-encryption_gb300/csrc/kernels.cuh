@@ -213,23 +213,28 @@ void launch_expand_combine(const CtxDev& c, uint64_t* base, const uint64_t* ks,
 // One RNS basis conversion between two prime sets of a context
 // (RnsPolynomial::SwitchRnsBasis, ScaleAndSwitchRnsBasis, ApproxSwitchRnsBasis,
 // rns/rns_polynomial.cc:419-724), kept in device memory.  Source limb i's
-// value is s_i = x_i * smul_i (Montgomery), v_i = ExportInt(s_i); destination
-// j gets sum_i v_i * w[i][j] mod p_j (w a Montgomery rep, so that product is
-// ImportInt(v_i) * w), then
+// exported value is v_i = ExportInt(x_i * S_i) = REDC(x_i * smul_i) with smul_i
+// the plain value S_i; destination j gets sum_i ImportInt(v_i) * W_ij mod p_j
+// (W_ij a Montgomery rep), then
 //   mode 0: minus u * (Q mod p_j),  mode 1: plus u,  mode 2: nothing,
 // with u = round(sum_i v_i / q_i) as the reference computes it in double
-// precision.  balanced (mode 2): v_i > q_i / 2 stands for v_i - q_i, whose
-// product is corrected by wq[i][j] = q_i * w[i][j] mod p_j.
+// precision.  Unbalanced conversions accumulate v_i * w2[i][j] (w2 = W * 2^64
+// mod p_j) and u * z2[j] in 128 bits, `chunk` source limbs per REDC, so one
+// REDC per chunk lands on the Montgomery rep of the sum.  balanced (mode 2):
+// v_i > q_i / 2 stands for v_i - q_i; that path multiplies with Shoup
+// constants (w, ws) and corrects by wq[i][j] = q_i * W_ij mod p_j.
 struct BasisConv {
   int ns, nd;          // source / destination prime counts
   int src0, dst0;      // first prime index of each set in the context
   int mode, balanced;
-  uint64_t smul[kMaxLimbs];     // Montgomery multiplier of source limb i
+  int chunk, pad_;     // source limbs per 128-bit accumulation
+  uint64_t smul[kMaxLimbs];     // plain multiplier S_i of source limb i
   uint64_t rinv[kMaxLimbs];     // floor(2^64 / q_i)
   uint64_t rho[kMaxLimbs];      // floor(frac(2^64 / q_i) * 2^64)
   double qd[kMaxLimbs];         // (double) q_i
-  uint64_t z[kMaxLimbs], zs[kMaxLimbs];  // per destination: u's multiplier, Shoup
+  uint64_t z2[kMaxLimbs];       // per destination: u's coefficient times 2^64 mod p_j
   // [i * nd + j], ns * nd entries used
+  uint64_t w2[kMaxLimbs * kMaxLimbs];
   uint64_t w[kMaxLimbs * kMaxLimbs], ws[kMaxLimbs * kMaxLimbs], wq[kMaxLimbs * kMaxLimbs];
 };
 
