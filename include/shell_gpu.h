@@ -169,7 +169,7 @@ int shg_ct_tensor(shg_context* ctx, uint64_t* out, const uint64_t* a,
  * Gadget key switching (relinearization and Galois keys)
  * ------------------------------------------------------------------------- */
 
-/* Uploads a gadget key: key_b, key_a [k][num_limbs][n] host arrays in NTT
+/* Uploads a gadget key: key_b, key_a [k][num_limbs][n] host or device arrays in NTT
  * form (Montgomery reps) with the RnsGadget of log_bs[num_limbs]
  * (rns/rns_gadget.cc:42-102).  `power` is the key's substitution power: 1
  * for an RnsRelinKey (GetKeyB/GetKeyA, rns/rns_relinearization_key.h:99-104),
@@ -221,6 +221,21 @@ int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key, uint64_t* out,
  * -> out [count][2][L][n]. */
 int shg_galois_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
                      const uint64_t* ct, int count, shg_stream stream);
+
+/* The key's rows key_b, key_a [k][L][n] as given to shg_key_create (the
+ * reference's GetKeyB / GetKeyA, rns/rns_galois_key.h:152-158), into host or
+ * device memory. */
+int shg_key_components(const shg_key* key, uint64_t* key_b, uint64_t* key_a);
+
+/* RnsGaloisKey::Compose (rns/rns_galois_key.h:214, .cc:349-406): the key for
+ * X -> X^(power * other.power) from `key` and `other` (same moduli and
+ * gadget dimension): each row (b_i, a_i) of `other`, substituted by key's
+ * power and key-switched with `key`.  *out is a new key with other's gadget.
+ * CreatePadOfComposedKey (.cc:408-434) is shg_galois_precompute_pad with the
+ * first key and the second key's a-row digits; ComposeWithPads (.cc:436-471)
+ * is shg_poly_substitute of the b rows followed by shg_galois_apply_with_pad. */
+int shg_galois_key_compose(shg_context* ctx, const shg_key* key, const shg_key* other,
+                           shg_key** out);
 
 /* RnsGaloisKey::PrecomputeRandomPad (rns/rns_galois_key.h:170-175,
  * .cc:289-306): pad_digits [count][k][L][n] = the gadget digits of each

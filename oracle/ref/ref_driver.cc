@@ -620,6 +620,48 @@ int ref_bfv(int log_n, const uint64_t* qs, int L, const uint64_t* ps, int K, uin
   return 0;
 }
 
+// RnsGaloisKey::Compose (rns/rns_galois_key.cc:349-406) of a key of power
+// `power` with another key (same gadget) of power `power2`: composed rows
+// out_b, out_a [k][L][n] and the composed power.
+int ref_galois_compose(int log_n, const uint64_t* qs, int L, const int* log_bs, int power,
+                       const uint64_t* key_b, const uint64_t* key_a, int power2,
+                       const uint64_t* key2_b, const uint64_t* key2_a, uint64_t* out_b,
+                       uint64_t* out_a, int* out_power) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  const size_t P = (size_t)L * n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto q_hats = ctx->MainPrimeModulusComplements(L - 1).value();
+  auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(L - 1).value();
+  auto gadget = rlwe::RnsGadget<M>::Create(
+      log_n, std::vector<size_t>(log_bs, log_bs + L), q_hats, q_hat_invs, moduli);
+  if (!gadget.ok()) return fail(gadget.status());
+  const int k = gadget->Dimension();
+  auto make_key = [&](int pw, const uint64_t* kb, const uint64_t* ka) {
+    std::vector<rlwe::RnsPolynomial<M>> kas, kbs;
+    for (int j = 0; j < k; ++j) {
+      kbs.push_back(make_poly(kb + (size_t)j * P, L, n, true));
+      kas.push_back(make_poly(ka + (size_t)j * P, L, n, true));
+    }
+    return rlwe::RnsGaloisKey<M>::CreateFromKeyComponents(
+        std::move(kas), std::move(kbs), pw, &*gadget, moduli, "", rlwe::PRNG_TYPE_HKDF);
+  };
+  auto k1 = make_key(power, key_b, key_a);
+  if (!k1.ok()) return fail(k1.status());
+  auto k2 = make_key(power2, key2_b, key2_a);
+  if (!k2.ok()) return fail(k2.status());
+  auto c = k1->Compose(*k2);
+  if (!c.ok()) return fail(c.status());
+  for (int j = 0; j < k; ++j) {
+    store_poly(c->key_bs_[j], out_b + (size_t)j * P);
+    store_poly(c->key_as_[j], out_a + (size_t)j * P);
+  }
+  *out_power = c->power_;
+  return 0;
+}
+
 // ObliviousExpander::ComputeNormalizer.
 uint64_t ref_compute_normalizer(int k, int log_t) {
   return rlwe::ObliviousExpander<M>::ComputeNormalizer(k, log_t);

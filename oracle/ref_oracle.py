@@ -64,6 +64,10 @@ def lib():
         L.ref_bfv.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _U64P, ctypes.c_int,
                               ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _U64P, _U64P,
                               ctypes.c_int, _U64P]
+        L.ref_galois_compose.argtypes = [ctypes.c_int, _U64P, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int), ctypes.c_int, _U64P,
+                                         _U64P, ctypes.c_int, _U64P, _U64P, _U64P, _U64P,
+                                         ctypes.POINTER(ctypes.c_int)]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -279,3 +283,15 @@ def bfv_absorb(log_n, qs, ps, t, cts, pt):
     _check(lib().ref_bfv(log_n, _p(q), len(q), _p(p), len(p), t, 1, cts.shape[1], _p(cts),
                          _p(pt), cts.shape[0], _p(out)))
     return out
+
+
+def galois_compose(log_n, qs, log_bs, power, kb, ka, power2, kb2, ka2):
+    """RnsGaloisKey::Compose: (composed key_b, key_a [k][L][n], composed power)."""
+    q = _qs(qs)
+    lb = (ctypes.c_int * len(log_bs))(*log_bs)
+    kb, ka, kb2, ka2 = (np.ascontiguousarray(x, dtype=np.uint64) for x in (kb, ka, kb2, ka2))
+    ob, oa = np.empty_like(kb), np.empty_like(ka)
+    pw = ctypes.c_int()
+    _check(lib().ref_galois_compose(log_n, _p(q), len(q), lb, power, _p(kb), _p(ka), power2,
+                                    _p(kb2), _p(ka2), _p(ob), _p(oa), ctypes.byref(pw)))
+    return ob, oa, pw.value

@@ -848,9 +848,9 @@ int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
   if (e == cudaSuccess) e = cudaMalloc(&key->ka, elems * sizeof(uint64_t));
   if (e == cudaSuccess) e = cudaMalloc(&key->d_digits, dd.size() * sizeof(DigitDesc));
   if (e == cudaSuccess)
-    e = cudaMemcpy(key->kb, key_b, elems * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(key->kb, key_b, elems * sizeof(uint64_t), cudaMemcpyDefault);
   if (e == cudaSuccess)
-    e = cudaMemcpy(key->ka, key_a, elems * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(key->ka, key_a, elems * sizeof(uint64_t), cudaMemcpyDefault);
   if (e == cudaSuccess)
     e = cudaMemcpy(key->d_digits, dd.data(), dd.size() * sizeof(DigitDesc),
                    cudaMemcpyHostToDevice);
@@ -1241,6 +1241,83 @@ int shg_bgv_rotate(shg_context* ctx, const shg_key* key, uint64_t* out,
   if (out == ct) return fail(SHG_INVALID_ARGUMENT, "`out` must not alias `ct`");
   return keyswitch(ctx, key, out, KsArgs{ct, 2, 1, key->power, 1}, count,
                    (cudaStream_t)s);
+}
+
+int shg_key_components(const shg_key* key, uint64_t* key_b, uint64_t* key_a) {
+  if (!key || !key_b || !key_a) return fail(SHG_INVALID_ARGUMENT, "null argument");
+  shg_context* ctx = key->ctx;
+  const size_t elems = (size_t)key->k * key->L * ctx->n;
+  uint64_t* tmp = nullptr;
+  cudaError_t e = cudaMalloc(&tmp, elems * sizeof(uint64_t));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SHG_RESOURCE_EXHAUSTED, "cannot reserve scratch for the key rows");
+  }
+  ScalarPack sc{};
+  for (int l = 0; l < key->L; ++l) {
+    sc.v[2 * l] = ctx->hp[l].inv_r;  // undo the 2^64 premultiplication
+    sc.v[2 * l + 1] = shoup_of(ctx->hp[l].inv_r, ctx->hp[l].q);
+  }
+  for (int c = 0; c < 2 && e == cudaSuccess; ++c) {
+    shg::launch_pointwise(ctx->dev(), shg::PW_MUL_SHOUP, tmp, c ? key->ka : key->kb, nullptr,
+                          sc, key->k, key->L, 0);
+    e = cudaMemcpy(c ? key_a : key_b, tmp, elems * sizeof(uint64_t), cudaMemcpyDefault);
+  }
+  cudaFree(tmp);
+  return e == cudaSuccess ? SHG_OK : cuda_fail(e, "key_components");
+}
+
+int shg_galois_key_compose(shg_context* ctx, const shg_key* key, const shg_key* other,
+                           shg_key** out) {
+  if (!out) return fail(SHG_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  int st = check_key(ctx, key);
+  if (st) return st;
+  if ((st = check_key(ctx, other))) return st;
+  if (key->L != other->L || key->k != other->k)
+    return fail(SHG_INVALID_ARGUMENT, "the keys must share moduli and gadget dimension");
+  const int L = key->L, k = key->k;
+  const size_t Ln = (size_t)L * ctx->n, bytes = Ln * sizeof(uint64_t);
+  // The other key's rows as k ciphertexts (b_i, a_i), un-premultiplied.
+  uint64_t *ct = nullptr, *res = nullptr;
+  cudaError_t e = cudaMalloc(&ct, 2 * k * bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&res, 2 * k * bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(ct);
+    return fail(SHG_RESOURCE_EXHAUSTED, "cannot reserve scratch for key composition");
+  }
+  ScalarPack sc{};
+  for (int l = 0; l < L; ++l) {
+    sc.v[2 * l] = ctx->hp[l].inv_r;
+    sc.v[2 * l + 1] = shoup_of(ctx->hp[l].inv_r, ctx->hp[l].q);
+  }
+  for (int i = 0; i < k && st == SHG_OK; ++i) {
+    shg::launch_pointwise(ctx->dev(), shg::PW_MUL_SHOUP, ct + (size_t)2 * i * Ln,
+                          other->kb + (size_t)i * Ln, nullptr, sc, 1, L, 0);
+    shg::launch_pointwise(ctx->dev(), shg::PW_MUL_SHOUP, ct + (size_t)(2 * i + 1) * Ln,
+                          other->ka + (size_t)i * Ln, nullptr, sc, 1, L, 0);
+  }
+  // RnsGaloisKey::Compose (rns/rns_galois_key.cc:349-406) substitutes each
+  // row by this key's power and key-switches its a part with this key: the
+  // rotation of that ciphertext.
+  st = launch_status("galois_key_compose");
+  if (st == SHG_OK)
+    st = keyswitch(ctx, key, res, KsArgs{ct, 2, 1, key->power, 1}, k, (cudaStream_t)0);
+  if (st == SHG_OK) {
+    e = cudaMemcpy2D(ct, bytes, res, 2 * bytes, bytes, k, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2D(ct + (size_t)k * Ln, bytes, res + Ln, 2 * bytes, bytes, k,
+                       cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) st = cuda_fail(e, "galois_key_compose");
+  }
+  if (st == SHG_OK) {
+    const int power = (int)(((int64_t)key->power * other->power) % (2 * ctx->n));
+    st = shg_key_create(ctx, L, other->log_bs.data(), power, ct, ct + (size_t)k * Ln, out);
+  }
+  cudaFree(ct);
+  cudaFree(res);
+  return st;
 }
 
 int shg_galois_precompute_pad(shg_context* ctx, const shg_key* key, uint64_t* out,

@@ -121,12 +121,10 @@ Status DeviceArray::Download(uint64_t* host, size_t elems, size_t offset) const 
 StatusOr<std::unique_ptr<const RnsContext>> RnsContext::Create(
     int log_n, std::vector<uint64_t> qs, std::vector<uint64_t> ps,
     uint64_t plaintext_modulus) {
-  if (!ps.empty())
-    return InvalidArgumentError(
-        "auxiliary primes `ps` are not supported by the device path");
   shg_context* h = nullptr;
-  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_context_create(
-      log_n, qs.data(), static_cast<int>(qs.size()), plaintext_modulus, &h)));
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_context_create_with_aux(
+      log_n, qs.data(), static_cast<int>(qs.size()), ps.data(), static_cast<int>(ps.size()),
+      plaintext_modulus, &h)));
   std::unique_ptr<RnsContext> ctx(new RnsContext());
   ctx->h_ = h;
   ctx->log_n_ = log_n;
@@ -134,7 +132,16 @@ StatusOr<std::unique_ptr<const RnsContext>> RnsContext::Create(
   for (size_t i = 0; i < qs.size(); ++i)
     ctx->moduli_.push_back(std::unique_ptr<PrimeModulus>(
         new PrimeModulus(ctx.get(), static_cast<int>(i), qs[i])));
+  for (size_t j = 0; j < ps.size(); ++j)
+    ctx->aux_.push_back(std::unique_ptr<PrimeModulus>(
+        new PrimeModulus(ctx.get(), static_cast<int>(qs.size() + j), ps[j])));
   return std::unique_ptr<const RnsContext>(std::move(ctx));
+}
+
+Moduli RnsContext::AuxPrimeModuli() const {
+  Moduli out;
+  for (const auto& m : aux_) out.push_back(m.get());
+  return out;
 }
 
 RnsContext::~RnsContext() { shg_context_destroy(h_); }
@@ -375,6 +382,26 @@ Status RnsPolynomial::ModReduceLsb(uint64_t t, const std::vector<uint64_t>& ql_i
   RLWE_GPU_RETURN_IF_ERROR(FromCode(
       shg_poly_modreduce_lsb(ContextOf(moduli), out.data(), data_.data(), t, ql_inv.data(),
                              is_ntt_ ? 1 : 0, 1, num_moduli_, g_stream)));
+  data_ = std::move(out);
+  --num_moduli_;
+  return OkStatus();
+}
+
+Status RnsPolynomial::ModReduceMsb(const std::vector<uint64_t>& ql_inv, const Moduli& moduli) {
+  // rns/rns_polynomial.cc:349-366
+  if (static_cast<int>(moduli.size()) != num_moduli_)
+    return InvalidArgumentError(ModuliMessage(num_moduli_));
+  if (num_moduli_ <= 1)
+    return InvalidArgumentError("ModReduceMsb cannot apply with only one prime modulus.");
+  if (static_cast<int>(ql_inv.size()) != num_moduli_ - 1)
+    return InvalidArgumentError("`ql_inv` must be defined with respect to " +
+                                std::to_string(num_moduli_ - 1) + " moduli.");
+  RLWE_GPU_RETURN_IF_ERROR(CheckModuli(moduli));
+  DeviceArray out((size_t)(num_moduli_ - 1) << log_n_);
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_poly_modreduce_msb(ContextOf(moduli), out.data(),
+                                                           data_.data(), ql_inv.data(),
+                                                           is_ntt_ ? 1 : 0, 1, num_moduli_,
+                                                           g_stream)));
   data_ = std::move(out);
   --num_moduli_;
   return OkStatus();
@@ -666,6 +693,70 @@ StatusOr<RnsBgvCiphertext> RnsRelinKey::ApplyTo(const RnsBgvCiphertext& ct) cons
                                                     out.data(), ct.device_data(), 1,
                                                     g_stream)));
   return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
+}
+
+// ---------------------------------------------------------------------------
+// RnsBfvCiphertext
+// ---------------------------------------------------------------------------
+
+StatusOr<RnsBfvCiphertext> RnsBfvCiphertext::operator*(const RnsBfvCiphertext& that) const {
+  // rns/rns_bfv_ciphertext.cc:100-108
+  if (Level() != that.Level()) return InvalidArgumentError("`that` has a mismatched level.");
+  if (PowerOfS() != that.PowerOfS())
+    return InvalidArgumentError("Ciphertexts must be encrypted with the same key power.");
+  if (Len() != 2 || that.Len() != 2)
+    return InvalidArgumentError("the device BFV product takes two-component ciphertexts");
+  if (!context_ || context_->NumAuxPrimeModuli() == 0)
+    return InvalidArgumentError("the context has no auxiliary prime moduli");
+  DeviceArray out(3 * component_elems());
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_bfv_mul(context_->handle(), out.data(), device_data(),
+                                                that.device_data(), 1, NumModuli(),
+                                                g_stream)));
+  return RnsBfvCiphertext(
+      FromDevice(std::move(out), 3, LogN(), moduli(), PowerOfS(), Error() * that.Error()),
+      context_);
+}
+
+Status RnsBfvCiphertext::AbsorbInPlace(const RnsPolynomial& plaintext) {
+  // rns/rns_bfv_ciphertext.cc:33-98
+  if (!plaintext.IsNttForm()) return InvalidArgumentError("`plaintext` must be in NTT form.");
+  if (plaintext.NumModuli() != NumModuli() || plaintext.LogN() != LogN())
+    return InvalidArgumentError("`plaintext` has a mismatched level.");
+  if (!context_ || context_->NumAuxPrimeModuli() == 0)
+    return InvalidArgumentError("the context has no auxiliary prime moduli");
+  DeviceArray out(data_.size());
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_bfv_absorb(context_->handle(), out.data(),
+                                                   data_.data(), plaintext.device_data(), len_,
+                                                   1, NumModuli(), g_stream)));
+  data_ = std::move(out);
+  return OkStatus();
+}
+
+Status RnsBfvCiphertext::ModReduce() {
+  // rns/rns_bfv_ciphertext.h:184-200
+  if (moduli_.size() <= 1)
+    return FailedPreconditionError(
+        "Cannot perform ModReduce with insufficient number of prime moduli.");
+  const int L = NumModuli();
+  RLWE_GPU_ASSIGN_OR_RETURN(std::vector<uint64_t> ql_inv,
+                            context_->MainPrimeModulusInverseResidues(L - 1));
+  DeviceArray out((size_t)len_ * (L - 1) << log_n_);
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_poly_modreduce_msb(
+      context_->handle(), out.data(), data_.data(), ql_inv.data(), 1, len_, L, g_stream)));
+  data_ = std::move(out);
+  moduli_.pop_back();
+  return OkStatus();
+}
+
+StatusOr<RnsGaloisKey> RnsGaloisKey::Compose(const RnsGaloisKey& other_key) const {
+  shg_key* k = nullptr;
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(
+      shg_galois_key_compose(ContextOf(moduli_), key_.get(), other_key.key_.get(), &k)));
+  RnsGaloisKey key;
+  key.key_ = std::shared_ptr<shg_key>(k, [](shg_key* p) { shg_key_destroy(p); });
+  key.moduli_ = moduli_;
+  key.power_ = shg_key_power(k);
+  return key;
 }
 
 StatusOr<RnsGaloisKey> RnsGaloisKey::CreateFromKeyComponents(

@@ -167,8 +167,8 @@ using Moduli = std::vector<const PrimeModulus*>;
 class RnsContext {
  public:
   // RnsContext::Create(log_n, qs, ps, plaintext_modulus)
-  // (rns/rns_context.h:62-72).  Auxiliary primes `ps` (BFV/CKKS basis
-  // extension) are not part of this device path and must be empty.
+  // (rns/rns_context.h:62-72); auxiliary primes `ps` serve the BFV basis
+  // extension (RnsBfvCiphertext).
   static StatusOr<std::unique_ptr<const RnsContext>> Create(
       int log_n, std::vector<uint64_t> qs, std::vector<uint64_t> ps,
       uint64_t plaintext_modulus);
@@ -181,6 +181,8 @@ class RnsContext {
   int NumMainPrimeModuli() const { return static_cast<int>(moduli_.size()); }
   uint64_t PlaintextModulus() const { return t_; }
   Moduli MainPrimeModuli() const;
+  int NumAuxPrimeModuli() const { return static_cast<int>(aux_.size()); }
+  Moduli AuxPrimeModuli() const;
   // MainPrimeModulusInverseResidues()[level].Prefix(level): Montgomery
   // residues of q_level^{-1} mod q_j, j < level (rns/rns_context.h:145-147),
   // the `ql_inv` argument of ModReduceLsb / ModReduce.
@@ -193,6 +195,7 @@ class RnsContext {
   int log_n_ = 0;
   uint64_t t_ = 0;
   std::vector<std::unique_ptr<PrimeModulus>> moduli_;
+  std::vector<std::unique_ptr<PrimeModulus>> aux_;
 };
 
 // ---------------------------------------------------------------------------
@@ -243,6 +246,8 @@ class RnsPolynomial {
   // ModReduceLsb(t, ql_inv, moduli) (rns/rns_polynomial.cc:262-344).
   Status ModReduceLsb(uint64_t t, const std::vector<uint64_t>& ql_inv,
                       const Moduli& moduli);
+  // ModReduceMsb(ql_inv, moduli) (rns/rns_polynomial.cc:349-417).
+  Status ModReduceMsb(const std::vector<uint64_t>& ql_inv, const Moduli& moduli);
 
   uint64_t* device_data() const { return data_.data(); }
 
@@ -322,7 +327,7 @@ class RnsBgvCiphertext {
   uint64_t* device_data() const { return data_.data(); }
   size_t component_elems() const { return (size_t)moduli_.size() << log_n_; }
 
- private:
+ protected:
   RnsBgvCiphertext() = default;
   Status CheckSameShape(const RnsBgvCiphertext& that, bool check_degree) const;
   DeviceArray data_;
@@ -333,6 +338,26 @@ class RnsBgvCiphertext {
   double error_ = 0;
 };
 using RnsRlweCiphertext = RnsBgvCiphertext;
+
+// rlwe::RnsBfvCiphertext (rns/rns_bfv_ciphertext.h): an RNS ciphertext whose
+// products extend to the context's auxiliary primes.  Addition, subtraction,
+// negation and Substitute are the base class's.
+class RnsBfvCiphertext : public RnsBgvCiphertext {
+ public:
+  RnsBfvCiphertext(RnsBgvCiphertext ct, const RnsContext* context)
+      : RnsBgvCiphertext(std::move(ct)), context_(context) {}
+  // Mul (rns/rns_bfv_ciphertext.cc:100-205).
+  StatusOr<RnsBfvCiphertext> operator*(const RnsBfvCiphertext& that) const;
+  // AbsorbInPlace(plaintext) (rns/rns_bfv_ciphertext.cc:33-98).
+  Status AbsorbInPlace(const RnsPolynomial& plaintext);
+  // ModReduce() (rns/rns_bfv_ciphertext.h:184-200): ModReduceMsb of every
+  // component with MainPrimeModulusInverseResidues()[level].
+  Status ModReduce();
+  const RnsContext* Context() const { return context_; }
+
+ private:
+  const RnsContext* context_;
+};
 
 // Gadget key for relinearization (power 1) or a Galois automorphism, held on
 // the device in the layout the key-switch kernels read.
@@ -375,6 +400,9 @@ class RnsGaloisKey {
       const RnsBgvCiphertext& ciphertext,
       const std::vector<RnsPolynomial>& ciphertext_pad_digits,
       const RnsPolynomial& ciphertext_pad_new) const;
+  // Compose(other_key) (rns/rns_galois_key.cc:349-406): the key for the
+  // product of the two substitution powers.
+  StatusOr<RnsGaloisKey> Compose(const RnsGaloisKey& other_key) const;
   int SubstitutionPower() const { return power_; }
   int Dimension() const;
   shg_key* handle() const { return key_.get(); }

@@ -101,6 +101,8 @@ SIGNATURES = {
     "shg_bfv_mul": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "shg_bfv_absorb": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, _vp]),
+    "shg_galois_key_compose": (ctypes.c_int, [_vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "shg_key_components": (ctypes.c_int, [_vp, _u64p, _u64p]),
     "shg_sample_uniform_error": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, _vp]),
     "shg_bgv_encrypt": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,

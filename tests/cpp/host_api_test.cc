@@ -112,7 +112,9 @@ void TestContextErrors() {
   auto bad = RnsContext::Create(10, {35184371138560ull}, {}, 65537);  // even
   EXPECT(!bad.ok(), "even modulus must be rejected");
   auto aux = RnsContext::Create(10, kQ45, {kQ50[0]}, 65537);
-  EXPECT(!aux.ok(), "auxiliary primes are rejected");
+  EXPECT(aux.ok() && (*aux)->NumAuxPrimeModuli() == 1, "auxiliary primes are accepted");
+  auto dup = RnsContext::Create(10, kQ45, {kQ45[2]}, 65537);
+  EXPECT(!dup.ok(), "an auxiliary prime equal to a main prime is rejected");
 }
 
 void TestPolynomial(int log_n, const std::vector<uint64_t>& qs) {
@@ -499,12 +501,104 @@ void TestRnsSecretKey(int log_n, const std::vector<uint64_t>& qs) {
   so_rns_destroy(r);
 }
 
+// RnsBfvCiphertext (operator*, AbsorbInPlace, ModReduce) on a context with
+// auxiliary primes, and RnsGaloisKey::Compose, against the oracle
+// (rns/rns_bfv_ciphertext_test.cc, rns/rns_galois_key_test.cc).
+void TestBfvAndCompose(int log_n, const std::vector<uint64_t>& qs,
+                       const std::vector<uint64_t>& ps) {
+  const int n = 1 << log_n, L = (int)qs.size(), K = (int)ps.size();
+  const uint64_t t = 40961;
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, qs, ps, t));
+  EXPECT(ctx->NumAuxPrimeModuli() == K, "AuxPrimeModuli");
+  const Moduli moduli = ctx->MainPrimeModuli();
+  std::vector<uint64_t> all = qs;
+  all.insert(all.end(), ps.begin(), ps.end());
+  so_rns* r = so_rns_create(log_n, all.data(), L + K);
+  std::vector<int> aux(K);
+  for (int j = 0; j < K; ++j) aux[j] = L + j;
+  auto make_ct = [&](uint64_t seed) {
+    std::vector<uint64_t> flat = Uniform(seed, qs, n, 2);
+    std::vector<RnsPolynomial> comps;
+    for (int c = 0; c < 2; ++c)
+      comps.push_back(*RnsPolynomial::Create(Limbs(flat.data() + (size_t)c * L * n, L, n), true));
+    return std::make_pair(RnsBfvCiphertext(RnsBgvCiphertext(comps, moduli, 1, 1.0), ctx.get()),
+                          flat);
+  };
+  auto [x, fx] = make_ct(71);
+  auto [y, fy] = make_ct(72);
+  RnsBfvCiphertext prod = x;
+  ASSERT_OK_AND_ASSIGN(prod, x * y);
+  std::vector<uint64_t> want((size_t)3 * L * n);
+  so_bfv_mul(r, L, aux.data(), K, t, fx.data(), fy.data(), want.data());
+  EXPECT(prod.Len() == 3 && FlatCt(prod) == want, "RnsBfvCiphertext::operator*");
+  std::vector<uint64_t> pt = Uniform(73, qs, n, 1);
+  RnsBfvCiphertext absorbed = x;
+  EXPECT_OK(absorbed.AbsorbInPlace(*RnsPolynomial::Create(Limbs(pt.data(), L, n), true)));
+  want.assign((size_t)2 * L * n, 0);
+  so_bfv_absorb(r, L, aux.data(), K, t, 2, fx.data(), pt.data(), want.data());
+  EXPECT(FlatCt(absorbed) == want, "RnsBfvCiphertext::AbsorbInPlace");
+  if (L > 1) {
+    RnsBfvCiphertext red = x;
+    EXPECT_OK(red.ModReduce());
+    std::vector<uint64_t> w2;
+    for (int c = 0; c < 2; ++c) {
+      std::vector<uint64_t> o((size_t)(L - 1) * n);
+      so_rns_modreduce_msb(r, L, 1, fx.data() + (size_t)c * L * n, o.data());
+      w2.insert(w2.end(), o.begin(), o.end());
+    }
+    EXPECT(red.NumModuli() == L - 1 && FlatCt(red) == w2, "RnsBfvCiphertext::ModReduce");
+  }
+  // Compose of two Galois keys = rotating the second key's rows with the first
+  std::vector<int> log_bs(L, 10);
+  RnsGadget gadget = *RnsGadget::Create(log_n, log_bs, moduli);
+  const int k = gadget.Dimension();
+  std::vector<uint64_t> kb1 = Uniform(81, qs, n, k), ka1 = Uniform(82, qs, n, k);
+  std::vector<uint64_t> kb2 = Uniform(83, qs, n, k), ka2 = Uniform(84, qs, n, k);
+  auto rows = [&](const std::vector<uint64_t>& f) {
+    std::vector<RnsPolynomial> v;
+    for (int j = 0; j < k; ++j)
+      v.push_back(*RnsPolynomial::Create(Limbs(f.data() + (size_t)j * L * n, L, n), true));
+    return v;
+  };
+  RnsGaloisKey g1 = *RnsGaloisKey::CreateFromKeyComponents(rows(ka1), rows(kb1), 5, &gadget,
+                                                           moduli);
+  RnsGaloisKey g2 = *RnsGaloisKey::CreateFromKeyComponents(rows(ka2), rows(kb2), 3, &gadget,
+                                                           moduli);
+  RnsGaloisKey g12 = g1;
+  ASSERT_OK_AND_ASSIGN(g12, g1.Compose(g2));
+  EXPECT(g12.SubstitutionPower() == 15, "composed power");
+  // apply the composed key and the oracle's composed rows to one ciphertext
+  std::vector<uint64_t> cb((size_t)k * L * n), ca((size_t)k * L * n);
+  for (int j = 0; j < k; ++j) {
+    std::vector<uint64_t> row((size_t)2 * L * n), sub((size_t)2 * L * n), o((size_t)2 * L * n);
+    std::copy(kb2.begin() + (size_t)j * L * n, kb2.begin() + (size_t)(j + 1) * L * n, row.begin());
+    std::copy(ka2.begin() + (size_t)j * L * n, ka2.begin() + (size_t)(j + 1) * L * n,
+              row.begin() + (size_t)L * n);
+    so_rns_substitute(r, L, 5, row.data(), sub.data());
+    so_rns_substitute(r, L, 5, row.data() + (size_t)L * n, sub.data() + (size_t)L * n);
+    so_rns_galois(r, L, log_bs.data(), sub.data(), kb1.data(), ka1.data(), o.data());
+    std::copy(o.begin(), o.begin() + (size_t)L * n, cb.begin() + (size_t)j * L * n);
+    std::copy(o.begin() + (size_t)L * n, o.end(), ca.begin() + (size_t)j * L * n);
+  }
+  std::vector<uint64_t> got_b(cb.size()), got_a(ca.size());
+  EXPECT_OK(Status(static_cast<StatusCode>(
+                       shg_key_components(g12.handle(), got_b.data(), got_a.data())),
+                   ""));
+  EXPECT(got_b == cb && got_a == ca, "RnsGaloisKey::Compose rows");
+  so_rns_destroy(r);
+}
+
 }  // namespace
 
 int main() {
   TestSymmetric();
   TestRnsSecretKey(10, {kQ45[0], kQ45[1]});
   TestRnsSecretKey(14, kQ45);
+  TestBfvAndCompose(11, {8589905921ull, 8589852673ull, 8589844481ull},
+                    {1073692673ull, 1073668097ull});
+  TestBfvAndCompose(12, {kQ45[0], kQ45[1]}, {35184368320513ull, 35184368025601ull,
+                                              35184367828993ull});
   TestContextErrors();
   TestPolynomial(4, {kQ45[0], kQ45[1]});
   TestPolynomial(11, kQ50);

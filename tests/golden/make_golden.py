@@ -143,6 +143,22 @@ def main():
         g[tag + "_m"] = m
         g[tag + "_seeds"] = np.frombuffer(b"".join(seeds), np.uint8).reshape(count, 32).copy()
         g[tag + "_out"] = R.encrypt_bgv(log_n, qs, t, var, key, m, seeds)
+    # RnsGaloisKey::Compose (rns/rns_galois_key.cc:349-406).
+    for log_n, qs, log_bs, p1, p2 in [(7, Q45[:2], [20, 20], 5, 25), (9, Q50[:3], [50, 16, 20],
+                                                                       3, 7)]:
+        tag = f"galcomp_{log_n}_{len(qs)}"
+        n = 1 << log_n
+        k = O.Rns(log_n, qs).gadget_dim(log_bs)
+        keys = [O.uniform_limbs(6400 + log_n + 10 * i, qs, n, k) for i in range(4)]
+        ob, oa, pw = R.galois_compose(log_n, qs, log_bs, p1, keys[0], keys[1], p2, keys[2],
+                                      keys[3])
+        g[tag + "_qs"] = np.array(qs, np.uint64)
+        g[tag + "_log_bs"] = np.array(log_bs, np.int32)
+        g[tag + "_powers"] = np.array([p1, p2, pw], np.int32)
+        for nm, v in zip(("kb1", "ka1", "kb2", "ka2"), keys):
+            g[f"{tag}_{nm}"] = v
+        g[tag + "_out_b"] = ob
+        g[tag + "_out_a"] = oa
     # RNS basis conversion and BFV (rns/rns_polynomial.cc:349-852,
     # rns/rns_bfv_ciphertext.cc) on the reference's own BFV test parameters
     # (rns/testing/parameters.h GetBfvParametersForFiniteFieldEncoding).

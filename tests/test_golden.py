@@ -602,3 +602,54 @@ def test_gpu_bfv_full_size_digest(sg, oracle):
     out = sg.DeviceBuffer(2 * 3 * 6 * (1 << 14) * 8)
     _run(sg, sg.lib().shg_bfv_mul, ctx.h, out.ptr, da.ptr, db.ptr, 2, 6, None)
     assert digest(out.download((2, 3, 6, 1 << 14))) == d["out_sha256"]
+
+
+# --------------------------------------------------------------------------
+# RnsGaloisKey::Compose
+# --------------------------------------------------------------------------
+
+COMP_TAGS = sorted({k[:-len("_out_b")] for k in SMALL.files
+                    if k.startswith("galcomp_") and k.endswith("_out_b")})
+
+
+@pytest.mark.parametrize("tag", COMP_TAGS)
+def test_oracle_galois_compose_golden(oracle, tag):
+    """Compose equals the rotation of the other key's rows (b_i, a_i)."""
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    lb = [int(b) for b in SMALL[tag + "_log_bs"]]
+    p1, p2, pw = (int(v) for v in SMALL[tag + "_powers"])
+    rns = oracle.Rns(log_n, qs)
+    kb1, ka1, kb2, ka2 = (SMALL[f"{tag}_{x}"] for x in ("kb1", "ka1", "kb2", "ka2"))
+    rows = [np.stack([rns.substitute(kb2[i], p1), rns.substitute(ka2[i], p1)])
+            for i in range(kb2.shape[0])]
+    out = np.stack([rns.galois(r, kb1, ka1, lb) for r in rows])
+    assert np.array_equal(out[:, 0], SMALL[tag + "_out_b"])
+    assert np.array_equal(out[:, 1], SMALL[tag + "_out_a"])
+    assert pw == (p1 * p2) % (2 << log_n)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", COMP_TAGS)
+def test_gpu_galois_compose_golden(sg, tag):
+    log_n = int(tag.split("_")[1])
+    qs = [int(q) for q in SMALL[tag + "_qs"]]
+    lb = [int(b) for b in SMALL[tag + "_log_bs"]]
+    p1, p2, pw = (int(v) for v in SMALL[tag + "_powers"])
+    lib = sg.lib()
+    ctx = sg.Context(log_n, qs)
+    k1 = sg.Key(ctx, lb, p1, SMALL[tag + "_kb1"], SMALL[tag + "_ka1"])
+    k2 = sg.Key(ctx, lb, p2, SMALL[tag + "_kb2"], SMALL[tag + "_ka2"])
+    h = ctypes.c_void_p()
+    sg.check(lib.shg_galois_key_compose(ctx.h, k1.h, k2.h, ctypes.byref(h)))
+    try:
+        assert lib.shg_key_power(h.value) == pw
+        want_b, want_a = SMALL[tag + "_out_b"], SMALL[tag + "_out_a"]
+        got_b, got_a = np.empty_like(want_b), np.empty_like(want_a)
+        p64 = ctypes.POINTER(ctypes.c_uint64)
+        sg.check(lib.shg_key_components(h.value, got_b.ctypes.data_as(p64),
+                                        got_a.ctypes.data_as(p64)))
+        assert np.array_equal(got_b, want_b)
+        assert np.array_equal(got_a, want_a)
+    finally:
+        lib.shg_key_destroy(h.value)
