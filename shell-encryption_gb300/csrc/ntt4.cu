@@ -234,7 +234,7 @@ struct FwdDstBgvEnc {
 };
 
 // ---------------------------------------------------------------------------
-// Inverse phase-1 sources: 16 values at idx0..idx0+15 of transform g (rows).
+// Inverse phase-1 sources: the values at i, i + 1 of transform g (rows).
 // ---------------------------------------------------------------------------
 
 template <int LOG_N>
@@ -243,13 +243,8 @@ struct InvSrcPlain {
   int first, stride;  // source limb of transform g: first + g * stride
   struct H {
     const uint64_t* base;
-    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
-#pragma unroll
-      for (int k = 0; k < 16; k += 2) {
-        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(base + i0 + k);
-        x[k] = v.x;
-        x[k + 1] = v.y;
-      }
+    __device__ __forceinline__ ulonglong2 pair(int i) const {
+      return *reinterpret_cast<const ulonglong2*>(base + i);
     }
   };
   __device__ H bind(int g, int, const CtxDev&) const {
@@ -267,23 +262,15 @@ struct InvSrcComponent {
   struct H {
     const uint64_t* base;
     int power;
-    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
-      if (power > 0) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const unsigned j = __brev((unsigned)(i0 + k)) >> (32 - LOG_N);
-          const unsigned t = ((unsigned)((power - 1) >> 1) + j * (unsigned)power) &
-                             ((1u << LOG_N) - 1);
-          x[k] = base[__brev(t) >> (32 - LOG_N)];
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < 16; k += 2) {
-          const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(base + i0 + k);
-          x[k] = v.x;
-          x[k + 1] = v.y;
-        }
-      }
+    __device__ __forceinline__ uint64_t at(int i) const {
+      const unsigned j = __brev((unsigned)i) >> (32 - LOG_N);
+      const unsigned t = ((unsigned)((power - 1) >> 1) + j * (unsigned)power) &
+                         ((1u << LOG_N) - 1);
+      return base[__brev(t) >> (32 - LOG_N)];
+    }
+    __device__ __forceinline__ ulonglong2 pair(int i) const {
+      if (power > 0) return make_ulonglong2(at(i), at(i + 1));
+      return *reinterpret_cast<const ulonglong2*>(base + i);
     }
   };
   __device__ H bind(int g, int l, const CtxDev&) const {
@@ -305,30 +292,26 @@ struct InvSrcTensor {
     uint64_t* o0;
     size_t Ln;
     uint64_t q, qinv;
-    __device__ __forceinline__ void operator()(int i0, uint64_t (&x)[16]) const {
-#pragma unroll
-      for (int k = 0; k < 16; k += 2) {
-        const ulonglong2 va0 = *reinterpret_cast<const ulonglong2*>(a0 + i0 + k);
-        const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a0 + Ln + i0 + k);
-        const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b0 + i0 + k);
-        const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b0 + Ln + i0 + k);
-        ulonglong2 r0, r1;
-        r0.x = mont_mul(va0.x, vb0.x, q, qinv);
-        r0.y = mont_mul(va0.y, vb0.y, q, qinv);
-        uint64_t lo = 0, hi = 0;
-        mac128(lo, hi, va0.x, vb1.x);
-        mac128(lo, hi, va1.x, vb0.x);
-        r1.x = redc128(lo, hi, q, qinv);
-        lo = 0;
-        hi = 0;
-        mac128(lo, hi, va0.y, vb1.y);
-        mac128(lo, hi, va1.y, vb0.y);
-        r1.y = redc128(lo, hi, q, qinv);
-        x[k] = mont_mul(va1.x, vb1.x, q, qinv);
-        x[k + 1] = mont_mul(va1.y, vb1.y, q, qinv);
-        *reinterpret_cast<ulonglong2*>(o0 + i0 + k) = r0;
-        *reinterpret_cast<ulonglong2*>(o0 + Ln + i0 + k) = r1;
-      }
+    __device__ __forceinline__ ulonglong2 pair(int i) const {
+      const ulonglong2 va0 = *reinterpret_cast<const ulonglong2*>(a0 + i);
+      const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a0 + Ln + i);
+      const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b0 + i);
+      const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b0 + Ln + i);
+      ulonglong2 r0, r1;
+      r0.x = mont_mul(va0.x, vb0.x, q, qinv);
+      r0.y = mont_mul(va0.y, vb0.y, q, qinv);
+      uint64_t lo = 0, hi = 0;
+      mac128(lo, hi, va0.x, vb1.x);
+      mac128(lo, hi, va1.x, vb0.x);
+      r1.x = redc128(lo, hi, q, qinv);
+      lo = 0;
+      hi = 0;
+      mac128(lo, hi, va0.y, vb1.y);
+      mac128(lo, hi, va1.y, vb0.y);
+      r1.y = redc128(lo, hi, q, qinv);
+      *reinterpret_cast<ulonglong2*>(o0 + i) = r0;
+      *reinterpret_cast<ulonglong2*>(o0 + Ln + i) = r1;
+      return make_ulonglong2(mont_mul(va1.x, vb1.x, q, qinv), mont_mul(va1.y, vb1.y, q, qinv));
     }
   };
   __device__ H bind(int g, int l, const CtxDev& c) const {
@@ -562,8 +545,33 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
   const int row = tile * S::ROWS + sub;
   const int l = pm(g);
   const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
+  // Whole sub-rows come in warp by warp, 32 consecutive pairs per access,
+  // through shared memory (pair slots XOR-swizzled, as in k4_fwd_rows'
+  // epilogue); thread tid then takes elements 16 tid .. 16 tid + 15.
+  static_assert(C::T == 8 && (1 << S::B) == 128 && C::inv_clo(0) == 0,
+                "row prologue assumes 8 threads x 16 consecutive values per row");
+  ulonglong2* t2 = reinterpret_cast<ulonglong2*>(smem);
+  {
+    const auto h = src.bind(g, l, c);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int s2 = warp; s2 < S::ROWS; s2 += S::ROW_THREADS / 32) {
+      const int row2 = tile * S::ROWS + s2;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int pp = half * 32 + lane, tq = pp >> 3;
+        t2[s2 * 64 + tq * 8 + ((pp ^ tq) & 7)] = h.pair((row2 << S::B) + 2 * pp);
+      }
+    }
+  }
+  __syncthreads();
   uint64_t x[C::E];
-  src.bind(g, l, c)((row << S::B) | C::inv_in_idx(tid, 0), x);
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const ulonglong2 v = t2[sub * 64 + tid * 8 + ((p ^ tid) & 7)];
+    x[2 * p] = v.x;
+    x[2 * p + 1] = v.y;
+  }
+  __syncthreads();  // the tile is the transform's exchange space next
   C::inverse_m(x, tid, RowMap<S::B>{smem, sub}, c.tw_inv + ((size_t)l << LOG_N),
                S::N, 0, row, q, two_q);
   uint64_t* dst = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
