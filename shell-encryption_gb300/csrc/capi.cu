@@ -231,7 +231,8 @@ struct shg_key {
   uint64_t* kb = nullptr;  // [k][L][n], premultiplied by 2^64 mod q
   uint64_t* ka = nullptr;
   int need_lift = 0;
-  int chunk = 1;
+  int chunk = 1;       // digits per REDC for canonical digit transforms
+  int chunk_lazy = 1;  // the same for lazily reduced ones (below 31 q)
   size_t bytes = 0;
 };
 
@@ -842,6 +843,13 @@ int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
   key->k = (int)dd.size();
   key->chunk = (int)std::max<uint64_t>(
       1, std::min<uint64_t>((uint64_t)key->k, (~(uint64_t)0) / qmax));
+  // The fused row kernel keeps the digit transforms lazily reduced when every
+  // prime is below 2^58: values below 31 q (2 log n + 1 levels of growth), so
+  // a REDC of `chunk_lazy` products stays below q * 2^64.
+  key->chunk_lazy = (qmax >> 58) ? key->chunk
+                                 : (int)std::max<uint64_t>(
+                                       1, std::min<uint64_t>((uint64_t)key->k,
+                                                             (~(uint64_t)0) / (31 * qmax)));
   const size_t elems = (size_t)key->k * num_limbs * ctx->n;
   key->bytes = 2 * elems * sizeof(uint64_t) + dd.size() * sizeof(DigitDesc);
   cudaError_t e = cudaMalloc(&key->kb, elems * sizeof(uint64_t));
@@ -944,7 +952,7 @@ int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
                             CtMap::identity(), cc, L, s);
     shg::KeyTable kt;
     if (keys) kt = shg::KeyTable{table.kb + c0, table.ka + c0, 0};
-    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk,
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src,
                           (size_t)a.ncomp * Ln, CtMap::identity(), a.base1_zero,
                           a.subst_power, cc, L, s, kt);
@@ -1052,7 +1060,7 @@ int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* k
     shg::KeyTable kc;
     if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0};
     shg::launch_keyswitch(dv, side ? D1 : D0, X + (size_t)c0 * Ln, key->d_digits, k,
-                          key->need_lift, key->chunk, key->kb, key->ka, o, o,
+                          key->need_lift, key->chunk, key->chunk_lazy, key->kb, key->ka, o, o,
                           2 * Ln, CtMap::identity(), 0, 0, cc, L, side ? ctx->ks_side : s,
                           kc);
   }
@@ -1473,7 +1481,7 @@ int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_
       shg::KeyTable kt;
       if (tables) kt = shg::KeyTable{tables[j].kb + q0, tables[j].ka + q0, j};
       shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->need_lift,
-                            key->chunk, key->kb, key->ka, KS, blk, 2 * (size_t)n,
+                            key->chunk, key->chunk_lazy, key->kb, key->ka, KS, blk, 2 * (size_t)n,
                             map, 1, power, mc, 1, s, kt);
       shg::launch_expand_combine(dv, blk, KS, mono + (size_t)j * n, map, 1 << j,
                                  mc, s);
@@ -2410,7 +2418,7 @@ extern "C" int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key,
     const int cc = std::min(C, count - c0);
     const uint64_t* src = ct + (size_t)c0 * 3 * Ln;
     shg::launch_intt_export(dv, X, src, 3, 2, 0, CtMap::identity(), cc, L, s);
-    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk,
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src, 3 * Ln,
                           CtMap::identity(), 0, 0, cc, L, s);
   }

@@ -1043,6 +1043,7 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
 
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       const DigitDesc* digits, int k, int need_lift, int chunk,
+                      int chunk_lazy,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
                       int base1_zero, int subst_power, int count, int L,
@@ -1054,7 +1055,9 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
       launch4_digit_cols(c, D, X, digits, k, need_lift, count, L, s);
     }
     LaunchScope scope_("ks_rows", s);
-    launch4_ks_rows(c, D, k, chunk, kb, ka, out, base, base_ct_elems, map,
+    // small primes: the row kernel skips the final reduction (chunk_lazy)
+    launch4_ks_rows(c, D, k, c.small_q ? chunk_lazy : chunk, kb, ka, out, base,
+                    base_ct_elems, map,
                     base1_zero, subst_power, count, L, s, kt);
     return;
   }

@@ -174,6 +174,7 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
 // D: [count][k][L][n] scratch.
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       const DigitDesc* digits, int k, int need_lift, int chunk,
+                      int chunk_lazy,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
                       int base1_zero, int subst_power, int count, int L,

@@ -483,7 +483,10 @@ __global__ void __maxnreg__(72)
   C::template forward_m<LAZY>(x, tid, RowMap<S::B>{smem, sub},
                               c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
                               two_q);
-  finish_fwd<LAZY>(x, q, two_q, P->barrett);
+  // LAZY (every prime below 2^58): the digit values stay below 31 q, which
+  // the inner product's 128-bit sums and REDC take as they are (chunk_lazy
+  // digits per REDC); otherwise reduce to canonical first.
+  if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
   __syncthreads();  // every sub-row is done with its exchange tile
   {
     const RowMap<S::B> park{smem, sub};
