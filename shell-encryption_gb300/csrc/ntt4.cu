@@ -130,11 +130,13 @@ struct FwdSrcError {
 };
 
 // ---------------------------------------------------------------------------
-// Forward phase-2 sinks: the canonical values at i, i + 1 of transform g.
+// Forward phase-2 sinks: the values at i, i + 1 of transform g -- canonical,
+// or below 31 q (lazy, small primes) for sinks with kTakesLazy.
 // ---------------------------------------------------------------------------
 
 template <int LOG_N>
 struct FwdDstPlain {
+  static constexpr bool kTakesLazy = false;  // writes canonical residues
   uint64_t* p;
   struct H {
     uint64_t* base;
@@ -150,6 +152,9 @@ struct FwdDstPlain {
 // (rns/rns_polynomial.cc:314-323).
 template <int LOG_N>
 struct FwdDstModCombine {
+  // Shoup products take any 64-bit x, so lazily reduced values need no
+  // final reduction first.
+  static constexpr bool kTakesLazy = true;
   uint64_t* out;
   const uint64_t* in;
   int L;
@@ -190,6 +195,8 @@ struct FwdDstModCombine {
 // out [count][2][L][n], m [count][L][n], key [L][n], tm.v[i] = t (Montgomery).
 template <int LOG_N>
 struct FwdDstBgvEnc {
+  // REDC(x * t) needs x * t < q 2^64, true for lazily reduced x < 31 q.
+  static constexpr bool kTakesLazy = true;
   uint64_t* out;
   const uint64_t* m;
   const uint64_t* key;
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
   C::template forward_m<LAZY>(x, tid, RowMap<S::B>{smem, sub},
                               c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
                               two_q);
-  finish_fwd<LAZY>(x, q, two_q, P->barrett);
+  if constexpr (!(LAZY && Dst::kTakesLazy)) finish_fwd<LAZY>(x, q, two_q, P->barrett);
   // Thread tid holds elements 16 tid .. 16 tid + 15 of its sub-row.  They
   // go through shared memory (pair slots XOR-swizzled by tid, so neither
   // side has bank conflicts) and each warp then hands whole sub-rows to the
