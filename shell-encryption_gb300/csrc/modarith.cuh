@@ -76,14 +76,32 @@ __device__ __forceinline__ uint64_t redc128(uint64_t lo, uint64_t hi,
   return reduce_2q(r, q);
 }
 
-// 128-bit multiply-accumulate: (hi:lo) += a*b.
+// 128-bit multiply-accumulate: (hi:lo) += a*b (the caller keeps the sum
+// below 2^128).  The four 32x32 partial products go straight into the
+// accumulator's 32-bit limbs with three carry chains.
 __device__ __forceinline__ void mac128(uint64_t& lo, uint64_t& hi, uint64_t a,
                                        uint64_t b) {
-  uint64_t plo = a * b;
-  uint64_t phi = mulhi64(a, b);
-  uint64_t nlo = lo + plo;
-  hi += phi + (nlo < lo);
-  lo = nlo;
+  asm("{\n\t"
+      ".reg .u32 al, ah, bl, bh, c0, c1, c2, c3;\n\t"
+      "mov.b64 {al, ah}, %2;\n\t"
+      "mov.b64 {bl, bh}, %3;\n\t"
+      "mov.b64 {c0, c1}, %0;\n\t"
+      "mov.b64 {c2, c3}, %1;\n\t"
+      "mad.lo.cc.u32 c0, al, bl, c0;\n\t"
+      "madc.hi.cc.u32 c1, al, bl, c1;\n\t"
+      "madc.lo.cc.u32 c2, ah, bh, c2;\n\t"
+      "madc.hi.u32 c3, ah, bh, c3;\n\t"
+      "mad.lo.cc.u32 c1, al, bh, c1;\n\t"
+      "madc.hi.cc.u32 c2, al, bh, c2;\n\t"
+      "addc.u32 c3, c3, 0;\n\t"
+      "mad.lo.cc.u32 c1, ah, bl, c1;\n\t"
+      "madc.hi.cc.u32 c2, ah, bl, c2;\n\t"
+      "addc.u32 c3, c3, 0;\n\t"
+      "mov.b64 %0, {c0, c1};\n\t"
+      "mov.b64 %1, {c2, c3};\n\t"
+      "}"
+      : "+l"(lo), "+l"(hi)
+      : "l"(a), "l"(b));
 }
 
 // Inputs may be any value in [0, q] (SHELL's NegateInPlace maps 0 to q,
