@@ -30,8 +30,27 @@ struct PrimeDev {
 };
 static_assert(sizeof(PrimeDev) == 128, "PrimeDev is one cache line");
 
+// High 64 bits of a * b from the four 32x32 partial products on carry
+// chains (inline PTX).
 __device__ __forceinline__ uint64_t mulhi64(uint64_t a, uint64_t b) {
-  return __umul64hi(a, b);
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 al, ah, bl, bh, c1, c2, c3;\n\t"
+      "mov.b64 {al, ah}, %1;\n\t"
+      "mov.b64 {bl, bh}, %2;\n\t"
+      "mul.hi.u32 c1, al, bl;\n\t"
+      "mad.lo.cc.u32 c1, al, bh, c1;\n\t"
+      "madc.hi.u32 c2, al, bh, 0;\n\t"
+      "mad.lo.cc.u32 c1, ah, bl, c1;\n\t"
+      "madc.hi.cc.u32 c2, ah, bl, c2;\n\t"
+      "addc.u32 c3, 0, 0;\n\t"
+      "mad.lo.cc.u32 c2, ah, bh, c2;\n\t"
+      "madc.hi.u32 c3, ah, bh, c3;\n\t"
+      "mov.b64 %0, {c2, c3};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
 }
 
 // x * w mod q using the Shoup constant wp = floor(w * 2^64 / q).
