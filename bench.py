@@ -1421,6 +1421,10 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--max-wait-us", type=int, default=500)
     ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--host-piece", type=int, default=0,
+                    help="e2e host pipeline: ciphertexts per piece (0: library default)")
+    ap.add_argument("--host-slots", type=int, default=0,
+                    help="e2e host pipeline: staging slots in flight (0: library default)")
     ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
@@ -1493,6 +1497,9 @@ def main():
         sg.check(lib.shg_context_set_four_step_min(ctx.h, args.four_step_min))
     if args.ks_unfused:
         sg.check(lib.shg_context_set_ks_fused(ctx.h, 0))
+    if args.host_piece or args.host_slots:
+        sg.check(lib.shg_context_set_host_pipeline(ctx.h, args.host_piece or 128,
+                                                   args.host_slots or 4))
     k = 18
     kb = splitmix_limbs(1000 + rank, k, QS, n)
     ka = splitmix_limbs(2000 + rank, k, QS, n)

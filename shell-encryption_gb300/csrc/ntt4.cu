@@ -450,8 +450,9 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
 // (rns_relinearization_key.cc:219-226, rns_galois_key.cc:265-283,
 // relinearization_key.cc:76-96).  The CTA runs rows tile*R .. tile*R+R-1 of
 // the k digit transforms (sub-row r*k + j: row r, digit j; they share the
-// prime and the row, so they read the same twiddles), parks the canonical NTT
-// values in shared memory, and then each thread produces output slots:
+// prime and the row, so they read the same twiddles), parks the NTT values in
+// shared memory (canonical, or lazily reduced below 31 q when LAZY), and then
+// each thread produces output slots:
 //   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
 // with 128-bit lazy accumulation, one REDC per `chunk` digits.  The digit
 // transforms never go back to memory.  Arguments as in launch_ks_inner.
