@@ -23,6 +23,9 @@ Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,
        1125899887312897, 1125899886395393, 1125899885740033, 1125899885412353]
 Q59 = 576460752303415297
 Q60 = 1152921504606830593
+# The largest primes below 2^58 that are 1 mod 2^16: still "small" primes (lazily
+# reduced transforms), where a REDC covers only two lazy digit products.
+P58 = [288230376147582977, 288230376147386369, 288230376147320833]
 
 
 @pytest.fixture(scope="session")

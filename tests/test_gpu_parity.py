@@ -13,7 +13,7 @@ oblivious expansion (oblivious_expand_test.cc:219-259).
 import numpy as np
 import pytest
 
-from conftest import Q45, Q50, Q59, Q60
+from conftest import P58, Q45, Q50, Q59, Q60
 
 pytestmark = pytest.mark.gpu
 
@@ -315,6 +315,8 @@ KS_CASES = [
     (15, Q50[:2], [50, 16]),
     (14, Q45[:2], [2, 2]),          # 46 digits: one row per CTA, partial last warp
     (14, Q45[:2], [1, 1]),          # 90 digits: too many for one CTA, unfused path
+    (14, P58[:2], [10, 10]),        # primes just below 2^58: lazy digits, 2 per REDC
+    (11, P58[:2], [10, 10]),        # the same in the CTA-resident path
 ]
 
 
@@ -395,7 +397,8 @@ def test_relin_rejects_galois_key(sg, oracle):
 
 @pytest.mark.parametrize("log_n,qs,is_ntt", [(4, Q45[:2], 1), (12, Q50[:5], 1),
                                              (14, Q45, 1), (10, Q50[:4], 0), (14, Q45, 0),
-                                             (15, Q50[:3], 1), (15, Q50[:3], 0)])
+                                             (15, Q50[:3], 1), (15, Q50[:3], 0),
+                                             (14, P58, 1)])
 def test_modreduce_lsb(sg, oracle, log_n, qs, is_ntt):
     n, L, count, t = 1 << log_n, len(qs), 3, 65537
     x = oracle.uniform_limbs(70, qs, n, count)
@@ -742,6 +745,7 @@ def test_sample_uniform_error(sg, oracle, log_n, qs, variance, count):
     (14, Q45, 45, 13, 16),      # three transform chunks
     (14, Q45, 20, 15, 8),       # CTA-resident transforms, three chunks
     (15, Q50[:2], 2, 13, 0),
+    (14, P58[:2], 2, 13, 0),     # lazily reduced error transform just below 2^58
 ])
 def test_bgv_encrypt(sg, oracle, log_n, qs, count, four_step_min, chunk):
     """RnsRlweSecretKey::EncryptPolynomialBgv with on-device sampling,
