@@ -923,6 +923,30 @@ def test_bfv_mul_and_absorb(sg, oracle, log_n, qs, ps, count, chunk):
         assert np.array_equal(got[c], rns.bfv_absorb(L, aux, t, a[c], pt)), c
 
 
+def test_bfv_mul_below_top_level(sg, oracle):
+    """shg_bfv_mul / shg_bfv_absorb on a three-limb ciphertext of a four-prime
+    context (the CRT tables of every level are built), against the oracle's
+    general restatement."""
+    lib = sg.lib()
+    log_n, qs, ps, t, count = 13, Q45[:4], P45[:5], 65537, 2
+    n, Lm, K = 1 << log_n, 3, len(ps)
+    rns = oracle.Rns(log_n, qs + ps)
+    aux = list(range(len(qs), len(qs) + K))
+    a = oracle.uniform_limbs(990, qs[:Lm], n, 2 * count).reshape(count, 2, Lm, n)
+    b = oracle.uniform_limbs(991, qs[:Lm], n, 2 * count).reshape(count, 2, Lm, n)
+    pt = oracle.uniform_limbs(992, qs[:Lm], n).reshape(Lm, n)
+    ctx = sg.Context(log_n, qs, t, ps=ps)
+    da, db, dp = _dev(sg, a), _dev(sg, b), _dev(sg, pt)
+    out = sg.DeviceBuffer(count * 3 * Lm * n * 8)
+    _run(sg, lib.shg_bfv_mul, ctx.h, out.ptr, da.ptr, db.ptr, count, Lm, None)
+    got = out.download((count, 3, Lm, n))
+    for c in range(count):
+        assert np.array_equal(got[c], rns.bfv_mul(Lm, aux, t, a[c], b[c])), c
+    _run(sg, lib.shg_bfv_absorb, ctx.h, out.ptr, da.ptr, dp.ptr, 2, count, Lm, None)
+    got = out.download((count, 2, Lm, n))
+    assert np.array_equal(got[1], rns.bfv_absorb(Lm, aux, t, a[1], pt))
+
+
 def test_bfv_validation(sg):
     lib = sg.lib()
     ctx = sg.Context(10, Q45[:2], 65537)
