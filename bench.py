@@ -1600,19 +1600,6 @@ def main():
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
                "ms_per_step": e2e_ms / args.steps}
-        # The host link on its own: one step's copies back to back (H2D of
-        # both inputs, D2H of the result) with no compute, the floor under
-        # e2e's step time.
-        c0, c1 = ev(), ev()
-        sg.check(lib.shg_event_record(c0, s))
-        sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, B * ct_bytes, s))
-        sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, B * ct_bytes, s))
-        sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, B * ct_bytes, s))
-        sg.check(lib.shg_event_record(c1, s))
-        sg.check(lib.shg_stream_synchronize(s))
-        copy_ms = elapsed(c0, c1)
-        e2e["copies_alone_ms_per_step"] = copy_ms
-        e2e["host_link_gbs"] = 3 * B * ct_bytes / (copy_ms / 1e3) / 1e9
 
     # End to end in the wire format: host ciphertexts serialized as the
     # reference serializes them (log q-bit packed limbs), packed bytes over the
