@@ -164,6 +164,7 @@ struct shg_context {
   int K = 0;  // auxiliary primes (BFV basis extension), after the L main ones
   // Basis-conversion tables (BasisConv) by slot, see conv_slot(); K > 0 only.
   shg::BasisConv* d_conv = nullptr;
+  std::vector<uint8_t> conv_fast;  // per table: takes the specialised kernel
   uint64_t t = 0;
   int device = 0;
   std::vector<HostPrime> hp;
@@ -498,6 +499,11 @@ int shg_context_create_with_aux(int log_n, const uint64_t* qs, int num_qs, const
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess && num_ps > 0) {
     std::vector<shg::BasisConv> tables = make_conv_tables(ctx);
+    ctx->conv_fast.resize(tables.size());
+    for (size_t i = 0; i < tables.size(); ++i) {
+      const shg::BasisConv& b = tables[i];
+      ctx->conv_fast[i] = !b.balanced && b.ns >= 1 && b.ns <= 8 && b.chunk >= b.ns;
+    }
     e = cudaMalloc(&ctx->d_conv, sizeof(shg::BasisConv) * tables.size());
     if (e == cudaSuccess)
       e = cudaMemcpy(ctx->d_conv, tables.data(), sizeof(shg::BasisConv) * tables.size(),
@@ -2003,8 +2009,9 @@ static int check_aux(shg_context* ctx, int count, int num_limbs) {
   return SHG_OK;
 }
 
-static const shg::BasisConv* conv(const shg_context* ctx, int kind, int level, int balanced = 0) {
-  return ctx->d_conv + conv_slot(ctx, kind, level, balanced);
+static shg::ConvRef conv(const shg_context* ctx, int kind, int level, int balanced = 0) {
+  const int slot = conv_slot(ctx, kind, level, balanced);
+  return shg::ConvRef{ctx->d_conv + slot, ctx->conv_fast[slot]};
 }
 
 int shg_poly_switch_rns_basis(shg_context* ctx, uint64_t* out, const uint64_t* in,
@@ -2120,7 +2127,7 @@ int shg_poly_scale_reduce_rns_basis(shg_context* ctx, uint64_t* out, const uint6
   uint64_t* aux_c = ctx->ws;
   uint64_t* delta = ctx->ws + a_elems;
   const shg::CtxDev aux_view = ctx->aux_dev();
-  const shg::BasisConv* bc;
+  shg::ConvRef bc;
   if (t == ctx->t) {  // t folded into the conversion's source factor
     if (is_ntt_aux) shg::launch_ntt_inv(aux_view, aux, aux_c, count * K, K, 0, s);
     bc = conv(ctx, CONV_SWITCH_DOWN_T, l);

@@ -243,7 +243,15 @@ struct BasisConv {
 // out [count][nd][n] (member p at out + p * out_stride) <- the conversion of
 // in [count][ns][n] (coefficient form, member p at in + p * in_stride);
 // `primes` = the context's full prime array.
-void launch_switch_basis(const PrimeDev* primes, const BasisConv* bc, int ns, int nd,
+// A conversion table on the device; `fast` when it is unbalanced, has at
+// most 8 source limbs and needs one 128-bit accumulation per output value
+// (chunk >= ns), which a kernel specialised on the source count handles.
+struct ConvRef {
+  const BasisConv* bc;
+  int fast;
+};
+
+void launch_switch_basis(const PrimeDev* primes, ConvRef conv, int ns, int nd,
                          const uint64_t* in, size_t in_stride, uint64_t* out,
                          size_t out_stride, int count, int log_n, cudaStream_t s);
 

@@ -14,8 +14,8 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
-# Primes used across the tests (the reference's configs; SURVEY appendix B
-# values re-derived in tests/test_oracle.py).
+# Primes used across the tests (the reference's test parameters, re-derived in
+# tests/test_oracle.py).
 Q45 = [35184371138561, 35184370941953, 35184370352129, 35184370155521,
        35184369893377, 35184368877569]
 Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,

@@ -820,6 +820,10 @@ def test_sampling_validation(sg):
 P45 = [35184368320513, 35184368025601, 35184367828993, 35184367337473, 35184366911489,
        35184366551041, 35184366223361]
 P50 = [1125899884625921, 1125899884167169, 1125899884036097]
+# Primes just below 2^62 and 2^61 (1 mod 2^12): four 62-bit sources overflow
+# one 128-bit accumulation, so the conversion reduces twice per value.
+Q62 = [4611686018427322369, 4611686018427289601, 4611686018427277313, 4611686018427228161]
+P61 = [2305843009213616129, 2305843009213554689, 2305843009213501441]
 
 
 @pytest.mark.parametrize("log_n,qs,ps,level", [
@@ -827,6 +831,8 @@ P50 = [1125899884625921, 1125899884167169, 1125899884036097]
     (12, Q45, P45, 2),          # a lower level: main prefix q_0..q_2
     (13, Q50[:3], P50[:2], 2),
     (14, Q45, P45, 5),
+    (11, Q50[:10], P50, 9),     # ten source limbs
+    (11, Q62, P61, 3),          # 62-bit sources
 ])
 def test_switch_rns_basis(sg, oracle, log_n, qs, ps, level):
     """SwitchRnsBasis both ways, ScaleAndSwitchRnsBasis and ApproxSwitchRnsBasis
@@ -899,6 +905,7 @@ def test_switch_rns_basis_rounding_ties(sg, oracle):
     (11, [8589905921, 8589852673, 8589844481], [1073692673, 1073668097], 3, 0),
     (13, Q45[:4], P45[:5], 2, 0),
     (14, Q45, P45, 5, 2),       # three chunks
+    (15, Q50[:2], P50[:2], 1, 0),   # the largest ring
 ])
 def test_bfv_mul_and_absorb(sg, oracle, log_n, qs, ps, count, chunk):
     """RnsBfvCiphertext::operator* and AbsorbInPlace, bit-exact per ciphertext."""
@@ -961,3 +968,7 @@ def test_bfv_validation(sg):
         sg.check(lib.shg_poly_switch_rns_basis(ctx.h, buf.ptr, buf.ptr, 2, 2, 1, None))
     with pytest.raises(sg.ShgError, match="RNS moduli"):
         sg.check(lib.shg_bfv_mul(ctx.h, buf.ptr, buf.ptr, buf.ptr, 1, 3, None))
+    # empty batches are no-ops, like the reference's loops over zero ciphertexts
+    sg.check(lib.shg_bfv_mul(ctx.h, buf.ptr, buf.ptr, buf.ptr, 0, 2, None))
+    sg.check(lib.shg_bfv_absorb(ctx.h, buf.ptr, buf.ptr, buf.ptr, 2, 0, 2, None))
+    sg.check(lib.shg_poly_switch_rns_basis(ctx.h, buf.ptr, buf.ptr, 0, 2, 0, None))
