@@ -326,7 +326,7 @@ def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs, ks_fused):
     if log_n < 14 and not ks_fused:
         pytest.skip("the fused key-switch row phase exists for n >= 2^14 only")
     n, L = 1 << log_n, len(qs)
-    count = 2 if log_n < 14 else 1
+    count = 2
     rns = oracle.Rns(log_n, qs)
     k = rns.gadget_dim(log_bs)
     kb = oracle.uniform_limbs(50, qs, n, k)
@@ -347,6 +347,24 @@ def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs, ks_fused):
     out2 = sg.DeviceBuffer(want.nbytes)
     _run(sg, lib.shg_bgv_mul_relin, ctx.h, key.h, out2.ptr, da.ptr, db.ptr, count, None)
     assert np.array_equal(out2.download(want.shape), want)
+
+
+def test_relin_odd_batch(sg, oracle):
+    """Three ciphertexts at n = 2^14 through the fused key switch."""
+    log_n, qs, log_bs, count = 14, Q45[:3], [20] * 3, 3
+    n = 1 << log_n
+    rns = oracle.Rns(log_n, qs)
+    k = rns.gadget_dim(log_bs)
+    kb = oracle.uniform_limbs(53, qs, n, k)
+    ka = oracle.uniform_limbs(54, qs, n, k)
+    a, b = _ct_pair(oracle, qs, n, count, 55)
+    want = np.stack([rns.relin(rns.tensor(a[i], b[i]), kb, ka, log_bs) for i in range(count)])
+    ctx = sg.Context(log_n, qs)
+    key = sg.Key(ctx, log_bs, 1, kb, ka)
+    da, db = _dev(sg, a), _dev(sg, b)
+    out = sg.DeviceBuffer(want.nbytes)
+    _run(sg, sg.lib().shg_bgv_mul_relin, ctx.h, key.h, out.ptr, da.ptr, db.ptr, count, None)
+    assert np.array_equal(out.download(want.shape), want)
 
 
 @pytest.mark.parametrize("log_n,qs,log_bs,power", [
