@@ -54,9 +54,49 @@ __device__ __forceinline__ uint64_t mulhi64(uint64_t a, uint64_t b) {
 }
 
 // x * w mod q using the Shoup constant wp = floor(w * 2^64 / q).
-// Valid for any x < 2^64 and w < q; result in [0, 2q).
+// Valid for any x < 2^64 and w < q; result in [0, 2q).  One carry chain
+// forms Q = floor(x * wp / 2^64); then x * w + Q * (2^64 - q) mod 2^64 comes
+// from two widening multiply-adds for the low products and four 32-bit
+// multiply-adds into the high word, instead of two 64-bit products and a
+// 64-bit subtraction.
 __device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w,
                                                uint64_t wp, uint64_t q) {
+  const uint64_t nq = 0 - q;  // loop-invariant: the compiler hoists it
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 xl, xh, wl, wh, pl, ph, nl, nh, c1, c2, c3, rl, rh;\n\t"
+      ".reg .u64 t;\n\t"
+      "mov.b64 {xl, xh}, %1;\n\t"
+      "mov.b64 {wl, wh}, %2;\n\t"
+      "mov.b64 {pl, ph}, %3;\n\t"
+      "mov.b64 {nl, nh}, %4;\n\t"
+      "mul.hi.u32 c1, xl, pl;\n\t"
+      "mad.lo.cc.u32 c1, xl, ph, c1;\n\t"
+      "madc.hi.u32 c2, xl, ph, 0;\n\t"
+      "mad.lo.cc.u32 c1, xh, pl, c1;\n\t"
+      "madc.hi.cc.u32 c2, xh, pl, c2;\n\t"
+      "addc.u32 c3, 0, 0;\n\t"
+      "mad.lo.cc.u32 c2, xh, ph, c2;\n\t"
+      "madc.hi.u32 c3, xh, ph, c3;\n\t"
+      "mul.wide.u32 t, xl, wl;\n\t"
+      "mad.wide.u32 t, c2, nl, t;\n\t"
+      "mov.b64 {rl, rh}, t;\n\t"
+      "mad.lo.u32 rh, xl, wh, rh;\n\t"
+      "mad.lo.u32 rh, xh, wl, rh;\n\t"
+      "mad.lo.u32 rh, c2, nh, rh;\n\t"
+      "mad.lo.u32 rh, c3, nl, rh;\n\t"
+      "mov.b64 %0, {rl, rh};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(x), "l"(w), "l"(wp), "l"(nq));
+  return r;
+}
+
+// The same product from two 64-bit products and a subtraction: the compiler
+// schedules it with fewer live registers, which a kernel at a tight register
+// cap needs (the fused form keeps -q and all 32-bit halves live).
+__device__ __forceinline__ uint64_t shoup_lazy_split(uint64_t x, uint64_t w,
+                                                     uint64_t wp, uint64_t q) {
   return x * w - mulhi64(x, wp) * q;
 }
 

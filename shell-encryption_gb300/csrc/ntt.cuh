@@ -40,10 +40,11 @@ __device__ __forceinline__ Tw load_tw(const Tw* p) {
 }
 
 // Cooley-Tukey butterfly, inputs/outputs in [0, 4q).
+template <bool FUSED = true>
 __device__ __forceinline__ void bf_ct(uint64_t& X, uint64_t& Y, Tw w,
                                       uint64_t q, uint64_t two_q) {
   uint64_t x = X >= two_q ? X - two_q : X;
-  uint64_t t = shoup_lazy(Y, w.w, w.wp, q);
+  uint64_t t = FUSED ? shoup_lazy(Y, w.w, w.wp, q) : shoup_lazy_split(Y, w.w, w.wp, q);
   X = x + t;
   Y = x - t + two_q;
 }
@@ -52,9 +53,11 @@ __device__ __forceinline__ void bf_ct(uint64_t& X, uint64_t& Y, Tw w,
 // is below 2q for every 64-bit input, so each level grows the bound by 2q:
 // after the 14 levels of n = 2^14 values stay below 29q, which fits 64 bits
 // for q < 2^58 (the path's 45- and 50-bit primes); the final pass reduces.
+// FUSED picks shoup_lazy over shoup_lazy_split (same value).
+template <bool FUSED = true>
 __device__ __forceinline__ void bf_ct_lazy(uint64_t& X, uint64_t& Y, Tw w,
                                            uint64_t q, uint64_t two_q) {
-  uint64_t t = shoup_lazy(Y, w.w, w.wp, q);
+  uint64_t t = FUSED ? shoup_lazy(Y, w.w, w.wp, q) : shoup_lazy_split(Y, w.w, w.wp, q);
   uint64_t x = X;
   X = x + t;
   Y = x - t + two_q;
@@ -139,8 +142,9 @@ struct NttCore {
   // One forward pass on registers.  tw is the limb's psi_bitrev table; stage s
   // reads tw[tw_mult * 2^s + (i >> (b+1))] (tw_mult = 1 for a full transform;
   // 2 + h for half h of a 2n transform whose first level ran elsewhere).
-  // LAZY selects bf_ct_lazy (valid when q < 2^58, see above).
-  template <int p, bool LAZY>
+  // LAZY selects bf_ct_lazy (valid when q < 2^58, see above); FUSED the
+  // butterflies' Shoup product form.
+  template <int p, bool LAZY, bool FUSED = true>
   __device__ __forceinline__ static void fwd_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
                                                   int tw_mult, uint64_t q,
@@ -161,9 +165,9 @@ struct NttCore {
           constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
           constexpr int k1 = k0 | (1 << lb);
           if constexpr (LAZY) {
-            bf_ct_lazy(x[k0], x[k1], w, q, two_q);
+            bf_ct_lazy<FUSED>(x[k0], x[k1], w, q, two_q);
           } else {
-            bf_ct(x[k0], x[k1], w, q, two_q);
+            bf_ct<FUSED>(x[k0], x[k1], w, q, two_q);
           }
         });
       });
@@ -232,7 +236,7 @@ struct NttCore {
   // Full forward transform on registers (input in fwd_in layout, values in
   // [0, 4q) -- below q for LAZY; output in fwd_out layout, values in [0, 4q),
   // or below (2 LOG_N + 1) q for LAZY).
-  template <bool LAZY = false, class Map = SwzMap>
+  template <bool LAZY = false, bool FUSED = true, class Map = SwzMap>
   __device__ __forceinline__ static void forward_m(uint64_t (&x)[E], int tid,
                                                    const Map& m,
                                                    const Tw* __restrict__ tw,
@@ -240,7 +244,7 @@ struct NttCore {
                                                    uint64_t two_q) {
     static_for<0, P>([&](auto pp) {
       constexpr int p = decltype(pp)::value;
-      fwd_pass<p, LAZY>(x, tid, tw, tw_mult, q, two_q);
+      fwd_pass<p, LAZY, FUSED>(x, tid, tw, tw_mult, q, two_q);
       if constexpr (p + 1 < P) exchange(x, tid, m, fwd_clo(p), fwd_clo(p + 1));
     });
   }

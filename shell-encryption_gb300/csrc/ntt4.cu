@@ -488,9 +488,10 @@ __global__ void __maxnreg__(72)
   uint64_t x[C::E];
 #pragma unroll
   for (int e = 0; e < C::E; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
-  C::template forward_m<LAZY>(x, tid, RowMap<S::B>{smem, sub},
-                              c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
-                              two_q);
+  // the split Shoup product: the fused one spills at this register cap
+  C::template forward_m<LAZY, false>(x, tid, RowMap<S::B>{smem, sub},
+                                     c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
+                                     two_q);
   // LAZY (every prime below 2^58): the digit values stay below 31 q, which
   // the inner product's 128-bit sums and REDC take as they are (chunk_lazy
   // digits per REDC); otherwise reduce to canonical first.
