@@ -546,6 +546,98 @@ __global__ void __maxnreg__(72)
   }
 }
 
+// Sub-row tile of the 8-value row core: NttCore<7, 3>'s own swizzle (index
+// bits 3..6 XORed into bits 0..3) on each 128-element sub-row; a half-warp
+// is one sub-row, so every exchange and the parked reads are conflict-free.
+template <int B>
+struct RowMap8 {
+  uint64_t* sm;
+  int sub;
+  __device__ __forceinline__ uint64_t& operator()(int i) const {
+    return sm[(sub << B) + (i ^ ((i >> 3) & 15))];
+  }
+};
+
+// k4_ks_rows with 8 values per thread (16 threads per 128-element row, one
+// row of all k digits per CTA).  Half the register array of the 16-value
+// core: 56 registers, so four 288-thread CTAs (k = 18) share an SM, and the
+// butterflies keep the fused Shoup product.  The inner product takes one key
+// component of one coefficient per thread.  Requires k * 16 threads to be
+// whole warps (k even) and at most kKsRowsMaxThreads.
+template <int LOG_N, bool LAZY>
+__global__ void __maxnreg__(56)
+    k4_ks_rows8(const uint64_t* buf, int k, int chunk, const uint64_t* kb,
+                const uint64_t* ka, uint64_t* out, const uint64_t* base,
+                size_t base_ct_elems, CtMap map, int base1_zero, int subst_power,
+                int L, KeyTable kt, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = NttCore<S::B, 3>;
+  extern __shared__ uint64_t smem[];
+  constexpr int rows = 1 << S::A;
+  const int row = blockIdx.x % rows;
+  const int pl = blockIdx.x / rows;
+  const int l = pl % L;
+  const size_t p = (size_t)(pl / L);
+  if (kt.kb) {
+    kb = kt.kb[p >> kt.shift];
+    ka = kt.ka[p >> kt.shift];
+  }
+  const int j = threadIdx.x / C::T, tid = threadIdx.x % C::T;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const uint64_t* src =
+      buf + (((p * k + j) * L + l) << LOG_N) + ((size_t)row << S::B);
+  uint64_t x[C::E];
+#pragma unroll
+  for (int e = 0; e < C::E; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
+  C::template forward_m<LAZY>(x, tid, RowMap8<S::B>{smem, j},
+                              c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q, two_q);
+  // LAZY: the digit values stay below 31 q for the inner product (chunk_lazy)
+  if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
+  {
+    const RowMap8<S::B> park{smem, j};
+    const int i0 = C::fwd_out_idx(tid, 0);
+#pragma unroll
+    for (int e = 0; e < C::E; ++e) park(i0 + e) = x[e];
+  }
+  __syncthreads();
+  const size_t n = (size_t)1 << LOG_N, Ln = (size_t)L * n;
+  const uint64_t qinv = P->inv_modulus;
+  for (int o = threadIdx.x; o < (2 << S::B); o += blockDim.x) {
+    const int comp = o >> S::B, e = o & ((1 << S::B) - 1);
+    const int pos = (row << S::B) | e;
+    const size_t kr = (size_t)l * n + pos;
+    const uint64_t* d = smem + (e ^ ((e >> 3) & 15));
+    const uint64_t* pk = (comp ? ka : kb) + kr;
+    uint64_t acc = 0;
+    for (int j0 = 0; j0 < k; j0 += chunk) {
+      const int j1 = min(k, j0 + chunk);
+      uint64_t lo = 0, hi = 0;
+#pragma unroll 6
+      for (int jj = j0; jj < j1; ++jj) {
+        mac128(lo, hi, d[jj << S::B], __ldg(pk));
+        pk += Ln;
+      }
+      acc = add_mod(acc, redc128(lo, hi, q, qinv), q);
+    }
+    const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
+    uint64_t b;
+    if (comp == 0) {
+      int pos0 = pos;
+      if (subst_power > 0) {
+        const unsigned jb = __brev((unsigned)pos) >> (32 - LOG_N);
+        const unsigned t = ((unsigned)((subst_power - 1) >> 1) + jb * (unsigned)subst_power) &
+                           ((1u << LOG_N) - 1);
+        pos0 = (int)(__brev(t) >> (32 - LOG_N));
+      }
+      b = bp[pos0];
+    } else {
+      b = base1_zero ? 0 : bp[Ln + pos];
+    }
+    out[p * 2 * Ln + comp * Ln + kr] = add_mod(b, acc, q);
+  }
+}
+
 template <int LOG_N, class Src>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
     k4_inv_rows(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
@@ -746,6 +838,21 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
                      cudaStream_t s, const KeyTable& kt) {
+  if (k % 2 == 0 && k * 16 <= kKsRowsMaxThreads) {
+#define F(LN)                                                                   \
+  {                                                                             \
+    using S = Ntt4<LN>;                                                         \
+    auto kern = c.small_q ? k4_ks_rows8<LN, true> : k4_ks_rows8<LN, false>;     \
+    const int smem = k * (1 << S::B) * 8;                                       \
+    set_smem4(kern, smem);                                                      \
+    kern<<<count * L * (1 << S::A), k * 16, smem, s>>>(                         \
+        D, k, chunk, kb, ka, out, base, base_ct_elems, map, base1_zero,         \
+        subst_power, L, kt, c);                                                 \
+  }
+    SHG_DISPATCH4(c.log_n, F)
+#undef F
+    return;
+  }
   const int R = ks4_rows_per_cta(k);
 #define F(LN)                                                                   \
   {                                                                             \
