@@ -317,6 +317,8 @@ KS_CASES = [
     (14, Q45[:2], [1, 1]),          # 90 digits: too many for one CTA, unfused path
     (14, P58[:2], [10, 10]),        # primes just below 2^58: lazy digits, 2 per REDC
     (11, P58[:2], [10, 10]),        # the same in the CTA-resident path
+    (14, Q45[:4], [6] * 4),         # 32 digits: 512 threads, the 8-value row kernel's most
+    (14, [1152921504606584833, 1152921504598720513], [30, 30]),  # 60-bit: canonical digits
 ]
 
 
