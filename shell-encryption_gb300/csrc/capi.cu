@@ -233,7 +233,7 @@ struct shg_key {
   uint64_t* ka = nullptr;
   int need_lift = 0;
   int chunk = 1;       // digits per REDC for canonical digit transforms
-  int chunk_lazy = 1;  // the same for lazily reduced ones (below 31 q)
+  int chunk_lazy = 1;  // the same for lazily reduced ones (below 62 q)
   size_t bytes = 0;
 };
 
@@ -850,12 +850,13 @@ int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
   key->chunk = (int)std::max<uint64_t>(
       1, std::min<uint64_t>((uint64_t)key->k, (~(uint64_t)0) / qmax));
   // The fused row kernel keeps the digit transforms lazily reduced when every
-  // prime is below 2^58: values below 31 q (2 log n + 1 levels of growth), so
-  // a REDC of `chunk_lazy` products stays below q * 2^64.
+  // prime is below 2^58: values below 62 q (inputs below 2q, at most 4q of
+  // growth in each of up to 15 levels), so a REDC of `chunk_lazy` products
+  // stays below q * 2^64.
   key->chunk_lazy = (qmax >> 58) ? key->chunk
                                  : (int)std::max<uint64_t>(
                                        1, std::min<uint64_t>((uint64_t)key->k,
-                                                             (~(uint64_t)0) / (31 * qmax)));
+                                                             (~(uint64_t)0) / (62 * qmax)));
   const size_t elems = (size_t)key->k * num_limbs * ctx->n;
   key->bytes = 2 * elems * sizeof(uint64_t) + dd.size() * sizeof(DigitDesc);
   cudaError_t e = cudaMalloc(&key->kb, elems * sizeof(uint64_t));

@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   }
   C::template forward<LAZY>(x, tid, smem + sub * C::N,
                             c.tw_fwd + (size_t)j * C::N, 1, q, two_q);
-  // LAZY: D stays below 29 q; the key inner product takes it as it is.
+  // LAZY: D stays below 62 q; the key inner product takes it as it is.
   if constexpr (!LAZY) finish_forward<LAZY, C::E>(x, q, two_q, P->barrett);
   if (active) store_contig(D + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
 }
@@ -1063,7 +1063,7 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
     return;
   }
   // The digit transforms come out lazily reduced for small primes (below
-  // 31 q), which chunk_lazy covers; canonical ones are covered a fortiori.
+  // 62 q), which chunk_lazy covers; canonical ones are covered a fortiori.
   launch_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
   launch_ks_inner(c, out, D, kb, ka, k, c.small_q ? chunk_lazy : chunk, base, base_ct_elems,
                   map,

@@ -151,7 +151,7 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
                         int count, int L, cudaStream_t s);
 
 // Digit decomposition + forward NTT: D [count][k][L][n] (NTT values of the
-// plain digits: canonical, or below 31 q when every prime is below 2^58) from
+// plain digits: canonical, or below 62 q when every prime is below 2^58) from
 // X [count][L][n].
 void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
                       const DigitDesc* digits, int k, int need_lift, int count,

@@ -92,6 +92,46 @@ __device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w,
   return r;
 }
 
+// x * w mod q up to 4q, for the lazily reduced forward butterflies.  The
+// quotient keeps three of the four partial products of x * wp:
+//   Q' = xh * ph + hi32(xh * pl) + hi32(xl * ph)
+// (x = xh 2^32 + xl, wp = ph 2^32 + pl).  The dropped terms lo32(xh * pl),
+// lo32(xl * ph) and hi32(xl * pl) are each below 2^32, so together they carry
+// at most 2 into bit 64: floor(x * wp / 2^64) - 2 <= Q' <= floor(x * wp / 2^64),
+// and x * w - Q' q = (Shoup's remainder in [0, 2q)) + (0, 1 or 2) q lies in
+// [0, 4q).  Four multiplies fewer than shoup_lazy.
+__device__ __forceinline__ uint64_t shoup_lazy4(uint64_t x, uint64_t w,
+                                                uint64_t wp, uint64_t q) {
+  const uint64_t nq = 0 - q;
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 xl, xh, wl, wh, pl, ph, nl, nh, h1, h2, ql, qh, rl, rh;\n\t"
+      ".reg .u64 t, qq;\n\t"
+      "mov.b64 {xl, xh}, %1;\n\t"
+      "mov.b64 {wl, wh}, %2;\n\t"
+      "mov.b64 {pl, ph}, %3;\n\t"
+      "mov.b64 {nl, nh}, %4;\n\t"
+      "mul.hi.u32 h1, xh, pl;\n\t"
+      "mul.hi.u32 h2, xl, ph;\n\t"
+      "add.cc.u32 h1, h1, h2;\n\t"
+      "addc.u32 h2, 0, 0;\n\t"
+      "mov.b64 t, {h1, h2};\n\t"
+      "mad.wide.u32 qq, xh, ph, t;\n\t"
+      "mov.b64 {ql, qh}, qq;\n\t"
+      "mul.wide.u32 t, xl, wl;\n\t"
+      "mad.wide.u32 t, ql, nl, t;\n\t"
+      "mov.b64 {rl, rh}, t;\n\t"
+      "mad.lo.u32 rh, xl, wh, rh;\n\t"
+      "mad.lo.u32 rh, xh, wl, rh;\n\t"
+      "mad.lo.u32 rh, ql, nh, rh;\n\t"
+      "mad.lo.u32 rh, qh, nl, rh;\n\t"
+      "mov.b64 %0, {rl, rh};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(x), "l"(w), "l"(wp), "l"(nq));
+  return r;
+}
+
 // The same product from two 64-bit products and a subtraction: the compiler
 // schedules it with fewer live registers, which a kernel at a tight register
 // cap needs (the fused form keeps -q and all 32-bit halves live).

@@ -49,18 +49,26 @@ __device__ __forceinline__ void bf_ct(uint64_t& X, uint64_t& Y, Tw w,
   Y = x - t + two_q;
 }
 
-// Cooley-Tukey butterfly without any per-level reduction.  The Shoup product
-// is below 2q for every 64-bit input, so each level grows the bound by 2q:
-// after the 14 levels of n = 2^14 values stay below 29q, which fits 64 bits
-// for q < 2^58 (the path's 45- and 50-bit primes); the final pass reduces.
-// FUSED picks shoup_lazy over shoup_lazy_split (same value).
+// Cooley-Tukey butterfly without any per-level reduction.  FUSED: the Shoup
+// product with the three-term quotient (shoup_lazy4, below 4q for every 64-bit
+// input), Y' = X - t + 4q; otherwise the exact split product (below 2q),
+// Y' = X - t + 2q.  Either way a level grows the bound by at most 4q: inputs
+// below 2q stay below (4 log n + 2) q <= 62 q after the at most 15 levels of
+// n <= 2^15, which fits 64 bits for q < 2^58 (the path's 45- and 50-bit
+// primes); the final pass (or a sink that takes lazy values) reduces.
 template <bool FUSED = true>
 __device__ __forceinline__ void bf_ct_lazy(uint64_t& X, uint64_t& Y, Tw w,
                                            uint64_t q, uint64_t two_q) {
-  uint64_t t = FUSED ? shoup_lazy(Y, w.w, w.wp, q) : shoup_lazy_split(Y, w.w, w.wp, q);
   uint64_t x = X;
-  X = x + t;
-  Y = x - t + two_q;
+  if constexpr (FUSED) {
+    const uint64_t t = shoup_lazy4(Y, w.w, w.wp, q);
+    X = x + t;
+    Y = x - t + 2 * two_q;
+  } else {
+    const uint64_t t = shoup_lazy_split(Y, w.w, w.wp, q);
+    X = x + t;
+    Y = x - t + two_q;
+  }
 }
 
 // x mod q for any x < 2^64 with bar = floor(2^64 / q).
@@ -234,8 +242,8 @@ struct NttCore {
   }
 
   // Full forward transform on registers (input in fwd_in layout, values in
-  // [0, 4q) -- below q for LAZY; output in fwd_out layout, values in [0, 4q),
-  // or below (2 LOG_N + 1) q for LAZY).
+  // [0, 4q) -- below 2q for LAZY; output in fwd_out layout, values in [0, 4q),
+  // or below (4 LOG_N + 2) q for LAZY).
   template <bool LAZY = false, bool FUSED = true, class Map = SwzMap>
   __device__ __forceinline__ static void forward_m(uint64_t (&x)[E], int tid,
                                                    const Map& m,

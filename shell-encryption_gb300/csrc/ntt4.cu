@@ -131,7 +131,7 @@ struct FwdSrcError {
 
 // ---------------------------------------------------------------------------
 // Forward phase-2 sinks: the values at i, i + 1 of transform g -- canonical,
-// or below 31 q (lazy, small primes) for sinks with kTakesLazy.
+// or below 62 q (lazy, small primes) for sinks with kTakesLazy.
 // ---------------------------------------------------------------------------
 
 template <int LOG_N>
@@ -195,7 +195,7 @@ struct FwdDstModCombine {
 // out [count][2][L][n], m [count][L][n], key [L][n], tm.v[i] = t (Montgomery).
 template <int LOG_N>
 struct FwdDstBgvEnc {
-  // REDC(x * t) needs x * t < q 2^64, true for lazily reduced x < 31 q.
+  // REDC(x * t) needs x * t < q 2^64, true for lazily reduced x < 62 q (62 q < 2^64).
   static constexpr bool kTakesLazy = true;
   uint64_t* out;
   const uint64_t* m;
@@ -367,8 +367,11 @@ struct InvDstScale {
 // Phase kernels.
 // ---------------------------------------------------------------------------
 
+// Occupancy for at most 72 registers per thread (seven 128-thread CTAs at
+// n = 2^14): left to itself the compiler spends up to 128 on some sources.
 template <int LOG_N, bool LAZY, class Src>
-__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
+__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
+                                  65536 / (Ntt4<LOG_N>::COL_THREADS * 72))
     k4_fwd_cols(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
   using S = Ntt4<LOG_N>;
   using C = typename S::CC;
@@ -451,7 +454,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
 // relinearization_key.cc:76-96).  The CTA runs rows tile*R .. tile*R+R-1 of
 // the k digit transforms (sub-row r*k + j: row r, digit j; they share the
 // prime and the row, so they read the same twiddles), parks the NTT values in
-// shared memory (canonical, or lazily reduced below 31 q when LAZY), and then
+// shared memory (canonical, or lazily reduced below 62 q when LAZY), and then
 // each thread produces output slots:
 //   out0 = base0 + REDC(sum_j D_j * kb_j), out1 = base1 + REDC(sum_j D_j * ka_j)
 // with 128-bit lazy accumulation, one REDC per `chunk` digits.  The digit
@@ -492,7 +495,7 @@ __global__ void __maxnreg__(72)
   C::template forward_m<LAZY, false>(x, tid, RowMap<S::B>{smem, sub},
                                      c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q,
                                      two_q);
-  // LAZY (every prime below 2^58): the digit values stay below 31 q, which
+  // LAZY (every prime below 2^58): the digit values stay below 62 q, which
   // the inner product's 128-bit sums and REDC take as they are (chunk_lazy
   // digits per REDC); otherwise reduce to canonical first.
   if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
@@ -592,7 +595,7 @@ __global__ void __maxnreg__(56)
   for (int e = 0; e < C::E; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
   C::template forward_m<LAZY>(x, tid, RowMap8<S::B>{smem, j},
                               c.tw_fwd + ((size_t)l << LOG_N), (1 << S::A) + row, q, two_q);
-  // LAZY: the digit values stay below 31 q for the inner product (chunk_lazy)
+  // LAZY: the digit values stay below 62 q for the inner product (chunk_lazy)
   if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
   {
     const RowMap8<S::B> park{smem, j};

@@ -24,7 +24,7 @@ Q50 = [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,
 Q59 = 576460752303415297
 Q60 = 1152921504606830593
 # The largest primes below 2^58 that are 1 mod 2^16: still "small" primes (lazily
-# reduced transforms), where a REDC covers only two lazy digit products.
+# reduced transforms), where a REDC covers only one lazy digit product.
 P58 = [288230376147582977, 288230376147386369, 288230376147320833]
 
 
