@@ -9,6 +9,8 @@ limb in Python and check it against exact integer arithmetic, and check the
 growth bound (inputs below 2q, at most 4q per level, at most 15 levels: below
 62 q < 2^64) and the key-switch chunk rule (chunk_lazy = floor(2^64 / (62 q_max))
 products of a lazy digit and a key value stay below q * 2^64 for one REDC).
+The other inline-PTX arithmetic (mulhi64, mac128, the exact fused shoup_lazy)
+is restated the same way and checked against exact products.
 """
 import random
 
@@ -80,3 +82,66 @@ def test_chunk_lazy_keeps_redc_input_below_q_2_64(qs, k):
         assert chunk * (62 * q - 1) * (q - 1) < q << 64
     if qmax < 1 << 46:
         assert chunk == k                   # one REDC for all digits at 45-bit primes
+
+
+def mulhi64(a, b):
+    """csrc/modarith.cuh mulhi64: the four partial products on carry chains."""
+    al, ah, bl, bh = a & M32, a >> 32, b & M32, b >> 32
+    c1 = (al * bl) >> 32                                    # mul.hi.u32
+    s = c1 + ((al * bh) & M32); c1, cy = s & M32, s >> 32   # mad.lo.cc
+    c2 = (((al * bh) >> 32) + cy) & M32                     # madc.hi
+    s = c1 + ((ah * bl) & M32); c1, cy = s & M32, s >> 32   # mad.lo.cc
+    s = ((ah * bl) >> 32) + c2 + cy; c2, cy = s & M32, s >> 32  # madc.hi.cc
+    c3 = cy                                                 # addc
+    s = ((ah * bh) & M32) + c2; c2, cy = s & M32, s >> 32   # mad.lo.cc
+    c3 = (((ah * bh) >> 32) + c3 + cy) & M32                # madc.hi
+    return (c3 << 32) | c2
+
+
+def mac128(lo, hi, a, b):
+    """csrc/modarith.cuh mac128: (hi:lo) += a * b on three carry chains."""
+    al, ah, bl, bh = a & M32, a >> 32, b & M32, b >> 32
+    c = [lo & M32, lo >> 32, hi & M32, hi >> 32]
+    s = c[0] + ((al * bl) & M32); c[0], cy = s & M32, s >> 32
+    s = c[1] + ((al * bl) >> 32) + cy; c[1], cy = s & M32, s >> 32
+    s = c[2] + ((ah * bh) & M32) + cy; c[2], cy = s & M32, s >> 32
+    c[3] = (c[3] + ((ah * bh) >> 32) + cy) & M32
+    for x, y in ((al, bh), (ah, bl)):
+        s = c[1] + ((x * y) & M32); c[1], cy = s & M32, s >> 32
+        s = c[2] + ((x * y) >> 32) + cy; c[2], cy = s & M32, s >> 32
+        c[3] = (c[3] + cy) & M32
+    return (c[1] << 32) | c[0], (c[3] << 32) | c[2]
+
+
+def shoup_lazy(x, w, wp, q):
+    """csrc/modarith.cuh shoup_lazy: exact quotient, fused x w + Q (2^64 - q)."""
+    nq = (-q) & M64
+    Q = mulhi64(x, wp)
+    ql, qh = Q & M32, Q >> 32
+    xl, xh, wl, wh, nl, nh = x & M32, x >> 32, w & M32, w >> 32, nq & M32, nq >> 32
+    t = ((xl * wl) + ql * nl) & M64
+    rl, rh = t & M32, t >> 32
+    rh = (rh + xl * wh + xh * wl + ql * nh + qh * nl) & M32
+    return (rh << 32) | rl
+
+
+def test_carry_chain_products():
+    rng = random.Random(7)
+    for _ in range(20000):
+        a = rng.choice([rng.randrange(1 << 64), M64, 0, rng.randrange(1 << 45)])
+        b = rng.choice([rng.randrange(1 << 64), M64, 0, rng.randrange(1 << 45)])
+        assert mulhi64(a, b) == (a * b) >> 64
+        acc = rng.randrange(1 << 100)
+        lo, hi = mac128(acc & M64, acc >> 64, a, b)
+        assert (hi << 64) | lo == (acc + a * b) % (1 << 128)
+
+
+@pytest.mark.parametrize("q", PRIMES)
+def test_shoup_lazy_exact(q):
+    rng = random.Random(q + 1)
+    for _ in range(5000):
+        w = rng.randrange(q)
+        wp = (w << 64) // q
+        x = rng.choice([rng.randrange(1 << 64), M64, 0, rng.randrange(4 * q) & M64])
+        r = shoup_lazy(x, w, wp, q)
+        assert r == x * w - ((x * wp) >> 64) * q and r < 2 * q
