@@ -564,7 +564,8 @@ struct RowMap8 {
 // k4_ks_rows with 8 values per thread (16 threads per 128-element row, one
 // row of all k digits per CTA).  Half the register array of the 16-value
 // core: 56 registers, so four 288-thread CTAs (k = 18) share an SM, and the
-// butterflies keep the fused Shoup product.  The inner product takes one key
+// butterflies keep the fused PTX Shoup products (three-term quotient when
+// LAZY) without spilling.  The inner product takes one key
 // component of one coefficient per thread.  Requires k * 16 threads to be
 // whole warps (k even) and at most kKsRowsMaxThreads.
 template <int LOG_N, bool LAZY>
