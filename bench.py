@@ -42,8 +42,8 @@ UNIT = "ct-mult+relin/s"
 # captures of the same kernels (profiles/); None where not captured.
 TRAFFIC_PER_CT = {
     # profiles/ks_rows_ct_mult_relin_n14.md: one 16-ciphertext launch
-    "ks_rows": (303.7e6 + 22.1e6) / 16,
-    "digit_cols": (12.6e6 + 165.3e6) / 16,
+    "ks_rows": (303.1e6 + 22.2e6) / 16,
+    "digit_cols": (12.6e6 + 166.4e6) / 16,
 }
 # Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
 # step; the four-step key switch runs digit_cols + ks_rows, the unfused one
