@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
 
 // scale_mode: 0 -> x n^{-1}; 1 -> x n^{-1} 2^-64 (iNTT fused with ExportInt);
 // 2 -> x (sw, swp) given by the caller.
-template <int LOG_N>
+template <int LOG_N, bool WIDE>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_ntt_inv(const uint64_t* in, uint64_t* out, int num, int L, int in_first,
               int in_stride, int scale_mode, uint64_t sw, uint64_t swp,
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   const uint64_t q = P->q, two_q = P->two_q;
   uint64_t x[C::E];
   load_contig(x, in + src_limb * C::N + C::inv_in_idx(tid, 0));
-  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
+  C::template inverse<WIDE>(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
              two_q);
   if (scale_mode == 0) {
     sw = P->n_inv;
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
 // fused with ConvertToCoeffForm + ExportInt of the degree-2 component as
 // RnsRelinKey::ApplyToRlweCiphertext needs it (rns_relinearization_key.cc:
 // 215-218, rns_gadget.cc:130-134).  One CTA per (ciphertext, limb).
-template <int LOG_N>
+template <int LOG_N, bool WIDE>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_tensor_intt(uint64_t* out01, uint64_t* X, const uint64_t* a,
                   const uint64_t* b, int num, int L, CtxDev c) {
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
       *reinterpret_cast<ulonglong2*>(out01 + off + Ln + k) = r1;
     }
   }
-  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0,
+  C::template inverse<WIDE>(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0,
              q, two_q);
   if (active) {
     uint64_t* dst = X + (size_t)g * C::N;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
 // ConvertToCoeffForm + ExportInt of one component (optionally substituted
 // first), as the key-switch input (rns_galois_key.cc:257-263,
 // relinearization_key.cc:148-150).
-template <int LOG_N>
+template <int LOG_N, bool WIDE>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_intt_export(uint64_t* X, const uint64_t* ct, int ncomp, int comp,
                   int subst_power, CtMap map, int num, int L, CtxDev c) {
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   } else {
     load_contig(x, src + C::inv_in_idx(tid, 0));
   }
-  C::inverse(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
+  C::template inverse<WIDE>(x, tid, smem + sub * C::N, c.tw_inv + (size_t)l * C::N, C::N, 0, q,
              two_q);
   if (active) {
     uint64_t* dst = X + (size_t)g * C::N;
@@ -912,7 +912,7 @@ static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
   }
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_ntt_inv<LN>;                                                \
+    auto kern = c.small_q ? k_ntt_inv<LN, true> : k_ntt_inv<LN, false>;                                                \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         in, out, num, L, in_first, in_stride, mode, sw, swp, c);              \
@@ -968,7 +968,7 @@ void launch_tensor_intt(const CtxDev& c, uint64_t* out01, uint64_t* X,
   }
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_tensor_intt<LN>;                                            \
+    auto kern = c.small_q ? k_tensor_intt<LN, true> : k_tensor_intt<LN, false>;                                            \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         out01, X, a, b, num, L, c);                                           \
@@ -990,7 +990,7 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
   }
 #define F(LN)                                                                 \
   {                                                                           \
-    auto kern = k_intt_export<LN>;                                            \
+    auto kern = c.small_q ? k_intt_export<LN, true> : k_intt_export<LN, false>;                                            \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         X, ct, ncomp, comp, subst_power, map, num, L, c);                     \

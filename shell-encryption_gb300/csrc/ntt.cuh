@@ -77,14 +77,27 @@ __device__ __forceinline__ uint64_t reduce_full(uint64_t x, uint64_t q,
   return reduce_2q(x - mulhi64(x, bar) * q, q);
 }
 
-// Gentleman-Sande butterfly, inputs/outputs in [0, 2q).
+// Gentleman-Sande butterfly, inputs/outputs in [0, 2q) with the exact Shoup
+// product; WIDE (primes below 2^58, so 8q < 2^64): inputs/outputs in [0, 4q)
+// with the three-term quotient (shoup_lazy4, below 4q), the same one
+// conditional subtraction, of 4q.
+template <bool WIDE = false>
 __device__ __forceinline__ void bf_gs(uint64_t& X, uint64_t& Y, Tw w,
                                       uint64_t q, uint64_t two_q) {
-  uint64_t s = X + Y;
-  s = s >= two_q ? s - two_q : s;
-  uint64_t d = X - Y + two_q;
-  X = s;
-  Y = shoup_lazy(d, w.w, w.wp, q);
+  if constexpr (WIDE) {
+    const uint64_t four_q = 2 * two_q;
+    uint64_t s = X + Y;
+    s = s >= four_q ? s - four_q : s;
+    const uint64_t d = X - Y + four_q;
+    X = s;
+    Y = shoup_lazy4(d, w.w, w.wp, q);
+  } else {
+    uint64_t s = X + Y;
+    s = s >= two_q ? s - two_q : s;
+    uint64_t d = X - Y + two_q;
+    X = s;
+    Y = shoup_lazy(d, w.w, w.wp, q);
+  }
 }
 
 // Coefficients per thread: 16, or 32 at n = 2^14 (512 threads, so a thread
@@ -188,7 +201,7 @@ struct NttCore {
   // transform (bit_off = 0, row = 0), for row r of a transform whose low
   // LOG_N bits form the rows (bit_off = 0, row = r), and for the columns of
   // one whose low bit_off bits were done first (row = 0).
-  template <int p>
+  template <int p, bool WIDE = false>
   __device__ __forceinline__ static void inv_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
                                                   int nfull, int bit_off,
@@ -209,7 +222,7 @@ struct NttCore {
         static_for<0, (1 << lb)>([&](auto ll) {
           constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
           constexpr int k1 = k0 | (1 << lb);
-          bf_gs(x[k0], x[k1], w, q, two_q);
+          bf_gs<WIDE>(x[k0], x[k1], w, q, two_q);
         });
       });
     });
@@ -266,8 +279,10 @@ struct NttCore {
   }
 
   // Full inverse transform without the n^{-1} scaling (input in inv_in
-  // layout, values in [0, 2q); output in inv_out layout, values in [0, 2q)).
-  template <class Map = SwzMap>
+  // layout, values in [0, 2q); output in inv_out layout, values in [0, 2q);
+  // WIDE: [0, 4q) both, for primes below 2^58).  Every caller finishes with
+  // an exact Shoup product (the n^{-1} scaling), which takes any 64-bit value.
+  template <bool WIDE = false, class Map = SwzMap>
   __device__ __forceinline__ static void inverse_m(uint64_t (&x)[E], int tid,
                                                    const Map& m,
                                                    const Tw* __restrict__ tw,
@@ -276,16 +291,17 @@ struct NttCore {
                                                    uint64_t two_q) {
     static_for<0, P>([&](auto pp) {
       constexpr int p = decltype(pp)::value;
-      inv_pass<p>(x, tid, tw, nfull, bit_off, row, q, two_q);
+      inv_pass<p, WIDE>(x, tid, tw, nfull, bit_off, row, q, two_q);
       if constexpr (p + 1 < P) exchange(x, tid, m, inv_clo(p), inv_clo(p + 1));
     });
   }
+  template <bool WIDE = false>
   __device__ __forceinline__ static void inverse(uint64_t (&x)[E], int tid,
                                                  uint64_t* sm,
                                                  const Tw* __restrict__ tw,
                                                  int nfull, int row, uint64_t q,
                                                  uint64_t two_q) {
-    inverse_m(x, tid, SwzMap{sm}, tw, nfull, 0, row, q, two_q);
+    inverse_m<WIDE>(x, tid, SwzMap{sm}, tw, nfull, 0, row, q, two_q);
   }
 };
 

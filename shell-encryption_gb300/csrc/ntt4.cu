@@ -642,7 +642,7 @@ __global__ void __maxnreg__(56)
   }
 }
 
-template <int LOG_N, class Src>
+template <int LOG_N, bool WIDE, class Src>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
     k4_inv_rows(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
   using S = Ntt4<LOG_N>;
@@ -680,14 +680,14 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
     x[2 * p + 1] = v.y;
   }
   __syncthreads();  // the tile is the transform's exchange space next
-  C::inverse_m(x, tid, RowMap<S::B>{smem, sub}, c.tw_inv + ((size_t)l << LOG_N),
+  C::template inverse_m<WIDE>(x, tid, RowMap<S::B>{smem, sub}, c.tw_inv + ((size_t)l << LOG_N),
                S::N, 0, row, q, two_q);
   uint64_t* dst = buf + ((size_t)g << LOG_N) + ((size_t)row << S::B);
 #pragma unroll
   for (int k = 0; k < C::E; ++k) dst[C::inv_out_idx(tid, k)] = x[k];
 }
 
-template <int LOG_N, class Dst>
+template <int LOG_N, bool WIDE, class Dst>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
     k4_inv_cols(const uint64_t* buf, Dst dst, PrimeMap pm, CtxDev c) {
   using S = Ntt4<LOG_N>;
@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
   uint64_t x[C::E];
 #pragma unroll
   for (int k = 0; k < C::E; ++k) x[k] = src[(C::inv_in_idx(t, k) << S::B) | col];
-  C::inverse_m(x, t, typename C::ColMap{smem, S::COLS, j},
+  C::template inverse_m<WIDE>(x, t, typename C::ColMap{smem, S::COLS, j},
                c.tw_inv + ((size_t)l << LOG_N), S::N, S::B, 0, q, two_q);
   const auto h = dst.bind(g, l, c);
 #pragma unroll
@@ -746,8 +746,8 @@ template <int LOG_N, class Src, class Dst>
 void inv4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s) {
   using S = Ntt4<LOG_N>;
-  auto k1 = k4_inv_rows<LOG_N, Src>;
-  auto k2 = k4_inv_cols<LOG_N, Dst>;
+  auto k1 = c.small_q ? k4_inv_rows<LOG_N, true, Src> : k4_inv_rows<LOG_N, false, Src>;
+  auto k2 = c.small_q ? k4_inv_cols<LOG_N, true, Dst> : k4_inv_cols<LOG_N, false, Dst>;
   set_smem4(k1, S::ROW_SMEM);
   set_smem4(k2, S::COL_SMEM);
   k1<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(src, pm, buf, c);
