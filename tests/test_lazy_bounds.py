@@ -145,3 +145,22 @@ def test_shoup_lazy_exact(q):
         x = rng.choice([rng.randrange(1 << 64), M64, 0, rng.randrange(4 * q) & M64])
         r = shoup_lazy(x, w, wp, q)
         assert r == x * w - ((x * wp) >> 64) * q and r < 2 * q
+
+
+@pytest.mark.parametrize("q", [Q45[0], Q50[0], P58[0], (1 << 58) - 27])
+def test_wide_inverse_butterfly_invariant(q):
+    """bf_gs<WIDE> (csrc/ntt.cuh): inputs in [0, 4q) give outputs in [0, 4q)
+    that agree mod q with the exact Gentleman-Sande butterfly."""
+    assert 8 * q < 1 << 64
+    rng = random.Random(q + 2)
+    for _ in range(20000):
+        w = rng.randrange(q)
+        wp = (w << 64) // q
+        X = rng.choice([rng.randrange(4 * q), 4 * q - 1, 0])
+        Y = rng.choice([rng.randrange(4 * q), 4 * q - 1, 0])
+        s = X + Y
+        s = s - 4 * q if s >= 4 * q else s
+        d = X - Y + 4 * q
+        y, _ = shoup_lazy4(d, w, wp, q)
+        assert 0 <= s < 4 * q and 0 <= y < 4 * q
+        assert s % q == (X + Y) % q and y % q == (X - Y) * w % q
