@@ -108,6 +108,9 @@ def lib():
                                           U64P, ctypes.c_char_p, U64P]),
             "so_sym_encrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, U64P, U64P, U64P]),
             "so_sym_decrypt": (None, [vp, ctypes.c_uint64, U64P, U64P, ctypes.c_int, U64P]),
+            "so_sym_key_sample": (None, [vp, ctypes.c_int, ctypes.c_char_p, U64P]),
+            "so_sym_encrypt_prng": (None, [vp, ctypes.c_uint64, ctypes.c_int, U64P, U64P,
+                                           ctypes.c_char_p, U64P]),
             "so_compute_normalizer": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int]),
         }
         for name, (res, args) in sig.items():
@@ -277,6 +280,21 @@ class Prime:
         arrs = [np.ascontiguousarray(x, dtype=np.uint64) for x in (s, a, e, m)]
         out = np.empty((2, self.n), np.uint64)
         lib().so_sym_encrypt(self._h, ctypes.c_uint64(int(t)), *[_p(x) for x in arrs], _p(out))
+        return out
+
+    def sym_key_sample(self, variance, seed):
+        """SymmetricRlweKey::Sample from the ChaCha PRNG of the 32-byte seed."""
+        out = np.empty(self.n, np.uint64)
+        lib().so_sym_key_sample(self._h, variance, bytes(seed), _p(out))
+        return out
+
+    def sym_encrypt_prng(self, t, variance, s, m, seed):
+        """rlwe::Encrypt with the ChaCha PRNG of the 32-byte seed."""
+        s = np.ascontiguousarray(s, dtype=np.uint64)
+        m = np.ascontiguousarray(m, dtype=np.uint64)
+        out = np.empty((2, self.n), np.uint64)
+        lib().so_sym_encrypt_prng(self._h, ctypes.c_uint64(int(t)), variance, _p(s), _p(m),
+                                  bytes(seed), _p(out))
         return out
 
     def sym_decrypt(self, t, s, ct):

@@ -667,4 +667,105 @@ uint64_t ref_compute_normalizer(int k, int log_t) {
   return rlwe::ObliviousExpander<M>::ComputeNormalizer(k, log_t);
 }
 
+// The single-modulus symmetric flow (symmetric_encryption.h):
+//  - the key: SymmetricRlweKey::Sample(log_n, variance, log_t) drawing from
+//    SingleThreadChaChaPrng::Create(key_seed) (:634-649);
+//  - message i (integers msgs[i][n] in [0, t)): plaintext ConvertToNtt of its
+//    imported coefficients, then rlwe::Encrypt (:1006-1021) with the PRNG of
+//    seeds[32 i..]; a second PRNG of the same seed replays what Encrypt draws
+//    (SamplePolynomialFromPrng, then SampleFromErrorDistribution), giving the
+//    injected-randomness inputs a [count][n] (NTT) and e [count][n]
+//    (coefficient form) of internal::Encrypt (:940-963);
+//  - pairs (i, half + i), half = count / 2: ct + ct (:111), ct * ct (:408),
+//    and ct_i absorbing plaintext half + i (:214-226);
+//  - Decrypt (:1138-1152) of every ciphertext, sum and product.
+// Outputs (Montgomery representations, NTT form): s [n], pt [count][n],
+// ct [count][2][n], sum [half][2][n], prod [half][3][n], absorb
+// [half][2][n]; decryptions dec [count][n], dec_sum, dec_prod, dec_absorb
+// [half][n]; err [4] = Error() of ct 0, sum 0, prod 0, absorb 0.
+int ref_sym_c1(uint64_t q, int log_n, int log_t, int variance, const uint8_t* key_seed,
+               const uint8_t* seeds, const uint64_t* msgs, int count, uint64_t* s_out,
+               uint64_t* pt_out, uint64_t* a_out, uint64_t* e_out, uint64_t* ct_out,
+               uint64_t* sum_out, uint64_t* prod_out, uint64_t* absorb_out,
+               uint64_t* dec_out, uint64_t* dec_sum, uint64_t* dec_prod,
+               uint64_t* dec_absorb, double* err) {
+  Prime pr;
+  if (int st = make_prime(q, log_n, &pr)) return st;
+  const Params* params = pr.params.get();
+  const size_t n = (size_t)1 << log_n;
+  const int half = count / 2;
+  auto seed_str = [](const uint8_t* s) {
+    return std::string(reinterpret_cast<const char*>(s), 32);
+  };
+  auto key_prng = rlwe::SingleThreadChaChaPrng::Create(seed_str(key_seed));
+  if (!key_prng.ok()) return fail(key_prng.status());
+  auto key = rlwe::SymmetricRlweKey<M>::Sample(log_n, variance, log_t, params, &pr.ntt,
+                                               key_prng->get());
+  if (!key.ok()) return fail(key.status());
+  auto ep = rlwe::ErrorParams<M>::Create(log_t, variance, params, &pr.ntt);
+  if (!ep.ok()) return fail(ep.status());
+  from_vec(key->Key().Coeffs(), s_out);
+  std::vector<rlwe::Polynomial<M>> pts;
+  std::vector<rlwe::SymmetricRlweCiphertext<M>> cts;
+  for (int i = 0; i < count; ++i) {
+    std::vector<M> coeffs;
+    coeffs.reserve(n);
+    for (size_t j = 0; j < n; ++j) {
+      auto v = M::ImportInt(msgs[(size_t)i * n + j], params);
+      if (!v.ok()) return fail(v.status());
+      coeffs.push_back(*v);
+    }
+    pts.push_back(rlwe::Polynomial<M>::ConvertToNtt(std::move(coeffs), &pr.ntt, params));
+    from_vec(pts.back().Coeffs(), pt_out + (size_t)i * n);
+    auto replay = rlwe::SingleThreadChaChaPrng::Create(seed_str(seeds + 32 * (size_t)i));
+    if (!replay.ok()) return fail(replay.status());
+    auto a = rlwe::SamplePolynomialFromPrng<M>(n, replay->get(), params);
+    if (!a.ok()) return fail(a.status());
+    auto e = rlwe::SampleFromErrorDistribution<M>(n, variance, replay->get(), params);
+    if (!e.ok()) return fail(e.status());
+    from_vec(a->Coeffs(), a_out + (size_t)i * n);
+    from_vec(*e, e_out + (size_t)i * n);
+    auto prng = rlwe::SingleThreadChaChaPrng::Create(seed_str(seeds + 32 * (size_t)i));
+    if (!prng.ok()) return fail(prng.status());
+    auto ct = rlwe::Encrypt<M>(*key, pts.back(), &*ep, prng->get());
+    if (!ct.ok()) return fail(ct.status());
+    for (int c = 0; c < 2; ++c)
+      from_vec(ct->Component(c)->Coeffs(), ct_out + ((size_t)i * 2 + c) * n);
+    auto dec = rlwe::Decrypt<M>(*key, *ct);
+    if (!dec.ok()) return fail(dec.status());
+    std::copy(dec->begin(), dec->end(), dec_out + (size_t)i * n);
+    cts.push_back(std::move(*ct));
+  }
+  for (int i = 0; i < half; ++i) {
+    auto sum = cts[i] + cts[half + i];
+    if (!sum.ok()) return fail(sum.status());
+    auto prod = cts[i] * cts[half + i];
+    if (!prod.ok()) return fail(prod.status());
+    auto ab = cts[i] * pts[half + i];
+    if (!ab.ok()) return fail(ab.status());
+    for (int c = 0; c < 2; ++c) {
+      from_vec(sum->Component(c)->Coeffs(), sum_out + ((size_t)i * 2 + c) * n);
+      from_vec(ab->Component(c)->Coeffs(), absorb_out + ((size_t)i * 2 + c) * n);
+    }
+    for (int c = 0; c < 3; ++c)
+      from_vec(prod->Component(c)->Coeffs(), prod_out + ((size_t)i * 3 + c) * n);
+    auto d1 = rlwe::Decrypt<M>(*key, *sum);
+    auto d2 = rlwe::Decrypt<M>(*key, *prod);
+    auto d3 = rlwe::Decrypt<M>(*key, *ab);
+    if (!d1.ok()) return fail(d1.status());
+    if (!d2.ok()) return fail(d2.status());
+    if (!d3.ok()) return fail(d3.status());
+    std::copy(d1->begin(), d1->end(), dec_sum + (size_t)i * n);
+    std::copy(d2->begin(), d2->end(), dec_prod + (size_t)i * n);
+    std::copy(d3->begin(), d3->end(), dec_absorb + (size_t)i * n);
+    if (i == 0) {
+      err[0] = cts[0].Error();
+      err[1] = sum->Error();
+      err[2] = prod->Error();
+      err[3] = ab->Error();
+    }
+  }
+  return 0;
+}
+
 }  // extern "C"

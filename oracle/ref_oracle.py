@@ -69,6 +69,9 @@ def lib():
                                          _U64P, ctypes.c_int, _U64P, _U64P, _U64P, _U64P,
                                          ctypes.POINTER(ctypes.c_int)]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
+        L.ref_sym_c1.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_char_p, ctypes.c_char_p, _U64P, ctypes.c_int] + \
+            [_U64P] * 12 + [ctypes.POINTER(ctypes.c_double)]
         L.ref_compute_normalizer.argtypes = [ctypes.c_int, ctypes.c_int]
         _lib = L
     return _lib
@@ -295,3 +298,29 @@ def galois_compose(log_n, qs, log_bs, power, kb, ka, power2, kb2, ka2):
     _check(lib().ref_galois_compose(log_n, _p(q), len(q), lb, power, _p(kb), _p(ka), power2,
                                     _p(kb2), _p(ka2), _p(ob), _p(oa), ctypes.byref(pw)))
     return ob, oa, pw.value
+
+
+def sym_c1(q, log_n, log_t, variance, key_seed, seeds, msgs):
+    """The single-modulus symmetric flow of the reference (SymmetricRlweKey::
+    Sample, Encrypt, ct + ct, ct * ct, absorb, Decrypt) on `msgs`
+    [count][n] (integers in [0, t)); key from key_seed, ciphertext i from
+    seeds[i] (32 bytes each).  Returns a dict of the outputs (see
+    oracle/ref/ref_driver.cc ref_sym_c1)."""
+    msgs = np.ascontiguousarray(msgs, dtype=np.uint64)
+    count, n = msgs.shape
+    half = count // 2
+    o = {"s": np.empty(n, np.uint64), "pt": np.empty((count, n), np.uint64),
+         "a": np.empty((count, n), np.uint64), "e": np.empty((count, n), np.uint64),
+         "ct": np.empty((count, 2, n), np.uint64), "sum": np.empty((half, 2, n), np.uint64),
+         "prod": np.empty((half, 3, n), np.uint64), "absorb": np.empty((half, 2, n), np.uint64),
+         "dec": np.empty((count, n), np.uint64), "dec_sum": np.empty((half, n), np.uint64),
+         "dec_prod": np.empty((half, n), np.uint64),
+         "dec_absorb": np.empty((half, n), np.uint64)}
+    err = (ctypes.c_double * 4)()
+    names = ("s", "pt", "a", "e", "ct", "sum", "prod", "absorb", "dec", "dec_sum", "dec_prod",
+             "dec_absorb")
+    _check(lib().ref_sym_c1(q, log_n, log_t, variance, bytes(key_seed),
+                            b"".join(bytes(s) for s in seeds), _p(msgs), count,
+                            *[_p(o[k]) for k in names], err))
+    o["err"] = np.array(list(err), np.float64)
+    return o

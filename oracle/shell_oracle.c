@@ -864,6 +864,32 @@ static int popcount64(uint64_t x) {
   return c;
 }
 
+/* One coefficient of SampleFromErrorDistribution (sample_error.h:43-100):
+ * the centred binomial sum over 2 * variance bit pairs (64 pairs per two
+ * Rand64, 8 per two Rand8, the rest from two masked Rand8), mod q. */
+static uint64_t cbd_mod_q(const so_prime* p, int variance, const uint8_t seed[32],
+                          uint64_t* pos) {
+  uint64_t c = p->q;
+  int k = 2 * variance;
+  while (k > 0) {
+    if (k >= 64) {
+      c += popcount64(prng_rand64(seed, pos));
+      c -= popcount64(prng_rand64(seed, pos));
+      k -= 64;
+    } else if (k >= 8) {
+      c += popcount64(prng_rand8(seed, pos));
+      c -= popcount64(prng_rand8(seed, pos));
+      k -= 8;
+    } else {
+      const uint8_t m = (uint8_t)((1u << k) - 1);
+      c += popcount64(prng_rand8(seed, pos) & m);
+      c -= popcount64(prng_rand8(seed, pos) & m);
+      break;
+    }
+  }
+  return c >= p->q ? c - p->q : c;
+}
+
 /* RnsPolynomial::SampleUniform (rns/rns_polynomial.h:638-667): limb by limb,
  * each coefficient the first 8-byte candidate (Rand64, masked to log q bits)
  * below q (MontgomeryInt::ImportRandom, montgomery.h:261-272, 629-655); the
@@ -888,25 +914,7 @@ static void sample_uniform_error(const so_rns* r, int L, int variance, const uin
   }
   const so_prime* p0 = r->primes[0];
   for (size_t j = 0; j < n; j++) {
-    uint64_t c = p0->q;
-    int k = 2 * variance;
-    while (k > 0) {
-      if (k >= 64) {
-        c += popcount64(prng_rand64(seed, pos));
-        c -= popcount64(prng_rand64(seed, pos));
-        k -= 64;
-      } else if (k >= 8) {
-        c += popcount64(prng_rand8(seed, pos));
-        c -= popcount64(prng_rand8(seed, pos));
-        k -= 8;
-      } else {
-        const uint8_t m = (uint8_t)((1u << k) - 1);
-        c += popcount64(prng_rand8(seed, pos) & m);
-        c -= popcount64(prng_rand8(seed, pos) & m);
-        break;
-      }
-    }
-    if (c >= p0->q) c -= p0->q;
+    const uint64_t c = cbd_mod_q(p0, variance, seed, pos);
     /* ConvertModulusBalanced (modulus_conversion.h:30-157) of c (mod q0) */
     for (int l = 0; l < L; l++) {
       const so_prime* p = r->primes[l];
@@ -947,6 +955,41 @@ void so_rns_encrypt_bgv(const so_rns* r, int L, uint64_t t, int variance, const 
     so_neg(p, a + (size_t)l * n, out + P + (size_t)l * n, n);
   }
   free(a);
+}
+
+/* SymmetricRlweKey::Sample (symmetric_encryption.h:634-649): n error
+ * coefficients (SampleFromErrorDistribution) from the start of the PRNG
+ * stream of `seed`, imported and put in NTT form -> s [n]. */
+void so_sym_key_sample(const so_prime* p, int variance, const uint8_t seed[32], uint64_t* s) {
+  const size_t n = (size_t)p->n;
+  uint64_t pos = 0;
+  for (size_t j = 0; j < n; j++) s[j] = mont_import(p, cbd_mod_q(p, variance, seed, &pos));
+  so_ntt_fwd(p, s);
+}
+
+/* rlwe::Encrypt (symmetric_encryption.h:1006-1021) with the PRNG of `seed`:
+ * a = SamplePolynomialFromPrng (polynomial.h:361-381; ImportRandom per
+ * coefficient, taken as NTT-form values), then internal::Encrypt's error
+ * (SampleFromErrorDistribution), c0 = NTT(e) t + m + a s, c1 = -a.
+ * s, m [n] NTT form; out [2][n]. */
+void so_sym_encrypt_prng(const so_prime* p, uint64_t t, int variance, const uint64_t* s,
+                         const uint64_t* m, const uint8_t seed[32], uint64_t* out) {
+  const size_t n = (size_t)p->n;
+  uint64_t* a = (uint64_t*)malloc(n * sizeof(uint64_t));
+  uint64_t* e = (uint64_t*)malloc(n * sizeof(uint64_t));
+  uint64_t pos = 0;
+  const uint64_t mask = p->log_q >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << p->log_q) - 1);
+  for (size_t j = 0; j < n; j++) {
+    uint64_t v;
+    do {
+      v = prng_rand64(seed, &pos) & mask;
+    } while (v >= p->q);
+    a[j] = v;
+  }
+  for (size_t j = 0; j < n; j++) e[j] = mont_import(p, cbd_mod_q(p, variance, seed, &pos));
+  so_sym_encrypt(p, t, s, a, e, m, out);
+  free(a);
+  free(e);
 }
 
 /* MontgomeryInt::SerializeVector (montgomery.cc:142-166) through

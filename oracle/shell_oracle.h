@@ -149,6 +149,11 @@ void so_absorb_sum(const so_prime* p, int count, const uint64_t* cts,
  * and e (error, coefficient form): out [2][n] = (NTT(e)*t + m + a*s, -a). */
 void so_sym_encrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* a,
                     const uint64_t* e, const uint64_t* m, uint64_t* out);
+/* SymmetricRlweKey::Sample from the PRNG of seed: s [n] NTT form. */
+void so_sym_key_sample(const so_prime* p, int variance, const uint8_t seed[32], uint64_t* s);
+/* rlwe::Encrypt drawing a, then e, from the PRNG of seed: out [2][n]. */
+void so_sym_encrypt_prng(const so_prime* p, uint64_t t, int variance, const uint64_t* s,
+                         const uint64_t* m, const uint8_t seed[32], uint64_t* out);
 /* Decrypt a ciphertext of `len` components [len][n]: out [n] in [0, t). */
 void so_sym_decrypt(const so_prime* p, uint64_t t, const uint64_t* s, const uint64_t* ct,
                     int len, uint64_t* out);

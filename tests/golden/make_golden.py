@@ -143,6 +143,22 @@ def main():
         g[tag + "_m"] = m
         g[tag + "_seeds"] = np.frombuffer(b"".join(seeds), np.uint8).reshape(count, 32).copy()
         g[tag + "_out"] = R.encrypt_bgv(log_n, qs, t, var, key, m, seeds)
+    # Single-modulus symmetric RLWE (symmetric_encryption.h): SymmetricRlweKey::
+    # Sample, Encrypt (each ciphertext with its own ChaCha PRNG; a and e are the
+    # values Encrypt draws, replayed), ct + ct, ct * ct, absorb, Decrypt.
+    for log_n, q, log_t, var, count in [(7, Q59, 16, 8, 4), (5, Q60, 2, 1, 2)]:
+        tag = f"sym_{log_n}_{log_t}"
+        n, t = 1 << log_n, (1 << log_t) + 1
+        msgs = O.splitmix64(9900 + log_n, count * n).reshape(count, n) % np.uint64(t)
+        key_seed = bytes((i * 11 + log_n) % 256 for i in range(32))
+        seeds = [bytes((i * 17 + c * 3 + log_t) % 256 for i in range(32)) for c in range(count)]
+        o = R.sym_c1(q, log_n, log_t, var, key_seed, seeds, msgs)
+        g[tag + "_params"] = np.array([q, log_t, var], np.uint64)
+        g[tag + "_msgs"] = msgs
+        g[tag + "_key_seed"] = np.frombuffer(key_seed, np.uint8).copy()
+        g[tag + "_seeds"] = np.frombuffer(b"".join(seeds), np.uint8).reshape(count, 32).copy()
+        for nm, v in o.items():
+            g[f"{tag}_{nm}"] = v
     # RnsGaloisKey::Compose (rns/rns_galois_key.cc:349-406).
     for log_n, qs, log_bs, p1, p2 in [(7, Q45[:2], [20, 20], 5, 25), (9, Q50[:3], [50, 16, 20],
                                                                        3, 7)]:
@@ -241,6 +257,22 @@ def main():
     d["bfv_mul_n14_L6_K7"] = {"log_n": 14, "qs": qs, "ps": P45, "t": 65537, "count": 2,
                               "seeds": {"a": 7040, "b": 7041},
                               "out_sha256": digest(R.bfv_mul(14, qs, P45, 65537, a, b))}
+    # The symmetric flow at n = 2^12 with the 59-bit prime, t = 2^16 + 1,
+    # 64 messages (the key's PRNG seed is 32 bytes of 200, ciphertext c's
+    # 32 bytes of (7 c + 3) mod 256).
+    log_n, count = 12, 64
+    n = 1 << log_n
+    msgs = O.splitmix64(7050, count * n).reshape(count, n) % np.uint64(65537)
+    o = R.sym_c1(Q59, log_n, 16, 8, bytes([200] * 32),
+                 [bytes([(7 * c + 3) % 256] * 32) for c in range(count)], msgs)
+    ent = {"q": Q59, "log_n": log_n, "log_t": 16, "variance": 8, "count": count,
+           "msgs": "splitmix64(7050) mod 65537, [count][n]",
+           "prng_seeds": "key: 32 bytes of 200; ciphertext c: 32 bytes of (7c + 3) mod 256",
+           "error": [float(x) for x in o["err"]]}
+    for nm in ("s", "pt", "ct", "sum", "prod", "absorb", "dec", "dec_sum", "dec_prod",
+               "dec_absorb"):
+        ent[nm + "_sha256"] = digest(o[nm])
+    d["sym_c1_n12_x64"] = ent
     with open(os.path.join(HERE, "digests.json"), "w") as fh:
         json.dump(d, fh, indent=1)
     print("wrote", os.path.join(HERE, "reference_small.npz"), "and digests.json")

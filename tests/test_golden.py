@@ -653,3 +653,164 @@ def test_gpu_galois_compose_golden(sg, tag):
         assert np.array_equal(got_a, want_a)
     finally:
         lib.shg_key_destroy(h.value)
+
+
+# --------------------------------------------------------------------------
+# Single-modulus symmetric RLWE (symmetric_encryption.h): SymmetricRlweKey::
+# Sample, Encrypt with the ChaCha PRNG, ct + ct, ct * ct, absorb, Decrypt
+# --------------------------------------------------------------------------
+
+SYM_TAGS = sorted({k[:-len("_msgs")] for k in SMALL.files
+                   if k.startswith("sym_") and k.endswith("_msgs")})
+
+
+def _sym_case(tag):
+    q, log_t, var = (int(x) for x in SMALL[tag + "_params"])
+    log_n = int(tag.split("_")[1])
+    return q, log_n, (1 << log_t) + 1, var
+
+
+def _sym_ops(p, ct, pts):
+    """ct + ct, ct * ct and ct * pt of pairs (i, half + i), with the oracle's
+    pointwise ops (symmetric_encryption.h:111-146, 214-226, 408-445)."""
+    half = ct.shape[0] // 2
+    lo, hi = ct[:half], ct[half:]
+    s = np.stack([[p.add(lo[i, c], hi[i, c]) for c in range(2)] for i in range(half)])
+    pr = np.stack([[p.mul(lo[i, 0], hi[i, 0]),
+                    p.add(p.mul(lo[i, 0], hi[i, 1]), p.mul(lo[i, 1], hi[i, 0])),
+                    p.mul(lo[i, 1], hi[i, 1])] for i in range(half)])
+    ab = np.stack([[p.mul(lo[i, c], pts[half + i]) for c in range(2)] for i in range(half)])
+    return s, pr, ab
+
+
+@pytest.mark.parametrize("tag", SYM_TAGS)
+def test_oracle_symmetric_golden(oracle, tag):
+    """The C restatement of Sample / Encrypt / Decrypt and the ciphertext ops
+    against the reference's outputs."""
+    q, log_n, t, var = _sym_case(tag)
+    p = oracle.Prime(q, log_n)
+    s = p.sym_key_sample(var, SMALL[tag + "_key_seed"].tobytes())
+    assert np.array_equal(s, SMALL[tag + "_s"])
+    msgs, seeds = SMALL[tag + "_msgs"], SMALL[tag + "_seeds"]
+    pts = np.stack([p.ntt_fwd(p.import_(m)) for m in msgs])
+    assert np.array_equal(pts, SMALL[tag + "_pt"])
+    ct = np.stack([p.sym_encrypt_prng(t, var, s, pts[i], seeds[i].tobytes())
+                   for i in range(len(msgs))])
+    assert np.array_equal(ct, SMALL[tag + "_ct"])
+    inj = np.stack([p.sym_encrypt(t, s, SMALL[tag + "_a"][i], SMALL[tag + "_e"][i], pts[i])
+                    for i in range(len(msgs))])
+    assert np.array_equal(inj, SMALL[tag + "_ct"])
+    assert np.array_equal(np.stack([p.sym_decrypt(t, s, c) for c in ct]), SMALL[tag + "_dec"])
+    assert np.array_equal(SMALL[tag + "_dec"], msgs)
+    for nm, got in zip(("sum", "prod", "absorb"), _sym_ops(p, ct, pts)):
+        assert np.array_equal(got, SMALL[f"{tag}_{nm}"]), nm
+        dec = np.stack([p.sym_decrypt(t, s, c) for c in got])
+        assert np.array_equal(dec, SMALL[f"{tag}_dec_{nm}"]), nm
+
+
+def _sym_digest_inputs(oracle):
+    d = DIGESTS["sym_c1_n12_x64"]
+    n, count = 1 << d["log_n"], d["count"]
+    msgs = (oracle.splitmix64(7050, count * n).reshape(count, n) %
+            np.uint64((1 << d["log_t"]) + 1))
+    seeds = np.array([[(7 * c + 3) % 256] * 32 for c in range(count)], np.uint8)
+    p = oracle.Prime(d["q"], d["log_n"])
+    s = p.sym_key_sample(d["variance"], bytes([200] * 32))
+    return d, p, s, msgs, seeds
+
+
+def test_oracle_symmetric_full_size_digest(oracle):
+    """The C1 flow: 64 messages at n = 2^12, the 59-bit prime, t = 65537."""
+    d, p, s, msgs, seeds = _sym_digest_inputs(oracle)
+    t = (1 << d["log_t"]) + 1
+    assert digest(s) == d["s_sha256"]
+    pts = np.stack([p.ntt_fwd(p.import_(m)) for m in msgs])
+    assert digest(pts) == d["pt_sha256"]
+    ct = np.stack([p.sym_encrypt_prng(t, d["variance"], s, pts[i], seeds[i].tobytes())
+                   for i in range(d["count"])])
+    assert digest(ct) == d["ct_sha256"]
+    dec = np.stack([p.sym_decrypt(t, s, c) for c in ct])
+    assert digest(dec) == d["dec_sha256"] and np.array_equal(dec, msgs)
+    for nm, got in zip(("sum", "prod", "absorb"), _sym_ops(p, ct, pts)):
+        assert digest(got) == d[nm + "_sha256"], nm
+        assert digest(np.stack([p.sym_decrypt(t, s, c) for c in got])) == \
+            d[f"dec_{nm}_sha256"], nm
+
+
+def _gpu_sym_flow(sg, ctx, t, var, s, pts, seeds, msgs_len):
+    """The symmetric flow through the C ABI: device-sampled Encrypt
+    (shg_bgv_encrypt on the one-prime context: SamplePolynomialFromPrng and
+    SampleFromErrorDistribution draw as RnsPolynomial::SampleUniform and
+    SampleError do for one prime), ct + ct, ct * ct, absorb, Decrypt."""
+    lib = sg.lib()
+    count, n = pts.shape
+    half = count // 2
+    ds, dp = sg.DeviceBuffer.from_array(s), sg.DeviceBuffer.from_array(pts)
+    dseed = sg.DeviceBuffer.from_array(_seed_words(seeds))
+    ct = sg.DeviceBuffer(count * 2 * n * 8)
+    _run(sg, lib.shg_bgv_encrypt, ctx.h, ct.ptr, ds.ptr, dp.ptr, dseed.ptr, 1, count, var, None)
+    cts = ct.download((count, 2, n))
+    lo, hi = sg.DeviceBuffer.from_array(cts[:half]), sg.DeviceBuffer.from_array(cts[half:])
+    summ = sg.DeviceBuffer(half * 2 * n * 8)
+    _run(sg, lib.shg_poly_add, ctx.h, summ.ptr, lo.ptr, hi.ptr, 2 * half, 1, None)
+    prod = sg.DeviceBuffer(half * 3 * n * 8)
+    _run(sg, lib.shg_ct_tensor, ctx.h, prod.ptr, lo.ptr, hi.ptr, half, 1, None)
+    pt2 = sg.DeviceBuffer.from_array(np.repeat(pts[half:], 2, axis=0))
+    ab = sg.DeviceBuffer(half * 2 * n * 8)
+    _run(sg, lib.shg_poly_mul, ctx.h, ab.ptr, lo.ptr, pt2.ptr, 2 * half, 1, None)
+    out = {"ct": cts, "sum": summ.download((half, 2, n)), "prod": prod.download((half, 3, n)),
+           "absorb": ab.download((half, 2, n))}
+    dec = sg.DeviceBuffer(count * n * 8)
+    for nm, buf, ln, c in (("dec", ct, 2, count), ("dec_sum", summ, 2, half),
+                           ("dec_prod", prod, 3, half), ("dec_absorb", ab, 2, half)):
+        _run(sg, lib.shg_symmetric_decrypt, ctx.h, dec.ptr, ds.ptr, buf.ptr, ln, c, None)
+        out[nm] = dec.download((c, n))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", SYM_TAGS)
+def test_gpu_symmetric_golden(sg, oracle, tag):
+    """Device Encrypt (injected randomness and device-sampled), the
+    ciphertext ops and Decrypt against the reference's outputs."""
+    q, log_n, t, var = _sym_case(tag)
+    n = 1 << log_n
+    msgs = SMALL[tag + "_msgs"]
+    count = len(msgs)
+    ctx = sg.Context(log_n, [q], t)
+    s, pts = SMALL[tag + "_s"], SMALL[tag + "_pt"]
+    # the plaintexts' NTT on the device
+    dp = sg.DeviceBuffer.from_array(oracle.Prime(q, log_n).import_(msgs.reshape(-1))
+                                    .reshape(count, n))
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, dp.ptr, count, 1, None)
+    assert np.array_equal(dp.download((count, n)), pts)
+    # internal::Encrypt with the reference's own a and e
+    ds = sg.DeviceBuffer.from_array(s)
+    da, de = sg.DeviceBuffer.from_array(SMALL[tag + "_a"]), sg.DeviceBuffer.from_array(
+        SMALL[tag + "_e"])
+    ct = sg.DeviceBuffer(count * 2 * n * 8)
+    _run(sg, sg.lib().shg_symmetric_encrypt, ctx.h, ct.ptr, ds.ptr, da.ptr, de.ptr, dp.ptr,
+         count, None)
+    assert np.array_equal(ct.download((count, 2, n)), SMALL[tag + "_ct"])
+    got = _gpu_sym_flow(sg, ctx, t, var, s, pts, SMALL[tag + "_seeds"], count)
+    for nm, v in got.items():
+        assert np.array_equal(v, SMALL[f"{tag}_{nm}"]), nm
+
+
+@pytest.mark.gpu
+def test_gpu_symmetric_full_size_digest(sg, oracle):
+    """C1 on the device: 64 messages at n = 2^12, q = 576460752303415297,
+    t = 65537 -- Encrypt with on-device ChaCha sampling, ct + ct, ct * ct,
+    absorb, Decrypt, every output's digest equal to the reference's."""
+    d, p, s, msgs, seeds = _sym_digest_inputs(oracle)
+    assert digest(s) == d["s_sha256"]
+    n, count = 1 << d["log_n"], d["count"]
+    ctx = sg.Context(d["log_n"], [d["q"]], (1 << d["log_t"]) + 1)
+    dp = sg.DeviceBuffer.from_array(p.import_(msgs.reshape(-1)).reshape(count, n))
+    _run(sg, sg.lib().shg_ntt_forward, ctx.h, dp.ptr, count, 1, None)
+    pts = dp.download((count, n))
+    assert digest(pts) == d["pt_sha256"]
+    got = _gpu_sym_flow(sg, ctx, (1 << d["log_t"]) + 1, d["variance"], s, pts, seeds, count)
+    for nm, v in got.items():
+        assert digest(v) == d[nm + "_sha256"], nm
+    assert np.array_equal(got["dec"], msgs)
