@@ -39,9 +39,9 @@ LOG_BS = [20] * 6
 METRIC = "RNS ct-mult+relin/sec (batched vs plain, same GPU, bit-exact); p50/p99 ms"
 UNIT = "ct-mult+relin/s"
 # DRAM bytes (read + write) per ciphertext of each kernel scope, from ncu
-# captures of the same kernels (profiles/); None where not captured.
+# captures of the same kernels (dram__bytes_read.sum + dram__bytes_write.sum
+# of one 16-ciphertext launch); None where not captured.
 TRAFFIC_PER_CT = {
-    # profiles/ks_rows_ct_mult_relin_n14.md: one 16-ciphertext launch
     "ks_rows": (303.1e6 + 22.2e6) / 16,
     "digit_cols": (12.6e6 + 166.4e6) / 16,
 }
@@ -1401,6 +1401,54 @@ def run_bfv(args, world, rank, local, dist):
         lib.shg_host_free(hp)
 
 
+# Limb-NTT throughput (the path's forward / inverse transforms on their own):
+# 1024 polynomials of six limbs per call (inputs larger than L2 at every
+# size).  n = 2^12 and 2^14 use the workload's 45-bit primes (1 mod 2^15);
+# n = 2^15 needs primes that are 1 mod 2^16 and takes six 50-bit ones.
+NTT_CASES = ((12, QS, "six 45-bit primes"), (14, QS, "six 45-bit primes"),
+             (15, [1125899904679937, 1125899903827969, 1125899903500289, 1125899903107073,
+                   1125899902124033, 1125899901665281], "six 50-bit primes"))
+NTT_POLYS = 1024
+
+
+def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10):
+    """Forward and inverse limb-NTTs/s (shg_ntt_forward / shg_ntt_inverse in
+    place over NTT_POLYS x 6 limbs), with the HBM fraction at 16 n bytes per
+    limb-NTT (each limb read and written once) and the butterfly rate against
+    the integer ceiling."""
+    out = {}
+    for log_n, qs, primes in NTT_CASES:
+        n, L = 1 << log_n, len(qs)
+        ctx = sg.Context(log_n, qs)
+        buf = sg.DeviceBuffer(NTT_POLYS * L * n * 8)
+        sg.check(lib.shg_poly_fill_uniform(ctx.h, buf.ptr, NTT_POLYS, L, 99, s))
+        limbs = NTT_POLYS * L
+        rec = {"n": n, "primes": primes, "limb_ntts_per_call": limbs,
+               "bytes_per_limb_ntt": 16 * n, "butterflies_per_limb_ntt": n // 2 * log_n}
+        for name, fn in (("fwd", lib.shg_ntt_forward), ("inv", lib.shg_ntt_inverse)):
+            for _ in range(3):
+                sg.check(fn(ctx.h, buf.ptr, NTT_POLYS, L, s))
+            e0, e1 = ev(), ev()
+            sg.check(lib.shg_event_record(e0, s))
+            for _ in range(reps):
+                sg.check(fn(ctx.h, buf.ptr, NTT_POLYS, L, s))
+            sg.check(lib.shg_event_record(e1, s))
+            sg.check(lib.shg_stream_synchronize(s))
+            call_s = elapsed(e0, e1) / reps / 1e3
+            gbs = 16 * n * limbs / call_s / 1e9
+            bps = (n // 2 * log_n) * limbs / call_s
+            rec[name] = {"limb_ntts_per_s": limbs / call_s, "ms_per_call": call_s * 1e3,
+                         "achieved_gbs": gbs, "hbm_frac": gbs / peak,
+                         "butterflies_per_s": bps, "int_frac": bps / bfly_peak}
+        buf.free()
+        ctx.close()
+        out[f"n{n}"] = rec
+    out["unit"] = "limb-NTT/s"
+    out["peak_gbs"] = peak
+    out["peak_butterflies_per_s"] = bfly_peak
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1437,6 +1485,7 @@ def main():
     ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ntt", action="store_true", help="skip the limb-NTT throughput record")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
 
@@ -1721,6 +1770,8 @@ def main():
         "kernels": kernels,
     }
 
+    ntt = None if args.no_ntt else ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak.value)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -1746,7 +1797,8 @@ def main():
                   "path": "shg_ct_tensor + shg_relin_apply per ciphertext"},
         "batched_over_plain": value / world / plain_rate,
         "bit_exact_batched_vs_plain": bit_exact,
-        "e2e": e2e, "e2e_wire": e2e_wire, "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": e2e, "e2e_wire": e2e_wire, "roofline": roofline, "ntt": ntt,
+        "cpu_baseline": cpu,
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clk,
     }

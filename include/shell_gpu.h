@@ -210,9 +210,16 @@ int shg_relin_apply(shg_context* ctx, const shg_key* key, uint64_t* out,
  * 14.9 MiB); larger shapes return SHG_INVALID_ARGUMENT.  Batches larger than
  * the scratch are processed in chunks.  The first call on each device looks
  * up the array's device address (with that device current) and should come
- * before any stream capture.  All calls on a device share the one array, so
- * calls whose work overlaps on the GPU (different streams, or host threads)
- * race: serialize them on one stream. */
+ * before any stream capture; that first call may also be what loads the
+ * library's device image (the 32 MiB array included) onto the device, so
+ * make one warm-up call before entering a region where nothing may
+ * allocate.  The looked-up address is kept for the life of the process and
+ * is valid only until the device is reset (cudaDeviceReset, or the primary
+ * context torn down and created again); do not call this entry point after
+ * such a reset.  With the library's per-kernel profiling switched on
+ * (shg_profile_start) every launch creates CUDA events.  All calls on a
+ * device share the one array, so calls whose work overlaps on the GPU
+ * (different streams, or host threads) race: serialize them on one stream. */
 int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key, uint64_t* out,
                             const uint64_t* ct, int count, shg_stream stream);
 

@@ -667,6 +667,99 @@ uint64_t ref_compute_normalizer(int k, int log_t) {
   return rlwe::ObliviousExpander<M>::ComputeNormalizer(k, log_t);
 }
 
+// The error bookkeeping of the reference's RNS ciphertexts: the constants of
+// RnsErrorParams::Create(log_n, main moduli, {}, log_t, sigma)
+// (rns/rns_error_params.h) and Error() after each operation of
+// rns/rns_ciphertext.h, rns/rns_bgv_ciphertext.h and the key switches
+// (rns/rns_relinearization_key.h:158-164, rns/rns_galois_key.h), starting
+// from two degree-1 ciphertexts with errors e0 and e1 (zero data: the
+// bookkeeping does not read it).  out: [0..3] B_plaintext,
+// B_secretkey_encryption, B_publickey_encryption, B_scale;
+// [4] BoundOnGadgetBasedKeySwitching(1, max log_b, k); [5] ct0 + ct1;
+// [6] ct0 - ct1; [7] ct0 absorbing a plaintext; [8] ct0 absorbing `scalar`;
+// [9] ct0 += ct1 * plaintext (FusedAbsorbAddInPlace); [10] ct0 * ct1;
+// [11] the relinearized product; [12] ct0 after ModReduce;
+// [13] ct0.Substitute(power); [14] that substitution Galois key-switched.
+int ref_error_flow(int log_n, const uint64_t* qs, int L, const int* log_bs, int log_t,
+                   double sigma, double e0, double e1, uint64_t scalar, int power,
+                   double* out) {
+  int st;
+  auto ctx = make_ctx(log_n, qs, L, 65537, &st);
+  if (!ctx) return st;
+  const int n = 1 << log_n;
+  auto moduli = ctx->MainPrimeModuli();
+  auto ep = rlwe::RnsErrorParams<M>::Create(log_n, moduli, {}, log_t, sigma);
+  if (!ep.ok()) return fail(ep.status());
+  auto q_hats = ctx->MainPrimeModulusComplements(L - 1).value();
+  auto q_hat_invs = ctx->MainPrimeModulusCrtFactors(L - 1).value();
+  auto gadget = rlwe::RnsGadget<M>::Create(
+      log_n, std::vector<size_t>(log_bs, log_bs + L), q_hats, q_hat_invs, moduli);
+  if (!gadget.ok()) return fail(gadget.status());
+  const int k = gadget->Dimension();
+  std::vector<uint64_t> zeros((size_t)L * n, 0);
+  auto zero = [&] { return make_poly(zeros.data(), L, n, true); };
+  auto ct = [&](double e) {
+    std::vector<rlwe::RnsPolynomial<M>> c{zero(), zero()};
+    return rlwe::RnsBgvCiphertext<M>(std::move(c), moduli, 1, e, &*ep);
+  };
+  out[0] = ep->B_plaintext();
+  out[1] = ep->B_secretkey_encryption();
+  out[2] = ep->B_publickey_encryption();
+  out[3] = ep->B_scale();
+  out[4] = ep->BoundOnGadgetBasedKeySwitching(1, gadget->LogGadgetBase(), k);
+  auto c0 = ct(e0), c1 = ct(e1);
+  auto sum = c0 + c1;
+  if (!sum.ok()) return fail(sum.status());
+  out[5] = sum->Error();
+  auto diff = c0 - c1;
+  if (!diff.ok()) return fail(diff.status());
+  out[6] = diff->Error();
+  {
+    auto x = ct(e0);
+    if (absl::Status s = x.AbsorbInPlace(zero()); !s.ok()) return fail(s);
+    out[7] = x.Error();
+  }
+  {
+    auto x = ct(e0);
+    if (absl::Status s = x.AbsorbInPlace(scalar); !s.ok()) return fail(s);
+    out[8] = x.Error();
+  }
+  {
+    auto x = ct(e0);
+    if (absl::Status s = x.FusedAbsorbAddInPlace(c1, zero()); !s.ok()) return fail(s);
+    out[9] = x.Error();
+  }
+  auto prod = c0 * c1;
+  if (!prod.ok()) return fail(prod.status());
+  out[10] = prod->Error();
+  std::vector<rlwe::RnsPolynomial<M>> kas, kbs;
+  for (int j = 0; j < k; ++j) {
+    kbs.push_back(zero());
+    kas.push_back(zero());
+  }
+  rlwe::RnsRelinKey<M> relin(kas, kbs, &*gadget, /*degree=*/2, moduli, "",
+                             rlwe::PRNG_TYPE_HKDF);
+  auto r = relin.ApplyTo(*prod);
+  if (!r.ok()) return fail(r.status());
+  out[11] = r->Error();
+  {
+    auto x = ct(e0);
+    auto ql_inv = ctx->MainPrimeModulusInverseResidues()[L - 1].Prefix(L - 1);
+    if (absl::Status s = x.ModReduce(65537, ql_inv); !s.ok()) return fail(s);
+    out[12] = x.Error();
+  }
+  auto sub = c0.Substitute(power);
+  if (!sub.ok()) return fail(sub.status());
+  out[13] = sub->Error();
+  auto gk = rlwe::RnsGaloisKey<M>::CreateFromKeyComponents(
+      std::move(kas), std::move(kbs), power, &*gadget, moduli, "", rlwe::PRNG_TYPE_HKDF);
+  if (!gk.ok()) return fail(gk.status());
+  auto g = gk->ApplyTo(*sub);
+  if (!g.ok()) return fail(g.status());
+  out[14] = g->Error();
+  return 0;
+}
+
 // The single-modulus symmetric flow (symmetric_encryption.h):
 //  - the key: SymmetricRlweKey::Sample(log_n, variance, log_t) drawing from
 //    SingleThreadChaChaPrng::Create(key_seed) (:634-649);

@@ -69,6 +69,10 @@ def lib():
                                          _U64P, ctypes.c_int, _U64P, _U64P, _U64P, _U64P,
                                          ctypes.POINTER(ctypes.c_int)]
         L.ref_compute_normalizer.restype = ctypes.c_uint64
+        L.ref_error_flow.argtypes = [ctypes.c_int, _U64P, ctypes.c_int, _IP, ctypes.c_int,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_uint64, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_double)]
         L.ref_sym_c1.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_char_p, ctypes.c_char_p, _U64P, ctypes.c_int] + \
             [_U64P] * 12 + [ctypes.POINTER(ctypes.c_double)]
@@ -324,3 +328,21 @@ def sym_c1(q, log_n, log_t, variance, key_seed, seeds, msgs):
                             *[_p(o[k]) for k in names], err))
     o["err"] = np.array(list(err), np.float64)
     return o
+
+
+ERROR_FLOW_FIELDS = ("B_plaintext", "B_secretkey_encryption", "B_publickey_encryption",
+                     "B_scale", "gadget_key_switching_bound", "add", "sub", "absorb",
+                     "absorb_scalar", "fused_absorb_add", "mul", "relin", "mod_reduce",
+                     "substitute", "galois")
+
+
+def error_flow(log_n, qs, log_bs, log_t, sigma, e0, e1, scalar, power):
+    """Error() of the reference's RNS ciphertexts after each operation (see
+    ref_error_flow in oracle/ref/ref_driver.cc); a dict keyed by
+    ERROR_FLOW_FIELDS."""
+    q = _qs(qs)
+    lb = (ctypes.c_int * len(log_bs))(*log_bs)
+    out = (ctypes.c_double * len(ERROR_FLOW_FIELDS))()
+    _check(lib().ref_error_flow(log_n, _p(q), len(q), lb, log_t, sigma, e0, e1, scalar, power,
+                                out))
+    return dict(zip(ERROR_FLOW_FIELDS, list(out)))

@@ -24,7 +24,11 @@ struct CtxDev {
   const Tw* tw_fwd;           // [L][n]  plain psi^{brv(i)} + Shoup constant
   const Tw* tw_inv;           // [L][n]  plain psis_inv_bitrev + Shoup constant
   const uint64_t* qmod;       // [L][L]  q_i mod q_j (plain), row i
-  int small_q;                // every q < 2^58: forward NTTs skip per-level reductions
+  // Every q < 2^58: forward NTTs skip per-level reductions (values below 62 q)
+  // and inverse NTTs run the WIDE butterflies, whose outputs lie in [0, 4q).
+  // Every inverse consumer ends with an exact Shoup scaling (which takes any
+  // 64-bit value); one that stores inverse output without it must reduce it.
+  int small_q;
   int ntt4_min;               // log_n from which transforms use the four-step kernels
   int ks_fused;               // four-step key switch: digit row phase fused with the inner product
 };

@@ -281,7 +281,9 @@ struct NttCore {
   // Full inverse transform without the n^{-1} scaling (input in inv_in
   // layout, values in [0, 2q); output in inv_out layout, values in [0, 2q);
   // WIDE: [0, 4q) both, for primes below 2^58).  Every caller finishes with
-  // an exact Shoup product (the n^{-1} scaling), which takes any 64-bit value.
+  // an exact Shoup product (the n^{-1} scaling), which takes any 64-bit value;
+  // a caller that stores the output without that product must reduce it
+  // (below 4q with WIDE, below 2q otherwise).
   template <bool WIDE = false, class Map = SwzMap>
   __device__ __forceinline__ static void inverse_m(uint64_t (&x)[E], int tid,
                                                    const Map& m,

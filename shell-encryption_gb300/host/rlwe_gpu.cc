@@ -3,6 +3,8 @@
 // every numeric operation is a libshellgpu.so call.
 #include "rlwe_gpu.h"
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include <utility>
@@ -459,17 +461,92 @@ StatusOr<std::vector<RnsPolynomial>> RnsGadget::Decompose(const RnsPolynomial& a
   return xs;
 }
 
+int RnsGadget::LogGadgetBase() const {
+  return log_bs_.empty() ? 0 : *std::max_element(log_bs_.begin(), log_bs_.end());
+}
+
+// ---------------------------------------------------------------------------
+// RnsErrorParams (rns/rns_error_params.h).  Each bound keeps the reference's
+// formula and evaluation order, so the doubles are the same.
+// ---------------------------------------------------------------------------
+
+StatusOr<RnsErrorParams> RnsErrorParams::Create(int log_n, const Moduli& main_moduli,
+                                                const Moduli& aux_moduli,
+                                                int log_plaintext_modulus, double sigma) {
+  std::vector<uint64_t> qs, ps;
+  for (const PrimeModulus* m : main_moduli) qs.push_back(m->Modulus());
+  for (const PrimeModulus* m : aux_moduli) ps.push_back(m->Modulus());
+  return Create(log_n, qs, ps, log_plaintext_modulus, sigma);
+}
+
+StatusOr<RnsErrorParams> RnsErrorParams::Create(int log_n, const std::vector<uint64_t>& main_qs,
+                                                const std::vector<uint64_t>&,
+                                                int log_plaintext_modulus, double sigma) {
+  // rns/rns_error_params.h:46-62
+  if (log_n <= 0) return InvalidArgumentError("`log_n` must be positive.");
+  if (main_qs.empty()) return InvalidArgumentError("`main_moduli` must not be empty.");
+  if (log_plaintext_modulus <= 0)
+    return InvalidArgumentError("`log_plaintext_modulus` must be positive.");
+  if (sigma <= 0) return InvalidArgumentError("`sigma` must be positive.");
+  return RnsErrorParams(log_n, log_plaintext_modulus, sigma);
+}
+
+double RnsErrorParams::T2() const {
+  // The reference's ExportDoubleT(): log_plaintext_modulus squared.
+  return std::pow(log_t_, 2);
+}
+
+RnsErrorParams::RnsErrorParams(int log_n, int log_t, double sigma)
+    : log_n_(log_n), log_t_(log_t), sigma_(sigma) {
+  const int dimension = 1 << log_n;
+  // rns/rns_error_params.h:127-167
+  b_plaintext_ = T2() * std::sqrt(3.0 * dimension);
+  b_secretkey_encryption_ = T2() * std::sqrt(dimension) * (std::sqrt(3.0) + 6.0 * sigma);
+  b_publickey_encryption_ =
+      T2() * (std::sqrt(dimension) * (6 * sigma + std::sqrt(3)) + 72 * dimension * sigma * sigma);
+  b_scale_ = T2() * (std::sqrt(3.0 * dimension) + 8.0 * dimension * std::sqrt(1 / 3.0));
+}
+
+double RnsErrorParams::BoundOnGadgetBasedKeySwitching(int num_components, int log_gadget_base,
+                                                      int num_digits) const {
+  // rns/rns_error_params.h:84-91
+  const int gadget_base = 1 << log_gadget_base;
+  const int dimension = 1 << log_n_;
+  return (8.0 / std::sqrt(3.0)) * T2() * num_digits * sigma_ * dimension * gadget_base *
+         num_components;
+}
+
+namespace {
+
+// The additive error of a gadget key switch with `key` on `num_components`
+// components (rns/rns_relinearization_key.h:158-164, rns/rns_galois_key.h:
+// 284-290); zero without error parameters.
+double KeySwitchError(const RnsBgvCiphertext& ct, shg_key* key, int num_components) {
+  if (!ct.ErrorParams()) return 0.0;
+  int log_bs[64];
+  const int L = shg_key_num_limbs(key);
+  if (L <= 0 || L > 64 || shg_key_log_bs(key, log_bs, 64) != SHG_OK) return 0.0;
+  int max_log_b = 0;
+  for (int i = 0; i < L; ++i) max_log_b = std::max(max_log_b, log_bs[i]);
+  return ct.ErrorParams()->BoundOnGadgetBasedKeySwitching(num_components, max_log_b,
+                                                          shg_key_dimension(key));
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // RnsBgvCiphertext
 // ---------------------------------------------------------------------------
 
 RnsBgvCiphertext::RnsBgvCiphertext(std::vector<RnsPolynomial> components, Moduli moduli,
-                                   int power_of_s, double error)
+                                   int power_of_s, double error,
+                                   const RnsErrorParams* error_params)
     : len_(static_cast<int>(components.size())),
       log_n_(components.empty() ? 0 : components[0].LogN()),
       moduli_(std::move(moduli)),
       power_of_s_(power_of_s),
-      error_(error) {
+      error_(error),
+      error_params_(error_params) {
   const size_t elems = component_elems();
   data_ = DeviceArray(elems * len_);
   for (int i = 0; i < len_; ++i)
@@ -479,8 +556,10 @@ RnsBgvCiphertext::RnsBgvCiphertext(std::vector<RnsPolynomial> components, Moduli
 
 RnsBgvCiphertext RnsBgvCiphertext::FromDevice(DeviceArray data, int num_components,
                                               int log_n, Moduli moduli, int power_of_s,
-                                              double error) {
+                                              double error,
+                                              const RnsErrorParams* error_params) {
   RnsBgvCiphertext ct;
+  ct.error_params_ = error_params;
   ct.data_ = std::move(data);
   ct.len_ = num_components;
   ct.log_n_ = log_n;
@@ -557,6 +636,36 @@ Status RnsBgvCiphertext::AbsorbInPlace(const RnsPolynomial& plaintext) {
     RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_poly_mul(
         ContextOf(moduli_), data_.data() + i * elems, data_.data() + i * elems,
         plaintext.device_data(), 1, NumModuli(), g_stream)));
+  if (error_params_) error_ *= error_params_->B_plaintext();
+  return OkStatus();
+}
+
+Status RnsBgvCiphertext::AbsorbInPlace(uint64_t scalar) {
+  // rns/rns_ciphertext.h:267-274: every component times the integer.
+  RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_poly_mul_integer(ContextOf(moduli_), data_.data(),
+                                                         data_.data(), scalar, len_,
+                                                         NumModuli(), g_stream)));
+  // The scalar is represented as a value in [-scalar/2, scalar/2].
+  error_ *= static_cast<double>(scalar) / 2;
+  return OkStatus();
+}
+
+Status RnsBgvCiphertext::FusedAbsorbAddInPlace(const RnsBgvCiphertext& ctxt,
+                                               const RnsPolynomial& ptxt) {
+  // rns/rns_ciphertext.h:277-298
+  if (Degree() != ctxt.Degree()) return InvalidArgumentError("`ctxt` has a mismatched degree.");
+  if (Level() != ctxt.Level()) return InvalidArgumentError("`ctxt` has a mismatched level.");
+  if (PowerOfS() != ctxt.PowerOfS())
+    return InvalidArgumentError("`ctxt` has a mismatched key power.");
+  if (ptxt.NumModuli() != NumModuli())
+    return InvalidArgumentError("`ptxt` has a mismatched level.");
+  if (!ptxt.IsNttForm()) return InvalidArgumentError("RNS polynomial `b` must be in NTT form.");
+  const size_t elems = component_elems();
+  for (int i = 0; i < len_; ++i)
+    RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_poly_fma(
+        ContextOf(moduli_), data_.data() + i * elems, ctxt.data_.data() + i * elems,
+        ptxt.device_data(), 1, NumModuli(), g_stream)));
+  if (error_params_) error_ += ctxt.error_ * error_params_->B_plaintext();
   return OkStatus();
 }
 
@@ -589,7 +698,7 @@ StatusOr<RnsBgvCiphertext> RnsBgvCiphertext::operator*(const RnsBgvCiphertext& t
             that.data_.data() + j * elems, 1, NumModuli(), g_stream)));
   }
   return FromDevice(std::move(out), out_len, log_n_, moduli_, power_of_s_,
-                    error_ * that.error_);
+                    error_ * that.error_, error_params_);
 }
 
 Status RnsBgvCiphertext::ModReduce(uint64_t t, const std::vector<uint64_t>& ql_inv) {
@@ -621,7 +730,7 @@ StatusOr<RnsBgvCiphertext> RnsBgvCiphertext::Substitute(int substitution_power) 
       ContextOf(moduli_), out.data(), data_.data(), substitution_power, len_, NumModuli(),
       g_stream)));
   const int power = (int)(((int64_t)power_of_s_ * substitution_power) % (2 * NumCoeffs()));
-  return FromDevice(std::move(out), len_, log_n_, moduli_, power, error_);
+  return FromDevice(std::move(out), len_, log_n_, moduli_, power, error_, error_params_);
 }
 
 // ---------------------------------------------------------------------------
@@ -659,7 +768,7 @@ StatusOr<std::shared_ptr<shg_key>> MakeKey(const std::vector<RnsPolynomial>& bs,
   }
   shg_key* k = nullptr;
   RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_key_create(ContextOf(moduli), L,
-                                                   gadget->LogGadgetBase().data(), power,
+                                                   gadget->LogGadgetBases().data(), power,
                                                    hb.data(), ha.data(), &k)));
   return std::shared_ptr<shg_key>(k, [](shg_key* p) { shg_key_destroy(p); });
 }
@@ -692,7 +801,10 @@ StatusOr<RnsBgvCiphertext> RnsRelinKey::ApplyTo(const RnsBgvCiphertext& ct) cons
   RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_relin_apply(ContextOf(moduli_), key_.get(),
                                                     out.data(), ct.device_data(), 1,
                                                     g_stream)));
-  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
+  // ErrorAfterApplication (rns/rns_relinearization_key.h:158-164)
+  const double error = ct.Error() + KeySwitchError(ct, key_.get(), ct.Degree() - 1);
+  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, error,
+                                      ct.ErrorParams());
 }
 
 // ---------------------------------------------------------------------------
@@ -783,7 +895,10 @@ StatusOr<RnsBgvCiphertext> RnsGaloisKey::ApplyTo(const RnsBgvCiphertext& ct) con
   RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_galois_apply(ContextOf(moduli_), key_.get(),
                                                      out.data(), ct.device_data(), 1,
                                                      g_stream)));
-  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
+  // ErrorAfterApplication (rns/rns_galois_key.h:284-290)
+  const double error = ct.Error() + KeySwitchError(ct, key_.get(), 1);
+  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, error,
+                                      ct.ErrorParams());
 }
 
 StatusOr<DeviceArray> RnsGaloisKey::PackDigits(
@@ -831,7 +946,9 @@ StatusOr<RnsBgvCiphertext> RnsGaloisKey::ApplyToWithRandomPad(
   RLWE_GPU_RETURN_IF_ERROR(FromCode(shg_galois_apply_with_pad(
       ContextOf(moduli_), key_.get(), out.data(), ct.device_data(), pad.data(),
       ciphertext_pad_new.device_data(), 1, g_stream)));
-  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, ct.Error());
+  const double error = ct.Error() + KeySwitchError(ct, key_.get(), 1);
+  return RnsBgvCiphertext::FromDevice(std::move(out), 2, ct.LogN(), moduli_, 1, error,
+                                      ct.ErrorParams());
 }
 
 // ---------------------------------------------------------------------------

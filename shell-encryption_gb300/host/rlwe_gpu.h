@@ -273,7 +273,9 @@ class RnsGadget {
   static StatusOr<RnsGadget> Create(int log_n, std::vector<int> log_bs,
                                     const Moduli& moduli);
   int Dimension() const { return dimension_; }
-  const std::vector<int>& LogGadgetBase() const { return log_bs_; }
+  // The largest per-limb base exponent (rns/rns_gadget.h:91-94).
+  int LogGadgetBase() const;
+  const std::vector<int>& LogGadgetBases() const { return log_bs_; }
   // Decompose(a, moduli): k polynomials in coefficient form
   // (rns/rns_gadget.cc:108-153).
   StatusOr<std::vector<RnsPolynomial>> Decompose(const RnsPolynomial& a,
@@ -285,6 +287,42 @@ class RnsGadget {
   std::vector<int> log_bs_;
 };
 
+// rlwe::RnsErrorParams (rns/rns_error_params.h): the heuristic error bounds
+// that RNS ciphertexts carry, as host-side doubles with the reference's
+// constants and evaluation order (so Error() values equal the reference's).
+// The plaintext-modulus factor is the reference's ExportDoubleT(), the square
+// of log_plaintext_modulus.
+class RnsErrorParams {
+ public:
+  // RnsErrorParams::Create(log_n, main_moduli, aux_moduli,
+  // log_plaintext_modulus, sigma) (rns/rns_error_params.h:46-82), with the
+  // reference's status messages.
+  static StatusOr<RnsErrorParams> Create(int log_n, const Moduli& main_moduli,
+                                         const Moduli& aux_moduli, int log_plaintext_modulus,
+                                         double sigma);
+  // The same from the primes themselves (no device context needed).
+  static StatusOr<RnsErrorParams> Create(int log_n, const std::vector<uint64_t>& main_qs,
+                                         const std::vector<uint64_t>& aux_qs,
+                                         int log_plaintext_modulus, double sigma);
+  // Error added by a gadget key switch of `num_components` components
+  // (rns/rns_error_params.h:84-91).
+  double BoundOnGadgetBasedKeySwitching(int num_components, int log_gadget_base,
+                                        int num_digits) const;
+  double B_plaintext() const { return b_plaintext_; }
+  double B_secretkey_encryption() const { return b_secretkey_encryption_; }
+  double B_publickey_encryption() const { return b_publickey_encryption_; }
+  double B_scale() const { return b_scale_; }
+
+ private:
+  RnsErrorParams(int log_n, int log_t, double sigma);
+  double T2() const;
+  int log_n_ = 0;
+  int log_t_ = 0;
+  double sigma_ = 0;
+  double b_plaintext_ = 0, b_secretkey_encryption_ = 0, b_publickey_encryption_ = 0,
+         b_scale_ = 0;
+};
+
 // ---------------------------------------------------------------------------
 // RnsRlweCiphertext / RnsBgvCiphertext (rns/rns_ciphertext.h,
 // rns/rns_bgv_ciphertext.h).  Components are stored contiguously on the
@@ -293,10 +331,15 @@ class RnsGadget {
 
 class RnsBgvCiphertext {
  public:
+  // `error_params` (borrowed, may be null) drives the Error() bookkeeping of
+  // the operations below as in the reference; without it Error() changes
+  // only under +, -, * and the key switches' additive terms are skipped.
   RnsBgvCiphertext(std::vector<RnsPolynomial> components, Moduli moduli,
-                   int power_of_s, double error);
+                   int power_of_s, double error,
+                   const RnsErrorParams* error_params = nullptr);
   static RnsBgvCiphertext FromDevice(DeviceArray data, int num_components, int log_n,
-                                     Moduli moduli, int power_of_s, double error);
+                                     Moduli moduli, int power_of_s, double error,
+                                     const RnsErrorParams* error_params = nullptr);
 
   int Len() const { return len_; }
   int Degree() const { return len_ - 1; }
@@ -306,6 +349,8 @@ class RnsBgvCiphertext {
   int NumModuli() const { return static_cast<int>(moduli_.size()); }
   int PowerOfS() const { return power_of_s_; }
   double Error() const { return error_; }
+  void SetError(double error) { error_ = error; }
+  const RnsErrorParams* ErrorParams() const { return error_params_; }
   const Moduli& moduli() const { return moduli_; }
   StatusOr<RnsPolynomial> Component(int index) const;
 
@@ -314,8 +359,15 @@ class RnsBgvCiphertext {
   Status NegateInPlace();
   StatusOr<RnsBgvCiphertext> operator+(const RnsBgvCiphertext& that) const;
   StatusOr<RnsBgvCiphertext> operator-(const RnsBgvCiphertext& that) const;
-  // AbsorbInPlace(plaintext): every component times an NTT-form plaintext.
+  // AbsorbInPlace(plaintext): every component times an NTT-form plaintext;
+  // Error() times B_plaintext (rns/rns_ciphertext.h:208-214).
   Status AbsorbInPlace(const RnsPolynomial& plaintext);
+  // AbsorbInPlace(scalar): every component times the integer; Error() times
+  // scalar / 2 (rns/rns_ciphertext.h:267-274).
+  Status AbsorbInPlace(uint64_t scalar);
+  // FusedAbsorbAddInPlace(ctxt, ptxt): this += ctxt * ptxt; Error() plus
+  // ctxt.Error() * B_plaintext (rns/rns_ciphertext.h:277-298).
+  Status FusedAbsorbAddInPlace(const RnsBgvCiphertext& ctxt, const RnsPolynomial& ptxt);
   StatusOr<RnsBgvCiphertext> operator*(const RnsPolynomial& plaintext) const;
   // RnsRlweCiphertext::Mul (rns/rns_ciphertext.h:501-524).
   StatusOr<RnsBgvCiphertext> operator*(const RnsBgvCiphertext& that) const;
@@ -336,6 +388,7 @@ class RnsBgvCiphertext {
   Moduli moduli_;
   int power_of_s_ = 1;
   double error_ = 0;
+  const RnsErrorParams* error_params_ = nullptr;
 };
 using RnsRlweCiphertext = RnsBgvCiphertext;
 

@@ -589,9 +589,110 @@ void TestBfvAndCompose(int log_n, const std::vector<uint64_t>& qs,
   so_rns_destroy(r);
 }
 
+// Error() bookkeeping (rns/rns_ciphertext.h, rns/rns_bgv_ciphertext.h,
+// rns/rns_relinearization_key.h:158-164, rns/rns_galois_key.h:284-290)
+// against the reference's own values for the same parameters, read from
+// `path` (one parameter set: "log_n log_t sigma e0 e1 scalar power L q... lb...",
+// then "name value" lines; written by tests/test_host_api.py from the golden
+// fixture).
+void TestErrorBookkeeping(const char* path) {
+  FILE* f = std::fopen(path, "r");
+  EXPECT(f != nullptr, "error flow file");
+  if (!f) return;
+  int log_n, log_t, scalar, power, L;
+  double sigma, e0, e1;
+  if (std::fscanf(f, "%d %d %lf %lf %lf %d %d %d", &log_n, &log_t, &sigma, &e0, &e1, &scalar,
+                  &power, &L) != 8) {
+    EXPECT(false, "error flow header");
+    std::fclose(f);
+    return;
+  }
+  std::vector<uint64_t> qs(L);
+  std::vector<int> log_bs(L);
+  for (auto& q : qs) EXPECT(std::fscanf(f, "%llu", (unsigned long long*)&q) == 1, "q");
+  for (auto& b : log_bs) EXPECT(std::fscanf(f, "%d", &b) == 1, "log_b");
+  std::vector<std::pair<std::string, double>> want;
+  char name[64];
+  double v;
+  while (std::fscanf(f, "%63s %lf", name, &v) == 2) want.emplace_back(name, v);
+  std::fclose(f);
+  auto expect_value = [&](const std::string& key, double got) {
+    for (const auto& kv : want)
+      if (kv.first == key) {
+        ++g_checks;
+        if (kv.second != got) {
+          ++g_failures;
+          std::printf("FAIL error %s: got %.17g want %.17g\n", key.c_str(), got, kv.second);
+        }
+        return;
+      }
+    EXPECT(false, ("missing expected value " + key).c_str());
+  };
+  const int n = 1 << log_n;
+  std::unique_ptr<const RnsContext> ctx;
+  ASSERT_OK_AND_ASSIGN(ctx, RnsContext::Create(log_n, qs, {}, 65537));
+  const Moduli moduli = ctx->MainPrimeModuli();
+  RnsErrorParams ep = *RnsErrorParams::Create(log_n, moduli, {}, log_t, sigma);
+  RnsGadget gadget;
+  ASSERT_OK_AND_ASSIGN(gadget, RnsGadget::Create(log_n, log_bs, moduli));
+  const int k = gadget.Dimension();
+  expect_value("B_plaintext", ep.B_plaintext());
+  expect_value("B_secretkey_encryption", ep.B_secretkey_encryption());
+  expect_value("B_publickey_encryption", ep.B_publickey_encryption());
+  expect_value("B_scale", ep.B_scale());
+  expect_value("gadget_key_switching_bound",
+               ep.BoundOnGadgetBasedKeySwitching(1, gadget.LogGadgetBase(), k));
+  auto poly = [&](int seed) {
+    auto v = Uniform(seed, qs, n, 1);
+    return *RnsPolynomial::Create(Limbs(v.data(), L, n), true);
+  };
+  auto ct = [&](double e, int seed) {
+    return RnsBgvCiphertext({poly(seed), poly(seed + 1)}, moduli, 1, e, &ep);
+  };
+  RnsBgvCiphertext c0 = ct(e0, 900), c1 = ct(e1, 910);
+  expect_value("add", (*(c0 + c1)).Error());
+  expect_value("sub", (*(c0 - c1)).Error());
+  {
+    RnsBgvCiphertext x = ct(e0, 900);
+    EXPECT_OK(x.AbsorbInPlace(poly(920)));
+    expect_value("absorb", x.Error());
+  }
+  {
+    RnsBgvCiphertext x = ct(e0, 900);
+    EXPECT_OK(x.AbsorbInPlace((uint64_t)scalar));
+    expect_value("absorb_scalar", x.Error());
+  }
+  {
+    RnsBgvCiphertext x = ct(e0, 900);
+    EXPECT_OK(x.FusedAbsorbAddInPlace(c1, poly(920)));
+    expect_value("fused_absorb_add", x.Error());
+  }
+  RnsBgvCiphertext prod = *(c0 * c1);
+  expect_value("mul", prod.Error());
+  auto kb = Uniform(930, qs, n, k), ka = Uniform(940, qs, n, k);
+  std::vector<RnsPolynomial> key_bs, key_as;
+  for (int j = 0; j < k; ++j) {
+    key_bs.push_back(*RnsPolynomial::Create(Limbs(&kb[(size_t)j * L * n], L, n), true));
+    key_as.push_back(*RnsPolynomial::Create(Limbs(&ka[(size_t)j * L * n], L, n), true));
+  }
+  RnsRelinKey relin = *RnsRelinKey::CreateFromKeyComponents(key_bs, key_as, &gadget, moduli);
+  expect_value("relin", (*relin.ApplyTo(prod)).Error());
+  {
+    RnsBgvCiphertext x = ct(e0, 900);
+    EXPECT_OK(x.ModReduce(65537, *ctx->MainPrimeModulusInverseResidues(L - 1)));
+    expect_value("mod_reduce", x.Error());
+  }
+  RnsBgvCiphertext sub = *c0.Substitute(power);
+  expect_value("substitute", sub.Error());
+  RnsGaloisKey galois =
+      *RnsGaloisKey::CreateFromKeyComponents(key_as, key_bs, power, &gadget, moduli);
+  expect_value("galois", (*galois.ApplyTo(sub)).Error());
+}
+
 }  // namespace
 
-int main() {
+int main(int argc, char** argv) {
+  if (argc > 1) TestErrorBookkeeping(argv[1]);
   TestSymmetric();
   TestRnsSecretKey(10, {kQ45[0], kQ45[1]});
   TestRnsSecretKey(14, kQ45);

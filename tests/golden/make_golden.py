@@ -273,6 +273,16 @@ def main():
                "dec_absorb"):
         ent[nm + "_sha256"] = digest(o[nm])
     d["sym_c1_n12_x64"] = ent
+    # Error() bookkeeping of RNS ciphertexts (rns/rns_error_params.h and the
+    # ciphertext / key-switch operations), two parameter sets.
+    d["error_flow"] = []
+    for log_n, qs, log_bs, log_t, sigma, e0, e1, scalar, power in [
+            (10, Q45[:3], [20] * 3, 16, 3.19, 100.0, 250.0, 7, 5),
+            (14, Q45, [20] * 6, 2, 1.5, 12.5, 3.25, 65537, 3)]:
+        d["error_flow"].append({
+            "log_n": log_n, "qs": qs, "log_bs": log_bs, "log_t": log_t, "sigma": sigma,
+            "e0": e0, "e1": e1, "scalar": scalar, "power": power,
+            "values": R.error_flow(log_n, qs, log_bs, log_t, sigma, e0, e1, scalar, power)})
     with open(os.path.join(HERE, "digests.json"), "w") as fh:
         json.dump(d, fh, indent=1)
     print("wrote", os.path.join(HERE, "reference_small.npz"), "and digests.json")

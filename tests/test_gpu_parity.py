@@ -325,8 +325,9 @@ KS_CASES = [
 @pytest.mark.parametrize("ks_fused", [1, 0])
 @pytest.mark.parametrize("log_n,qs,log_bs", KS_CASES)
 def test_relin_plain_and_fused(sg, oracle, log_n, qs, log_bs, ks_fused):
-    if log_n < 14 and not ks_fused:
-        pytest.skip("the fused key-switch row phase exists for n >= 2^14 only")
+    if log_n < 13 and not ks_fused:
+        pytest.skip("below the four-step threshold (n < 2^13) the key switch has one path; "
+                    "ks_fused chooses between the four-step row kernels")
     n, L = 1 << log_n, len(qs)
     count = 2
     rns = oracle.Rns(log_n, qs)
@@ -374,8 +375,9 @@ def test_relin_odd_batch(sg, oracle):
     (13, Q50[:2], [50, 50], 8191), (14, Q45, [20] * 6, 5), (15, Q50[:2], [20, 20], 25)])
 @pytest.mark.parametrize("ks_fused", [1, 0])
 def test_galois_and_rotate(sg, oracle, log_n, qs, log_bs, power, ks_fused):
-    if log_n < 14 and not ks_fused:
-        pytest.skip("the fused key-switch row phase exists for n >= 2^14 only")
+    if log_n < 13 and not ks_fused:
+        pytest.skip("below the four-step threshold (n < 2^13) the key switch has one path; "
+                    "ks_fused chooses between the four-step row kernels")
     n, L, count = 1 << log_n, len(qs), 2
     rns = oracle.Rns(log_n, qs)
     k = rns.gadget_dim(log_bs)

@@ -26,13 +26,17 @@ def _inputs(oracle, qs, log_n, log_bs, count, seed):
     return kb, ka, ct3
 
 
-@pytest.mark.parametrize("log_n,qs,log_bs,count", [
-    (12, Q50[:4], [20] * 4, 3),
-    (14, Q45, [20] * 6, 3),   # 14.9 MiB per ciphertext: chunks of two
+@pytest.mark.parametrize("log_n,qs,log_bs,count,ks_fused", [
+    (12, Q50[:4], [20] * 4, 3, 1),
+    (14, Q45, [20] * 6, 3, 1),   # 14.9 MiB per ciphertext: chunks of two
+    (14, Q45, [20] * 6, 3, 0),   # the separate digit-NTT and inner-product kernels
+    # 60-bit primes: canonical digit transforms, one digit per REDC
+    (14, [1152921504606584833, 1152921504598720513], [30, 30], 2, 1),
 ])
-def test_noalloc_matches_relin_apply_twice(sg, oracle, log_n, qs, log_bs, count):
+def test_noalloc_matches_relin_apply_twice(sg, oracle, log_n, qs, log_bs, count, ks_fused):
     lib = sg.lib()
     ctx = sg.Context(log_n, qs)
+    sg.check(lib.shg_context_set_ks_fused(ctx.h, ks_fused))
     kb, ka, _ = _inputs(oracle, qs, log_n, log_bs, count, 300)
     key = sg.Key(ctx, log_bs, 1, kb, ka)
     shape = (count, 2, len(qs), 1 << log_n)
