@@ -1411,7 +1411,7 @@ NTT_CASES = ((12, QS, "six 45-bit primes"), (14, QS, "six 45-bit primes"),
 NTT_POLYS = 1024
 
 
-def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10):
+def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10, polys=NTT_POLYS):
     """Forward and inverse limb-NTTs/s (shg_ntt_forward / shg_ntt_inverse in
     place over NTT_POLYS x 6 limbs), with the HBM fraction at 16 n bytes per
     limb-NTT (each limb read and written once) and the butterfly rate against
@@ -1420,18 +1420,18 @@ def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10):
     for log_n, qs, primes in NTT_CASES:
         n, L = 1 << log_n, len(qs)
         ctx = sg.Context(log_n, qs)
-        buf = sg.DeviceBuffer(NTT_POLYS * L * n * 8)
-        sg.check(lib.shg_poly_fill_uniform(ctx.h, buf.ptr, NTT_POLYS, L, 99, s))
-        limbs = NTT_POLYS * L
+        buf = sg.DeviceBuffer(polys * L * n * 8)
+        sg.check(lib.shg_poly_fill_uniform(ctx.h, buf.ptr, polys, L, 99, s))
+        limbs = polys * L
         rec = {"n": n, "primes": primes, "limb_ntts_per_call": limbs,
                "bytes_per_limb_ntt": 16 * n, "butterflies_per_limb_ntt": n // 2 * log_n}
         for name, fn in (("fwd", lib.shg_ntt_forward), ("inv", lib.shg_ntt_inverse)):
             for _ in range(3):
-                sg.check(fn(ctx.h, buf.ptr, NTT_POLYS, L, s))
+                sg.check(fn(ctx.h, buf.ptr, polys, L, s))
             e0, e1 = ev(), ev()
             sg.check(lib.shg_event_record(e0, s))
             for _ in range(reps):
-                sg.check(fn(ctx.h, buf.ptr, NTT_POLYS, L, s))
+                sg.check(fn(ctx.h, buf.ptr, polys, L, s))
             sg.check(lib.shg_event_record(e1, s))
             sg.check(lib.shg_stream_synchronize(s))
             call_s = elapsed(e0, e1) / reps / 1e3
@@ -1447,6 +1447,42 @@ def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10):
     out["peak_gbs"] = peak
     out["peak_butterflies_per_s"] = bfly_peak
     return out
+
+
+def run_ntt(args, rank):
+    """--workload ntt: the limb-NTT record alone (forward and inverse
+    transforms at n = 2^12, 2^14, 2^15 over six primes)."""
+    import shell_gpu as sg
+    lib = sg.lib()
+    s = ctypes.c_void_p()
+    sg.check(lib.shg_stream_create(ctypes.byref(s)))
+    s = s.value
+
+    def ev():
+        e = ctypes.c_void_p()
+        sg.check(lib.shg_event_create(ctypes.byref(e)))
+        return e.value
+
+    def elapsed(a, b):
+        ms = ctypes.c_float()
+        sg.check(lib.shg_event_elapsed_ms(a, b, ctypes.byref(ms)))
+        return ms.value
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak = float(peaks["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        peak = 6800.0
+    bfly = ctypes.c_double()
+    sg.check(lib.shg_measure_butterfly_rate(ctypes.byref(bfly)))
+    rec = ntt_record(sg, lib, s, ev, elapsed, peak, bfly.value, reps=max(args.steps, 1),
+                     polys=args.ntt_polys)
+    n14 = rec["n16384"]["fwd"]
+    if rank == 0:
+        print(json.dumps({"metric": "limb-NTT/s (forward, n=2^14, six 45-bit primes)",
+                          "value": n14["limb_ntts_per_s"], "unit": "limb-NTT/s",
+                          "higher_is_better": True, "dtype": "u64", "data": "synthetic",
+                          "config": {"workload": f"{args.ntt_polys} polynomials x 6 limbs"},
+                          "ntt": rec}), flush=True)
 
 
 def main():
@@ -1476,20 +1512,33 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
-                    choices=["ct-mult-relin", "pir", "uneven", "serve", "encrypt", "bfv-mul"],
+                    choices=["ct-mult-relin", "pir", "uneven", "serve", "encrypt", "bfv-mul",
+                             "ntt"],
                     help="ct-mult-relin: RNS BGV ct x ct + relinearization (n=2^14, 6 primes); "
                          "pir: oblivious expansion + database absorb (n=2^12, one prime); "
                          "uneven: 4096 mixed instances through the batch executor; "
                          "encrypt: EncryptPolynomialBgv with on-device ChaCha sampling; "
-                         "bfv-mul: RnsBfvCiphertext ct x ct with basis extension")
+                         "bfv-mul: RnsBfvCiphertext ct x ct with basis extension; "
+                         "ntt: the forward / inverse limb-NTT record alone")
     ap.add_argument("--queries", type=int, default=PIR_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ntt", action="store_true", help="skip the limb-NTT throughput record")
+    ap.add_argument("--ntt-polys", type=int, default=NTT_POLYS,
+                    help="polynomials (of six limbs) per transform call in the NTT record")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
 
     world, rank, local, dist = dist_setup(args)
+    if args.workload == "ntt":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": "limb-NTT/s",
+                                  "unavailable": "timed only for the ct-mult-relin and pir "
+                                                 "workloads"}), flush=True)
+        else:
+            run_ntt(args, rank)
+        return
     if args.workload == "serve":
         if args.impl == "reference":
             if rank == 0:
@@ -1770,7 +1819,8 @@ def main():
         "kernels": kernels,
     }
 
-    ntt = None if args.no_ntt else ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak.value)
+    ntt = None if args.no_ntt else ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak.value,
+                                              polys=args.ntt_polys)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -69,9 +69,19 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n);
  * inner product as one kernel; 0: separate row phase, digit NTTs written to
  * scratch, then the inner product.  Results are identical. */
 int shg_context_set_ks_fused(shg_context* ctx, int on);
-/* Streams the chunks of a batched ct-mult+relin alternate over (2 = default:
- * the caller's stream and a second one, so one chunk fills the other's tail;
- * 1 = the caller's stream only, e.g. to time kernels one at a time). */
+/* Index checks of a debug build (no counterpart in the reference; the
+ * library compiled with SHG_DEBUG, see __graft_entry__.build_debug).  Debug
+ * kernels check computed indices before they address memory (substitution
+ * gathers, per-member key tables, gadget digit descriptors, limb indices);
+ * a failing check records its tag (1 substitution, 2 key table, 3 digit,
+ * 4 limb), the index is replaced by 0 so nothing faults, and the call goes
+ * on.  Reads and clears the current device's records: *first_failure = 0 when
+ * no check failed.  A release build always reports 0. */
+int shg_debug_status(unsigned* first_failure);
+/* Streams the chunks of a batched ct-mult+relin rotate over, 1 to 4 (2 =
+ * default: the caller's stream and a second one, so one chunk fills the
+ * other's tail; 1 = the caller's stream only, e.g. to time kernels one at a
+ * time).  Each lane holds its own chunk of digit scratch. */
 int shg_context_set_ks_lanes(shg_context* ctx, int lanes);
 /* shg_bgv_mul_relin_host pipeline shape: ciphertexts per piece (default 128)
  * and device staging slots in flight (default 4, at most 8). */

@@ -180,7 +180,7 @@ struct shg_context {
   int ntt4_min = 13;  // four-step transforms from this log_n up (measured faster
                       // for every operation from n = 2^13; mixed at 2^12)
   int ks_fused = 1;   // fused digit row phase + key inner product
-  int ks_lanes = 2;      // streams the batched key-switch chunks alternate over
+  int ks_lanes = 2;      // streams the batched key-switch chunks rotate over (1..4)
   int host_piece = 128;  // host pipeline: ciphertexts per piece
   int host_slots = 4;    // host pipeline: device staging slots in flight
   std::mutex mu;
@@ -190,8 +190,10 @@ struct shg_context {
   cudaStream_t io_streams[4] = {nullptr, nullptr, nullptr, nullptr};
   // Second stream of the batched key switch (chunks alternate between the
   // caller's stream and this one) with its fork / join events.
-  cudaStream_t ks_side = nullptr;
-  cudaEvent_t ks_fork = nullptr, ks_join = nullptr;
+  static constexpr int kMaxKsLanes = 4;
+  cudaStream_t ks_side[kMaxKsLanes - 1] = {};
+  cudaEvent_t ks_fork = nullptr;
+  cudaEvent_t ks_join[kMaxKsLanes - 1] = {};
   std::mutex io_mu;
 
   CtxDev dev() const {
@@ -531,9 +533,11 @@ void shg_context_destroy(shg_context* ctx) {
   cudaFree(ctx->io);
   for (cudaStream_t s : ctx->io_streams)
     if (s) cudaStreamDestroy(s);
-  if (ctx->ks_side) cudaStreamDestroy(ctx->ks_side);
+  for (int i = 0; i < shg_context::kMaxKsLanes - 1; ++i) {
+    if (ctx->ks_side[i]) cudaStreamDestroy(ctx->ks_side[i]);
+    if (ctx->ks_join[i]) cudaEventDestroy(ctx->ks_join[i]);
+  }
   if (ctx->ks_fork) cudaEventDestroy(ctx->ks_fork);
-  if (ctx->ks_join) cudaEventDestroy(ctx->ks_join);
   delete ctx;
 }
 
@@ -958,7 +962,7 @@ int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
     shg::launch_intt_export(dv, X, src, a.ncomp, a.comp, a.subst_power,
                             CtMap::identity(), cc, L, s);
     shg::KeyTable kt;
-    if (keys) kt = shg::KeyTable{table.kb + c0, table.ka + c0, 0};
+    if (keys) kt = shg::KeyTable{table.kb + c0, table.ka + c0, 0, count - c0};
     shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src,
                           (size_t)a.ncomp * Ln, CtMap::identity(), a.base1_zero,
@@ -1007,7 +1011,7 @@ int upload_key_table(const shg_key* const* keys, int count, int stride, int offs
   }
   SHG_CUDA(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(void*), cudaMemcpyHostToDevice,
                            s));
-  *out = shg::KeyTable{dst, dst + count, 0};
+  *out = shg::KeyTable{dst, dst + count, 0, count};
   return SHG_OK;
 }
 
@@ -1032,22 +1036,24 @@ int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* k
   C = std::max(1, std::min(C, count));
   const size_t tab_bytes = keys ? 2 * (size_t)count * sizeof(void*) : 0;
   std::lock_guard<std::mutex> lock(ctx->mu);
-  // Chunks alternate between the caller's stream and a second one, each with
-  // its own digit scratch, so one chunk's kernels fill the other's tail.  The
-  // second stream is created outside any stream capture (the first call).
+  // Chunks rotate over the caller's stream and up to three more (ks_lanes in
+  // all), each lane with its own digit scratch, so one chunk's kernels fill
+  // another's tail.  The extra streams are created outside any stream
+  // capture (the first call).
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   SHG_CUDA(cudaStreamIsCapturing(s, &cap));
-  if (!ctx->ks_side && cap == cudaStreamCaptureStatusNone) {
-    SHG_CUDA(cudaStreamCreateWithFlags(&ctx->ks_side, cudaStreamNonBlocking));
+  if (!ctx->ks_fork && cap == cudaStreamCaptureStatusNone) {
     SHG_CUDA(cudaEventCreateWithFlags(&ctx->ks_fork, cudaEventDisableTiming));
-    SHG_CUDA(cudaEventCreateWithFlags(&ctx->ks_join, cudaEventDisableTiming));
+    for (int i = 0; i < shg_context::kMaxKsLanes - 1; ++i) {
+      SHG_CUDA(cudaStreamCreateWithFlags(&ctx->ks_side[i], cudaStreamNonBlocking));
+      SHG_CUDA(cudaEventCreateWithFlags(&ctx->ks_join[i], cudaEventDisableTiming));
+    }
   }
   const int nchunks = (count + C - 1) / C;
-  const int lanes = (ctx->ks_side && nchunks > 1 && ctx->ks_lanes > 1) ? 2 : 1;
+  const int lanes = ctx->ks_fork ? std::max(1, std::min(ctx->ks_lanes, nchunks)) : 1;
   if ((st = ctx->ensure_ws(x_bytes + lanes * d_per_ct * C + tab_bytes))) return st;
   uint64_t* X = ctx->ws;
   uint64_t* D0 = X + (size_t)count * Ln;
-  uint64_t* D1 = D0 + (size_t)C * k * Ln;
   shg::KeyTable kt;
   if (keys &&
       (st = upload_key_table(keys, count, 1, 0,
@@ -1056,24 +1062,25 @@ int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* k
     return st;
   const CtxDev dv = ctx->dev();
   shg::launch_tensor_intt(dv, out, X, a, b, count, L, s);
-  if (lanes == 2) {
+  if (lanes > 1) {
     SHG_CUDA(cudaEventRecord(ctx->ks_fork, s));
-    SHG_CUDA(cudaStreamWaitEvent(ctx->ks_side, ctx->ks_fork, 0));
+    for (int i = 0; i + 1 < lanes; ++i)
+      SHG_CUDA(cudaStreamWaitEvent(ctx->ks_side[i], ctx->ks_fork, 0));
   }
   for (int i = 0; i < nchunks; ++i) {
     const int c0 = i * C, cc = std::min(C, count - c0);
-    const bool side = lanes == 2 && (i & 1);
+    const int lane = i % lanes;
     uint64_t* o = out + (size_t)c0 * 2 * Ln;
     shg::KeyTable kc;
-    if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0};
-    shg::launch_keyswitch(dv, side ? D1 : D0, X + (size_t)c0 * Ln, key->d_digits, k,
-                          key->need_lift, key->chunk, key->chunk_lazy, key->kb, key->ka, o, o,
-                          2 * Ln, CtMap::identity(), 0, 0, cc, L, side ? ctx->ks_side : s,
-                          kc);
+    if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0, count - c0};
+    shg::launch_keyswitch(dv, D0 + (size_t)lane * C * k * Ln, X + (size_t)c0 * Ln,
+                          key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
+                          key->kb, key->ka, o, o, 2 * Ln, CtMap::identity(), 0, 0, cc, L,
+                          lane ? ctx->ks_side[lane - 1] : s, kc);
   }
-  if (lanes == 2) {
-    SHG_CUDA(cudaEventRecord(ctx->ks_join, ctx->ks_side));
-    SHG_CUDA(cudaStreamWaitEvent(s, ctx->ks_join, 0));
+  for (int i = 0; i + 1 < lanes; ++i) {
+    SHG_CUDA(cudaEventRecord(ctx->ks_join[i], ctx->ks_side[i]));
+    SHG_CUDA(cudaStreamWaitEvent(s, ctx->ks_join[i], 0));
   }
   return launch_status("bgv_mul_relin");
 }
@@ -1486,7 +1493,9 @@ int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_
       uint64_t* blk = out + (size_t)q0 * per_query;
       shg::launch_intt_export(dv, X, blk, 2, 1, power, map, mc, 1, s);
       shg::KeyTable kt;
-      if (tables) kt = shg::KeyTable{tables[j].kb + q0, tables[j].ka + q0, j};
+      if (tables)
+        kt = shg::KeyTable{tables[j].kb + q0, tables[j].ka + q0, j,
+                           tables[j].entries ? tables[j].entries - q0 : 0};
       shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->need_lift,
                             key->chunk, key->chunk_lazy, key->kb, key->ka, KS, blk, 2 * (size_t)n,
                             map, 1, power, mc, 1, s, kt);
@@ -1548,7 +1557,8 @@ int pir_impl(shg_context* ctx, const shg_key* const* keys, bool per_query_keys, 
                                2 * n * sizeof(uint64_t), gc, cudaMemcpyDeviceToDevice, s));
     std::vector<shg::KeyTable> gt(tables.size());
     for (size_t j = 0; j < tables.size(); ++j)
-      gt[j] = shg::KeyTable{tables[j].kb + g0, tables[j].ka + g0, 0};
+      gt[j] = shg::KeyTable{tables[j].kb + g0, tables[j].ka + g0, 0,
+                            tables[j].entries ? tables[j].entries - g0 : 0};
     if ((st = run_expand(ctx, level_keys, levels, blocks, gc, plan, ctx->ws, s,
                          per_query_keys ? gt.data() : nullptr)))
       return st;
@@ -1885,9 +1895,17 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
   ctx->ntt4_min = log_n;
   return SHG_OK;
 }
+int shg_debug_status(unsigned* first_failure) {
+  if (!first_failure) return fail(SHG_INVALID_ARGUMENT, "null argument");
+  const unsigned a = shg::take_debug_word_kernels();
+  const unsigned b = shg::take_debug_word_ntt4();
+  *first_failure = a ? a : b;
+  return SHG_OK;
+}
+
 int shg_context_set_ks_lanes(shg_context* ctx, int lanes) {
-  if (!ctx || lanes < 1 || lanes > 2)
-    return fail(SHG_INVALID_ARGUMENT, "key-switch lanes must be 1 or 2");
+  if (!ctx || lanes < 1 || lanes > shg_context::kMaxKsLanes)
+    return fail(SHG_INVALID_ARGUMENT, "key-switch lanes must be 1 to 4");
   ctx->ks_lanes = lanes;
   return SHG_OK;
 }

@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   if (subst_power > 0) {
 #pragma unroll
     for (int k = 0; k < C::E; ++k)
-      x[k] = src[subst_src<LOG_N>(C::inv_in_idx(tid, k), subst_power)];
+      x[k] = src[dbg_index(subst_src<LOG_N>(C::inv_in_idx(tid, k), subst_power), C::N, kDbgSubst)];
   } else {
     load_contig(x, src + C::inv_in_idx(tid, 0));
   }
@@ -262,10 +262,11 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
   int g = blockIdx.x * G::LPC + sub;
   const bool active = g < num;
   if (!active) g = num - 1;
-  const int j = g % L;
+  const int j = dbg_index(g % L, c.L, kDbgLimb);
   const int pd = g / L;
   const int idx = pd % k, p = pd / k;
-  const DigitDesc dd = digits[idx];
+  DigitDesc dd = digits[idx];
+  dd.src_limb = dbg_index(dd.src_limb, L, kDbgDigit);
   const PrimeDev* P = c.primes + j;
   const uint64_t q = P->q, two_q = P->two_q;
   const uint64_t* src = X + ((size_t)p * L + dd.src_limb) * C::N;
@@ -421,7 +422,8 @@ __global__ void k_substitute(uint64_t* out, const uint64_t* in, int power,
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += stride) {
     const int pos = (int)(e & nmask);
-    out[e] = in[(e & ~nmask) | (size_t)subst_src_rt(pos, power, log_n)];
+    out[e] = in[(e & ~nmask) |
+               (size_t)dbg_index(subst_src_rt(pos, power, log_n), 1LL << log_n, kDbgSubst)];
   }
 }
 
@@ -461,8 +463,9 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
   if (r >= Ln) return;
   const size_t p = (size_t)p0 + blockIdx.y;
   if (kt.kb) {
-    kb = kt.kb[p >> kt.shift];
-    ka = kt.ka[p >> kt.shift];
+    const size_t e = dbg_index(p >> kt.shift, kt.entries ? kt.entries : (1LL << 62), kDbgKeyTable);
+    kb = kt.kb[e];
+    ka = kt.ka[e];
   }
   const int l = r >> log_n;
   const int pos = r & ((1 << log_n) - 1);
@@ -488,7 +491,9 @@ __global__ void k_ks_inner(uint64_t* out, const uint64_t* D, const uint64_t* kb,
     s1 = add_mod(s1, redc128(lo1, hi1, q, qinv), q);
   }
   const uint64_t* bp = base + map(p) * base_ct_elems + ((size_t)l << log_n);
-  const int pos0 = subst_power > 0 ? subst_src_rt(pos, subst_power, log_n) : pos;
+  const int pos0 = subst_power > 0
+                       ? dbg_index(subst_src_rt(pos, subst_power, log_n), 1LL << log_n, kDbgSubst)
+                       : pos;
   const uint64_t b0 = bp[pos0];
   const uint64_t b1 = base1_zero ? 0 : bp[(size_t)Ln + pos];
   out[p * 2 * Ln + r] = add_mod(b0, s0, q);
@@ -1293,6 +1298,13 @@ int measure_butterfly_rate(double* per_second) {
   if (e != cudaSuccess || ms <= 0) return -1;
   *per_second = (double)blocks * kThreads * kIlp * kIters / (ms * 1e-3);
   return 0;
+}
+
+unsigned take_debug_word_kernels() {
+  unsigned v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_shg_dbg, sizeof(v)) != cudaSuccess) return 0;
+  if (v) cudaMemcpyToSymbol(g_shg_dbg, &z, sizeof(z));
+  return v;
 }
 
 }  // namespace shg

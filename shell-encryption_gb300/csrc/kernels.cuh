@@ -49,6 +49,7 @@ struct KeyTable {
   const uint64_t* const* kb = nullptr;
   const uint64_t* const* ka = nullptr;
   int shift = 0;
+  int entries = 0;  // table entries from kb / ka on (debug builds check p >> shift)
 };
 
 // Gadget base exponents per limb (RnsGadget log_bs), passed by value.
@@ -72,6 +73,38 @@ struct CtMap {
     return ((p >> grp_log) << stride_log) | (p & ((size_t(1) << grp_log) - 1));
   }
 };
+
+// Debug builds (compiled with SHG_DEBUG) check computed indices before they
+// address memory -- substitution gathers, key-table members, gadget digit
+// descriptors, limb indices.  An index outside [0, bound) records its check's
+// tag in this translation unit's debug word (the first failure wins) and is
+// replaced by 0, so the access stays inside its buffer and nothing traps;
+// shg_debug_status() reads and clears the words.  Release builds compile the
+// checks away.
+enum DbgTag : unsigned {
+  kDbgSubst = 1,     // NTT-domain substitution gather position
+  kDbgKeyTable = 2,  // per-member key table entry
+  kDbgDigit = 3,     // gadget digit descriptor / its source limb
+  kDbgLimb = 4,      // limb (prime) index of a transform
+};
+static __device__ unsigned g_shg_dbg;
+template <class I>
+__device__ __forceinline__ I dbg_index(I idx, long long bound, unsigned tag) {
+#ifdef SHG_DEBUG
+  if ((long long)idx < 0 || (long long)idx >= bound) {
+    atomicCAS(&g_shg_dbg, 0u, tag);
+    return 0;
+  }
+#else
+  (void)bound;
+  (void)tag;
+#endif
+  return idx;
+}
+// The debug words of kernels.cu and ntt4.cu on the current device, cleared
+// after reading (0: no check failed).
+unsigned take_debug_word_kernels();
+unsigned take_debug_word_ntt4();
 
 // Number of kernels this library has launched (host-side counter).
 extern std::atomic<uint64_t> g_launch_count;

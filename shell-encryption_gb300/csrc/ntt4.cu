@@ -65,7 +65,8 @@ struct FwdSrcDigit {
   __device__ H bind(int g, int j, const CtxDev& c) const {
     const int pd = g / L;
     const int di = pd % k, p = pd / k;
-    const DigitDesc dd = digits[di];
+    DigitDesc dd = digits[di];
+    dd.src_limb = dbg_index(dd.src_limb, L, kDbgDigit);
     H h;
     h.base = X + (((size_t)p * L + dd.src_limb) << LOG_N);
     h.shift = dd.shift;
@@ -273,7 +274,7 @@ struct InvSrcComponent {
       const unsigned j = __brev((unsigned)i) >> (32 - LOG_N);
       const unsigned t = ((unsigned)((power - 1) >> 1) + j * (unsigned)power) &
                          ((1u << LOG_N) - 1);
-      return base[__brev(t) >> (32 - LOG_N)];
+      return base[dbg_index(__brev(t) >> (32 - LOG_N), 1LL << LOG_N, kDbgSubst)];
     }
     __device__ __forceinline__ ulonglong2 pair(int i) const {
       if (power > 0) return make_ulonglong2(at(i), at(i + 1));
@@ -379,7 +380,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
   const int g = blockIdx.x / S::COL_TILES, tile = blockIdx.x % S::COL_TILES;
   const int j = threadIdx.x % S::COLS, t = threadIdx.x / S::COLS;
   const int col = tile * S::COLS + j;
-  const int l = pm(g);
+  const int l = dbg_index(pm(g), c.L, kDbgLimb);
   const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
   const auto h = src.bind(g, l, c);
   uint64_t x[C::E];
@@ -406,7 +407,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
   const int groups = (per_class + S::ROWS - 1) / S::ROWS;
   const int row = blockIdx.x % rows;
   const int cg = blockIdx.x / rows;
-  const int l = cg / groups, grp = cg % groups;
+  const int l = dbg_index(cg / groups, c.L, kDbgLimb), grp = cg % groups;
   const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
   const int m = grp * S::ROWS + sub;
   const bool active = m < per_class;
@@ -475,11 +476,12 @@ __global__ void __maxnreg__(72)
   const int tiles = (1 << S::A) / R;
   const int tile = blockIdx.x % tiles;
   const int pl = blockIdx.x / tiles;
-  const int l = pl % L;
+  const int l = dbg_index(pl % L, c.L, kDbgLimb);
   const size_t p = (size_t)(pl / L);
   if (kt.kb) {
-    kb = kt.kb[p >> kt.shift];
-    ka = kt.ka[p >> kt.shift];
+    const size_t e = dbg_index(p >> kt.shift, kt.entries ? kt.entries : (1LL << 62), kDbgKeyTable);
+    kb = kt.kb[e];
+    ka = kt.ka[e];
   }
   const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
   const int r = sub / k, j = sub % k;
@@ -540,7 +542,7 @@ __global__ void __maxnreg__(72)
       const unsigned jb = __brev((unsigned)pos) >> (32 - LOG_N);
       const unsigned t = ((unsigned)((subst_power - 1) >> 1) + jb * (unsigned)subst_power) &
                          ((1u << LOG_N) - 1);
-      pos0 = (int)(__brev(t) >> (32 - LOG_N));
+      pos0 = dbg_index((int)(__brev(t) >> (32 - LOG_N)), 1LL << LOG_N, kDbgSubst);
     }
     const uint64_t b0 = bp[pos0];
     const uint64_t b1 = base1_zero ? 0 : bp[Ln + pos];
@@ -580,11 +582,12 @@ __global__ void __maxnreg__(56)
   constexpr int rows = 1 << S::A;
   const int row = blockIdx.x % rows;
   const int pl = blockIdx.x / rows;
-  const int l = pl % L;
+  const int l = dbg_index(pl % L, c.L, kDbgLimb);
   const size_t p = (size_t)(pl / L);
   if (kt.kb) {
-    kb = kt.kb[p >> kt.shift];
-    ka = kt.ka[p >> kt.shift];
+    const size_t e = dbg_index(p >> kt.shift, kt.entries ? kt.entries : (1LL << 62), kDbgKeyTable);
+    kb = kt.kb[e];
+    ka = kt.ka[e];
   }
   const int j = threadIdx.x / C::T, tid = threadIdx.x % C::T;
   const PrimeDev* P = c.primes + l;
@@ -632,13 +635,158 @@ __global__ void __maxnreg__(56)
         const unsigned jb = __brev((unsigned)pos) >> (32 - LOG_N);
         const unsigned t = ((unsigned)((subst_power - 1) >> 1) + jb * (unsigned)subst_power) &
                            ((1u << LOG_N) - 1);
-        pos0 = (int)(__brev(t) >> (32 - LOG_N));
+        pos0 = dbg_index((int)(__brev(t) >> (32 - LOG_N)), 1LL << LOG_N, kDbgSubst);
       }
       b = bp[pos0];
     } else {
       b = base1_zero ? 0 : bp[Ln + pos];
     }
     out[p * 2 * Ln + comp * Ln + kr] = add_mod(b, acc, q);
+  }
+}
+
+// Rows (warps) per CTA of k4_ks_rows_warp.
+constexpr int kKsWarpRows = 4;
+
+// The key switch's row phase with one warp per row of one (ciphertext,
+// limb): its 32 threads run that row of every digit transform in turn (4
+// values per thread, NttCore<7, 2>: four passes, exchanges in the warp's own
+// swizzled shared tile with warp-level synchronisation only) and keep the key
+// inner product of their 4 consecutive output slots in registers (two
+// components, 128-bit sums).  The digit values are never parked, no CTA-wide
+// barrier is taken, and key rows and the base are read 16 bytes at a time.
+// For a chunk covering every digit (chunk >= k), as lazily reduced digits of
+// primes below 2^58 give at up to a few dozen digits.  W rows (warps) per CTA,
+// at least MB CTAs per SM; PF & 1: the next digit's row is loaded while this
+// one is transformed, PF & 2: this digit's key values are loaded before its
+// transform.  Against k4_ks_rows8 (one row of all digits per CTA, values
+// parked in shared memory, CTA barriers) it runs alone at the same speed but
+// shares the SMs far better with the next chunk's column kernel on the
+// other key-switch stream (ct-mult+relin 53.4 k -> 56.1 k/s with W = 4,
+// MB = 5, PF = 3).
+template <int LOG_N, bool LAZY, int W, int MB, int PF>
+__global__ void __launch_bounds__(32 * W, MB)
+    k4_ks_rows_warp(const uint64_t* buf, int k, const uint64_t* kb, const uint64_t* ka,
+                    uint64_t* out, const uint64_t* base, size_t base_ct_elems, CtMap map,
+                    int base1_zero, int subst_power, int L, KeyTable kt, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = NttCore<S::B, 2>;
+  static_assert(C::T == 32 && C::E == 4 && C::P == 4, "32 threads x 4 values per row");
+  extern __shared__ uint64_t smem[];
+  constexpr int tiles = (1 << S::A) / W;
+  const int tile = blockIdx.x % tiles;
+  const int pl = blockIdx.x / tiles;
+  const int l = dbg_index(pl % L, c.L, kDbgLimb);
+  const size_t p = (size_t)(pl / L);
+  if (kt.kb) {
+    const size_t e = dbg_index(p >> kt.shift, kt.entries ? kt.entries : (1LL << 62), kDbgKeyTable);
+    kb = kt.kb[e];
+    ka = kt.ka[e];
+  }
+  const int warp = threadIdx.x >> 5, tid = threadIdx.x & 31;
+  const int row = tile * W + warp;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const size_t n = (size_t)1 << LOG_N, Ln = (size_t)L * n;
+  const Tw* tw0 = c.tw_fwd + ((size_t)l << LOG_N);
+  const int tm = (1 << S::A) + row;
+  const typename C::SwzMap m{smem + ((size_t)warp << S::B)};
+  // this thread's output slots after the last pass: 4 consecutive positions
+  const int pos0 = (row << S::B) | C::fwd_out_idx(tid, 0);
+  const size_t kr0 = (size_t)l * n + pos0;
+  const uint64_t* src = buf + (((p * k) * L + l) << LOG_N) + ((size_t)row << S::B);
+  uint64_t lo0[4], hi0[4], lo1[4], hi1[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) lo0[e] = hi0[e] = lo1[e] = hi1[e] = 0;
+  uint64_t xn[4];
+  if constexpr (PF & 1) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) xn[e] = src[C::fwd_in_idx(tid, e)];
+  }
+#pragma unroll 1
+  for (int j = 0; j < k; ++j, src += Ln) {
+    // The twiddles are the same for every digit; reloading them per digit
+    // (L1 hits) keeps the compiler from holding all of them in registers.
+    const Tw* tw;
+    asm volatile("mov.b64 %0, %1;" : "=l"(tw) : "l"(tw0));
+    uint64_t x[4];
+    if constexpr (PF & 1) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) x[e] = xn[e];
+      if (j + 1 < k) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) xn[e] = src[Ln + C::fwd_in_idx(tid, e)];
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
+    }
+    ulonglong2 kv[4];
+    const ulonglong2* b2 = reinterpret_cast<const ulonglong2*>(kb + kr0 + (size_t)j * Ln);
+    const ulonglong2* a2 = reinterpret_cast<const ulonglong2*>(ka + kr0 + (size_t)j * Ln);
+    if constexpr (PF & 2) {
+      kv[0] = __ldg(b2);
+      kv[1] = __ldg(b2 + 1);
+      kv[2] = __ldg(a2);
+      kv[3] = __ldg(a2 + 1);
+    }
+    static_for<0, C::P>([&](auto pp) {
+      constexpr int ps = decltype(pp)::value;
+      C::template fwd_pass<ps, LAZY>(x, tid, tw, tm, q, two_q);
+      if constexpr (ps + 1 < C::P) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) m(C::idx(tid, e, C::fwd_clo(ps))) = x[e];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 4; ++e) x[e] = m(C::idx(tid, e, C::fwd_clo(ps + 1)));
+        __syncwarp();  // every read is done before the tile is rewritten
+      }
+    });
+    if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const ulonglong2 vb = (PF & 2) ? kv[h] : __ldg(b2 + h);
+      const ulonglong2 va = (PF & 2) ? kv[2 + h] : __ldg(a2 + h);
+      mac128(lo0[2 * h], hi0[2 * h], x[2 * h], vb.x);
+      mac128(lo0[2 * h + 1], hi0[2 * h + 1], x[2 * h + 1], vb.y);
+      mac128(lo1[2 * h], hi1[2 * h], x[2 * h], va.x);
+      mac128(lo1[2 * h + 1], hi1[2 * h + 1], x[2 * h + 1], va.y);
+    }
+  }
+  const uint64_t qinv = P->inv_modulus;
+  const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
+  uint64_t* o0 = out + p * 2 * Ln + kr0;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint64_t b0[2], b1[2];
+    if (subst_power > 0) {
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int pos = pos0 + 2 * h + t;
+        const unsigned jb = __brev((unsigned)pos) >> (32 - LOG_N);
+        const unsigned tt = ((unsigned)((subst_power - 1) >> 1) + jb * (unsigned)subst_power) &
+                            ((1u << LOG_N) - 1);
+        b0[t] = bp[dbg_index(__brev(tt) >> (32 - LOG_N), 1LL << LOG_N, kDbgSubst)];
+      }
+    } else {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(bp + pos0 + 2 * h);
+      b0[0] = v.x;
+      b0[1] = v.y;
+    }
+    if (base1_zero) {
+      b1[0] = b1[1] = 0;
+    } else {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(bp + Ln + pos0 + 2 * h);
+      b1[0] = v.x;
+      b1[1] = v.y;
+    }
+    ulonglong2 r0, r1;
+    r0.x = add_mod(b0[0], redc128(lo0[2 * h], hi0[2 * h], q, qinv), q);
+    r0.y = add_mod(b0[1], redc128(lo0[2 * h + 1], hi0[2 * h + 1], q, qinv), q);
+    r1.x = add_mod(b1[0], redc128(lo1[2 * h], hi1[2 * h], q, qinv), q);
+    r1.y = add_mod(b1[1], redc128(lo1[2 * h + 1], hi1[2 * h + 1], q, qinv), q);
+    *reinterpret_cast<ulonglong2*>(o0 + 2 * h) = r0;
+    *reinterpret_cast<ulonglong2*>(o0 + Ln + 2 * h) = r1;
   }
 }
 
@@ -651,7 +799,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
   const int g = blockIdx.x / S::ROW_TILES, tile = blockIdx.x % S::ROW_TILES;
   const int sub = threadIdx.x / C::T, tid = threadIdx.x % C::T;
   const int row = tile * S::ROWS + sub;
-  const int l = pm(g);
+  const int l = dbg_index(pm(g), c.L, kDbgLimb);
   const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
   // Whole sub-rows come in warp by warp, 32 consecutive pairs per access,
   // through shared memory (pair slots XOR-swizzled, as in k4_fwd_rows'
@@ -696,7 +844,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS)
   const int g = blockIdx.x / S::COL_TILES, tile = blockIdx.x % S::COL_TILES;
   const int j = threadIdx.x % S::COLS, t = threadIdx.x / S::COLS;
   const int col = tile * S::COLS + j;
-  const int l = pm(g);
+  const int l = dbg_index(pm(g), c.L, kDbgLimb);
   const uint64_t q = c.primes[l].q, two_q = c.primes[l].two_q;
   const uint64_t* src = buf + ((size_t)g << LOG_N);
   uint64_t x[C::E];
@@ -842,6 +990,23 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                      const uint64_t* base, size_t base_ct_elems, CtMap map,
                      int base1_zero, int subst_power, int count, int L,
                      cudaStream_t s, const KeyTable& kt) {
+  // One REDC covers every digit (lazily reduced digits of primes below 2^58
+  // at the usual digit counts, canonical ones of larger primes at up to
+  // floor(2^64 / q) digits): one warp per row, all digits in turn.
+  if (chunk >= k) {
+#define F(LN)                                                                   \
+  {                                                                             \
+    auto kern = c.small_q ? k4_ks_rows_warp<LN, true, kKsWarpRows, 5, 3>        \
+                          : k4_ks_rows_warp<LN, false, kKsWarpRows, 5, 3>;      \
+    const int smem = kKsWarpRows * 128 * 8;                                     \
+    set_smem4(kern, smem);                                                      \
+    kern<<<count * L * ((1 << (LN - 7)) / kKsWarpRows), 32 * kKsWarpRows, smem, s>>>( \
+        D, k, kb, ka, out, base, base_ct_elems, map, base1_zero, subst_power, L, kt, c); \
+  }
+    SHG_DISPATCH4(c.log_n, F)
+#undef F
+    return;
+  }
   if (k % 2 == 0 && k * 16 <= kKsRowsMaxThreads) {
 #define F(LN)                                                                   \
   {                                                                             \
@@ -894,6 +1059,13 @@ void launch4_bgv_encrypt(const CtxDev& c, uint64_t* out, const int32_t* err,
            PrimeMap{0, 1, L}, buf, count * L, s)
   SHG_DISPATCH4(c.log_n, F)
 #undef F
+}
+
+unsigned take_debug_word_ntt4() {
+  unsigned v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_shg_dbg, sizeof(v)) != cudaSuccess) return 0;
+  if (v) cudaMemcpyToSymbol(g_shg_dbg, &z, sizeof(z));
+  return v;
 }
 
 }  // namespace shg

@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libshellgpu.so")
+# SHELL_GPU_LIB selects another build of the library (the SHG_DEBUG build).
+LIB_PATH = os.environ.get("SHELL_GPU_LIB") or os.path.join(_HERE, "libshellgpu.so")
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -138,6 +139,7 @@ SIGNATURES = {
     "shg_measure_butterfly_rate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "shg_profile_start": (ctypes.c_int, []),
     "shg_profile_stop": (ctypes.c_int, []),
+    "shg_debug_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint)]),
     "shg_profile_query": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_uint64)]),
     "shg_context_reserve": (ctypes.c_int, [_vp, _sz]),

@@ -40,3 +40,20 @@ def sg():
     import shell_gpu
     shell_gpu.lib()
     return shell_gpu
+
+
+@pytest.fixture(autouse=True)
+def _debug_checks_clean():
+    """With SHG_DEBUG_CHECK set (the tests run against the SHG_DEBUG build,
+    tests/test_debug_build.py), every test must leave the device-side index
+    checks clean."""
+    yield
+    if not os.environ.get("SHG_DEBUG_CHECK"):
+        return
+    import ctypes
+    import shell_gpu
+    if shell_gpu._lib is None:
+        return
+    code = ctypes.c_uint(0)
+    shell_gpu.check(shell_gpu.lib().shg_debug_status(ctypes.byref(code)))
+    assert code.value == 0, f"a device-side index check failed (tag {code.value})"
