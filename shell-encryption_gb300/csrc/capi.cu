@@ -167,6 +167,7 @@ struct shg_context {
   std::vector<uint8_t> conv_fast;  // per table: takes the specialised kernel
   uint64_t t = 0;
   int device = 0;
+  int sms = 152;  // multiprocessors of `device`
   std::vector<HostPrime> hp;
   PrimeDev* d_primes = nullptr;
   Tw* d_tw_fwd = nullptr;
@@ -198,13 +199,13 @@ struct shg_context {
 
   CtxDev dev() const {
     return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min,
-                  ks_fused};
+                  ks_fused, sms};
   }
   // The auxiliary primes as a context of their own (NTTs and pointwise ops
   // over aux limbs); there is no cross-prime table in this view.
   CtxDev aux_dev() const {
     return CtxDev{log_n, n, K, d_primes + L, d_tw_fwd + (size_t)L * n,
-                  d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused};
+                  d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused, sms};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -234,6 +235,7 @@ struct shg_key {
   uint64_t* kb = nullptr;  // [k][L][n], premultiplied by 2^64 mod q
   uint64_t* ka = nullptr;
   int need_lift = 0;
+  int digit_flags = 0;  // shg::digit_flags(need_lift, largest log_b)
   int chunk = 1;       // digits per REDC for canonical digit transforms
   int chunk_lazy = 1;  // the same for lazily reduced ones (below 62 q)
   size_t bytes = 0;
@@ -444,6 +446,7 @@ int shg_context_create_with_aux(int log_n, const uint64_t* qs, int num_qs, const
   ctx->K = num_ps;
   ctx->t = plaintext_modulus;
   cudaGetDevice(&ctx->device);
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int NP = num_qs + num_ps;  // main primes, then auxiliary ones
   ctx->hp.resize(NP);
   for (int i = 0; i < NP; ++i) {
@@ -851,6 +854,8 @@ int shg_key_create(shg_context* ctx, int num_limbs, const int* log_bs,
     qmax = std::max(qmax, h.q);
   }
   key->k = (int)dd.size();
+  key->digit_flags =
+      shg::digit_flags(key->need_lift, *std::max_element(key->log_bs.begin(), key->log_bs.end()));
   key->chunk = (int)std::max<uint64_t>(
       1, std::min<uint64_t>((uint64_t)key->k, (~(uint64_t)0) / qmax));
   // The fused row kernel keeps the digit transforms lazily reduced when every
@@ -963,7 +968,7 @@ int keyswitch(shg_context* ctx, const shg_key* key, uint64_t* out,
                             CtMap::identity(), cc, L, s);
     shg::KeyTable kt;
     if (keys) kt = shg::KeyTable{table.kb + c0, table.ka + c0, 0, count - c0};
-    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->digit_flags, key->chunk, key->chunk_lazy,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src,
                           (size_t)a.ncomp * Ln, CtMap::identity(), a.base1_zero,
                           a.subst_power, cc, L, s, kt);
@@ -1070,13 +1075,14 @@ int mul_relin_impl(shg_context* ctx, const shg_key* key, const shg_key* const* k
   for (int i = 0; i < nchunks; ++i) {
     const int c0 = i * C, cc = std::min(C, count - c0);
     const int lane = i % lanes;
+    cudaStream_t ls = lane ? ctx->ks_side[lane - 1] : s;
     uint64_t* o = out + (size_t)c0 * 2 * Ln;
     shg::KeyTable kc;
     if (keys) kc = shg::KeyTable{kt.kb + c0, kt.ka + c0, 0, count - c0};
     shg::launch_keyswitch(dv, D0 + (size_t)lane * C * k * Ln, X + (size_t)c0 * Ln,
-                          key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
-                          key->kb, key->ka, o, o, 2 * Ln, CtMap::identity(), 0, 0, cc, L,
-                          lane ? ctx->ks_side[lane - 1] : s, kc);
+                          key->d_digits, k, key->digit_flags, key->chunk, key->chunk_lazy,
+                          key->kb, key->ka, o, o, 2 * Ln, CtMap::identity(), 0, 0, cc, L, ls,
+                          kc);
   }
   for (int i = 0; i + 1 < lanes; ++i) {
     SHG_CUDA(cudaEventRecord(ctx->ks_join[i], ctx->ks_side[i]));
@@ -1496,7 +1502,7 @@ int run_expand(shg_context* ctx, const shg_key* const* keys, int levels, uint64_
       if (tables)
         kt = shg::KeyTable{tables[j].kb + q0, tables[j].ka + q0, j,
                            tables[j].entries ? tables[j].entries - q0 : 0};
-      shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->need_lift,
+      shg::launch_keyswitch(dv, D, X, key->d_digits, key->k, key->digit_flags,
                             key->chunk, key->chunk_lazy, key->kb, key->ka, KS, blk, 2 * (size_t)n,
                             map, 1, power, mc, 1, s, kt);
       shg::launch_expand_combine(dv, blk, KS, mono + (size_t)j * n, map, 1 << j,
@@ -2444,7 +2450,7 @@ extern "C" int shg_relin_apply_noalloc(shg_context* ctx, const shg_key* key,
     const int cc = std::min(C, count - c0);
     const uint64_t* src = ct + (size_t)c0 * 3 * Ln;
     shg::launch_intt_export(dv, X, src, 3, 2, 0, CtMap::identity(), cc, L, s);
-    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->need_lift, key->chunk, key->chunk_lazy,
+    shg::launch_keyswitch(dv, D, X, key->d_digits, k, key->digit_flags, key->chunk, key->chunk_lazy,
                           key->kb, key->ka, out + (size_t)c0 * 2 * Ln, src, 3 * Ln,
                           CtMap::identity(), 0, 0, cc, L, s);
   }

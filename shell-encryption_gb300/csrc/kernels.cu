@@ -1048,17 +1048,18 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
 }
 
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                      const DigitDesc* digits, int k, int need_lift, int chunk,
+                      const DigitDesc* digits, int k, int digit_flags, int chunk,
                       int chunk_lazy,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
                       int base1_zero, int subst_power, int count, int L,
                       cudaStream_t s, const KeyTable& kt) {
   if (count <= 0) return;
+  const int need_lift = digit_flags & 1;
   if (use_ntt4(c) && c.ks_fused && ks4_rows_per_cta(k) > 0) {
     {
       LaunchScope scope_("digit_cols", s);
-      launch4_digit_cols(c, D, X, digits, k, need_lift, count, L, s);
+      launch4_digit_cols(c, D, X, digits, k, digit_flags, count, L, s);
     }
     LaunchScope scope_("ks_rows", s);
     // small primes: the row kernel skips the final reduction (chunk_lazy)

@@ -31,6 +31,7 @@ struct CtxDev {
   int small_q;
   int ntt4_min;               // log_n from which transforms use the four-step kernels
   int ks_fused;               // four-step key switch: digit row phase fused with the inner product
+  int sms;                    // multiprocessors of the context's device (launch-shape choices)
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,
@@ -209,9 +210,13 @@ void launch_ks_inner(const CtxDev& c, uint64_t* out, const uint64_t* D,
 
 // Gadget key switch core: digit decomposition + NTT of every digit + key
 // inner product + base add (launch_digit_ntt then launch_ks_inner).
-// D: [count][k][L][n] scratch.
+// D: [count][k][L][n] scratch.  digit_flags (digit_flags() below): bit 0 the
+// digits need the balanced lift, bit 1 some digit is wider than 32 bits.
+inline int digit_flags(int need_lift, int max_log_b) {
+  return (need_lift ? 1 : 0) | (max_log_b > 32 ? 2 : 0);
+}
 void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                      const DigitDesc* digits, int k, int need_lift, int chunk,
+                      const DigitDesc* digits, int k, int digit_flags, int chunk,
                       int chunk_lazy,
                       const uint64_t* kb, const uint64_t* ka, uint64_t* out,
                       const uint64_t* base, size_t base_ct_elems, CtMap map,
@@ -401,7 +406,7 @@ void launch4_bgv_encrypt(const CtxDev& c, uint64_t* out, const int32_t* err,
 // of launch4_ks_rows takes, 0 if k digits do not fit one CTA.
 int ks4_rows_per_cta(int k);
 void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                        const DigitDesc* digits, int k, int need_lift, int count,
+                        const DigitDesc* digits, int k, int digit_flags, int count,
                         int L, cudaStream_t s);
 void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                      const uint64_t* kb, const uint64_t* ka, uint64_t* out,

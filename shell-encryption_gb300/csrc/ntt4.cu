@@ -393,6 +393,61 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
   for (int k = 0; k < C::E; ++k) dst[(C::fwd_out_idx(t, k) << S::B) | col] = x[k];
 }
 
+// Digit extraction and column phase of one gadget digit for every output
+// limb: the CTA takes 16 columns of digit j of ciphertext p, extracts the
+// digit once from the exported source limb (rns/rns_gadget.cc:108-153) and
+// runs the column phase of its transform modulo each prime in turn (the
+// digit is the same integer for every limb; the balanced lift, when the
+// gadget needs it, is applied per limb).  D [count][k][L][n] as
+// k4_fwd_cols<FwdSrcDigit> writes it.
+template <int LOG_N, bool LAZY, class DT>
+__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS, sizeof(DT) == 4 ? 6 : 5)
+    k4_digit_cols_all(const uint64_t* X, const DigitDesc* digits, int k, int L, int need_lift,
+                      uint64_t* D, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = typename S::CC;
+  extern __shared__ uint64_t smem[];
+  const int pj = blockIdx.x / S::COL_TILES, tile = blockIdx.x % S::COL_TILES;
+  const int j = pj % k;
+  const size_t p = (size_t)(pj / k);
+  const int jc = threadIdx.x % S::COLS, t = threadIdx.x / S::COLS;
+  const int col = tile * S::COLS + jc;
+  DigitDesc dd = digits[j];
+  dd.src_limb = dbg_index(dd.src_limb, L, kDbgDigit);
+  const uint64_t* src = X + ((p * L + dd.src_limb) << LOG_N);
+  // DT = uint32_t holds digits of at most 32 bits in half the registers.
+  DT dv[C::E];
+#pragma unroll
+  for (int e = 0; e < C::E; ++e)
+    dv[e] = (DT)((src[(C::fwd_in_idx(t, e) << S::B) | col] >> dd.shift) & dd.mask);
+  const uint64_t half_qi = c.primes[dd.src_limb].half_q;
+#pragma unroll 1
+  for (int l = 0; l < L; ++l) {
+    const PrimeDev* P = c.primes + l;
+    const uint64_t q = P->q, two_q = P->two_q;
+    uint64_t x[C::E];
+    if (!need_lift) {
+#pragma unroll
+      for (int e = 0; e < C::E; ++e) x[e] = dv[e];
+    } else {
+      const uint64_t bar = P->barrett;
+      const uint64_t add = dd.src_limb != l ? q - c.qmod[dd.src_limb * c.L + l] : 0;
+#pragma unroll
+      for (int e = 0; e < C::E; ++e) {
+        uint64_t v = dv[e];
+        const bool neg = v > half_qi;
+        v = reduce_2q(v - mulhi64(v, bar) * q, q);
+        x[e] = neg ? v + add : v;
+      }
+    }
+    C::template forward_m<LAZY>(x, t, typename C::ColMap{smem, S::COLS, jc},
+                                c.tw_fwd + ((size_t)l << LOG_N), 1, q, two_q);
+    uint64_t* dst = D + (((p * k + j) * L + l) << LOG_N);
+#pragma unroll
+    for (int e = 0; e < C::E; ++e) dst[(C::fwd_out_idx(t, e) << S::B) | col] = x[e];
+  }
+}
+
 // The CTA takes row `row` of ROWS transforms that share a prime (transform g
 // has limb g mod pm.L for every forward use), so the sub-rows read the same
 // twiddles and the loads hit in L1.
@@ -969,8 +1024,27 @@ int ks4_rows_per_cta(int k) {
 }
 
 void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                        const DigitDesc* digits, int k, int need_lift, int count,
+                        const DigitDesc* digits, int k, int digit_flags, int count,
                         int L, cudaStream_t s) {
+  // Digits of at most 32 bits without the balanced lift (every gadget base up
+  // to 2^32 below the primes' halves): one CTA per digit tile for all limbs,
+  // when that still gives two full waves of CTAs (six per SM); a handful of
+  // ciphertexts (one-call-per-op use) keeps one CTA per digit and limb.
+  if (digit_flags == 0 &&
+      (long long)count * k * Ntt4<14>::COL_TILES >= 2LL * 6 * c.sms) {  // tiles: any n
+#define F(LN)                                                                   \
+  {                                                                             \
+    using S = Ntt4<LN>;                                                         \
+    auto k1 = c.small_q ? k4_digit_cols_all<LN, true, uint32_t>                 \
+                        : k4_digit_cols_all<LN, false, uint32_t>;               \
+    set_smem4(k1, S::COL_SMEM);                                                 \
+    k1<<<count * k * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(X, digits, k, L, 0, D, c); \
+  }
+    SHG_DISPATCH4(c.log_n, F)
+#undef F
+    return;
+  }
+  const int need_lift = digit_flags & 1;
 #define F(LN)                                                                   \
   {                                                                             \
     using S = Ntt4<LN>;                                                         \
@@ -993,7 +1067,12 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
   // One REDC covers every digit (lazily reduced digits of primes below 2^58
   // at the usual digit counts, canonical ones of larger primes at up to
   // floor(2^64 / q) digits): one warp per row, all digits in turn.
-  if (chunk >= k) {
+  // ... and the launch still gives two full waves of CTAs (five per SM); a
+  // handful of ciphertexts keeps the row kernels below, which spread one
+  // row's digits over a CTA.
+  const bool fits_rows8 = k % 2 == 0 && k * 16 <= kKsRowsMaxThreads;
+  if (chunk >= k && (!fits_rows8 || (long long)count * L * ((1 << (c.log_n - 7)) / kKsWarpRows) >=
+                                        2LL * 5 * c.sms)) {
 #define F(LN)                                                                   \
   {                                                                             \
     auto kern = c.small_q ? k4_ks_rows_warp<LN, true, kKsWarpRows, 5, 3>        \
