@@ -42,8 +42,8 @@ UNIT = "ct-mult+relin/s"
 # captures of the same kernels (dram__bytes_read.sum + dram__bytes_write.sum
 # of one 16-ciphertext launch); None where not captured.
 TRAFFIC_PER_CT = {
-    "ks_rows": (303.1e6 + 22.2e6) / 16,
-    "digit_cols": (12.6e6 + 166.4e6) / 16,
+    "ks_rows": (302.4e6 + 20.5e6) / 16,     # k4_ks_rows_warp
+    "digit_cols": (12.6e6 + 166.5e6) / 16,  # k4_digit_cols_all
 }
 # Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
 # step; the four-step key switch runs digit_cols + ks_rows, the unfused one
