@@ -1485,6 +1485,34 @@ def run_ntt(args, rank):
                           "ntt": rec}), flush=True)
 
 
+def other_workloads(args, world, rank, local, dist):
+    """Compact runs of the path's other workloads for the default line (so they
+    are timed under the same clocks): PIR expand + absorb, BGV encryption with
+    on-device sampling, BFV multiplication -- each its own workload function
+    with 3 warm-up and 3 timed steps, device-resident inputs, no CPU leg and
+    no host-copy leg.  Their full lines come from --workload."""
+    import contextlib
+    import io
+    out = {}
+    for wl, runner in (("pir", run_pir), ("encrypt", run_encrypt), ("bfv-mul", run_bfv)):
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.steps, a.warmup = wl, 3, 3
+        a.no_cpu_baseline, a.no_e2e = True, True
+        buf = io.StringIO()
+        with contextlib.redirect_stdout(buf):
+            runner(a, world, rank, local, dist)
+        lines = [ln for ln in buf.getvalue().splitlines() if ln.startswith("{")]
+        if not lines:
+            continue
+        d = json.loads(lines[-1])
+        rec = {k: d.get(k) for k in ("metric", "value", "unit", "ms_per_step")}
+        rec["workload"] = (d.get("config") or {}).get("workload")
+        if d.get("roofline"):
+            rec["roofline_frac"] = d["roofline"].get("frac")
+        out[wl] = rec
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1524,6 +1552,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ntt", action="store_true", help="skip the limb-NTT throughput record")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the compact PIR / encryption / BFV records of the default line")
     ap.add_argument("--ntt-polys", type=int, default=NTT_POLYS,
                     help="polynomials (of six limbs) per transform call in the NTT record")
     args = ap.parse_args()
@@ -1670,9 +1700,11 @@ def main():
     ops_all = sum_over_ranks(dist, float(B * args.steps))
     value = ops_all / (total_ms / 1e3)
 
-    # Bit-exactness spot check of the timed graph's output against the
-    # non-graph call (the parity tests cover the oracle side).
-    out_graph = np.empty(ct_elems * 2, np.uint64)
+    # Bit-exactness check of the timed graph's output against the plain
+    # one-call-per-op path, which recomputes the first min(plain ops, 64)
+    # ciphertexts (the parity tests cover the oracle side).
+    check_cts = max(1, min(args.plain_ops, B, 64))
+    out_graph = np.empty(ct_elems * check_cts, np.uint64)
     sg.check(lib.shg_memcpy_d2h(out_graph.ctypes.data, d_out.ptr, out_graph.nbytes, s))
     sg.check(lib.shg_stream_synchronize(s))
 
@@ -1758,7 +1790,7 @@ def main():
     plain_total = elapsed(op_evs[0], op_evs[-1])
     plain_rate = P / (plain_total / 1e3)
     # plain outputs must equal the batched ones (same inputs, same key)
-    out_plain = np.empty(ct_elems * 2, np.uint64)
+    out_plain = np.empty(ct_elems * check_cts, np.uint64)
     sg.check(lib.shg_memcpy_d2h(out_plain.ctypes.data, d_out.ptr, out_plain.nbytes, s))
     sg.check(lib.shg_stream_synchronize(s))
     bit_exact = bool(np.array_equal(out_graph, out_plain))
@@ -1836,6 +1868,10 @@ def main():
     def pct(v, p):
         return v[min(len(v) - 1, int(round(p / 100 * (len(v) - 1))))]
 
+    others = None
+    if world == 1 and not args.no_others:
+        others = other_workloads(args, world, rank, local, dist)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -1846,9 +1882,9 @@ def main():
         "plain": {"value": plain_rate, "unit": UNIT, "ops": P,
                   "path": "shg_ct_tensor + shg_relin_apply per ciphertext"},
         "batched_over_plain": value / world / plain_rate,
-        "bit_exact_batched_vs_plain": bit_exact,
+        "bit_exact_batched_vs_plain": bit_exact, "bit_exact_checked_cts": check_cts,
         "e2e": e2e, "e2e_wire": e2e_wire, "roofline": roofline, "ntt": ntt,
-        "cpu_baseline": cpu,
+        "other_workloads": others, "cpu_baseline": cpu,
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clk,
     }
