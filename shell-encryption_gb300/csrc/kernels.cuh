@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -120,13 +122,16 @@ extern std::atomic<bool> g_prof_on;
 extern std::mutex g_prof_mu;
 extern std::vector<ProfEntry> g_prof_pending;
 
-// Counts every launch; with profiling on, brackets it with CUDA events on the
-// launch stream (these also work inside stream capture).
+// Counts every launch and names it as an NVTX range (visible in Nsight
+// timelines; a no-op without an attached tool); with profiling on, brackets
+// it with CUDA events on the launch stream (these also work inside stream
+// capture).
 struct LaunchScope {
   const char* name;
   cudaStream_t s;
   cudaEvent_t a = nullptr, b = nullptr;
   LaunchScope(const char* n, cudaStream_t st) : name(n), s(st) {
+    nvtxRangePushA(n);
     g_launch_count++;
     if (g_prof_on.load()) {
       cudaEventCreate(&a);
@@ -135,6 +140,7 @@ struct LaunchScope {
     }
   }
   ~LaunchScope() {
+    nvtxRangePop();
     if (a) {
       cudaEventRecord(b, s);
       std::lock_guard<std::mutex> lock(g_prof_mu);
