@@ -700,26 +700,27 @@ __global__ void __maxnreg__(56)
   }
 }
 
-// Rows (warps) per CTA of k4_ks_rows_warp.
+// Rows (warps) per CTA of k4_ks_rows_warp, and digits each warp transforms
+// together (1, 2, 3, 4, 6 digits: 57.2, 60.8, 62.3, 62.6, 62.2 k ct-mult+relin/s).
 constexpr int kKsWarpRows = 4;
+constexpr int kKsWarpDigits = 3;
 
 // The key switch's row phase with one warp per row of one (ciphertext,
-// limb): its 32 threads run that row of every digit transform in turn (4
-// values per thread, NttCore<7, 2>: four passes, exchanges in the warp's own
-// swizzled shared tile with warp-level synchronisation only) and keep the key
-// inner product of their 4 consecutive output slots in registers (two
-// components, 128-bit sums).  The digit values are never parked, no CTA-wide
-// barrier is taken, and key rows and the base are read 16 bytes at a time.
-// For a chunk covering every digit (chunk >= k), as lazily reduced digits of
-// primes below 2^58 give at up to a few dozen digits.  W rows (warps) per CTA,
-// at least MB CTAs per SM; PF & 1: the next digit's row is loaded while this
-// one is transformed, PF & 2: this digit's key values are loaded before its
-// transform.  Against k4_ks_rows8 (one row of all digits per CTA, values
-// parked in shared memory, CTA barriers) it runs alone at the same speed but
-// shares the SMs far better with the next chunk's column kernel on the
-// other key-switch stream (ct-mult+relin 53.4 k -> 56.1 k/s with W = 4,
-// MB = 5, PF = 3).
-template <int LOG_N, bool LAZY, int W, int MB, int PF>
+// limb): its 32 threads run that row of every digit transform (4 values per
+// thread, NttCore<7, 2>: four passes, exchanges in the warp's own swizzled
+// shared tiles with warp-level synchronisation only), DPI digits at a time,
+// and keep the key inner product of their 4 consecutive output slots in
+// registers (two components, 128-bit sums).  The digit values are never
+// parked, no CTA-wide barrier is taken, each digit's key values are loaded
+// before its transform, and key rows and the base are read 16 bytes at a
+// time.  For a chunk covering every digit (chunk >= k), as lazily reduced
+// digits of primes below 2^58 give at up to a few dozen digits.  W rows
+// (warps) per CTA, at least MB CTAs per SM.  Against k4_ks_rows8 (one row of
+// all digits per CTA, values parked in shared memory, CTA barriers) it shares
+// the SMs far better with the next chunk's column kernel on the other
+// key-switch stream (ct-mult+relin 53.4 k -> 56.1 k/s one digit at a time,
+// 62.3 k/s three at a time).
+template <int LOG_N, bool LAZY, int W, int MB, int DPI>
 __global__ void __launch_bounds__(32 * W, MB)
     k4_ks_rows_warp(const uint64_t* buf, int k, const uint64_t* kb, const uint64_t* ka,
                     uint64_t* out, const uint64_t* base, size_t base_ct_elems, CtMap map,
@@ -745,7 +746,7 @@ __global__ void __launch_bounds__(32 * W, MB)
   const size_t n = (size_t)1 << LOG_N, Ln = (size_t)L * n;
   const Tw* tw0 = c.tw_fwd + ((size_t)l << LOG_N);
   const int tm = (1 << S::A) + row;
-  const typename C::SwzMap m{smem + ((size_t)warp << S::B)};
+  const typename C::SwzMap m{smem + ((size_t)warp * DPI << S::B)};
   // this thread's output slots after the last pass: 4 consecutive positions
   const int pos0 = (row << S::B) | C::fwd_out_idx(tid, 0);
   const size_t kr0 = (size_t)l * n + pos0;
@@ -753,61 +754,65 @@ __global__ void __launch_bounds__(32 * W, MB)
   uint64_t lo0[4], hi0[4], lo1[4], hi1[4];
 #pragma unroll
   for (int e = 0; e < 4; ++e) lo0[e] = hi0[e] = lo1[e] = hi1[e] = 0;
-  uint64_t xn[4];
-  if constexpr (PF & 1) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) xn[e] = src[C::fwd_in_idx(tid, e)];
-  }
-#pragma unroll 1
-  for (int j = 0; j < k; ++j, src += Ln) {
-    // The twiddles are the same for every digit; reloading them per digit
-    // (L1 hits) keeps the compiler from holding all of them in registers.
+  // DPI digits at a time, interleaved: their transforms use the same
+  // twiddles and tile offsets (tile d at d KB above the first), so the index
+  // work is shared and each level has DPI times the independent butterflies;
+  // the last k mod DPI digits go one by one.
+  auto digits = [&](int j, auto dn) {
+    constexpr int D = decltype(dn)::value;
     const Tw* tw;
     asm volatile("mov.b64 %0, %1;" : "=l"(tw) : "l"(tw0));
-    uint64_t x[4];
-    if constexpr (PF & 1) {
+    uint64_t x[D][4];
+    ulonglong2 kv[D][4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) x[e] = xn[e];
-      if (j + 1 < k) {
+    for (int d = 0; d < D; ++d) {
+      const uint64_t* sd = src + (size_t)(j + d) * Ln;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) xn[e] = src[Ln + C::fwd_in_idx(tid, e)];
-      }
-    } else {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) x[e] = src[C::fwd_in_idx(tid, e)];
-    }
-    ulonglong2 kv[4];
-    const ulonglong2* b2 = reinterpret_cast<const ulonglong2*>(kb + kr0 + (size_t)j * Ln);
-    const ulonglong2* a2 = reinterpret_cast<const ulonglong2*>(ka + kr0 + (size_t)j * Ln);
-    if constexpr (PF & 2) {
-      kv[0] = __ldg(b2);
-      kv[1] = __ldg(b2 + 1);
-      kv[2] = __ldg(a2);
-      kv[3] = __ldg(a2 + 1);
+      for (int e = 0; e < 4; ++e) x[d][e] = sd[C::fwd_in_idx(tid, e)];
+      const ulonglong2* b2 = reinterpret_cast<const ulonglong2*>(kb + kr0 + (size_t)(j + d) * Ln);
+      const ulonglong2* a2 = reinterpret_cast<const ulonglong2*>(ka + kr0 + (size_t)(j + d) * Ln);
+      kv[d][0] = __ldg(b2);
+      kv[d][1] = __ldg(b2 + 1);
+      kv[d][2] = __ldg(a2);
+      kv[d][3] = __ldg(a2 + 1);
     }
     static_for<0, C::P>([&](auto pp) {
       constexpr int ps = decltype(pp)::value;
-      C::template fwd_pass<ps, LAZY>(x, tid, tw, tm, q, two_q);
+#pragma unroll
+      for (int d = 0; d < D; ++d) C::template fwd_pass<ps, LAZY>(x[d], tid, tw, tm, q, two_q);
       if constexpr (ps + 1 < C::P) {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) m(C::idx(tid, e, C::fwd_clo(ps))) = x[e];
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) (&m(C::idx(tid, e, C::fwd_clo(ps))))[d << S::B] = x[d][e];
         __syncwarp();
 #pragma unroll
-        for (int e = 0; e < 4; ++e) x[e] = m(C::idx(tid, e, C::fwd_clo(ps + 1)));
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) x[d][e] = (&m(C::idx(tid, e, C::fwd_clo(ps + 1))))[d << S::B];
         __syncwarp();  // every read is done before the tile is rewritten
       }
     });
-    if constexpr (!LAZY) finish_fwd<LAZY>(x, q, two_q, P->barrett);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const ulonglong2 vb = (PF & 2) ? kv[h] : __ldg(b2 + h);
-      const ulonglong2 va = (PF & 2) ? kv[2 + h] : __ldg(a2 + h);
-      mac128(lo0[2 * h], hi0[2 * h], x[2 * h], vb.x);
-      mac128(lo0[2 * h + 1], hi0[2 * h + 1], x[2 * h + 1], vb.y);
-      mac128(lo1[2 * h], hi1[2 * h], x[2 * h], va.x);
-      mac128(lo1[2 * h + 1], hi1[2 * h + 1], x[2 * h + 1], va.y);
+    for (int d = 0; d < D; ++d) {
+      if constexpr (!LAZY) finish_fwd<LAZY>(x[d], q, two_q, P->barrett);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const ulonglong2 vb = kv[d][h], va = kv[d][2 + h];
+        mac128(lo0[2 * h], hi0[2 * h], x[d][2 * h], vb.x);
+        mac128(lo0[2 * h + 1], hi0[2 * h + 1], x[d][2 * h + 1], vb.y);
+        mac128(lo1[2 * h], hi1[2 * h], x[d][2 * h], va.x);
+        mac128(lo1[2 * h + 1], hi1[2 * h + 1], x[d][2 * h + 1], va.y);
+      }
     }
+  };
+  int j = 0;
+  if constexpr (DPI > 1) {
+#pragma unroll 1
+    for (; j + DPI <= k; j += DPI) digits(j, std::integral_constant<int, DPI>{});
   }
+#pragma unroll 1
+  for (; j < k; ++j) digits(j, std::integral_constant<int, 1>{});
   const uint64_t qinv = P->inv_modulus;
   const uint64_t* bp = base + map(p) * base_ct_elems + (size_t)l * n;
   uint64_t* o0 = out + p * 2 * Ln + kr0;
@@ -1075,9 +1080,9 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
                                         2LL * 5 * c.sms)) {
 #define F(LN)                                                                   \
   {                                                                             \
-    auto kern = c.small_q ? k4_ks_rows_warp<LN, true, kKsWarpRows, 5, 3>        \
-                          : k4_ks_rows_warp<LN, false, kKsWarpRows, 5, 3>;      \
-    const int smem = kKsWarpRows * 128 * 8;                                     \
+    auto kern = c.small_q ? k4_ks_rows_warp<LN, true, kKsWarpRows, 4, kKsWarpDigits>   \
+                          : k4_ks_rows_warp<LN, false, kKsWarpRows, 4, kKsWarpDigits>; \
+    const int smem = kKsWarpRows * kKsWarpDigits * 128 * 8;                     \
     set_smem4(kern, smem);                                                      \
     kern<<<count * L * ((1 << (LN - 7)) / kKsWarpRows), 32 * kKsWarpRows, smem, s>>>( \
         D, k, kb, ka, out, base, base_ct_elems, map, base1_zero, subst_power, L, kt, c); \
