@@ -3,6 +3,8 @@
 // produced) and a sink policy (where its outputs go); see ntt4.cuh.
 #include "ntt4.cuh"
 
+#include <cstdlib>
+
 namespace shg {
 namespace {
 
@@ -850,6 +852,134 @@ __global__ void __launch_bounds__(32 * W, MB)
   }
 }
 
+// Row phases with one warp per row of DPI transforms that share a prime
+// (same twiddles; 4 values per thread per transform, NttCore<7, 2>, four
+// passes exchanged through the warp's own swizzled tiles with warp-level
+// synchronisation only).  A thread's 4 values are consecutive at the
+// forward phase's end and the inverse phase's start, so the sink and source
+// move 16-byte pairs and every warp access covers whole rows.  Work item w =
+// blockIdx.x * W + warp: row w mod 2^A of the group of DPI transforms
+// (w / 2^A) -- prime class first, as in k4_fwd_rows.
+template <int LOG_N, bool LAZY, class Dst, int W, int DPI>
+__global__ void __launch_bounds__(32 * W)
+    k4_fwd_rows_warp(const uint64_t* buf, Dst dst, PrimeMap pm, int num, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = NttCore<S::B, 2>;
+  static_assert(C::T == 32 && C::E == 4 && C::P == 4, "32 threads x 4 values per row");
+  extern __shared__ uint64_t smem[];
+  constexpr int rows = 1 << S::A;
+  const int warp = threadIdx.x >> 5, tid = threadIdx.x & 31;
+  const int w = blockIdx.x * W + warp;
+  const int per_class = num / pm.L;
+  const int groups = (per_class + DPI - 1) / DPI;
+  const int row = w % rows;
+  const int cg = w / rows;
+  const int l = dbg_index(cg / groups, c.L, kDbgLimb), grp = cg % groups;
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const Tw* tw = c.tw_fwd + ((size_t)l << LOG_N);
+  const int tm = (1 << S::A) + row;
+  const typename C::SwzMap m{smem + ((size_t)warp * DPI << S::B)};
+  const int pos0 = (row << S::B) | C::fwd_out_idx(tid, 0);
+  uint64_t x[DPI][4];
+  int g[DPI];
+#pragma unroll
+  for (int d = 0; d < DPI; ++d) {
+    const int mm = min(grp * DPI + d, per_class - 1);
+    g[d] = l + pm.L * mm;
+    if (grp * DPI + d < per_class) dst.prefetch(g[d], l, pos0);
+    const uint64_t* src = buf + ((size_t)g[d] << LOG_N) + ((size_t)row << S::B);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) x[d][e] = src[C::fwd_in_idx(tid, e)];
+  }
+  static_for<0, C::P>([&](auto pp) {
+    constexpr int ps = decltype(pp)::value;
+#pragma unroll
+    for (int d = 0; d < DPI; ++d) C::template fwd_pass<ps, LAZY>(x[d], tid, tw, tm, q, two_q);
+    if constexpr (ps + 1 < C::P) {
+#pragma unroll
+      for (int d = 0; d < DPI; ++d)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) (&m(C::idx(tid, e, C::fwd_clo(ps))))[d << S::B] = x[d][e];
+      __syncwarp();
+#pragma unroll
+      for (int d = 0; d < DPI; ++d)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) x[d][e] = (&m(C::idx(tid, e, C::fwd_clo(ps + 1))))[d << S::B];
+      __syncwarp();
+    }
+  });
+#pragma unroll
+  for (int d = 0; d < DPI; ++d) {
+    if constexpr (!(LAZY && Dst::kTakesLazy)) finish_fwd<LAZY>(x[d], q, two_q, P->barrett);
+    if (grp * DPI + d < per_class) {
+      const auto h = dst.bind(g[d], l, c);
+      h.pair(pos0, x[d][0], x[d][1]);
+      h.pair(pos0 + 2, x[d][2], x[d][3]);
+    }
+  }
+}
+
+template <int LOG_N, bool WIDE, class Src, int W, int DPI>
+__global__ void __launch_bounds__(32 * W)
+    k4_inv_rows_warp(Src src, PrimeMap pm, uint64_t* buf, int num, CtxDev c) {
+  using S = Ntt4<LOG_N>;
+  using C = NttCore<S::B, 2>;
+  static_assert(C::T == 32 && C::E == 4 && C::P == 4, "32 threads x 4 values per row");
+  extern __shared__ uint64_t smem[];
+  constexpr int rows = 1 << S::A;
+  const int warp = threadIdx.x >> 5, tid = threadIdx.x & 31;
+  const int w = blockIdx.x * W + warp;
+  const int groups = (num + DPI - 1) / DPI;
+  const int row = w % rows;
+  const int grp = w / rows;
+  const typename C::SwzMap m{smem + ((size_t)warp * DPI << S::B)};
+  const int pos0 = (row << S::B) | C::inv_in_idx(tid, 0);
+  // transforms g = grp * DPI + d (clamped; the clamped ones are not stored);
+  // they need not share a prime, so each keeps its own constants
+  uint64_t x[DPI][4];
+  int g[DPI], l[DPI];
+#pragma unroll
+  for (int d = 0; d < DPI; ++d) {
+    g[d] = min(grp * DPI + d, num - 1);
+    l[d] = dbg_index(pm(g[d]), c.L, kDbgLimb);
+    const auto h = src.bind(g[d], l[d], c);
+    const ulonglong2 v0 = h.pair(pos0), v1 = h.pair(pos0 + 2);
+    x[d][0] = v0.x;
+    x[d][1] = v0.y;
+    x[d][2] = v1.x;
+    x[d][3] = v1.y;
+  }
+  static_for<0, C::P>([&](auto pp) {
+    constexpr int ps = decltype(pp)::value;
+#pragma unroll
+    for (int d = 0; d < DPI; ++d) {
+      const PrimeDev* P = c.primes + l[d];
+      C::template inv_pass<ps, WIDE>(x[d], tid, c.tw_inv + ((size_t)l[d] << LOG_N), S::N, 0, row,
+                                     P->q, P->two_q);
+    }
+    if constexpr (ps + 1 < C::P) {
+#pragma unroll
+      for (int d = 0; d < DPI; ++d)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) (&m(C::idx(tid, e, C::inv_clo(ps))))[d << S::B] = x[d][e];
+      __syncwarp();
+#pragma unroll
+      for (int d = 0; d < DPI; ++d)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) x[d][e] = (&m(C::idx(tid, e, C::inv_clo(ps + 1))))[d << S::B];
+      __syncwarp();
+    }
+  });
+#pragma unroll
+  for (int d = 0; d < DPI; ++d) {
+    if (grp * DPI + d >= num) continue;
+    uint64_t* dstp = buf + ((size_t)g[d] << LOG_N) + ((size_t)row << S::B);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) dstp[C::inv_out_idx(tid, e)] = x[d][e];
+  }
+}
+
 template <int LOG_N, bool WIDE, class Src>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::ROW_THREADS)
     k4_inv_rows(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
@@ -927,10 +1057,32 @@ int row_blocks(int num, PrimeMap pm) {
   return pm.L * groups * (1 << S::A);
 }
 
+int rows_warp_env() {
+  static const int v = [] {
+    const char* e = getenv("SHG_ROWS_WARP");
+    return e ? atoi(e) : 0;
+  }();
+  return v;
+}
+
 template <int LOG_N, class Src, class Dst>
 void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s) {
   using S = Ntt4<LOG_N>;
+  const int rw = rows_warp_env();
+  if (rw) {
+    constexpr int W = 4, DPI = 3;
+    const int groups = (num / pm.L + DPI - 1) / DPI;
+    const int blocks = pm.L * groups * (1 << S::A) / W;
+    auto k1 = c.small_q ? k4_fwd_cols<LOG_N, true, Src> : k4_fwd_cols<LOG_N, false, Src>;
+    auto k2 = c.small_q ? k4_fwd_rows_warp<LOG_N, true, Dst, W, DPI>
+                        : k4_fwd_rows_warp<LOG_N, false, Dst, W, DPI>;
+    set_smem4(k1, S::COL_SMEM);
+    set_smem4(k2, W * DPI * (1 << S::B) * 8);
+    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
+    k2<<<blocks, 32 * W, W * DPI * (1 << S::B) * 8, s>>>(buf, dst, pm, num, c);
+    return;
+  }
   if (c.small_q) {
     auto k1 = k4_fwd_cols<LOG_N, true, Src>;
     auto k2 = k4_fwd_rows<LOG_N, true, Dst>;
@@ -954,11 +1106,20 @@ template <int LOG_N, class Src, class Dst>
 void inv4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s) {
   using S = Ntt4<LOG_N>;
-  auto k1 = c.small_q ? k4_inv_rows<LOG_N, true, Src> : k4_inv_rows<LOG_N, false, Src>;
   auto k2 = c.small_q ? k4_inv_cols<LOG_N, true, Dst> : k4_inv_cols<LOG_N, false, Dst>;
-  set_smem4(k1, S::ROW_SMEM);
   set_smem4(k2, S::COL_SMEM);
-  k1<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(src, pm, buf, c);
+  if (rows_warp_env()) {
+    constexpr int W = 4, DPI = 3;
+    const int groups = (num + DPI - 1) / DPI;
+    auto k1 = c.small_q ? k4_inv_rows_warp<LOG_N, true, Src, W, DPI>
+                        : k4_inv_rows_warp<LOG_N, false, Src, W, DPI>;
+    set_smem4(k1, W * DPI * (1 << S::B) * 8);
+    k1<<<groups * (1 << S::A) / W, 32 * W, W * DPI * (1 << S::B) * 8, s>>>(src, pm, buf, num, c);
+  } else {
+    auto k1 = c.small_q ? k4_inv_rows<LOG_N, true, Src> : k4_inv_rows<LOG_N, false, Src>;
+    set_smem4(k1, S::ROW_SMEM);
+    k1<<<num * S::ROW_TILES, S::ROW_THREADS, S::ROW_SMEM, s>>>(src, pm, buf, c);
+  }
   k2<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(buf, dst, pm, c);
 }
 
