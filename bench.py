@@ -1537,6 +1537,8 @@ def main():
                     help="e2e host pipeline: ciphertexts per piece (0: library default)")
     ap.add_argument("--host-slots", type=int, default=0,
                     help="e2e host pipeline: staging slots in flight (0: library default)")
+    ap.add_argument("--host-ramp", type=int, default=-1,
+                    help="e2e host pipeline: piece ramp (-1: library default)")
     ap.add_argument("--hbm-budget-gb", type=int, default=32)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="ct-mult-relin",
@@ -1626,8 +1628,10 @@ def main():
     if args.ks_unfused:
         sg.check(lib.shg_context_set_ks_fused(ctx.h, 0))
     if args.host_piece or args.host_slots:
-        sg.check(lib.shg_context_set_host_pipeline(ctx.h, args.host_piece or 128,
+        sg.check(lib.shg_context_set_host_pipeline(ctx.h, args.host_piece or 32,
                                                    args.host_slots or 4))
+    if args.host_ramp >= 0:
+        sg.check(lib.shg_context_set_host_ramp(ctx.h, args.host_ramp))
     k = 18
     kb = splitmix_limbs(1000 + rank, k, QS, n)
     ka = splitmix_limbs(2000 + rank, k, QS, n)

@@ -83,9 +83,14 @@ int shg_debug_status(unsigned* first_failure);
  * other's tail; 1 = the caller's stream only, e.g. to time kernels one at a
  * time).  Each lane holds its own chunk of digit scratch. */
 int shg_context_set_ks_lanes(shg_context* ctx, int lanes);
-/* shg_bgv_mul_relin_host pipeline shape: ciphertexts per piece (default 128)
+/* shg_bgv_mul_relin_host pipeline shape: ciphertexts per piece (default 32)
  * and device staging slots in flight (default 4, at most 8). */
 int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots);
+/* shg_bgv_mul_relin_host piece ramp: with ramp r > 0 the first and last
+ * pieces hold piece_cts >> r ciphertexts, doubling towards the middle, so the
+ * pipeline fills and drains in short steps; 0 = every piece full (default 2,
+ * at most 16). */
+int shg_context_set_host_ramp(shg_context* ctx, int ramp);
 /* Current values of the three settings above (chunk 0 = default). */
 int shg_context_get_tuning(const shg_context* ctx, int* chunk_cts, int* four_step_min,
                            int* ks_fused);

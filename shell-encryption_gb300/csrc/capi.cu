@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -182,8 +183,11 @@ struct shg_context {
                       // for every operation from n = 2^13; mixed at 2^12)
   int ks_fused = 1;   // fused digit row phase + key inner product
   int ks_lanes = 2;      // streams the batched key-switch chunks rotate over (1..4)
-  int host_piece = 128;  // host pipeline: ciphertexts per piece
-  int host_slots = 4;    // host pipeline: device staging slots in flight
+  // Host pipeline shape, measured fastest on a GB300 for 1024 pairs at
+  // n = 2^14, L = 6 (18.2 ms against 22.3 ms with fixed pieces of 128):
+  int host_piece = 32;  // ciphertexts per piece
+  int host_slots = 4;   // device staging slots in flight
+  int host_ramp = 2;    // first/last pieces start at piece >> ramp (0: none)
   std::mutex mu;
   // Host-buffer pipeline: device staging slots and three streams.
   uint64_t* io = nullptr;
@@ -195,6 +199,8 @@ struct shg_context {
   cudaStream_t ks_side[kMaxKsLanes - 1] = {};
   cudaEvent_t ks_fork = nullptr;
   cudaEvent_t ks_join[kMaxKsLanes - 1] = {};
+  // Key-switch lanes of the host-buffer pipeline.
+  cudaStream_t io_lanes[kMaxKsLanes] = {};
   std::mutex io_mu;
 
   CtxDev dev() const {
@@ -535,6 +541,8 @@ void shg_context_destroy(shg_context* ctx) {
   cudaFree(ctx->ws);
   cudaFree(ctx->io);
   for (cudaStream_t s : ctx->io_streams)
+    if (s) cudaStreamDestroy(s);
+  for (cudaStream_t s : ctx->io_lanes)
     if (s) cudaStreamDestroy(s);
   for (int i = 0; i < shg_context::kMaxKsLanes - 1; ++i) {
     if (ctx->ks_side[i]) cudaStreamDestroy(ctx->ks_side[i]);
@@ -1145,13 +1153,25 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
   const uint8_t* b = static_cast<const uint8_t*>(b_v);
   uint8_t* out = static_cast<uint8_t*>(out_v);
   // Pieces of host_piece ciphertexts through host_slots staging slots of
-  // (a, b, out) plus, when wire, their packed forms; a and b come in on two
-  // copy streams.
+  // (a, b, out, exported degree-2 component) plus, when wire, their packed
+  // forms; a and b come in on two copy streams.  The compute stream runs each
+  // piece's tensor product and export; the piece's key-switch chunks go to
+  // the pipeline's own lanes (chunks rotate over them across pieces), so the
+  // next piece's tensor product starts while the lanes still work, and a
+  // piece's copy-out waits for the lanes that ran its chunks.
+  const int L = key->L, k = key->k;
+  const size_t Ln = (size_t)L * ctx->n;
   const int P = std::min(count, ctx->host_piece);
   const int S = ctx->host_slots;
   const size_t packed = wire ? 3 * (size_t)P * host_ct_pad : 0;
-  const size_t slot = 3 * (size_t)P * ct_bytes + packed;
+  const size_t slot = 3 * (size_t)P * ct_bytes + (size_t)P * Ln * sizeof(uint64_t) + packed;
+  const size_t d_per_ct = (size_t)k * Ln * sizeof(uint64_t);
+  int C = ctx->chunk_cts > 0 ? ctx->chunk_cts
+                             : (int)std::max<size_t>(1, ((size_t)256 << 20) / d_per_ct);
+  C = std::max(1, std::min({C, 16, P}));
+  const int lanes = std::max(1, std::min(ctx->ks_lanes, (int)shg_context::kMaxKsLanes));
   std::lock_guard<std::mutex> io_lock(ctx->io_mu);
+  std::lock_guard<std::mutex> lock(ctx->mu);
   if (ctx->io_bytes < S * slot) {
     SHG_CUDA(cudaDeviceSynchronize());
     cudaFree(ctx->io);
@@ -1164,40 +1184,73 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
     }
     ctx->io_bytes = S * slot;
   }
+  if ((st = ctx->ensure_ws((size_t)lanes * C * d_per_ct))) return st;
+  uint64_t* D0 = ctx->ws;
   for (cudaStream_t& s : ctx->io_streams)
     if (!s) SHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  for (int i = 0; i < lanes; ++i)
+    if (!ctx->io_lanes[i]) SHG_CUDA(cudaStreamCreateWithFlags(&ctx->io_lanes[i], cudaStreamNonBlocking));
   cudaStream_t s_in = ctx->io_streams[0], s_comp = ctx->io_streams[1],
                s_out = ctx->io_streams[2], s_in2 = ctx->io_streams[3];
   cudaStream_t user = (cudaStream_t)stream;
-  const int pieces = (count + P - 1) / P;
+  // Piece schedule: full pieces of P in the middle; when ramping, the
+  // pipeline fills and drains through pieces of P >> ramp, doubling, at both
+  // ends, so the first copy-in and the last compute + copy-out are short.
+  std::vector<int> sizes;
+  {
+    const int ramp = ctx->host_ramp;
+    std::vector<int> back;
+    int rem = count;
+    for (int r = 0; rem > 0; ++r) {
+      const int sz = ramp ? std::min(P, std::max(1, P >> ramp) << std::min(r, 20)) : P;
+      const int f = std::min(sz, rem);
+      sizes.push_back(f);
+      rem -= f;
+      if (rem == 0 || !ramp) continue;
+      const int bk = std::min(sz, rem);
+      back.push_back(bk);
+      rem -= bk;
+    }
+    sizes.insert(sizes.end(), back.rbegin(), back.rend());
+  }
+  const int pieces = (int)sizes.size();
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaEvent_t* e) -> int {
     SHG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     evs.push_back(*e);
     return SHG_OK;
   };
+  auto release = [&] {
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+  };
   cudaEvent_t start;
   if ((st = event(&start))) return st;
   SHG_CUDA(cudaEventRecord(start, user));
   SHG_CUDA(cudaStreamWaitEvent(s_in, start, 0));
   SHG_CUDA(cudaStreamWaitEvent(s_in2, start, 0));
-  std::vector<cudaEvent_t> loaded(pieces), loaded2(pieces), computed(pieces), stored(pieces);
-  for (int i = 0; i < pieces; ++i) {
-    if ((st = event(&loaded[i])) || (st = event(&loaded2[i])) || (st = event(&computed[i])) ||
-        (st = event(&stored[i])))
+  std::vector<cudaEvent_t> loaded(pieces), loaded2(pieces), tensored(pieces), stored(pieces);
+  for (int i = 0; i < pieces && st == SHG_OK; ++i) {
+    if ((st = event(&loaded[i])) || (st = event(&loaded2[i])) || (st = event(&tensored[i])))
       break;
+    st = event(&stored[i]);
   }
-  int rc = st;
-  for (int i = 0; i < pieces && rc == SHG_OK; ++i) {
-    const int c0 = i * P, cc = std::min(P, count - c0);
+  if (st) {
+    release();
+    return st;
+  }
+  const CtxDev dv = ctx->dev();
+  int c0 = 0, chunk_no = 0;
+  for (int i = 0; i < pieces; c0 += sizes[i], ++i) {
+    const int cc = sizes[i];
     uint64_t* da = ctx->io + (size_t)(i % S) * (slot / sizeof(uint64_t));
     uint64_t* db = da + (size_t)P * ct_elems;
     uint64_t* dout = db + (size_t)P * ct_elems;
-    uint8_t* pa = reinterpret_cast<uint8_t*>(dout + (size_t)P * ct_elems);
+    uint64_t* dx = dout + (size_t)P * ct_elems;
+    uint8_t* pa = reinterpret_cast<uint8_t*>(dx + (size_t)P * Ln);
     uint8_t* pb = pa + (size_t)P * host_ct_pad;
     uint8_t* pout = pb + (size_t)P * host_ct_pad;
-    // Slot reuse: piece i-S must have been copied back (its compute also
-    // finished reading a, b before that).
+    // Slot reuse: piece i-S must have been copied back (its tensor product
+    // and key switch finished reading the slot before that).
     if (i >= S) {
       SHG_CUDA(cudaStreamWaitEvent(s_in, stored[i - S], 0));
       SHG_CUDA(cudaStreamWaitEvent(s_in2, stored[i - S], 0));
@@ -1219,27 +1272,45 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
     SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded[i], 0));
     SHG_CUDA(cudaStreamWaitEvent(s_comp, loaded2[i], 0));
     if (wire) {
-      shg::launch_deserialize(ctx->dev(), da, pa, lay, 2 * cc, key->L, s_comp);
-      shg::launch_deserialize(ctx->dev(), db, pb, lay, 2 * cc, key->L, s_comp);
+      shg::launch_deserialize(dv, da, pa, lay, 2 * cc, L, s_comp);
+      shg::launch_deserialize(dv, db, pb, lay, 2 * cc, L, s_comp);
     }
-    rc = shg_bgv_mul_relin(ctx, key, dout, da, db, cc, (shg_stream)s_comp);
-    if (rc) break;
-    if (wire) shg::launch_serialize(ctx->dev(), pout, dout, lay, 2 * cc, key->L, s_comp);
-    SHG_CUDA(cudaEventRecord(computed[i], s_comp));
-    SHG_CUDA(cudaStreamWaitEvent(s_out, computed[i], 0));
-    if (wire)
+    shg::launch_tensor_intt(dv, dout, dx, da, db, cc, L, s_comp);
+    SHG_CUDA(cudaEventRecord(tensored[i], s_comp));
+    bool used[shg_context::kMaxKsLanes] = {};
+    for (int j = 0; j < cc; j += C, ++chunk_no) {
+      const int lane = chunk_no % lanes, nc = std::min(C, cc - j);
+      cudaStream_t ls = ctx->io_lanes[lane];
+      if (!used[lane]) SHG_CUDA(cudaStreamWaitEvent(ls, tensored[i], 0));
+      used[lane] = true;
+      uint64_t* o = dout + (size_t)j * 2 * Ln;
+      shg::launch_keyswitch(dv, D0 + (size_t)lane * C * k * Ln, dx + (size_t)j * Ln,
+                            key->d_digits, k, key->digit_flags, key->chunk, key->chunk_lazy,
+                            key->kb, key->ka, o, o, 2 * Ln, CtMap::identity(), 0, 0, nc, L, ls,
+                            shg::KeyTable{});
+    }
+    for (int lane = 0; lane < lanes; ++lane) {
+      if (!used[lane]) continue;
+      cudaEvent_t done;
+      if ((st = event(&done))) break;
+      SHG_CUDA(cudaEventRecord(done, ctx->io_lanes[lane]));
+      SHG_CUDA(cudaStreamWaitEvent(s_out, done, 0));
+    }
+    if (st) break;
+    if (wire) {
+      shg::launch_serialize(dv, pout, dout, lay, 2 * cc, L, s_out);
       SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * host_ct, pout, cc * host_ct,
                                cudaMemcpyDeviceToHost, s_out));
-    else
+    } else {
       SHG_CUDA(cudaMemcpyAsync(out + (size_t)c0 * ct_bytes, dout, cc * ct_bytes,
                                cudaMemcpyDeviceToHost, s_out));
+    }
     SHG_CUDA(cudaEventRecord(stored[i], s_out));
   }
-  if (rc == SHG_OK) {
-    SHG_CUDA(cudaStreamWaitEvent(user, stored[pieces - 1], 0));
-  }
-  for (cudaEvent_t e : evs) cudaEventDestroy(e);
-  return rc;
+  if (st == SHG_OK) st = launch_status("bgv_mul_relin_host");
+  if (st == SHG_OK) SHG_CUDA(cudaStreamWaitEvent(user, stored[pieces - 1], 0));
+  release();
+  return st;
 }
 }  // namespace
 
@@ -1920,6 +1991,13 @@ int shg_context_set_host_pipeline(shg_context* ctx, int piece_cts, int slots) {
     return fail(SHG_INVALID_ARGUMENT, "piece must be positive and slots in [2, 8]");
   ctx->host_piece = piece_cts;
   ctx->host_slots = slots;
+  return SHG_OK;
+}
+
+int shg_context_set_host_ramp(shg_context* ctx, int ramp) {
+  if (!ctx || ramp < 0 || ramp > 16)
+    return fail(SHG_INVALID_ARGUMENT, "ramp must be in [0, 16]");
+  ctx->host_ramp = ramp;
   return SHG_OK;
 }
 int shg_context_get_tuning(const shg_context* ctx, int* chunk, int* four_step_min,

@@ -88,8 +88,8 @@ __device__ __forceinline__ void finish_forward(uint64_t (&x)[E], uint64_t q,
 // --------------------------------------------------------------------------
 
 template <int LOG_N, bool LAZY>
-__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
-    k_ntt_fwd(const uint64_t* in, uint64_t* out, int num, int L, CtxDev c) {
+__device__ __forceinline__ void ntt_fwd_body(const uint64_t* in, uint64_t* out, int num, int L,
+                                             const CtxDev& c) {
   using C = NttCore<LOG_N>;
   using G = Cfg<LOG_N>;
   extern __shared__ uint64_t smem[];
@@ -107,6 +107,15 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
                             c.tw_fwd + (size_t)l * C::N, 1, q, two_q);
   finish_forward<LAZY, C::E>(x, q, two_q, c.primes[l].barrett);
   if (active) store_contig(out + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
+}
+
+// The body stays a separate inlined function: written directly in the kernel
+// the same code measured 7 % slower at n = 2^12 (a different register
+// allocation).
+template <int LOG_N, bool LAZY>
+__global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
+    k_ntt_fwd(const uint64_t* in, uint64_t* out, int num, int L, CtxDev c) {
+  ntt_fwd_body<LOG_N, LAZY>(in, out, num, L, c);
 }
 
 // scale_mode: 0 -> x n^{-1}; 1 -> x n^{-1} 2^-64 (iNTT fused with ExportInt);

@@ -3,7 +3,7 @@
 // produced) and a sink policy (where its outputs go); see ntt4.cuh.
 #include "ntt4.cuh"
 
-#include <cstdlib>
+#include <type_traits>
 
 namespace shg {
 namespace {
@@ -866,6 +866,7 @@ __global__ void __launch_bounds__(32 * W)
   using S = Ntt4<LOG_N>;
   using C = NttCore<S::B, 2>;
   static_assert(C::T == 32 && C::E == 4 && C::P == 4, "32 threads x 4 values per row");
+  static_assert((1 << S::A) % W == 0, "whole CTAs of rows");
   extern __shared__ uint64_t smem[];
   constexpr int rows = 1 << S::A;
   const int warp = threadIdx.x >> 5, tid = threadIdx.x & 31;
@@ -926,24 +927,30 @@ __global__ void __launch_bounds__(32 * W)
   using S = Ntt4<LOG_N>;
   using C = NttCore<S::B, 2>;
   static_assert(C::T == 32 && C::E == 4 && C::P == 4, "32 threads x 4 values per row");
+  static_assert((1 << S::A) % W == 0, "whole CTAs of rows");
   extern __shared__ uint64_t smem[];
   constexpr int rows = 1 << S::A;
   const int warp = threadIdx.x >> 5, tid = threadIdx.x & 31;
   const int w = blockIdx.x * W + warp;
-  const int groups = (num + DPI - 1) / DPI;
+  // transforms g = cls + L m share limb pm(cls) for any PrimeMap (num is a
+  // multiple of L); the warp takes DPI of one class
+  const int per_class = num / pm.L;
+  const int groups = (per_class + DPI - 1) / DPI;
   const int row = w % rows;
-  const int grp = w / rows;
+  const int cg = w / rows;
+  const int cls = cg / groups, grp = cg % groups;
+  const int l = dbg_index(pm(cls), c.L, kDbgLimb);
+  const PrimeDev* P = c.primes + l;
+  const uint64_t q = P->q, two_q = P->two_q;
+  const Tw* tw = c.tw_inv + ((size_t)l << LOG_N);
   const typename C::SwzMap m{smem + ((size_t)warp * DPI << S::B)};
   const int pos0 = (row << S::B) | C::inv_in_idx(tid, 0);
-  // transforms g = grp * DPI + d (clamped; the clamped ones are not stored);
-  // they need not share a prime, so each keeps its own constants
   uint64_t x[DPI][4];
-  int g[DPI], l[DPI];
+  int g[DPI];
 #pragma unroll
   for (int d = 0; d < DPI; ++d) {
-    g[d] = min(grp * DPI + d, num - 1);
-    l[d] = dbg_index(pm(g[d]), c.L, kDbgLimb);
-    const auto h = src.bind(g[d], l[d], c);
+    g[d] = cls + pm.L * min(grp * DPI + d, per_class - 1);
+    const auto h = src.bind(g[d], l, c);
     const ulonglong2 v0 = h.pair(pos0), v1 = h.pair(pos0 + 2);
     x[d][0] = v0.x;
     x[d][1] = v0.y;
@@ -953,11 +960,8 @@ __global__ void __launch_bounds__(32 * W)
   static_for<0, C::P>([&](auto pp) {
     constexpr int ps = decltype(pp)::value;
 #pragma unroll
-    for (int d = 0; d < DPI; ++d) {
-      const PrimeDev* P = c.primes + l[d];
-      C::template inv_pass<ps, WIDE>(x[d], tid, c.tw_inv + ((size_t)l[d] << LOG_N), S::N, 0, row,
-                                     P->q, P->two_q);
-    }
+    for (int d = 0; d < DPI; ++d)
+      C::template inv_pass<ps, WIDE>(x[d], tid, tw, S::N, 0, row, q, two_q);
     if constexpr (ps + 1 < C::P) {
 #pragma unroll
       for (int d = 0; d < DPI; ++d)
@@ -973,7 +977,7 @@ __global__ void __launch_bounds__(32 * W)
   });
 #pragma unroll
   for (int d = 0; d < DPI; ++d) {
-    if (grp * DPI + d >= num) continue;
+    if (grp * DPI + d >= per_class) continue;
     uint64_t* dstp = buf + ((size_t)g[d] << LOG_N) + ((size_t)row << S::B);
 #pragma unroll
     for (int e = 0; e < 4; ++e) dstp[C::inv_out_idx(tid, e)] = x[d][e];
@@ -1057,21 +1061,20 @@ int row_blocks(int num, PrimeMap pm) {
   return pm.L * groups * (1 << S::A);
 }
 
-int rows_warp_env() {
-  static const int v = [] {
-    const char* e = getenv("SHG_ROWS_WARP");
-    return e ? atoi(e) : 0;
-  }();
-  return v;
-}
+// Row-phase choice (measured on a GB300, n = 2^14 and 2^15): the warp-per-row
+// kernels, three transforms of one prime per warp, are 2-3 % faster for the
+// plain sink and for the plain and component sources; the CTA-per-row
+// kernels stay faster for the fused sinks (encryption, ModReduce), whose
+// loads want 32 consecutive pairs per warp access, and for the tensor
+// source.
+constexpr int kRowsWarpW = 4, kRowsWarpDpi = 3;
 
 template <int LOG_N, class Src, class Dst>
 void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s) {
   using S = Ntt4<LOG_N>;
-  const int rw = rows_warp_env();
-  if (rw) {
-    constexpr int W = 4, DPI = 3;
+  if constexpr (std::is_same_v<Dst, FwdDstPlain<LOG_N>>) {
+    constexpr int W = kRowsWarpW, DPI = kRowsWarpDpi;
     const int groups = (num / pm.L + DPI - 1) / DPI;
     const int blocks = pm.L * groups * (1 << S::A) / W;
     auto k1 = c.small_q ? k4_fwd_cols<LOG_N, true, Src> : k4_fwd_cols<LOG_N, false, Src>;
@@ -1081,9 +1084,7 @@ void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
     set_smem4(k2, W * DPI * (1 << S::B) * 8);
     k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
     k2<<<blocks, 32 * W, W * DPI * (1 << S::B) * 8, s>>>(buf, dst, pm, num, c);
-    return;
-  }
-  if (c.small_q) {
+  } else if (c.small_q) {
     auto k1 = k4_fwd_cols<LOG_N, true, Src>;
     auto k2 = k4_fwd_rows<LOG_N, true, Dst>;
     set_smem4(k1, S::COL_SMEM);
@@ -1108,9 +1109,11 @@ void inv4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
   using S = Ntt4<LOG_N>;
   auto k2 = c.small_q ? k4_inv_cols<LOG_N, true, Dst> : k4_inv_cols<LOG_N, false, Dst>;
   set_smem4(k2, S::COL_SMEM);
-  if (rows_warp_env()) {
-    constexpr int W = 4, DPI = 3;
-    const int groups = (num + DPI - 1) / DPI;
+  constexpr bool warp_rows = std::is_same_v<Src, InvSrcPlain<LOG_N>> ||
+                             std::is_same_v<Src, InvSrcComponent<LOG_N>>;
+  if (warp_rows && num % pm.L == 0) {
+    constexpr int W = kRowsWarpW, DPI = kRowsWarpDpi;
+    const int groups = pm.L * ((num / pm.L + DPI - 1) / DPI);
     auto k1 = c.small_q ? k4_inv_rows_warp<LOG_N, true, Src, W, DPI>
                         : k4_inv_rows_warp<LOG_N, false, Src, W, DPI>;
     set_smem4(k1, W * DPI * (1 << S::B) * 8);

@@ -148,6 +148,7 @@ SIGNATURES = {
     "shg_context_set_ks_fused": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_set_ks_lanes": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_set_host_pipeline": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "shg_context_set_host_ramp": (ctypes.c_int, [_vp, ctypes.c_int]),
     "shg_context_get_tuning": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "shg_poly_fill_uniform": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_uint64, _vp]),

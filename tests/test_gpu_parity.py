@@ -690,12 +690,17 @@ def test_serialize_deserialize(sg, oracle, log_n, qs):
     assert np.array_equal(back.download(x.shape), x)
 
 
-@pytest.mark.parametrize("piece,slots", [(2, 2), (64, 4)])
-def test_mul_relin_host_serialized(sg, oracle, piece, slots):
-    """Host ciphertexts in the wire format in, wire format out: equals the
-    oracle's ct-mult+relin serialized like the reference would."""
+@pytest.mark.parametrize("piece,slots,ramp,wire", [(2, 2, 0, True), (64, 4, 0, True),
+                                                   (8, 3, 3, True), (8, 3, 3, False),
+                                                   (4, 2, 2, False)])
+def test_mul_relin_host_pipeline(sg, oracle, piece, slots, ramp, wire):
+    """Host ciphertexts in, host results out, through the piece pipeline
+    (fixed pieces, or ramped: 1, 2, 4 ... ciphertexts at both ends), in the
+    wire format (serialized like the reference) or as limbs: equals the
+    oracle's ct-mult+relin."""
     lib = sg.lib()
-    log_n, qs, log_bs, count = 12, Q50[:3], [20] * 3, 5
+    log_n, qs, log_bs = 12, Q50[:3], [20] * 3
+    count = 13 if ramp else 5
     n, L = 1 << log_n, len(qs)
     rns = oracle.Rns(log_n, qs)
     k = rns.gadget_dim(log_bs)
@@ -710,12 +715,26 @@ def test_mul_relin_host_serialized(sg, oracle, piece, slots):
     want = np.stack([rns.relin(rns.tensor(a[i], b[i]), kb, ka, log_bs) for i in range(count)])
     ctx = sg.Context(log_n, qs)
     sg.check(lib.shg_context_set_host_pipeline(ctx.h, piece, slots))
+    sg.check(lib.shg_context_set_host_ramp(ctx.h, ramp))
     key = sg.Key(ctx, log_bs, 1, kb, ka)
-    sa, sb = ser(a), ser(b)
-    out = np.zeros_like(sa)
-    _run(sg, lib.shg_bgv_mul_relin_host_serialized, ctx.h, key.h, out.ctypes.data,
-         sa.ctypes.data, sb.ctypes.data, count, None)
-    assert np.array_equal(out, ser(want))
+    if wire:
+        sa, sb = ser(a), ser(b)
+        out = np.zeros_like(sa)
+        _run(sg, lib.shg_bgv_mul_relin_host_serialized, ctx.h, key.h, out.ctypes.data,
+             sa.ctypes.data, sb.ctypes.data, count, None)
+        assert np.array_equal(out, ser(want))
+    else:
+        a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+        out = np.zeros_like(a)
+        _run(sg, lib.shg_bgv_mul_relin_host, ctx.h, key.h, out.ctypes.data, a.ctypes.data,
+             b.ctypes.data, count, None)
+        assert np.array_equal(out, want)
+
+
+def test_host_ramp_rejects_out_of_range(sg):
+    ctx = sg.Context(12, Q50[:3])
+    assert sg.lib().shg_context_set_host_ramp(ctx.h, -1) != 0
+    assert sg.lib().shg_context_set_host_ramp(ctx.h, 17) != 0
 
 
 # --------------------------------------------------------------------------
