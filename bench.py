@@ -1712,9 +1712,36 @@ def main():
     sg.check(lib.shg_memcpy_d2h(out_graph.ctypes.data, d_out.ptr, out_graph.nbytes, s))
     sg.check(lib.shg_stream_synchronize(s))
 
+    def link_probe():
+        """Host-link bandwidth now (GB/s): 1.6 GB pinned->device, device->
+        pinned, and both at once on two streams."""
+        nb = B * ct_bytes
+        s2 = ctypes.c_void_p()
+        sg.check(lib.shg_stream_create(ctypes.byref(s2)))
+        a0, a1, b0, b1 = ev(), ev(), ev(), ev()
+        rates = {}
+        for name, h2d, d2h in (("h2d", True, False), ("d2h", False, True), ("duplex", True, True)):
+            sg.check(lib.shg_device_synchronize())
+            sg.check(lib.shg_event_record(a0, s))
+            sg.check(lib.shg_event_record(b0, s2.value))
+            if h2d:
+                sg.check(lib.shg_memcpy_h2d(d_a.ptr, h_a, nb, s))
+            if d2h:
+                sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, nb, s2.value))
+            sg.check(lib.shg_event_record(a1, s))
+            sg.check(lib.shg_event_record(b1, s2.value))
+            sg.check(lib.shg_device_synchronize())
+            if name == "duplex":
+                rates[name] = [nb / elapsed(a0, a1) / 1e6, nb / elapsed(b0, b1) / 1e6]
+            else:
+                rates[name] = nb / elapsed(*((a0, a1) if h2d else (b0, b1))) / 1e6
+        sg.check(lib.shg_stream_destroy(s2.value))
+        return rates
+
     # End to end: pinned host buffers in, result back to the host, per step.
     e2e = None
     if not args.no_e2e:
+        link_before = link_probe()
         def step_e2e():
             # The host-buffer entry point: pinned inputs in, results back in
             # host memory, copies pipelined against compute inside the call.
@@ -1731,9 +1758,16 @@ def main():
         sg.check(lib.shg_stream_synchronize(s))
         barrier(dist)
         e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        link_after = link_probe()
+        # The step's copies alone at the probed rates: the host link bounds
+        # the step when this exceeds the device step.
+        h2d_ms = 2 * B * ct_bytes / (link_before["duplex"][0] * 1e6)
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
-               "ms_per_step": e2e_ms / args.steps}
+               "ms_per_step": e2e_ms / args.steps,
+               "link": {"unit": "GB/s", "before": link_before, "after": link_after,
+                        "h2d_ms_per_step_at_duplex_rate": h2d_ms,
+                        "device_ms_per_step": total_ms / args.steps}}
 
     # End to end in the wire format: host ciphertexts serialized as the
     # reference serializes them (log q-bit packed limbs), packed bytes over the
