@@ -1488,15 +1488,20 @@ def run_ntt(args, rank):
 def other_workloads(args, world, rank, local, dist):
     """Compact runs of the path's other workloads for the default line (so they
     are timed under the same clocks): PIR expand + absorb, BGV encryption with
-    on-device sampling, BFV multiplication -- each its own workload function
-    with 3 warm-up and 3 timed steps, device-resident inputs, no CPU leg and
-    no host-copy leg.  Their full lines come from --workload."""
+    on-device sampling, BFV multiplication, the uneven batch (C3: 4096 mixed
+    instances, autotuned, against one call per instance) -- each its own
+    workload function with 3 warm-up and 3 timed steps, device-resident
+    inputs, no CPU leg and no host-copy leg -- and serving (C5) at its
+    saturating offered rate of 50 k requests/s for one second of arrivals.
+    Their full lines come from --workload."""
     import contextlib
     import io
     out = {}
-    for wl, runner in (("pir", run_pir), ("encrypt", run_encrypt), ("bfv-mul", run_bfv)):
+    for wl, runner in (("pir", run_pir), ("encrypt", run_encrypt), ("bfv-mul", run_bfv),
+                       ("uneven", run_uneven), ("serve", run_serve)):
         a = argparse.Namespace(**vars(args))
         a.workload, a.steps, a.warmup = wl, 3, 3
+        a.rates = "50000"  # serving: the saturating rate only
         a.no_cpu_baseline, a.no_e2e = True, True
         buf = io.StringIO()
         with contextlib.redirect_stdout(buf):
@@ -1509,6 +1514,16 @@ def other_workloads(args, world, rank, local, dist):
         rec["workload"] = (d.get("config") or {}).get("workload")
         if d.get("roofline"):
             rec["roofline_frac"] = d["roofline"].get("frac")
+        if wl == "serve" and d.get("sweep"):
+            top = d["sweep"][-1]
+            rec.update({k: top.get(k) for k in ("offered_req_s", "throughput_req_s", "p50_ms",
+                                                 "p99_ms", "mean_batch")})
+            rec["served_over_plain"] = d.get("served_over_plain_at_top_rate")
+        for k in ("batched_over_plain", "bit_exact_batched_vs_plain"):
+            if k in d:
+                rec[k] = d[k]
+        if d.get("plain"):
+            rec["plain"] = d["plain"].get("value")
         out[wl] = rec
     return out
 
@@ -1741,30 +1756,34 @@ def main():
     # End to end: pinned host buffers in, result back to the host, per step.
     e2e = None
     if not args.no_e2e:
-        link_before = link_probe()
         def step_e2e():
             # The host-buffer entry point: pinned inputs in, results back in
             # host memory, copies pipelined against compute inside the call.
             sg.check(lib.shg_bgv_mul_relin_host(ctx.h, key.h, h_out, h_a, h_b, B, s))
-        for _ in range(2):
+        # Warm-up calls first: the first large host copies after the device-only
+        # phase run at a fraction of the link's rate (probes there read 10-20
+        # GB/s against 211), so the probe and the timing come after them.
+        for _ in range(max(3, args.warmup)):
             step_e2e()
         sg.check(lib.shg_stream_synchronize(s))
-        e0, e1 = ev(), ev()
+        link_before = link_probe()
+        xev = [ev() for _ in range(args.steps + 1)]
         barrier(dist)
-        sg.check(lib.shg_event_record(e0, s))
-        for _ in range(args.steps):
+        sg.check(lib.shg_event_record(xev[0], s))
+        for i in range(args.steps):
             step_e2e()
-        sg.check(lib.shg_event_record(e1, s))
+            sg.check(lib.shg_event_record(xev[i + 1], s))
         sg.check(lib.shg_stream_synchronize(s))
         barrier(dist)
-        e2e_ms = max_over_ranks(dist, elapsed(e0, e1))
+        e2e_ms = max_over_ranks(dist, elapsed(xev[0], xev[-1]))
+        e2e_step_ms = [round(elapsed(xev[i], xev[i + 1]), 3) for i in range(args.steps)]
         link_after = link_probe()
         # The step's copies alone at the probed rates: the host link bounds
         # the step when this exceeds the device step.
         h2d_ms = 2 * B * ct_bytes / (link_before["duplex"][0] * 1e6)
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
-               "ms_per_step": e2e_ms / args.steps,
+               "ms_per_step": e2e_ms / args.steps, "step_ms": e2e_step_ms,
                "link": {"unit": "GB/s", "before": link_before, "after": link_after,
                         "h2d_ms_per_step_at_duplex_rate": h2d_ms,
                         "device_ms_per_step": total_ms / args.steps}}
@@ -1787,7 +1806,7 @@ def main():
         def step_wire():
             sg.check(lib.shg_bgv_mul_relin_host_serialized(ctx.h, key.h, hw_out, hw_a, hw_b, B,
                                                            s))
-        for _ in range(2):
+        for _ in range(max(3, args.warmup)):
             step_wire()
         sg.check(lib.shg_stream_synchronize(s))
         w0, w1 = ev(), ev()
