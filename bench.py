@@ -1781,12 +1781,25 @@ def main():
         # The step's copies alone at the probed rates: the host link bounds
         # the step when this exceeds the device step.
         h2d_ms = 2 * B * ct_bytes / (link_before["duplex"][0] * 1e6)
+        # Fastest schedule of the step's copies on this link: the copy-out
+        # runs beside copy-in at the both-ways rates, the rest of the
+        # copy-in alone at the one-way rate.
+        bi, bo = 2 * B * ct_bytes / 1e6, B * ct_bytes / 1e6  # MB -> ms at GB/s
+        lk = link_before
+        t_both = bo / lk["duplex"][1]
+        rest = bi - lk["duplex"][0] * t_both
+        link_ms = t_both + rest / lk["h2d"] if rest > 0 else max(t_both, bi / lk["duplex"][0])
+        bound_ms = max(link_ms, total_ms / args.steps)
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
                "ms_per_step": e2e_ms / args.steps, "step_ms": e2e_step_ms,
                "link": {"unit": "GB/s", "before": link_before, "after": link_after,
                         "h2d_ms_per_step_at_duplex_rate": h2d_ms,
-                        "device_ms_per_step": total_ms / args.steps}}
+                        "link_ms_per_step": link_ms,
+                        "device_ms_per_step": total_ms / args.steps},
+               "roofline": {"bound": "host link" if link_ms >= total_ms / args.steps
+                            else "device", "bound_ms_per_step": bound_ms,
+                            "frac": bound_ms / (e2e_ms / args.steps)}}
 
     # End to end in the wire format: host ciphertexts serialized as the
     # reference serializes them (log q-bit packed limbs), packed bytes over the
