@@ -45,6 +45,14 @@ TRAFFIC_PER_CT = {
     "ks_rows": (302.4e6 + 20.5e6) / 16,     # k4_ks_rows_warp
     "digit_cols": (12.6e6 + 166.5e6) / 16,  # k4_digit_cols_all
 }
+# What bounds those kernels instead: the FMA-heavy pipe (the IMAD family,
+# every 32 x 32-bit partial product of the 64-bit modular arithmetic), from
+# the same ncu capture (sm__pipe_fmaheavy_cycles_active, one 16-ciphertext
+# launch).
+MULPIPE_BUSY = {
+    "ks_rows": 0.798,     # k4_ks_rows_warp
+    "digit_cols": 0.799,  # k4_digit_cols_all
+}
 # Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
 # step; the four-step key switch runs digit_cols + ks_rows, the unfused one
 # digit_ntt + ks_inner.
@@ -1912,6 +1920,10 @@ def main():
         "traffic": traffic,
         "algorithmic_bytes_per_launch": tk["algorithmic_bytes_per_launch"],
         "avg_launch_ms": tk["avg_launch_ms"],
+        "multiply_pipe": {"busy_frac": MULPIPE_BUSY.get(top),
+                          "source": "ncu sm__pipe_fmaheavy_cycles_active of one 16-ciphertext "
+                                    "launch: the kernel is bound by 64-bit integer multiply "
+                                    "throughput, not HBM"} if top in MULPIPE_BUSY else None,
         # The transforms are bound by 64-bit integer multiply issue, not HBM:
         # butterflies/s of the NTT-bearing kernels against the live probe.
         "integer": {"peak_butterflies_per_s": bfly_peak.value,
