@@ -71,6 +71,16 @@ __device__ __forceinline__ void bf_ct_lazy(uint64_t& X, uint64_t& Y, Tw w,
   }
 }
 
+// First-level lazy butterfly on raw inputs below 2^32 (Y's product from
+// shoup_lazy_x32, below 3q; the outputs stay within bf_ct_lazy's ranges).
+__device__ __forceinline__ void bf_ct_lazy_x32(uint64_t& X, uint64_t& Y, Tw w, uint64_t q,
+                                               uint64_t two_q) {
+  const uint64_t x = X;
+  const uint64_t t = shoup_lazy_x32((uint32_t)Y, w.w, w.wp, q);
+  X = x + t;
+  Y = x - t + 2 * two_q;
+}
+
 // x mod q for any x < 2^64 with bar = floor(2^64 / q).
 __device__ __forceinline__ uint64_t reduce_full(uint64_t x, uint64_t q,
                                                 uint64_t bar) {
@@ -165,7 +175,9 @@ struct NttCore {
   // 2 + h for half h of a 2n transform whose first level ran elsewhere).
   // LAZY selects bf_ct_lazy (valid when q < 2^58, see above); FUSED the
   // butterflies' Shoup product form.
-  template <int p, bool LAZY, bool FUSED = true>
+  // SMALL_IN (pass 0 only): every input is below 2^32, so the first level's
+  // products take bf_ct_lazy_x32 (LAZY only).
+  template <int p, bool LAZY, bool FUSED = true, bool SMALL_IN = false>
   __device__ __forceinline__ static void fwd_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
                                                   int tw_mult, uint64_t q,
@@ -185,7 +197,9 @@ struct NttCore {
         static_for<0, (1 << lb)>([&](auto ll) {
           constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
           constexpr int k1 = k0 | (1 << lb);
-          if constexpr (LAZY) {
+          if constexpr (LAZY && SMALL_IN && p == 0 && decltype(ii)::value == 0) {
+            bf_ct_lazy_x32(x[k0], x[k1], w, q, two_q);
+          } else if constexpr (LAZY) {
             bf_ct_lazy<FUSED>(x[k0], x[k1], w, q, two_q);
           } else {
             bf_ct<FUSED>(x[k0], x[k1], w, q, two_q);
@@ -257,7 +271,7 @@ struct NttCore {
   // Full forward transform on registers (input in fwd_in layout, values in
   // [0, 4q) -- below 2q for LAZY; output in fwd_out layout, values in [0, 4q),
   // or below (4 LOG_N + 2) q for LAZY).
-  template <bool LAZY = false, bool FUSED = true, class Map = SwzMap>
+  template <bool LAZY = false, bool FUSED = true, class Map = SwzMap, bool SMALL_IN = false>
   __device__ __forceinline__ static void forward_m(uint64_t (&x)[E], int tid,
                                                    const Map& m,
                                                    const Tw* __restrict__ tw,
@@ -265,7 +279,7 @@ struct NttCore {
                                                    uint64_t two_q) {
     static_for<0, P>([&](auto pp) {
       constexpr int p = decltype(pp)::value;
-      fwd_pass<p, LAZY, FUSED>(x, tid, tw, tw_mult, q, two_q);
+      fwd_pass<p, LAZY, FUSED, SMALL_IN>(x, tid, tw, tw_mult, q, two_q);
       if constexpr (p + 1 < P) exchange(x, tid, m, fwd_clo(p), fwd_clo(p + 1));
     });
   }

@@ -401,9 +401,11 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
 // runs the column phase of its transform modulo each prime in turn (the
 // digit is the same integer for every limb; the balanced lift, when the
 // gadget needs it, is applied per limb).  D [count][k][L][n] as
-// k4_fwd_cols<FwdSrcDigit> writes it.
+// k4_fwd_cols<FwdSrcDigit> writes it.  DT = uint32_t is the form for digits
+// of at most 32 bits without the lift (need_lift is ignored there).
 template <int LOG_N, bool LAZY, class DT>
-__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS, sizeof(DT) == 4 ? 6 : 5)
+__global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
+                                  (sizeof(DT) == 4 ? 6 : 5) * 128 / Ntt4<LOG_N>::COL_THREADS)
     k4_digit_cols_all(const uint64_t* X, const DigitDesc* digits, int k, int L, int need_lift,
                       uint64_t* D, CtxDev c) {
   using S = Ntt4<LOG_N>;
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS, sizeof(DT) == 4 ? 6 
     const PrimeDev* P = c.primes + l;
     const uint64_t q = P->q, two_q = P->two_q;
     uint64_t x[C::E];
-    if (!need_lift) {
+    if (sizeof(DT) == 4 || !need_lift) {
 #pragma unroll
       for (int e = 0; e < C::E; ++e) x[e] = dv[e];
     } else {
@@ -442,8 +444,11 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS, sizeof(DT) == 4 ? 6 
         x[e] = neg ? v + add : v;
       }
     }
-    C::template forward_m<LAZY>(x, t, typename C::ColMap{smem, S::COLS, jc},
-                                c.tw_fwd + ((size_t)l << LOG_N), 1, q, two_q);
+    // 32-bit digits without the lift (the only launch of the 32-bit form)
+    // enter the first level below 2^32.
+    C::template forward_m<LAZY, true, typename C::ColMap, sizeof(DT) == 4>(
+        x, t, typename C::ColMap{smem, S::COLS, jc}, c.tw_fwd + ((size_t)l << LOG_N), 1, q,
+        two_q);
     uint64_t* dst = D + (((p * k + j) * L + l) << LOG_N);
 #pragma unroll
     for (int e = 0; e < C::E; ++e) dst[(C::fwd_out_idx(t, e) << S::B) | col] = x[e];
