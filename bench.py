@@ -138,6 +138,21 @@ def sum_over_ranks(dist, v):
     return float(t.item())
 
 
+def warm_link(step, sync, min_calls, seconds=0.5):
+    """Untimed warm-up of a host-buffer leg: at least `min_calls` calls and at
+    least `seconds` of them.  After a second or two without host-link traffic
+    (device-only work, or idle) the first copies run at about 10 GB/s for some
+    0.3 s before the link returns to its steady 211 / 193 GB/s (measured on
+    the GB300 machines), so a few calls alone can leave the timing on the slow
+    start."""
+    t0 = time.perf_counter()
+    i = 0
+    while i < min_calls or time.perf_counter() - t0 < seconds:
+        step()
+        sync()
+        i += 1
+
+
 class Clocks:
     """Samples nvidia-smi clocks and throttle reasons in the background."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -447,8 +462,8 @@ def run_pir(args, world, rank, local, dist):
             sg.check(lib.shg_memcpy_h2d(d_q.ptr, h_q, q_bytes, s))
             step_device()
             sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, q_bytes, s))
-        step_e2e()
-        sg.check(lib.shg_stream_synchronize(s))
+        warm_link(step_e2e, lambda: sg.check(lib.shg_stream_synchronize(s)),
+                  max(3, args.warmup))
         e0, e1 = ev(), ev()
         barrier(dist)
         sg.check(lib.shg_event_record(e0, s))
@@ -721,13 +736,18 @@ def run_uneven(args, world, rank, local, dist):
         h_in, h_out = host(in_off), host(out_off)
         sg.check(lib.shg_memcpy_d2h(h_in, d_in.ptr, in_off, s))
         sg.check(lib.shg_stream_synchronize(s))
+
+        def step_e2e():
+            sg.check(lib.shg_memcpy_h2d(d_in.ptr, h_in, in_off, s))
+            sg.check(lib.shg_graph_launch(graph, s))
+            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, out_off, s))
+        warm_link(step_e2e, lambda: sg.check(lib.shg_stream_synchronize(s)),
+                  max(3, args.warmup))
         x0, x1 = ev(), ev()
         barrier(dist)
         sg.check(lib.shg_event_record(x0, s))
         for _ in range(args.steps):
-            sg.check(lib.shg_memcpy_h2d(d_in.ptr, h_in, in_off, s))
-            sg.check(lib.shg_graph_launch(graph, s))
-            sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, out_off, s))
+            step_e2e()
         sg.check(lib.shg_event_record(x1, s))
         sg.check(lib.shg_stream_synchronize(s))
         e2e_ms = max_over_ranks(dist, elapsed(x0, x1))
@@ -1102,8 +1122,8 @@ def run_encrypt(args, world, rank, local, dist):
             sg.check(lib.shg_memcpy_h2d(d_seeds.ptr, h_seeds, seed_bytes, s))
             step_device()
             sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, ct_bytes, s))
-        step_e2e()
-        sg.check(lib.shg_stream_synchronize(s))
+        warm_link(step_e2e, lambda: sg.check(lib.shg_stream_synchronize(s)),
+                  max(3, args.warmup))
         e0, e1 = ev(), ev()
         barrier(dist)
         sg.check(lib.shg_event_record(e0, s))
@@ -1334,8 +1354,8 @@ def run_bfv(args, world, rank, local, dist):
             sg.check(lib.shg_memcpy_h2d(d_b.ptr, h_b, in_bytes, s))
             step_device()
             sg.check(lib.shg_memcpy_d2h(h_out, d_out.ptr, out_bytes, s))
-        step_e2e()
-        sg.check(lib.shg_stream_synchronize(s))
+        warm_link(step_e2e, lambda: sg.check(lib.shg_stream_synchronize(s)),
+                  max(3, args.warmup))
         e0, e1 = ev(), ev()
         barrier(dist)
         sg.check(lib.shg_event_record(e0, s))
@@ -1771,9 +1791,7 @@ def main():
         # Warm-up calls first: the first large host copies after the device-only
         # phase run at a fraction of the link's rate (probes there read 10-20
         # GB/s against 211), so the probe and the timing come after them.
-        for _ in range(max(3, args.warmup)):
-            step_e2e()
-        sg.check(lib.shg_stream_synchronize(s))
+        warm_link(step_e2e, lambda: sg.check(lib.shg_stream_synchronize(s)), max(3, args.warmup))
         link_before = link_probe()
         xev = [ev() for _ in range(args.steps + 1)]
         barrier(dist)
@@ -1827,9 +1845,7 @@ def main():
         def step_wire():
             sg.check(lib.shg_bgv_mul_relin_host_serialized(ctx.h, key.h, hw_out, hw_a, hw_b, B,
                                                            s))
-        for _ in range(max(3, args.warmup)):
-            step_wire()
-        sg.check(lib.shg_stream_synchronize(s))
+        warm_link(step_wire, lambda: sg.check(lib.shg_stream_synchronize(s)), max(3, args.warmup))
         w0, w1 = ev(), ev()
         barrier(dist)
         sg.check(lib.shg_event_record(w0, s))

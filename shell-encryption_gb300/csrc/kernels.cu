@@ -260,7 +260,9 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
 // (rns_relinearization_key.cc:219-226).  One CTA per (ct, digit, out limb).
 // The NTT runs on the plain digits; the key is premultiplied by 2^64 so the
 // inner product's REDC restores Montgomery form.
-template <int LOG_N, bool LAZY>
+// SMALL_IN: digits of at most 32 bits without the lift (need_lift = 0), so
+// the first butterfly level takes the 32-bit-operand product.
+template <int LOG_N, bool LAZY, bool SMALL_IN = false>
 __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     k_digit_ntt(uint64_t* D, const uint64_t* X, const DigitDesc* digits, int k,
                 int need_lift, int num, int L, CtxDev c) {
@@ -298,8 +300,8 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
       x[kk] = v;
     }
   }
-  C::template forward<LAZY>(x, tid, smem + sub * C::N,
-                            c.tw_fwd + (size_t)j * C::N, 1, q, two_q);
+  C::template forward_m<LAZY, true, typename C::SwzMap, SMALL_IN>(
+      x, tid, typename C::SwzMap{smem + sub * C::N}, c.tw_fwd + (size_t)j * C::N, 1, q, two_q);
   // LAZY: D stays below 62 q; the key inner product takes it as it is.
   if constexpr (!LAZY) finish_forward<LAZY, C::E>(x, q, two_q, P->barrett);
   if (active) store_contig(D + (size_t)g * C::N + C::fwd_out_idx(tid, 0), x);
@@ -1014,19 +1016,21 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
 }
 
 void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                      const DigitDesc* digits, int k, int need_lift, int count,
+                      const DigitDesc* digits, int k, int digit_flags, int count,
                       int L, cudaStream_t s) {
   const int num = count * k * L;
   if (num <= 0) return;
+  const int need_lift = digit_flags & 1;
   LaunchScope scope_("digit_ntt", s);
   if (use_ntt4(c)) {
     g_launch_count++;  // second phase kernel
-    launch4_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
+    launch4_digit_ntt(c, D, X, digits, k, digit_flags, count, L, s);
     return;
   }
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = c.small_q ? k_digit_ntt<LN, true> : k_digit_ntt<LN, false>;  \
+    if (digit_flags == 0 && c.small_q) kern = k_digit_ntt<LN, true, true>;    \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         D, X, digits, k, need_lift, num, L, c);                               \
@@ -1079,7 +1083,7 @@ void launch_keyswitch(const CtxDev& c, uint64_t* D, const uint64_t* X,
   }
   // The digit transforms come out lazily reduced for small primes (below
   // 62 q), which chunk_lazy covers; canonical ones are covered a fortiori.
-  launch_digit_ntt(c, D, X, digits, k, need_lift, count, L, s);
+  launch_digit_ntt(c, D, X, digits, k, digit_flags, count, L, s);
   launch_ks_inner(c, out, D, kb, ka, k, c.small_q ? chunk_lazy : chunk, base, base_ct_elems,
                   map,
                   base1_zero, subst_power, count, L, s, kt);

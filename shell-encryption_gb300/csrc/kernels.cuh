@@ -198,7 +198,7 @@ void launch_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
 // plain digits: canonical, or below 62 q when every prime is below 2^58) from
 // X [count][L][n].
 void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                      const DigitDesc* digits, int k, int need_lift, int count,
+                      const DigitDesc* digits, int k, int digit_flags, int count,
                       int L, cudaStream_t s);
 
 // Key inner product, per ciphertext p and limb:
@@ -392,7 +392,7 @@ void launch4_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
                          int ncomp, int comp, int subst_power, CtMap map,
                          int count, int L, cudaStream_t s);
 void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                       const DigitDesc* digits, int k, int need_lift, int count,
+                       const DigitDesc* digits, int k, int digit_flags, int count,
                        int L, cudaStream_t s);
 void launch4_modreduce_lift(const CtxDev& c, uint64_t* out, const uint64_t* Y,
                             const uint64_t* in, const ScalarPack& sc, int count,

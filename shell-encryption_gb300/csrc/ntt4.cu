@@ -372,7 +372,10 @@ struct InvDstScale {
 
 // Occupancy for at most 72 registers per thread (seven 128-thread CTAs at
 // n = 2^14): left to itself the compiler spends up to 128 on some sources.
-template <int LOG_N, bool LAZY, class Src>
+// SMALL_IN: every source value is below 2^32 (digits of at most 32 bits
+// without the lift), so the first butterfly level takes the 32-bit-operand
+// product.
+template <int LOG_N, bool LAZY, class Src, bool SMALL_IN = false>
 __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
                                   65536 / (Ntt4<LOG_N>::COL_THREADS * 72))
     k4_fwd_cols(Src src, PrimeMap pm, uint64_t* buf, CtxDev c) {
@@ -388,8 +391,8 @@ __global__ void __launch_bounds__(Ntt4<LOG_N>::COL_THREADS,
   uint64_t x[C::E];
 #pragma unroll
   for (int k = 0; k < C::E; ++k) x[k] = h((C::fwd_in_idx(t, k) << S::B) | col);
-  C::template forward_m<LAZY>(x, t, typename C::ColMap{smem, S::COLS, j},
-                              c.tw_fwd + ((size_t)l << LOG_N), 1, q, two_q);
+  C::template forward_m<LAZY, true, typename C::ColMap, SMALL_IN>(
+      x, t, typename C::ColMap{smem, S::COLS, j}, c.tw_fwd + ((size_t)l << LOG_N), 1, q, two_q);
   uint64_t* dst = buf + ((size_t)g << LOG_N);
 #pragma unroll
   for (int k = 0; k < C::E; ++k) dst[(C::fwd_out_idx(t, k) << S::B) | col] = x[k];
@@ -1076,33 +1079,33 @@ constexpr int kRowsWarpW = 4, kRowsWarpDpi = 3;
 
 template <int LOG_N, class Src, class Dst>
 void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
-          uint64_t* buf, int num, cudaStream_t s) {
+          uint64_t* buf, int num, cudaStream_t s, bool small_in = false) {
   using S = Ntt4<LOG_N>;
+  // column kernel; small_in (LAZY only): every source value below 2^32
+  auto cols = [&](auto lazy) {
+    constexpr bool LZ = decltype(lazy)::value;
+    auto k1 = k4_fwd_cols<LOG_N, LZ, Src>;
+    if constexpr (LZ && std::is_same_v<Src, FwdSrcDigit<LOG_N>>) {
+      if (small_in) k1 = k4_fwd_cols<LOG_N, true, Src, true>;
+    }
+    set_smem4(k1, S::COL_SMEM);
+    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
+  };
+  if (c.small_q)
+    cols(std::true_type{});
+  else
+    cols(std::false_type{});
   if constexpr (std::is_same_v<Dst, FwdDstPlain<LOG_N>>) {
     constexpr int W = kRowsWarpW, DPI = kRowsWarpDpi;
     const int groups = (num / pm.L + DPI - 1) / DPI;
     const int blocks = pm.L * groups * (1 << S::A) / W;
-    auto k1 = c.small_q ? k4_fwd_cols<LOG_N, true, Src> : k4_fwd_cols<LOG_N, false, Src>;
     auto k2 = c.small_q ? k4_fwd_rows_warp<LOG_N, true, Dst, W, DPI>
                         : k4_fwd_rows_warp<LOG_N, false, Dst, W, DPI>;
-    set_smem4(k1, S::COL_SMEM);
     set_smem4(k2, W * DPI * (1 << S::B) * 8);
-    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
     k2<<<blocks, 32 * W, W * DPI * (1 << S::B) * 8, s>>>(buf, dst, pm, num, c);
-  } else if (c.small_q) {
-    auto k1 = k4_fwd_cols<LOG_N, true, Src>;
-    auto k2 = k4_fwd_rows<LOG_N, true, Dst>;
-    set_smem4(k1, S::COL_SMEM);
-    set_smem4(k2, S::ROW_SMEM);
-    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
-    k2<<<row_blocks<LOG_N>(num, pm), S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm,
-                                                                      num, c);
   } else {
-    auto k1 = k4_fwd_cols<LOG_N, false, Src>;
-    auto k2 = k4_fwd_rows<LOG_N, false, Dst>;
-    set_smem4(k1, S::COL_SMEM);
+    auto k2 = c.small_q ? k4_fwd_rows<LOG_N, true, Dst> : k4_fwd_rows<LOG_N, false, Dst>;
     set_smem4(k2, S::ROW_SMEM);
-    k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
     k2<<<row_blocks<LOG_N>(num, pm), S::ROW_THREADS, S::ROW_SMEM, s>>>(buf, dst, pm,
                                                                       num, c);
   }
@@ -1181,11 +1184,12 @@ void launch4_intt_export(const CtxDev& c, uint64_t* X, const uint64_t* ct,
 }
 
 void launch4_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
-                       const DigitDesc* digits, int k, int need_lift, int count,
+                       const DigitDesc* digits, int k, int digit_flags, int count,
                        int L, cudaStream_t s) {
+  const int need_lift = digit_flags & 1;
 #define F(LN)                                                                  \
   fwd4<LN>(c, FwdSrcDigit<LN>{X, digits, k, L, need_lift}, FwdDstPlain<LN>{D}, \
-           PrimeMap{0, 1, L}, D, count * k * L, s)
+           PrimeMap{0, 1, L}, D, count * k * L, s, digit_flags == 0)
   SHG_DISPATCH4(c.log_n, F)
 #undef F
 }
@@ -1225,6 +1229,8 @@ void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
     const FwdSrcDigit<LN> src{X, digits, k, L, need_lift};                      \
     auto k1 = c.small_q ? k4_fwd_cols<LN, true, FwdSrcDigit<LN>>                \
                         : k4_fwd_cols<LN, false, FwdSrcDigit<LN>>;              \
+    if (c.small_q && digit_flags == 0)                                          \
+      k1 = k4_fwd_cols<LN, true, FwdSrcDigit<LN>, true>;                        \
     set_smem4(k1, S::COL_SMEM);                                                 \
     k1<<<count * k * L * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(       \
         src, PrimeMap{0, 1, L}, D, c);                                          \
