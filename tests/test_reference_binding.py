@@ -16,6 +16,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "shell-encryption_gb300")
 SRC = os.path.join(ROOT, "tests", "cpp", "reference_binding_test.cc")
 REF_LIB_DIR = os.path.join(ROOT, "oracle", "_ref")
+# The reference checkout: SHELL_REFERENCE_DIR, by default the build
+# container's read-only copy (absent on GPU machines: the test then skips).
 REF = os.environ.get("SHELL_REFERENCE_DIR", "/root/reference")
 
 
