@@ -1439,7 +1439,8 @@ NTT_CASES = ((12, QS, "six 45-bit primes"), (14, QS, "six 45-bit primes"),
 NTT_POLYS = 1024
 
 
-def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10, polys=NTT_POLYS):
+def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10, polys=NTT_POLYS,
+               four_step_min=0):
     """Forward and inverse limb-NTTs/s (shg_ntt_forward / shg_ntt_inverse in
     place over NTT_POLYS x 6 limbs), with the HBM fraction at 16 n bytes per
     limb-NTT (each limb read and written once) and the butterfly rate against
@@ -1448,6 +1449,8 @@ def ntt_record(sg, lib, s, ev, elapsed, peak, bfly_peak, reps=10, polys=NTT_POLY
     for log_n, qs, primes in NTT_CASES:
         n, L = 1 << log_n, len(qs)
         ctx = sg.Context(log_n, qs)
+        if four_step_min:
+            sg.check(lib.shg_context_set_four_step_min(ctx.h, four_step_min))
         buf = sg.DeviceBuffer(polys * L * n * 8)
         sg.check(lib.shg_poly_fill_uniform(ctx.h, buf.ptr, polys, L, 99, s))
         limbs = polys * L
@@ -1503,7 +1506,7 @@ def run_ntt(args, rank):
     bfly = ctypes.c_double()
     sg.check(lib.shg_measure_butterfly_rate(ctypes.byref(bfly)))
     rec = ntt_record(sg, lib, s, ev, elapsed, peak, bfly.value, reps=max(args.steps, 1),
-                     polys=args.ntt_polys)
+                     polys=args.ntt_polys, four_step_min=args.four_step_min)
     n14 = rec["n16384"]["fwd"]
     if rank == 0:
         print(json.dumps({"metric": "limb-NTT/s (forward, n=2^14, six 45-bit primes)",

@@ -63,7 +63,8 @@ int shg_context_set_chunk(shg_context* ctx, int cts_per_chunk);
 /* Transforms of n >= 2^log_n use the two-kernel four-step NTT, log_n in
  * [12, 16] (13 = default; 12 also moves n = 2^12 off the one-CTA-per-limb
  * kernels; 14 or more keeps smaller n on them; n = 2^15 always uses the
- * four-step kernels). */
+ * four-step kernels).  Plain shg_ntt_forward / shg_ntt_inverse calls use the
+ * four-step kernels from n = 2^12 at 12 and 13, and follow higher values. */
 int shg_context_set_four_step_min(shg_context* ctx, int log_n);
 /* 1 (default): four-step key switches run the digit row phase and the key
  * inner product as one kernel; 0: separate row phase, digit NTTs written to

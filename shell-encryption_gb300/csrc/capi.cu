@@ -181,6 +181,9 @@ struct shg_context {
   int small_q = 0;  // all moduli below 2^58
   int ntt4_min = 13;  // four-step transforms from this log_n up (measured faster
                       // for every operation from n = 2^13; mixed at 2^12)
+  int ntt4_plain_min = 12;  // plain forward / inverse NTTs: four-step from 2^12
+                            // (8-10 % faster there) unless the threshold is set
+                            // above 13
   int ks_fused = 1;   // fused digit row phase + key inner product
   int ks_lanes = 2;      // streams the batched key-switch chunks rotate over (1..4)
   // Host pipeline shape, measured fastest on a GB300 for 1024 pairs at
@@ -205,13 +208,14 @@ struct shg_context {
 
   CtxDev dev() const {
     return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min,
-                  ks_fused, sms};
+                  ks_fused, sms, ntt4_plain_min};
   }
   // The auxiliary primes as a context of their own (NTTs and pointwise ops
   // over aux limbs); there is no cross-prime table in this view.
   CtxDev aux_dev() const {
     return CtxDev{log_n, n, K, d_primes + L, d_tw_fwd + (size_t)L * n,
-                  d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused, sms};
+                  d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused, sms,
+                  ntt4_plain_min};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -1970,6 +1974,7 @@ int shg_context_set_four_step_min(shg_context* ctx, int log_n) {
   if (!ctx || log_n < 12 || log_n > 16)
     return fail(SHG_INVALID_ARGUMENT, "four-step threshold must lie in [12, 16]");
   ctx->ntt4_min = log_n;
+  ctx->ntt4_plain_min = log_n <= 13 ? 12 : log_n;
   return SHG_OK;
 }
 int shg_debug_status(unsigned* first_failure) {

@@ -887,6 +887,9 @@ namespace {
 // Transforms of n >= 2^ntt4_min (always n = 2^15) run as two four-step
 // phase kernels (ntt4.cu); smaller ones as one CTA-resident kernel.
 bool use_ntt4(const CtxDev& c) { return c.log_n >= c.ntt4_min || c.log_n > 14; }
+bool use_ntt4_plain(const CtxDev& c) {
+  return c.log_n >= 12 && (c.log_n >= c.ntt4_plain_min || c.log_n > 14);
+}
 
 template <int LOG_N>
 int blocks_for(int num) {
@@ -899,7 +902,7 @@ void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                     int L, cudaStream_t s) {
   if (num <= 0) return;
   LaunchScope scope_("ntt_fwd", s);
-  if (use_ntt4(c)) {
+  if (use_ntt4_plain(c)) {
     g_launch_count++;  // second phase kernel
     launch4_ntt_fwd(c, in, out, num, L, s);
     return;
@@ -915,13 +918,14 @@ void launch_ntt_fwd(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
 #undef F
 }
 
+// plain: a plain inverse NTT call (the plain-NTT threshold applies).
 static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
                                   uint64_t* out, int num, int L, int in_first,
                                   int in_stride, int mode, uint64_t sw,
-                                  uint64_t swp, cudaStream_t s) {
+                                  uint64_t swp, cudaStream_t s, bool plain = false) {
   if (num <= 0) return;
   LaunchScope scope_("ntt_inv", s);
-  if (use_ntt4(c)) {
+  if (plain ? use_ntt4_plain(c) : use_ntt4(c)) {
     g_launch_count++;  // second phase kernel
     launch4_ntt_inv(c, in, out, num, L, in_first, in_stride, mode, sw, swp, s);
     return;
@@ -940,7 +944,7 @@ static void launch_ntt_inv_scaled(const CtxDev& c, const uint64_t* in,
 void launch_ntt_inv(const CtxDev& c, const uint64_t* in, uint64_t* out, int num,
                     int L, int scale_export, cudaStream_t s) {
   launch_ntt_inv_scaled(c, in, out, num, L, 0, 1, scale_export ? 1 : 0, 0, 0,
-                        s);
+                        s, /*plain=*/true);
 }
 
 void launch_pointwise(const CtxDev& c, PwOp op, uint64_t* out, const uint64_t* a,

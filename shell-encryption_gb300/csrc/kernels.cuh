@@ -34,6 +34,7 @@ struct CtxDev {
   int ntt4_min;               // log_n from which transforms use the four-step kernels
   int ks_fused;               // four-step key switch: digit row phase fused with the inner product
   int sms;                    // multiprocessors of the context's device (launch-shape choices)
+  int ntt4_plain_min;         // the same threshold for plain forward / inverse NTTs
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,

@@ -711,9 +711,10 @@ __global__ void __maxnreg__(56)
 }
 
 // Rows (warps) per CTA of k4_ks_rows_warp, and digits each warp transforms
-// together (1, 2, 3, 4, 6 digits: 57.2, 60.8, 62.3, 62.6, 62.2 k ct-mult+relin/s).
+// together (1, 2, 3, 4, 6 digits: 57.2, 60.8, 62.3, 62.6, 62.2 k ct-mult+relin/s;
+// with the 32-bit first digit level, 3 and 4 digits: 64.23 and 64.52 k/s).
 constexpr int kKsWarpRows = 4;
-constexpr int kKsWarpDigits = 3;
+constexpr int kKsWarpDigits = 4;
 
 // The key switch's row phase with one warp per row of one (ciphertext,
 // limb): its 32 threads run that row of every digit transform (4 values per
@@ -767,7 +768,7 @@ __global__ void __launch_bounds__(32 * W, MB)
   // DPI digits at a time, interleaved: their transforms use the same
   // twiddles and tile offsets (tile d at d KB above the first), so the index
   // work is shared and each level has DPI times the independent butterflies;
-  // the last k mod DPI digits go one by one.
+  // of the last k mod DPI digits, two go together and the rest one by one.
   auto digits = [&](int j, auto dn) {
     constexpr int D = decltype(dn)::value;
     const Tw* tw;
@@ -820,6 +821,12 @@ __global__ void __launch_bounds__(32 * W, MB)
   if constexpr (DPI > 1) {
 #pragma unroll 1
     for (; j + DPI <= k; j += DPI) digits(j, std::integral_constant<int, DPI>{});
+  }
+  if constexpr (DPI > 2) {
+    if (j + 2 <= k) {
+      digits(j, std::integral_constant<int, 2>{});
+      j += 2;
+    }
   }
 #pragma unroll 1
   for (; j < k; ++j) digits(j, std::integral_constant<int, 1>{});
