@@ -17,7 +17,8 @@
  * checks.  Return values are absl::StatusCode numbers (0 = OK,
  * 3 = INVALID_ARGUMENT, 9 = FAILED_PRECONDITION, 8 = RESOURCE_EXHAUSTED,
  * 13 = INTERNAL); shg_last_error() returns the message of the calling
- * thread's last failure.
+ * thread's last failure.  Batched calls of one context share its device
+ * scratch: issue them on one stream, or order their streams with events.
  *
  * Reference interfaces cited below are paths inside google/shell-encryption.
  */

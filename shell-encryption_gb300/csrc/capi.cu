@@ -1218,14 +1218,18 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
     sizes.insert(sizes.end(), back.rbegin(), back.rend());
   }
   const int pieces = (int)sizes.size();
-  std::vector<cudaEvent_t> evs;
+  // Every event of the call goes back on every return path (an event still
+  // pending when destroyed is released once it completes).
+  struct Events {
+    std::vector<cudaEvent_t> v;
+    ~Events() {
+      for (cudaEvent_t e : v) cudaEventDestroy(e);
+    }
+  } evs;
   auto event = [&](cudaEvent_t* e) -> int {
     SHG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    evs.push_back(*e);
+    evs.v.push_back(*e);
     return SHG_OK;
-  };
-  auto release = [&] {
-    for (cudaEvent_t e : evs) cudaEventDestroy(e);
   };
   cudaEvent_t start;
   if ((st = event(&start))) return st;
@@ -1238,10 +1242,7 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
       break;
     st = event(&stored[i]);
   }
-  if (st) {
-    release();
-    return st;
-  }
+  if (st) return st;
   const CtxDev dv = ctx->dev();
   int c0 = 0, chunk_no = 0;
   for (int i = 0; i < pieces; c0 += sizes[i], ++i) {
@@ -1313,7 +1314,6 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
   }
   if (st == SHG_OK) st = launch_status("bgv_mul_relin_host");
   if (st == SHG_OK) SHG_CUDA(cudaStreamWaitEvent(user, stored[pieces - 1], 0));
-  release();
   return st;
 }
 }  // namespace
