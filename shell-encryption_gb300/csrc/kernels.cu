@@ -188,20 +188,10 @@ __global__ void __launch_bounds__(Cfg<LOG_N>::THREADS)
     const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a + off + Ln + k);
     const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b + off + k);
     const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b + off + Ln + k);
-    ulonglong2 r0, r1;
-    r0.x = mont_mul(va0.x, vb0.x, q, qinv);
-    r0.y = mont_mul(va0.y, vb0.y, q, qinv);
-    uint64_t lo = 0, hi = 0;
-    mac128(lo, hi, va0.x, vb1.x);
-    mac128(lo, hi, va1.x, vb0.x);
-    r1.x = redc128(lo, hi, q, qinv);
-    lo = 0;
-    hi = 0;
-    mac128(lo, hi, va0.y, vb1.y);
-    mac128(lo, hi, va1.y, vb0.y);
-    r1.y = redc128(lo, hi, q, qinv);
-    x[k] = mont_mul(va1.x, vb1.x, q, qinv);  // degree-2 component
-    x[k + 1] = mont_mul(va1.y, vb1.y, q, qinv);
+    ulonglong2 r0, r1, r2;
+    tensor3_pair(va0, va1, vb0, vb1, q, qinv, r0, r1, r2);
+    x[k] = r2.x;  // the degree-2 component
+    x[k + 1] = r2.y;
     if (active) {
       *reinterpret_cast<ulonglong2*>(out01 + off + k) = r0;
       *reinterpret_cast<ulonglong2*>(out01 + off + Ln + k) = r1;
@@ -451,12 +441,11 @@ __global__ void k_tensor(uint64_t* out, const uint64_t* a, const uint64_t* b,
     const uint64_t q = P->q, qinv = P->inv_modulus;
     const uint64_t a0 = a[ct * 2 * Ln + r], a1 = a[ct * 2 * Ln + Ln + r];
     const uint64_t b0 = b[ct * 2 * Ln + r], b1 = b[ct * 2 * Ln + Ln + r];
-    uint64_t lo = 0, hi = 0;
-    mac128(lo, hi, a0, b1);
-    mac128(lo, hi, a1, b0);
-    out[ct * 3 * Ln + r] = mont_mul(a0, b0, q, qinv);
-    out[ct * 3 * Ln + Ln + r] = redc128(lo, hi, q, qinv);
-    out[ct * 3 * Ln + 2 * Ln + r] = mont_mul(a1, b1, q, qinv);
+    uint64_t c0, c1, c2;
+    tensor3(a0, a1, b0, b1, q, qinv, c0, c1, c2);
+    out[ct * 3 * Ln + r] = c0;
+    out[ct * 3 * Ln + Ln + r] = c1;
+    out[ct * 3 * Ln + 2 * Ln + r] = c2;
   }
 }
 

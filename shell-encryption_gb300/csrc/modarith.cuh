@@ -231,6 +231,41 @@ __device__ __forceinline__ void mac128(uint64_t& lo, uint64_t& hi, uint64_t a,
       : "l"(a), "l"(b));
 }
 
+// The three products of a ciphertext tensor: c0 = a0 b0, c1 = a0 b1 + a1 b0,
+// c2 = a1 b1, each times 2^-64 mod q (Montgomery), canonical.  c1 comes from
+// Karatsuba's (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 on exact 128-bit products:
+// three 128-bit products and three REDCs (54 multiplies) instead of two
+// Montgomery products, two multiply-accumulates and a REDC (66).  Inputs below q.
+__device__ __forceinline__ void tensor3(uint64_t a0, uint64_t a1, uint64_t b0, uint64_t b1,
+                                        uint64_t q, uint64_t qinv, uint64_t& c0,
+                                        uint64_t& c1, uint64_t& c2) {
+  uint64_t p0l = 0, p0h = 0, p2l = 0, p2h = 0, sl = 0, sh = 0;
+  mac128(p0l, p0h, a0, b0);
+  mac128(p2l, p2h, a1, b1);
+  mac128(sl, sh, a0 + a1, b0 + b1);
+  // s - p0 - p2 = a0 b1 + a1 b0, exact (no borrow out of 128 bits)
+  uint64_t l = sl - p0l;
+  uint64_t h = sh - p0h - (sl < p0l);
+  const uint64_t l2 = l - p2l;
+  h = h - p2h - (l < p2l);
+  c0 = redc128(p0l, p0h, q, qinv);
+  c1 = redc128(l2, h, q, qinv);
+  c2 = redc128(p2l, p2h, q, qinv);
+}
+
+// tensor3 of two adjacent coefficients.
+__device__ __forceinline__ void tensor3_pair(const ulonglong2& a0, const ulonglong2& a1,
+                                             const ulonglong2& b0, const ulonglong2& b1,
+                                             uint64_t q, uint64_t qinv, ulonglong2& c0,
+                                             ulonglong2& c1, ulonglong2& c2) {
+  uint64_t x0, x1, x2, y0, y1, y2;
+  tensor3(a0.x, a1.x, b0.x, b1.x, q, qinv, x0, x1, x2);
+  tensor3(a0.y, a1.y, b0.y, b1.y, q, qinv, y0, y1, y2);
+  c0 = make_ulonglong2(x0, y0);
+  c1 = make_ulonglong2(x1, y1);
+  c2 = make_ulonglong2(x2, y2);
+}
+
 // Inputs may be any value in [0, q] (SHELL's NegateInPlace maps 0 to q,
 // montgomery.h:405-408); results are canonical like the reference's Barrett
 // AddInPlace / SubInPlace (montgomery.h:383-415).

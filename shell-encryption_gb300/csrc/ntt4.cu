@@ -307,21 +307,11 @@ struct InvSrcTensor {
       const ulonglong2 va1 = *reinterpret_cast<const ulonglong2*>(a0 + Ln + i);
       const ulonglong2 vb0 = *reinterpret_cast<const ulonglong2*>(b0 + i);
       const ulonglong2 vb1 = *reinterpret_cast<const ulonglong2*>(b0 + Ln + i);
-      ulonglong2 r0, r1;
-      r0.x = mont_mul(va0.x, vb0.x, q, qinv);
-      r0.y = mont_mul(va0.y, vb0.y, q, qinv);
-      uint64_t lo = 0, hi = 0;
-      mac128(lo, hi, va0.x, vb1.x);
-      mac128(lo, hi, va1.x, vb0.x);
-      r1.x = redc128(lo, hi, q, qinv);
-      lo = 0;
-      hi = 0;
-      mac128(lo, hi, va0.y, vb1.y);
-      mac128(lo, hi, va1.y, vb0.y);
-      r1.y = redc128(lo, hi, q, qinv);
+      ulonglong2 r0, r1, r2;
+      tensor3_pair(va0, va1, vb0, vb1, q, qinv, r0, r1, r2);
       *reinterpret_cast<ulonglong2*>(o0 + i) = r0;
       *reinterpret_cast<ulonglong2*>(o0 + Ln + i) = r1;
-      return make_ulonglong2(mont_mul(va1.x, vb1.x, q, qinv), mont_mul(va1.y, vb1.y, q, qinv));
+      return r2;
     }
   };
   __device__ H bind(int g, int l, const CtxDev& c) const {
