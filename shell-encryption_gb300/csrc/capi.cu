@@ -179,6 +179,7 @@ struct shg_context {
   size_t ws_bytes = 0;
   int chunk_cts = 0;
   int small_q = 0;  // all moduli below 2^58
+  int narrow_q = 0;  // all moduli below 2^45
   int ntt4_min = 13;  // four-step transforms from this log_n up (measured faster
                       // for every operation from n = 2^13; mixed at 2^12)
   int ntt4_plain_min = 12;  // plain forward / inverse NTTs: four-step from 2^12
@@ -208,14 +209,14 @@ struct shg_context {
 
   CtxDev dev() const {
     return CtxDev{log_n, n, L, d_primes, d_tw_fwd, d_tw_inv, d_qmod, small_q, ntt4_min,
-                  ks_fused, sms, ntt4_plain_min};
+                  ks_fused, sms, ntt4_plain_min, narrow_q};
   }
   // The auxiliary primes as a context of their own (NTTs and pointwise ops
   // over aux limbs); there is no cross-prime table in this view.
   CtxDev aux_dev() const {
     return CtxDev{log_n, n, K, d_primes + L, d_tw_fwd + (size_t)L * n,
                   d_tw_inv + (size_t)L * n, nullptr, small_q, ntt4_min, ks_fused, sms,
-                  ntt4_plain_min};
+                  ntt4_plain_min, narrow_q};
   }
   int ensure_ws(size_t bytes) {
     if (bytes <= ws_bytes) return SHG_OK;
@@ -493,8 +494,11 @@ int shg_context_create_with_aux(int log_n, const uint64_t* qs, int num_qs, const
     }
   }
   ctx->small_q = 1;
-  for (int i = 0; i < NP; ++i)
+  ctx->narrow_q = 1;
+  for (int i = 0; i < NP; ++i) {
     if ((all[i] >> 58) != 0) ctx->small_q = 0;
+    if ((all[i] >> 45) != 0) ctx->narrow_q = 0;
+  }
   ctx->qmod.resize((size_t)L * L);
   for (int i = 0; i < L; ++i)
     for (int j = 0; j < L; ++j) ctx->qmod[(size_t)i * L + j] = qs[i] % qs[j];

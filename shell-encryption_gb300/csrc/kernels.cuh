@@ -35,6 +35,7 @@ struct CtxDev {
   int ks_fused;               // four-step key switch: digit row phase fused with the inner product
   int sms;                    // multiprocessors of the context's device (launch-shape choices)
   int ntt4_plain_min;         // the same threshold for plain forward / inverse NTTs
+  int narrow_q;               // every q below 2^45 (implies small_q)
 };
 
 // Per-digit description of a gadget key (RnsGadget::Decompose order,

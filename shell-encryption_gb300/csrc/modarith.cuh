@@ -266,6 +266,36 @@ __device__ __forceinline__ void tensor3_pair(const ulonglong2& a0, const ulonglo
   c2 = make_ulonglong2(x2, y2);
 }
 
+// mac128 when the high partial product fits 32 bits: hi32(a) * hi32(b) <
+// 2^32, so its high word is zero and one multiply becomes a carry add.  That
+// holds for the key inner product when every prime is below 2^45: lazy digit
+// transforms below 62 q give hi32(a) <= 507903, canonical key values
+// hi32(b) <= 8191, and 507903 * 8191 < 2^32.
+__device__ __forceinline__ void mac128_narrow(uint64_t& lo, uint64_t& hi, uint64_t a,
+                                              uint64_t b) {
+  asm("{\n\t"
+      ".reg .u32 al, ah, bl, bh, c0, c1, c2, c3;\n\t"
+      "mov.b64 {al, ah}, %2;\n\t"
+      "mov.b64 {bl, bh}, %3;\n\t"
+      "mov.b64 {c0, c1}, %0;\n\t"
+      "mov.b64 {c2, c3}, %1;\n\t"
+      "mad.lo.cc.u32 c0, al, bl, c0;\n\t"
+      "madc.hi.cc.u32 c1, al, bl, c1;\n\t"
+      "madc.lo.cc.u32 c2, ah, bh, c2;\n\t"
+      "addc.u32 c3, c3, 0;\n\t"
+      "mad.lo.cc.u32 c1, al, bh, c1;\n\t"
+      "madc.hi.cc.u32 c2, al, bh, c2;\n\t"
+      "addc.u32 c3, c3, 0;\n\t"
+      "mad.lo.cc.u32 c1, ah, bl, c1;\n\t"
+      "madc.hi.cc.u32 c2, ah, bl, c2;\n\t"
+      "addc.u32 c3, c3, 0;\n\t"
+      "mov.b64 %0, {c0, c1};\n\t"
+      "mov.b64 %1, {c2, c3};\n\t"
+      "}"
+      : "+l"(lo), "+l"(hi)
+      : "l"(a), "l"(b));
+}
+
 // Inputs may be any value in [0, q] (SHELL's NegateInPlace maps 0 to q,
 // montgomery.h:405-408); results are canonical like the reference's Barrett
 // AddInPlace / SubInPlace (montgomery.h:383-415).

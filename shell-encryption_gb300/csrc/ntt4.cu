@@ -721,7 +721,9 @@ constexpr int kKsWarpDigits = 4;
 // the SMs far better with the next chunk's column kernel on the other
 // key-switch stream (ct-mult+relin 53.4 k -> 56.1 k/s one digit at a time,
 // 62.3 k/s three at a time).
-template <int LOG_N, bool LAZY, int W, int MB, int DPI>
+// NARROW (every prime below 2^45): the inner product's multiply-accumulates
+// drop the zero high word of the high partial product (mac128_narrow).
+template <int LOG_N, bool LAZY, int W, int MB, int DPI, bool NARROW = false>
 __global__ void __launch_bounds__(32 * W, MB)
     k4_ks_rows_warp(const uint64_t* buf, int k, const uint64_t* kb, const uint64_t* ka,
                     uint64_t* out, const uint64_t* base, size_t base_ct_elems, CtMap map,
@@ -800,10 +802,17 @@ __global__ void __launch_bounds__(32 * W, MB)
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const ulonglong2 vb = kv[d][h], va = kv[d][2 + h];
-        mac128(lo0[2 * h], hi0[2 * h], x[d][2 * h], vb.x);
-        mac128(lo0[2 * h + 1], hi0[2 * h + 1], x[d][2 * h + 1], vb.y);
-        mac128(lo1[2 * h], hi1[2 * h], x[d][2 * h], va.x);
-        mac128(lo1[2 * h + 1], hi1[2 * h + 1], x[d][2 * h + 1], va.y);
+        auto mac = [](uint64_t& lo, uint64_t& hi, uint64_t a, uint64_t b) {
+          if constexpr (NARROW && LAZY) {
+            mac128_narrow(lo, hi, a, b);
+          } else {
+            mac128(lo, hi, a, b);
+          }
+        };
+        mac(lo0[2 * h], hi0[2 * h], x[d][2 * h], vb.x);
+        mac(lo0[2 * h + 1], hi0[2 * h + 1], x[d][2 * h + 1], vb.y);
+        mac(lo1[2 * h], hi1[2 * h], x[d][2 * h], va.x);
+        mac(lo1[2 * h + 1], hi1[2 * h + 1], x[d][2 * h + 1], va.y);
       }
     }
   };
@@ -1254,6 +1263,7 @@ void launch4_ks_rows(const CtxDev& c, const uint64_t* D, int k, int chunk,
   {                                                                             \
     auto kern = c.small_q ? k4_ks_rows_warp<LN, true, kKsWarpRows, 4, kKsWarpDigits>   \
                           : k4_ks_rows_warp<LN, false, kKsWarpRows, 4, kKsWarpDigits>; \
+    if (c.narrow_q) kern = k4_ks_rows_warp<LN, true, kKsWarpRows, 4, kKsWarpDigits, true>; \
     const int smem = kKsWarpRows * kKsWarpDigits * 128 * 8;                     \
     set_smem4(kern, smem);                                                      \
     kern<<<count * L * ((1 << (LN - 7)) / kKsWarpRows), 32 * kKsWarpRows, smem, s>>>( \
