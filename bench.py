@@ -42,16 +42,16 @@ UNIT = "ct-mult+relin/s"
 # captures of the same kernels (dram__bytes_read.sum + dram__bytes_write.sum
 # of one 16-ciphertext launch); None where not captured.
 TRAFFIC_PER_CT = {
-    "ks_rows": (302.4e6 + 20.5e6) / 16,     # k4_ks_rows_warp
-    "digit_cols": (12.6e6 + 166.5e6) / 16,  # k4_digit_cols_all
+    "ks_rows": (300.8e6 + 20.6e6) / 16,     # k4_ks_rows_warp
+    "digit_cols": (12.7e6 + 169.2e6) / 16,  # k4_digit_cols_all
 }
 # What bounds those kernels instead: the FMA-heavy pipe (the IMAD family,
 # every 32 x 32-bit partial product of the 64-bit modular arithmetic), from
 # the same ncu capture (sm__pipe_fmaheavy_cycles_active, one 16-ciphertext
 # launch).
 MULPIPE_BUSY = {
-    "ks_rows": 0.798,     # k4_ks_rows_warp
-    "digit_cols": 0.799,  # k4_digit_cols_all
+    "ks_rows": 0.772,     # k4_ks_rows_warp
+    "digit_cols": 0.761,  # k4_digit_cols_all
 }
 # Kernel scopes the library times (shg_profile_query) in one ct-mult+relin
 # step; the four-step key switch runs digit_cols + ks_rows, the unfused one
