@@ -138,6 +138,20 @@ def sum_over_ranks(dist, v):
     return float(t.item())
 
 
+def host_link_ms(h2d_bytes, d2h_bytes, rates):
+    """Fastest time (ms) for one step's copies on the host link, from probed
+    rates (GB/s: "h2d" and "d2h" one way, "duplex" [h2d, d2h] both ways at
+    once): both directions run side by side at the both-ways rates until the
+    shorter one is done, and the rest of the longer one runs alone at its
+    one-way rate."""
+    up, down = rates["duplex"]
+    t_in, t_out = h2d_bytes / (up * 1e6), d2h_bytes / (down * 1e6)
+    t_both = min(t_in, t_out)
+    if t_in >= t_out:
+        return t_both + (h2d_bytes - up * 1e6 * t_both) / (rates["h2d"] * 1e6)
+    return t_both + (d2h_bytes - down * 1e6 * t_both) / (rates["d2h"] * 1e6)
+
+
 def warm_link(step, sync, min_calls, seconds=0.5):
     """Untimed warm-up of a host-buffer leg: at least `min_calls` calls and at
     least `seconds` of them.  After a second or two without host-link traffic
@@ -1810,14 +1824,7 @@ def main():
         # The step's copies alone at the probed rates: the host link bounds
         # the step when this exceeds the device step.
         h2d_ms = 2 * B * ct_bytes / (link_before["duplex"][0] * 1e6)
-        # Fastest schedule of the step's copies on this link: the copy-out
-        # runs beside copy-in at the both-ways rates, the rest of the
-        # copy-in alone at the one-way rate.
-        bi, bo = 2 * B * ct_bytes / 1e6, B * ct_bytes / 1e6  # MB -> ms at GB/s
-        lk = link_before
-        t_both = bo / lk["duplex"][1]
-        rest = bi - lk["duplex"][0] * t_both
-        link_ms = t_both + rest / lk["h2d"] if rest > 0 else max(t_both, bi / lk["duplex"][0])
+        link_ms = host_link_ms(2 * B * ct_bytes, B * ct_bytes, link_before)
         bound_ms = max(link_ms, total_ms / args.steps)
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
