@@ -266,7 +266,8 @@ def run_reference(args, world, rank, dist):
         "config": dict(config(threads), batch=threads),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"each step: about 2 s of ct-mult+relin at n=2^14, L=6, "
-                                   f"one ciphertext pair per host thread per round"},
+                                   f"one ciphertext pair per host thread per round",
+                         "single_thread_ms_per_op": 1e3 / cpu_reference(1.0, 1, seed=99)[0]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -1966,9 +1967,11 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, ops, dt = cpu_reference(10.0, threads)
+        rate1, _, _ = cpu_reference(1.0, 1)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{ops} ct-mult+relin ops at n=2^14, L=6 in {dt:.1f} s "
-                         f"(one ciphertext pair per host thread per round)"}
+                         f"(one ciphertext pair per host thread per round)",
+               "single_thread_ms_per_op": 1e3 / rate1}
 
     lat = sorted(step_ms)
     oplat = sorted(op_ms)
