@@ -1023,7 +1023,8 @@ void launch_digit_ntt(const CtxDev& c, uint64_t* D, const uint64_t* X,
 #define F(LN)                                                                 \
   {                                                                           \
     auto kern = c.small_q ? k_digit_ntt<LN, true> : k_digit_ntt<LN, false>;  \
-    if (digit_flags == 0 && c.small_q) kern = k_digit_ntt<LN, true, true>;    \
+    if (digit_flags == 0)                                                     \
+      kern = c.small_q ? k_digit_ntt<LN, true, true> : k_digit_ntt<LN, false, true>; \
     set_smem(kern, Cfg<LN>::SMEM);                                            \
     kern<<<blocks_for<LN>(num), Cfg<LN>::THREADS, Cfg<LN>::SMEM, s>>>(        \
         D, X, digits, k, need_lift, num, L, c);                               \

@@ -71,6 +71,18 @@ __device__ __forceinline__ void bf_ct_lazy(uint64_t& X, uint64_t& Y, Tw w,
   }
 }
 
+// First-level butterfly on raw inputs below 2^32 for the exact path (bf_ct's
+// ranges): the 32-bit-operand product is below 3q, one conditional
+// subtraction brings it below 2q.
+__device__ __forceinline__ void bf_ct_x32(uint64_t& X, uint64_t& Y, Tw w, uint64_t q,
+                                          uint64_t two_q) {
+  const uint64_t x = X;  // below 2^32 < 2q
+  uint64_t t = shoup_lazy_x32((uint32_t)Y, w.w, w.wp, q);
+  t = t >= two_q ? t - q : t;
+  X = x + t;
+  Y = x - t + two_q;
+}
+
 // First-level lazy butterfly on raw inputs below 2^32 (Y's product from
 // shoup_lazy_x32, below 3q; the outputs stay within bf_ct_lazy's ranges).
 __device__ __forceinline__ void bf_ct_lazy_x32(uint64_t& X, uint64_t& Y, Tw w, uint64_t q,
@@ -176,7 +188,7 @@ struct NttCore {
   // LAZY selects bf_ct_lazy (valid when q < 2^58, see above); FUSED the
   // butterflies' Shoup product form.
   // SMALL_IN (pass 0 only): every input is below 2^32, so the first level's
-  // products take bf_ct_lazy_x32 (LAZY only).
+  // products take the 32-bit-operand butterflies (bf_ct_lazy_x32 / bf_ct_x32).
   template <int p, bool LAZY, bool FUSED = true, bool SMALL_IN = false>
   __device__ __forceinline__ static void fwd_pass(uint64_t (&x)[E], int tid,
                                                   const Tw* __restrict__ tw,
@@ -197,8 +209,12 @@ struct NttCore {
         static_for<0, (1 << lb)>([&](auto ll) {
           constexpr int k0 = (u << (lb + 1)) | decltype(ll)::value;
           constexpr int k1 = k0 | (1 << lb);
-          if constexpr (LAZY && SMALL_IN && p == 0 && decltype(ii)::value == 0) {
-            bf_ct_lazy_x32(x[k0], x[k1], w, q, two_q);
+          if constexpr (SMALL_IN && p == 0 && decltype(ii)::value == 0) {
+            if constexpr (LAZY) {
+              bf_ct_lazy_x32(x[k0], x[k1], w, q, two_q);
+            } else {
+              bf_ct_x32(x[k0], x[k1], w, q, two_q);
+            }
           } else if constexpr (LAZY) {
             bf_ct_lazy<FUSED>(x[k0], x[k1], w, q, two_q);
           } else {

@@ -1087,12 +1087,12 @@ template <int LOG_N, class Src, class Dst>
 void fwd4(const CtxDev& c, const Src& src, const Dst& dst, PrimeMap pm,
           uint64_t* buf, int num, cudaStream_t s, bool small_in = false) {
   using S = Ntt4<LOG_N>;
-  // column kernel; small_in (LAZY only): every source value below 2^32
+  // column kernel; small_in: every source value below 2^32
   auto cols = [&](auto lazy) {
     constexpr bool LZ = decltype(lazy)::value;
     auto k1 = k4_fwd_cols<LOG_N, LZ, Src>;
-    if constexpr (LZ && std::is_same_v<Src, FwdSrcDigit<LOG_N>>) {
-      if (small_in) k1 = k4_fwd_cols<LOG_N, true, Src, true>;
+    if constexpr (std::is_same_v<Src, FwdSrcDigit<LOG_N>>) {
+      if (small_in) k1 = k4_fwd_cols<LOG_N, LZ, Src, true>;
     }
     set_smem4(k1, S::COL_SMEM);
     k1<<<num * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(src, pm, buf, c);
@@ -1235,8 +1235,9 @@ void launch4_digit_cols(const CtxDev& c, uint64_t* D, const uint64_t* X,
     const FwdSrcDigit<LN> src{X, digits, k, L, need_lift};                      \
     auto k1 = c.small_q ? k4_fwd_cols<LN, true, FwdSrcDigit<LN>>                \
                         : k4_fwd_cols<LN, false, FwdSrcDigit<LN>>;              \
-    if (c.small_q && digit_flags == 0)                                          \
-      k1 = k4_fwd_cols<LN, true, FwdSrcDigit<LN>, true>;                        \
+    if (digit_flags == 0)                                                       \
+      k1 = c.small_q ? k4_fwd_cols<LN, true, FwdSrcDigit<LN>, true>             \
+                     : k4_fwd_cols<LN, false, FwdSrcDigit<LN>, true>;           \
     set_smem4(k1, S::COL_SMEM);                                                 \
     k1<<<count * k * L * S::COL_TILES, S::COL_THREADS, S::COL_SMEM, s>>>(       \
         src, PrimeMap{0, 1, L}, D, c);                                          \
