@@ -1210,7 +1210,9 @@ int mul_relin_host_impl(shg_context* ctx, const shg_key* key, void* out_v, const
     std::vector<int> back;
     int rem = count;
     for (int r = 0; rem > 0; ++r) {
-      const int sz = ramp ? std::min(P, std::max(1, P >> ramp) << std::min(r, 20)) : P;
+      const int sz =
+          ramp ? (int)std::min<long long>(P, (long long)std::max(1, P >> ramp) << std::min(r, 20))
+               : P;
       const int f = std::min(sz, rem);
       sizes.push_back(f);
       rem -= f;
