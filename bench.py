@@ -152,7 +152,7 @@ def host_link_ms(h2d_bytes, d2h_bytes, rates):
     return t_both + (d2h_bytes - down * 1e6 * t_both) / (rates["d2h"] * 1e6)
 
 
-def warm_link(step, sync, min_calls, seconds=0.5):
+def warm_link(step, sync, min_calls, seconds=1.0):
     """Untimed warm-up of a host-buffer leg: at least `min_calls` calls and at
     least `seconds` of them.  After a second or two without host-link traffic
     (device-only work, or idle) the first copies run at about 10 GB/s for some
@@ -1824,8 +1824,13 @@ def main():
         link_after = link_probe()
         # The step's copies alone at the probed rates: the host link bounds
         # the step when this exceeds the device step.
-        h2d_ms = 2 * B * ct_bytes / (link_before["duplex"][0] * 1e6)
-        link_ms = host_link_ms(2 * B * ct_bytes, B * ct_bytes, link_before)
+        h2d_ms = 2 * B * ct_bytes / (max(link_before["duplex"][0], link_after["duplex"][0]) * 1e6)
+        # the link's capacity: the better of the two probes, rate by rate
+        best = {"h2d": max(link_before["h2d"], link_after["h2d"]),
+                "d2h": max(link_before["d2h"], link_after["d2h"]),
+                "duplex": [max(a, b) for a, b in zip(link_before["duplex"],
+                                                     link_after["duplex"])]}
+        link_ms = host_link_ms(2 * B * ct_bytes, B * ct_bytes, best)
         bound_ms = max(link_ms, total_ms / args.steps)
         e2e = {"value": ops_all / (e2e_ms / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": 2 * B * ct_bytes, "d2h_bytes_per_step": B * ct_bytes,
